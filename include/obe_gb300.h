@@ -1,0 +1,240 @@
+/*
+ * obe_gb300.h -- C ABI of the GB300 Lindblad `expanded_sparse` solver.
+ *
+ * This is the native boundary that replaces the reference's PyO3 extension for the Lindblad
+ * hot path (crate `centrex_tlf_rust`, rust/src/lindblad/python_api.rs).  Every entry point
+ * takes plain pointers and sizes; nothing here names a Python, Rust or torch type.  All
+ * arithmetic on the device is FP64 unless a solve asks for OBE_PRECISION_MIXED.
+ *
+ * Error convention: every function returns an obe_status.  On failure the message of the
+ * matching reference error (a Python ValueError there) is available from obe_last_error()
+ * in the calling thread until that thread's next call.
+ */
+#ifndef OBE_GB300_H
+#define OBE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OBE_ABI_VERSION 1
+
+typedef enum {
+    OBE_OK = 0,
+    OBE_ERR_INVALID = 1,      /* bad argument or payload (reference: ValueError)            */
+    OBE_ERR_TRAJECTORY = 2,   /* a trajectory failed; message "trajectory {i}: {msg}"        */
+    OBE_ERR_UNSUPPORTED = 3,  /* valid in the reference, outside this library's path          */
+    OBE_ERR_CUDA = 4,         /* CUDA runtime error or no usable device                       */
+    OBE_ERR_TIMEOUT = 5       /* a bounded device-side wait gave up                           */
+} obe_status;
+
+/* Solvers, rust/src/ode/batch.rs:8-30 (OdeSolver::from_str). */
+typedef enum { OBE_SOLVER_DOPRI5 = 0, OBE_SOLVER_TSIT5 = 1 } obe_solver;
+
+/* Observables, rust/src/lindblad/ode_batch.rs:103-163 (OutputSpec). */
+typedef enum {
+    OBE_OUTPUT_POPULATIONS = 0,        /* y[0..n]                                           */
+    OBE_OUTPUT_SELECTED = 1,           /* complex rho_ij for (i, j) pairs                   */
+    OBE_OUTPUT_FULL = 2,               /* the packed state                                   */
+    OBE_OUTPUT_WEIGHTED_INTEGRAL = 3,  /* trapezoid of sum w_i y_i over pushed points       */
+    OBE_OUTPUT_WEIGHTED_RATE = 4       /* sum w_i y_i at each pushed point                   */
+} obe_output_kind;
+
+typedef enum { OBE_EVENT_NONE = 0, OBE_EVENT_POPULATION = 1, OBE_EVENT_EXPRESSION = 2 } obe_event_kind;
+
+typedef enum { OBE_PRECISION_FP64 = 0, OBE_PRECISION_MIXED = 1 } obe_precision;
+
+/*
+ * A compiled expression program: the reference's bytecode (centrex_tlf/lindblad/ir.py:28-47,
+ * rust/src/lindblad/eval.rs:11-57) as parallel arrays.  `value` holds (re, im) pairs.
+ */
+typedef struct {
+    int64_t n_instr;
+    const int32_t* op;
+    const int64_t* index;
+    const int32_t* argc;
+    const int32_t* function;
+    const double* value;        /* [2 * n_instr] */
+    int32_t scalar_only;
+    int32_t output_is_tuple;
+} obe_expr;
+
+/*
+ * Plan descriptor: the payload of prepare_lindblad_problem_py
+ * (rust/src/lindblad/plan.rs:1155-1308; centrex_tlf/lindblad/plan_static.py:58-68) as flat
+ * arrays.  The library copies what it needs; the caller may free these after create.
+ */
+typedef struct {
+    int32_t n_states;
+
+    /* parameter graph (plan.rs:19-25) */
+    int32_t n_slots;                 /* len(slot_names)                                        */
+    int32_t n_base;                  /* len(base_values)                                       */
+    const int32_t* base_is_tuple;    /* [n_base]                                               */
+    const double* base_scalar;       /* [2 * n_base]  (re, im) of scalar base values           */
+    const int64_t* base_tuple_ptr;   /* [n_base + 1]  offsets into base_tuple_items            */
+    const double* base_tuple_items;  /* [2 * base_tuple_ptr[n_base]]                           */
+    int32_t n_compounds;
+    const int32_t* compound_slot;    /* [n_compounds]                                          */
+    const obe_expr* compound_expr;   /* [n_compounds]                                          */
+    int32_t n_pchip;
+    const int64_t* pchip_ptr;        /* [n_pchip + 1]                                          */
+    const double* pchip_grid;        /* [pchip_ptr[n_pchip]]                                   */
+    const double* pchip_values;      /* [pchip_ptr[n_pchip]]                                   */
+
+    /* decomposed Hamiltonian coefficients (plan.rs:242-276) */
+    int32_t hamiltonian_decomposed;  /* 1 for kind == "decomposed"                              */
+    int32_t n_coefficients;
+    const obe_expr* coefficient_expr;/* [n_coefficients]                                        */
+
+    /* expanded_sparse RHS plan (plan.rs:1069-1153; ir.py:447-613); has_expanded == 0 when the
+       payload's expanded_rhs_plan is None */
+    int32_t has_expanded;
+    int64_t n_terms;
+    const int64_t* output_ptrs;      /* [n(n+1)/2 + 1]                                          */
+    const int64_t* input_indices;    /* [n_terms] upper-triangle index                          */
+    const int64_t* coeff_indices;    /* [n_terms] -1 = static                                   */
+    const uint8_t* coeff_conj;       /* [n_terms]                                               */
+    const uint8_t* input_conj;       /* [n_terms]                                               */
+    const double* factors_re;        /* [n_terms]                                               */
+    const double* factors_im;        /* [n_terms]                                               */
+
+    /* dissipator (plan.rs:1174-1185), kept for validation of the payload */
+    const double* source_decay_rates;/* [n_states]                                             */
+} obe_plan_desc;
+
+/*
+ * Per-solve options: the arguments of solve_lindblad_ode_py / solve_lindblad_batch_ode_py /
+ * solve_lindblad_grid_ode_py (python_api.rs:422-799) after the reference's option mapping
+ * (python_api.rs:589-617): callers pass the *effective* saveat and save_start.
+ */
+typedef struct {
+    double t0, t1, abstol, reltol, dt;
+    int64_t maxiters;
+    int32_t solver;                  /* obe_solver                                              */
+    int32_t save_start;
+    int32_t has_saveat;              /* 0 = saveat None                                         */
+    int64_t n_saveat;
+    const double* saveat;            /* [n_saveat]                                              */
+    int32_t output;                  /* obe_output_kind                                         */
+    int32_t store_trace;             /* integral outputs: 1 when output_when == "saveat"        */
+    int32_t n_weights;
+    const int64_t* weight_index;     /* [n_weights]                                             */
+    const double* weight_value;      /* [n_weights]                                             */
+    int32_t n_selected;
+    const int64_t* selected_i;       /* [n_selected]                                            */
+    const int64_t* selected_j;       /* [n_selected]                                            */
+    int32_t event_kind;              /* obe_event_kind                                          */
+    int32_t n_event_indices;
+    const int64_t* event_indices;    /* population event                                        */
+    double event_threshold;
+    obe_expr event_expr;             /* runtime-expression event                                */
+    int32_t precision;               /* obe_precision                                           */
+} obe_solve_options;
+
+/* Per-trajectory solver statistics (rust/src/ode/mod.rs:27-35). */
+typedef struct {
+    int64_t accepted_steps;
+    int64_t rejected_steps;
+    int64_t rhs_calls;
+    int32_t event_triggered;
+    int32_t status;                  /* 0 = ok, otherwise an internal code, see obe_last_error */
+    double event_time;
+    int64_t n_points;                /* points pushed into the output                          */
+} obe_traj_stats;
+
+typedef struct obe_plan obe_plan;
+typedef struct obe_result obe_result;
+
+/* Thread-local message of the last failure in this thread ("" if none). */
+const char* obe_last_error(void);
+
+/* ABI version of the loaded library (OBE_ABI_VERSION). */
+int32_t obe_abi_version(void);
+
+/* Number of CUDA devices the library can use; 0 without a GPU (never an error). */
+int32_t obe_device_count(void);
+
+/*
+ * prepare_lindblad_problem_py (python_api.rs:271-274 -> plan.rs:1155-1308): validate the
+ * payload and build the packed term tables (the coefficient packer).  Validation messages are
+ * those of plan.rs:1096-1150.  Runs on the host; no device memory is touched until a solve.
+ */
+obe_status obe_plan_create(const obe_plan_desc* desc, obe_plan** out_plan);
+void obe_plan_destroy(obe_plan* plan);
+
+/* Packed length n*n and state count of a plan. */
+int64_t obe_plan_packed_len(const obe_plan* plan);
+int32_t obe_plan_n_states(const obe_plan* plan);
+
+/*
+ * One RHS evaluation per state on the device: lindblad_rhs_py(plan, packed_state, t,
+ * "expanded_sparse") (python_api.rs:294-316 -> rhs.rs:2090-2148), batched over `count`
+ * states with optional per-state base-slot overrides.  Host pointers.
+ *   y[count * N], t[count], overrides[count * n_slots * 2] (complex, may be NULL), dy[count * N]
+ */
+obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, const double* y,
+                        int32_t n_override_slots, const int64_t* override_slots,
+                        const double* override_values, int32_t precision, double* dy);
+
+/*
+ * solve_lindblad_ode_py (python_api.rs:422-528): one trajectory.  The number of output points
+ * is not known in advance (every accepted step when saveat is None), so the result is a
+ * library-owned object read with obe_result_*.  Host pointers.
+ */
+obe_status obe_solve_single(const obe_plan* plan, const obe_solve_options* opt, const double* rho0,
+                            obe_result** out_result);
+void obe_result_shape(const obe_result* res, int64_t* n_times, int64_t* width, int32_t* is_complex);
+void obe_result_stats(const obe_result* res, obe_traj_stats* stats);
+/* times[n_times]; values[n_times * width] (doubles, or interleaved re/im when is_complex) */
+void obe_result_copy(const obe_result* res, double* times, double* values);
+void obe_result_destroy(obe_result* res);
+
+/*
+ * solve_lindblad_batch_ode_py (python_api.rs:530-669 -> ode_batch.rs:176-351): B trajectories,
+ * each with its own packed rho0 and optional scalar overrides of base slots.  Outputs have a
+ * fixed count per trajectory (`time_count` points of `width` values; interleaved re/im for
+ * OBE_OUTPUT_SELECTED), written to values[B * time_count * width (*2)].  Host pointers; the
+ * copies to and from the device happen inside the call.
+ *   rho0[B * N]; param_values[B * n_param_slots * 2] (complex) or NULL;
+ *   stats[B] may be NULL; times[time_count] receives the output times (t1 for final outputs).
+ */
+obe_status obe_solve_batch(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
+                           const double* rho0, int32_t n_param_slots, const int64_t* param_slots,
+                           const double* param_values, int64_t time_count, int64_t width,
+                           double* values, obe_traj_stats* stats);
+
+/*
+ * solve_lindblad_grid_ode_py (python_api.rs:671-799 -> ode_batch.rs:571-1040): a row-major
+ * grid over scalar base slots (last axis fastest, ode_batch.rs:353-391) from one rho0.
+ *   rho0[N]; axes[2 * sum(axis_lengths)] (complex); axis_lengths[n_axes].
+ */
+obe_status obe_solve_grid(const obe_plan* plan, const obe_solve_options* opt, const double* rho0,
+                          int32_t n_axes, const int64_t* axis_slots, const int64_t* axis_lengths,
+                          const double* axes, int64_t time_count, int64_t width, double* values,
+                          obe_traj_stats* stats);
+
+/*
+ * Device-resident form of obe_solve_batch: every pointer is device memory and the call is
+ * asynchronous on `stream` (a cudaStream_t, or NULL for the legacy default stream).  It does
+ * not synchronise; statuses land in d_stats.  This is the call a GPU-side caller (and the
+ * benchmark's device-resident timing) uses; it allocates nothing per call once a plan has
+ * been uploaded by its first solve.
+ */
+obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options* opt,
+                                  int64_t n_traj, const double* d_rho0, int32_t n_param_slots,
+                                  const int64_t* param_slots, const double* d_param_values,
+                                  int64_t time_count, int64_t width, double* d_values,
+                                  obe_traj_stats* d_stats, void* stream);
+
+/* Number of kernel launches issued by the last solve in this thread (for accounting). */
+int64_t obe_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OBE_GB300_H */

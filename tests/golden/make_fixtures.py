@@ -1,0 +1,414 @@
+"""Generate the golden fixtures under tests/golden/ from the reference's own Python code.
+
+Run in a container that has the CeNTREX-TlF reference checkout (default path below, or the
+``CENTREX_REFERENCE`` environment variable):
+
+    python tests/golden/make_fixtures.py
+
+What it writes (all JSON through ``codec.py``):
+
+* ``plan_<name>.json``: the plan payload dict exactly as the reference's
+  ``PreparedLindbladProblem.to_payload()`` returns it (centrex_tlf/lindblad/plan_static.py:58-68),
+  built by the reference's unchanged builders (``prepare_lindblad_problem`` with
+  ``backend="python"``, centrex_tlf/lindblad/plan_static.py:137-185), plus the packed initial
+  state, the time span and the metadata a test needs.
+* ``rhs_<name>.json``: packed states, times, base-parameter overrides and the packed RHS from
+  the reference's Python FP64 evaluators ``structured_rhs`` and ``reference_rhs``
+  (centrex_tlf/lindblad/reference_dense.py:60-77) for each of them.
+* ``rk45_<name>.json``: trajectories from the reference's SciPy RK45 solve
+  (``solve_lindblad(..., backend="python")``, centrex_tlf/lindblad/solve.py:155-199):
+  tolerance-level anchors for whole solves.
+* ``ffi_calls.json``: the positional arguments the reference's Python surface
+  (solve.py:419, batch.py:235, batch.py:440) passes across its native boundary, recorded by
+  installing a recording stand-in module as ``centrex_tlf.centrex_tlf_rust``.
+
+pandas and matplotlib are stubbed: the reference imports them only for DataFrames and plotting
+(centrex_tlf/couplings/branching.py:5, centrex_tlf/utils/plotting.py:9-13).
+"""
+
+from __future__ import annotations
+
+import copy
+import importlib.abc
+import importlib.machinery
+import os
+import sys
+import time
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import codec  # noqa: E402
+
+REFERENCE = Path(os.environ.get("CENTREX_REFERENCE", "/root/reference"))
+
+# Γ for the benchmark configurations: 2π·1.56 MHz, passed explicitly to the builders.
+GAMMA = 2.0 * np.pi * 1.56e6
+
+
+class _StubModule(types.ModuleType):
+    def __getattr__(self, attr):
+        if attr.startswith("__"):
+            raise AttributeError(attr)
+        return type(attr, (), {"__init__": lambda self, *a, **k: None})
+
+
+class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
+    def find_spec(self, fullname, path, target=None):
+        if fullname.split(".")[0] in ("pandas", "matplotlib"):
+            return importlib.machinery.ModuleSpec(fullname, self, is_package=True)
+        return None
+
+    def create_module(self, spec):
+        module = _StubModule(spec.name)
+        module.__path__ = []
+        return module
+
+    def exec_module(self, module):
+        pass
+
+
+def _import_reference():
+    sys.meta_path.insert(0, _StubFinder())
+    sys.path.insert(0, str(REFERENCE))
+    import sympy as smp  # noqa: F401
+
+    import centrex_tlf  # noqa: F401
+
+    return centrex_tlf
+
+
+def _hermitian(rng: np.random.Generator, n: int, scale: float = 1.0) -> np.ndarray:
+    m = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return scale * (m + m.conj().T)
+
+
+def _density(rng: np.random.Generator, n: int) -> np.ndarray:
+    m = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    rho = m @ m.conj().T
+    return rho / np.trace(rho).real
+
+
+def build_two_level(centrex_tlf, omega=0.6, delta=0.0, time_dependent=False):
+    """Two-level system of the reference's benchmark and tests
+    (benchmarks/bench_expanded_sparse_packed_rhs_kernels.py:102-157,
+    tests/lindblad/test_rust_backend.py:35-58)."""
+    import sympy as smp
+    from centrex_tlf.lindblad.plan_static import prepare_lindblad_problem
+    from centrex_tlf.lindblad.utils_setup import OBESystem
+
+    om, de = smp.symbols("Omega delta", real=True)
+    hamiltonian = smp.Matrix([[0, om / 2], [smp.conjugate(om) / 2, -de]])
+    c_array = np.zeros((1, 2, 2), dtype=np.complex128)
+    c_array[0, 0, 1] = np.sqrt(0.3)
+    zeros = np.zeros((2, 2), dtype=np.complex128)
+    system = OBESystem(
+        ground=[], excited=[], QN=[], H_int=zeros, V_ref_int=zeros, couplings=[],
+        H_symbolic=hamiltonian, C_array=c_array, system=None,
+        coupling_symbols=[om, de], polarization_symbols=[],
+    )
+    if time_dependent:
+        params = {
+            "omega0": 1.0,
+            "modulation_depth": 0.5,
+            "modulation_frequency": 1.9,
+            "delta": -0.1,
+            "Omega": "omega0*phase_modulation(t, modulation_depth, modulation_frequency)",
+        }
+    else:
+        params = {"Omega": omega, "delta": delta}
+    return prepare_lindblad_problem(system, params, backend="python", hamiltonian_representation="decomposed")
+
+
+def build_chain(centrex_tlf, n_states: int):
+    """Nearest-neighbour chain of the reference's partition-gate test
+    (tests/lindblad/test_rust_backend.py:489-568)."""
+    import sympy as smp
+    from centrex_tlf.lindblad.plan_static import prepare_lindblad_problem
+    from centrex_tlf.lindblad.utils_setup import OBESystem
+
+    om, de = smp.symbols("Omega delta", real=True)
+    hamiltonian = smp.zeros(n_states, n_states)
+    for i in range(n_states):
+        hamiltonian[i, i] = de * i
+    for i in range(n_states - 1):
+        hamiltonian[i, i + 1] = om / 2
+        hamiltonian[i + 1, i] = smp.conjugate(om) / 2
+    c_array = np.zeros((n_states - 1, n_states, n_states), dtype=np.complex128)
+    for i in range(n_states - 1):
+        c_array[i, i, i + 1] = np.sqrt(0.1)
+    zeros = np.zeros((n_states, n_states), dtype=np.complex128)
+    system = OBESystem(
+        ground=[], excited=[], QN=[], H_int=zeros, V_ref_int=zeros, couplings=[],
+        H_symbolic=hamiltonian, C_array=c_array, system=None,
+        coupling_symbols=[om, de], polarization_symbols=[],
+    )
+    params = {
+        "omega0": 1.0,
+        "modulation_depth": 0.5,
+        "modulation_frequency": 1.9,
+        "delta": 0.2,
+        "Omega": "omega0*phase_modulation(t, modulation_depth, modulation_frequency)",
+    }
+    return prepare_lindblad_problem(system, params, backend="python", hamiltonian_representation="decomposed")
+
+
+def build_q1_16(centrex_tlf):
+    """The 16-state TlF system of the single-solve and scan benchmarks.
+
+    X J=1 (12 hyperfine states) + B J'=1 F1'=1/2 F'=1 (3 mF states) + the X J=3 level the
+    B state also decays to, lumped into one state by the builder's own ``qn_compact=True``
+    (centrex_tlf/lindblad/utils_setup.py:515-629).  Q(1) F'=1 drive with z- and x-linear
+    polarisation components; a Gaussian-in-time Rabi pulse; Γ = 2π·1.56 MHz.
+    """
+    from centrex_tlf import couplings, lindblad, transitions
+    from centrex_tlf.lindblad.parameters import LindbladParameters
+    from centrex_tlf.lindblad.plan_static import prepare_lindblad_problem
+
+    trans = [transitions.Q1_F1_1o2_F1]
+    selectors = couplings.generate_transition_selectors(
+        trans, [[couplings.polarization_Z, couplings.polarization_X]]
+    )
+    obe = lindblad.generate_OBE_system_transitions(trans, selectors, qn_compact=True, Γ=GAMMA)
+    params = LindbladParameters.from_kwargs(
+        rabi=GAMMA,
+        detuning=0.0,
+        theta=0.0,
+        t_center=100.0 / GAMMA,
+        sigma=20.0 / GAMMA,
+        Ω0="rabi*exp(-(t-t_center)**2/(2*sigma**2))",
+        δ0="detuning",
+        PZ0="cos(theta)",
+        PX0="sin(theta)",
+    )
+    prepared = prepare_lindblad_problem(obe, params, backend="python", hamiltonian_representation="decomposed")
+    labels = [str(s.largest) for s in obe.QN]
+    return prepared, labels
+
+
+def _with_base_overrides(prepared, overrides: dict[int, complex]):
+    """A shallow stand-in of ``prepared`` whose parameter graph has some base values replaced
+    (what the batch drivers' scalar overrides do, rust/src/lindblad/rhs.rs:1176-1197)."""
+    graph = copy.deepcopy(prepared.parameter_graph)
+    for slot, value in overrides.items():
+        graph["base_values"][slot] = {"kind": "scalar", "re": float(np.real(value)), "im": float(np.imag(value))}
+    return types.SimpleNamespace(
+        layout=prepared.layout,
+        parameter_graph=graph,
+        hamiltonian_plan=prepared.hamiltonian_plan,
+        structured_jumps=prepared.structured_jumps,
+        source_decay_rates=prepared.source_decay_rates,
+        dense_c_array=prepared.dense_c_array,
+    )
+
+
+def rhs_vectors(prepared, times, overrides_list, seed, scale=1.0):
+    from centrex_tlf.lindblad.reference_dense import reference_rhs, structured_rhs
+
+    rng = np.random.default_rng(seed)
+    n = prepared.layout.n
+    cases = []
+    for overrides in overrides_list:
+        view = _with_base_overrides(prepared, overrides)
+        for t in times:
+            rho = _hermitian(rng, n, scale)
+            packed = prepared.layout.pack(rho)
+            cases.append(
+                {
+                    "t": float(t),
+                    "override_slots": np.array(sorted(overrides), dtype=np.int64),
+                    "override_values": np.array([overrides[k] for k in sorted(overrides)], dtype=np.complex128),
+                    "packed": packed,
+                    "structured": structured_rhs(view, packed, float(t)),
+                    "reference": reference_rhs(view, packed, float(t)),
+                }
+            )
+    return cases
+
+
+def rk45_solve(prepared, rho0, t_span, saveat, abstol, reltol, overrides=None):
+    from centrex_tlf.lindblad.solve import solve_lindblad
+
+    target = prepared if not overrides else _reprepared(prepared, overrides)
+    result = solve_lindblad(
+        target, rho0, t_span, backend="python", abstol=abstol, reltol=reltol, saveat=saveat
+    )
+    return {"t": np.asarray(result.t), "packed_y": np.asarray(result.packed_y)}
+
+
+def _reprepared(prepared, overrides):
+    view = copy.copy(prepared)
+    view.parameter_graph = _with_base_overrides(prepared, overrides).parameter_graph
+    return view
+
+
+def record_ffi_calls(centrex_tlf, prepared, rho0):
+    """Run the reference's Python surface with a recording stand-in for its native module and
+    keep the positional arguments of each call."""
+    import centrex_tlf.lindblad.batch as batch_mod
+    import centrex_tlf.lindblad.solve as solve_mod
+
+    calls = []
+    n = prepared.layout.n
+    N = prepared.layout.packed_len
+
+    class _Plan:
+        pass
+
+    def _solve_single(*args):
+        calls.append({"fn": "solve_lindblad_ode_py", "args": list(args[1:])})
+        output = args[12]
+        if output == "full":
+            width = N
+        elif output == "populations":
+            width = n
+        elif output == "selected":
+            width = len(args[13])
+        else:
+            width = 1
+        return np.array([args[3]]), np.zeros(width), width, {"accepted_steps": 0, "rejected_steps": 0, "rhs_calls": 0, "event_triggered": False}
+
+    def _solve_batch(*args):
+        calls.append({"fn": "solve_lindblad_batch_ode_py", "args": list(args[1:])})
+        b = args[1].shape[0]
+        output = args[12]
+        width = n if output == "populations" else (len(args[13]) if output == "selected" else 1)
+        tc = 1 if args[14] == "final" else len(args[7])
+        vals = np.zeros(b * tc * width, dtype=np.complex128 if output == "selected" else np.float64)
+        return np.array([args[3]]), vals, width, tc, {"accepted_steps": 0, "rejected_steps": 0, "rhs_calls": 0, "event_triggered": False, "event_triggered_by_trajectory": [False] * b, "event_times": [args[3]] * b, "event_count": 0}
+
+    def _solve_grid(*args):
+        calls.append({"fn": "solve_lindblad_grid_ode_py", "args": list(args[1:])})
+        b = int(np.prod(args[9]))
+        output = args[15]
+        width = n if output == "populations" else (len(args[16]) if output == "selected" else 1)
+        tc = 1 if args[17] == "final" else len(args[10])
+        vals = np.zeros(b * tc * width, dtype=np.complex128 if output == "selected" else np.float64)
+        return np.array([args[3]]), vals, width, tc, {"accepted_steps": 0, "rejected_steps": 0, "rhs_calls": 0, "event_triggered": False, "event_triggered_by_trajectory": [False] * b, "event_times": [args[3]] * b, "event_count": 0}
+
+    stand_in = types.ModuleType("centrex_tlf.centrex_tlf_rust")
+    stand_in.solve_lindblad_ode_py = _solve_single
+    stand_in.solve_lindblad_batch_ode_py = _solve_batch
+    stand_in.solve_lindblad_grid_ode_py = _solve_grid
+    sys.modules["centrex_tlf.centrex_tlf_rust"] = stand_in
+    view = copy.copy(prepared)
+    view.rust_plan = _Plan()
+    view.backend = "rust"
+    t_span = (0.0, 200.0 / GAMMA)
+    weights = [(13, 1.0), (14, 1.0), (15, 1.0)]
+    slots = prepared.parameter_graph["slot_names"]
+    solve_mod.solve_lindblad(view, rho0, t_span, solver="dopri5", abstol=1e-11, reltol=1e-8, dt=1e-3 / GAMMA,
+                             output="populations", output_when="final")
+    solve_mod.solve_lindblad(view, rho0, t_span, solver="tsit5", abstol=1e-11, reltol=1e-8, dt=1e-3 / GAMMA,
+                             output="excited_population", output_when="final", integral_weights=weights)
+    solve_mod.solve_lindblad(view, rho0, t_span, solver="dopri5", abstol=1e-11, reltol=1e-8, dt=1e-3 / GAMMA,
+                             output="selected", output_indices=[(0, 13), (14, 2), (5, 5)],
+                             saveat=np.linspace(0.0, t_span[1], 11))
+    pb = np.array([[GAMMA * 0.5, 0.3 * GAMMA, 0.2], [GAMMA * 2.0, -1.0 * GAMMA, 1.1]], dtype=np.complex128)
+    batch_mod.parameter_scan(view, rho0, t_span, parameter_slots=["rabi", "detuning", "theta"], parameter_batch=pb,
+                             solver="tsit5", abstol=1e-11, reltol=1e-8, dt=1e-3 / GAMMA,
+                             output="excited_population", integral_weights=weights)
+    batch_mod.solve_lindblad_batch(view, np.stack([rho0, rho0]), t_span, solver="dopri5", abstol=1e-11, reltol=1e-8,
+                                   dt=1e-3 / GAMMA, output="populations", output_when="saveat",
+                                   saveat=np.linspace(0.0, t_span[1], 5))
+    batch_mod.grid_scan(view, rho0, t_span, scan={"detuning": np.linspace(-GAMMA, GAMMA, 3), "rabi": [GAMMA, 2 * GAMMA]},
+                        solver="dopri5", abstol=1e-11, reltol=1e-8, dt=1e-3 / GAMMA,
+                        output="photon_integral", integral_weights=[(13, GAMMA), (14, GAMMA), (15, GAMMA)])
+    del sys.modules["centrex_tlf.centrex_tlf_rust"]
+    return {"slot_names": slots, "calls": calls}
+
+
+def main() -> None:
+    centrex_tlf = _import_reference()
+    started = time.perf_counter()
+
+    # --- two-level known-answer system -----------------------------------------------------
+    two = build_two_level(centrex_tlf, omega=0.6, delta=0.0)
+    rho2 = np.zeros((2, 2), dtype=np.complex128)
+    rho2[0, 0] = 1.0
+    codec.save(
+        "plan_two_level",
+        {
+            "payload": two.to_payload(),
+            "rho0_packed": two.layout.pack(rho2),
+            "t_span": [0.0, 0.5],
+            # benchmarks/expanded_sparse_packed_rhs_results/validation.csv:6 and
+            # solve_timings.csv:2 (Rust FP64 Dopri5, rtol 1e-8, atol 1e-10, dt 1e-3,
+            # photon_integral weights [(1, 0.3)], output_when="final").
+            "kat": {
+                "photon_integral": 0.001068126891997914,
+                "accepted_steps": 10,
+                "rejected_steps": 0,
+                "rhs_calls": 61,
+                "abstol": 1e-10,
+                "reltol": 1e-8,
+                "dt": 1e-3,
+                "weights": [[1, 0.3]],
+            },
+            # grid_timings.csv:2: 25-point detuning grid, 4 threads.
+            "kat_grid": {"detuning": np.linspace(-0.4, 0.4, 25), "accepted_steps": 252, "rejected_steps": 0, "rhs_calls": 1537},
+        },
+    )
+    codec.save("rhs_two_level", {"cases": rhs_vectors(two, [0.0, 0.41], [{}, {0: 0.9, 1: 0.2}], seed=1)})
+    codec.save("rk45_two_level", rk45_solve(two, rho2, (0.0, 0.5), np.linspace(0.0, 0.5, 11), 1e-10, 1e-8))
+
+    two_td = build_two_level(centrex_tlf, time_dependent=True)
+    codec.save("plan_two_level_td", {"payload": two_td.to_payload(), "rho0_packed": two_td.layout.pack(rho2), "t_span": [0.0, 5.0]})
+    codec.save("rhs_two_level_td", {"cases": rhs_vectors(two_td, [0.0, 0.41, 2.3], [{}], seed=2)})
+    codec.save("rk45_two_level_td", rk45_solve(two_td, rho2, (0.0, 5.0), np.linspace(0.0, 5.0, 21), 1e-10, 1e-8))
+
+    # --- chains on both sides of the 40-state partition gate -------------------------------
+    for n_states in (3, 45):
+        chain = build_chain(centrex_tlf, n_states)
+        rho_c = np.zeros((n_states, n_states), dtype=np.complex128)
+        rho_c[0, 0] = 1.0
+        codec.save(
+            f"plan_chain{n_states}",
+            {"payload": chain.to_payload(), "rho0_packed": chain.layout.pack(rho_c), "t_span": [0.0, 4.0]},
+        )
+        codec.save(f"rhs_chain{n_states}", {"cases": rhs_vectors(chain, [0.0, 0.41], [{}, {3: 0.35}], seed=3 + n_states)})
+        if n_states == 3:
+            codec.save("rk45_chain3", rk45_solve(chain, rho_c, (0.0, 4.0), np.linspace(0.0, 4.0, 9), 1e-10, 1e-8))
+
+    # --- 16-state TlF Q(1) system ----------------------------------------------------------
+    q1, labels = build_q1_16(centrex_tlf)
+    rho_q = np.zeros((16, 16), dtype=np.complex128)
+    for i in range(12):
+        rho_q[i, i] = 1.0 / 12.0
+    slots = q1.parameter_graph["slot_names"]
+    codec.save(
+        "plan_q1_16",
+        {
+            "payload": q1.to_payload(),
+            "rho0_packed": q1.layout.pack(rho_q),
+            "t_span": [0.0, 200.0 / GAMMA],
+            "gamma": GAMMA,
+            "state_labels": labels,
+            "excited_indices": [13, 14, 15],
+            "scan_slots": ["rabi", "detuning", "theta", "t_center"],
+        },
+    )
+    ov = [
+        {},
+        {slots.index("rabi"): 3.0 * GAMMA, slots.index("detuning"): -2.0 * GAMMA, slots.index("theta"): 0.7},
+        {slots.index("rabi"): 0.2 * GAMMA, slots.index("detuning"): 4.5 * GAMMA, slots.index("theta"): 2.9},
+    ]
+    codec.save("rhs_q1_16", {"cases": rhs_vectors(q1, [0.0, 80.0 / GAMMA, 100.0 / GAMMA, 130.0 / GAMMA], ov, seed=16, scale=0.05)})
+    t_q = (0.0, 200.0 / GAMMA)
+    rk = {}
+    for key, over in (("nominal", {}), ("detuned", ov[1])):
+        rk[key] = rk45_solve(q1, rho_q, t_q, np.linspace(0.0, t_q[1], 9), 1e-11, 1e-8, overrides=over)
+        rk[key]["override_slots"] = np.array(sorted(over), dtype=np.int64)
+        rk[key]["override_values"] = np.array([over[k] for k in sorted(over)], dtype=np.complex128)
+    codec.save("rk45_q1_16", rk)
+
+    # --- the native-boundary call contract of the reference's Python surface ----------------
+    codec.save("ffi_calls", record_ffi_calls(centrex_tlf, q1, rho_q))
+    print(f"fixtures written in {time.perf_counter() - started:.1f} s")
+
+
+if __name__ == "__main__":
+    main()

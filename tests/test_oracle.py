@@ -1,0 +1,190 @@
+"""Pin the CPU oracle (oracle/obe_oracle.c) before any GPU result is compared with it.
+
+Anchors, all from the reference itself:
+* the two-level known answer of its packed-RHS benchmark
+  (benchmarks/expanded_sparse_packed_rhs_results/validation.csv:5-8, solve_timings.csv:2,
+  grid_timings.csv:2);
+* its Python FP64 RHS evaluators run on the same payloads (tests/golden/rhs_*.json, made by
+  tests/golden/make_fixtures.py from centrex_tlf/lindblad/reference_dense.py:60-77);
+* its SciPy RK45 solves (tests/golden/rk45_*.json, centrex_tlf/lindblad/solve.py:155-199);
+* its error messages (rust/src/ode/dopri5.rs:167-231, common.rs:124-151).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+
+PLANS = ["two_level", "two_level_td", "chain3", "chain45", "q1_16"]
+
+
+def _plan(golden, name):
+    return oracle.OraclePlan(golden(f"plan_{name}")["payload"])
+
+
+def _opts(plan, **kw):
+    base = dict(
+        t0=0.0, t1=1.0, abstol=1e-10, reltol=1e-8, dt=1e-3, saveat=None, save_start=True,
+        maxiters=100000, solver="dopri5", output="populations", output_indices=None,
+        output_when="final", integral_weights=None, stop_event=None,
+    )
+    base.update(kw)
+    return plan.options(**base)
+
+
+def test_two_level_known_answer(golden):
+    d = golden("plan_two_level")
+    kat = d["kat"]
+    p = oracle.OraclePlan(d["payload"])
+    o = _opts(p, t1=0.5, abstol=kat["abstol"], reltol=kat["reltol"], dt=kat["dt"],
+              output="photon_integral", integral_weights=[(1, 0.3)])
+    _, v, st = p.solve_single(o, d["rho0_packed"])
+    assert st["accepted_steps"] == kat["accepted_steps"] == 10
+    assert st["rejected_steps"] == kat["rejected_steps"] == 0
+    assert st["rhs_calls"] == kat["rhs_calls"] == 61
+    # bit-identical to the reference's split-input kernel run (validation.csv:7-8)
+    assert v[-1, 0] == 0.0010681268919861524
+    # and within 1.1e-11 relative of its recorded baseline value (validation.csv:5)
+    assert abs(v[-1, 0] - kat["photon_integral"]) <= 2e-11 * kat["photon_integral"]
+
+
+def test_two_level_grid_known_answer(golden):
+    d = golden("plan_two_level")
+    kat = d["kat"]
+    p = oracle.OraclePlan(d["payload"])
+    o = _opts(p, t1=0.5, abstol=kat["abstol"], reltol=kat["reltol"], dt=kat["dt"],
+              output="photon_integral", integral_weights=[(1, 0.3)])
+    det = d["kat_grid"]["detuning"]
+    slot = p.slot_names.index("delta")
+    vals, times, stats = p.solve_batch(o, d["rho0_packed"], [slot], det.reshape(-1, 1).astype(complex))
+    assert int(stats["accepted_steps"].sum()) == d["kat_grid"]["accepted_steps"] == 252
+    assert int(stats["rejected_steps"].sum()) == 0
+    assert int(stats["rhs_calls"].sum()) == d["kat_grid"]["rhs_calls"] == 1537
+    assert times[0] == 0.5
+    # the photon line is symmetric in the detuning and peaks on resonance
+    line = vals[:, 0, 0]
+    assert int(np.argmax(line)) == 12
+    np.testing.assert_allclose(line, line[::-1], rtol=1e-6)
+
+
+@pytest.mark.parametrize("name", PLANS)
+def test_rhs_matches_python_reference(golden, name):
+    p = _plan(golden, name)
+    for case in golden(f"rhs_{name}")["cases"]:
+        dy = p.rhs(case["packed"], case["t"], case["override_slots"], case["override_values"])
+        ref = case["structured"]
+        scale = float(np.max(np.abs(ref)))
+        np.testing.assert_allclose(dy, ref, rtol=1e-9, atol=1e-12 * scale)
+        # the dense C rho C^dagger form agrees as well (test_rust_backend.py:568 tolerance)
+        np.testing.assert_allclose(dy, case["reference"], rtol=1e-9, atol=1e-12 * scale)
+
+
+def test_split_input_orders_agree(golden):
+    p = _plan(golden, "chain45")
+    for case in golden("rhs_chain45")["cases"]:
+        a = p.rhs(case["packed"], case["t"], case["override_slots"], case["override_values"], use_split_input_rhs=True)
+        b = p.rhs(case["packed"], case["t"], case["override_slots"], case["override_values"], use_split_input_rhs=False)
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-13 * np.max(np.abs(a)))
+
+
+@pytest.mark.parametrize("name,solver", [("two_level", "dopri5"), ("two_level_td", "tsit5"), ("chain3", "dopri5")])
+def test_trajectory_matches_scipy_rk45(golden, name, solver):
+    d = golden(f"plan_{name}")
+    rk = golden(f"rk45_{name}")
+    p = oracle.OraclePlan(d["payload"])
+    t0, t1 = d["t_span"]
+    o = _opts(p, t0=t0, t1=t1, abstol=1e-10, reltol=1e-8, dt=1e-3, saveat=rk["t"], output="full",
+              output_when="saveat", solver=solver)
+    t, v, _ = p.solve_single(o, d["rho0_packed"])
+    np.testing.assert_allclose(t, rk["t"], rtol=0, atol=1e-15)
+    # Rust-vs-RK45 tolerance of the reference (test_rust_backend.py:2118-2149)
+    np.testing.assert_allclose(v, rk["packed_y"], atol=5e-7, rtol=5e-6)
+
+
+@pytest.mark.parametrize("case", ["nominal", "detuned"])
+def test_q1_trajectory_matches_scipy_rk45(golden, case):
+    d = golden("plan_q1_16")
+    rk = golden("rk45_q1_16")[case]
+    p = oracle.OraclePlan(d["payload"])
+    t0, t1 = d["t_span"]
+    gamma = d["gamma"]
+    o = _opts(p, t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=rk["t"], output="full",
+              output_when="saveat")
+    t, v, st = p.solve_single(o, d["rho0_packed"], rk["override_slots"], rk["override_values"])
+    np.testing.assert_allclose(v, rk["packed_y"], atol=5e-7, rtol=5e-6)
+    trace = v[:, :16].sum(axis=1)
+    np.testing.assert_allclose(trace, 1.0, atol=2e-6)
+    assert st["accepted_steps"] > 50
+
+
+def test_outputs_are_consistent_with_full_trajectory(golden):
+    """populations / selected / final-only agree with the full trajectory
+    (test_rust_backend.py:873-927 tolerances)."""
+    d = golden("plan_q1_16")
+    p = oracle.OraclePlan(d["payload"])
+    gamma = d["gamma"]
+    t1 = d["t_span"][1]
+    common = dict(t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma)
+    saveat = np.linspace(0.0, t1, 7)
+    _, full, _ = p.solve_single(_opts(p, saveat=saveat, output="full", output_when="saveat", **common), d["rho0_packed"])
+    _, pops, _ = p.solve_single(_opts(p, saveat=saveat, output="populations", output_when="saveat", **common), d["rho0_packed"])
+    np.testing.assert_allclose(pops, full[:, :16], atol=1e-12, rtol=1e-10)
+    pairs = [(0, 13), (14, 2), (5, 5)]
+    _, sel, _ = p.solve_single(_opts(p, saveat=saveat, output="selected", output_indices=pairs, output_when="saveat", **common), d["rho0_packed"])
+    from centrex_tlf_gb300._options import packed_upper_real_index
+
+    r = packed_upper_real_index(16, 0, 13)
+    np.testing.assert_allclose(sel[:, 0], full[:, r] + 1j * full[:, r + 1], atol=1e-12)
+    r = packed_upper_real_index(16, 2, 14)
+    np.testing.assert_allclose(sel[:, 1], full[:, r] - 1j * full[:, r + 1], atol=1e-12)
+    np.testing.assert_allclose(sel[:, 2], full[:, 5], atol=1e-12)
+
+
+def test_integral_trace_final_and_rate_agree(golden):
+    """The integral trace ends at the final integral; the rate trace integrates to it
+    (test_rust_backend.py:1615-1694)."""
+    d = golden("plan_q1_16")
+    p = oracle.OraclePlan(d["payload"])
+    gamma = d["gamma"]
+    t1 = d["t_span"][1]
+    w = [(13, 1.0), (14, 1.0), (15, 1.0)]
+    common = dict(t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, integral_weights=w, solver="tsit5")
+    _, fin, st = p.solve_single(_opts(p, output="excited_population", output_when="final", **common), d["rho0_packed"])
+    t, trace, st2 = p.solve_single(_opts(p, output="excited_population", output_when="saveat", **common), d["rho0_packed"])
+    assert fin.shape == (1, 1)
+    assert trace.shape[0] == st2["accepted_steps"] + 1
+    assert trace[-1, 0] == fin[0, 0]
+    saveat = np.linspace(0.0, t1, 2001)
+    ts, rate, _ = p.solve_single(_opts(p, output="excited_population_rate", output_when="saveat", saveat=saveat, **common), d["rho0_packed"])
+    approx = np.trapezoid(rate[:, 0], ts)
+    assert abs(approx - fin[0, 0]) <= 1e-3 * abs(fin[0, 0])
+
+
+def test_population_stop_event(golden):
+    d = golden("plan_two_level")
+    p = oracle.OraclePlan(d["payload"])
+    ev = {"kind": "population", "indices": [1], "threshold": 0.05}
+    o = _opts(p, t1=5.0, stop_event=ev, output="populations", output_when="final", saveat=np.array([5.0]), save_start=False)
+    t, v, st = p.solve_single(o, d["rho0_packed"])
+    assert st["event_triggered"]
+    assert t[-1] == st["event_time"] < 5.0
+    assert abs(v[-1, 1] - 0.05) < 1e-9
+
+
+def test_error_messages(golden):
+    d = golden("plan_two_level")
+    p = oracle.OraclePlan(d["payload"])
+    with pytest.raises(oracle.OracleError, match=r"^Stopped at x=0\.\d+\. Need more than 2 steps\.$"):
+        p.solve_single(_opts(p, maxiters=1), d["rho0_packed"])
+    with pytest.raises(oracle.OracleError, match="only forward integration"):
+        p.solve_single(_opts(p, t0=1.0, t1=0.5), d["rho0_packed"])
+    with pytest.raises(oracle.OracleError, match=r"saveat value 2 is outside \[0, 1\]"):
+        p.solve_single(_opts(p, saveat=np.array([0.5, 2.0]), output_when="saveat"), d["rho0_packed"])
+    with pytest.raises(oracle.OracleError, match="maxiters must be positive"):
+        p.solve_single(_opts(p, maxiters=0), d["rho0_packed"])
+    # batch: first failing trajectory index prefix (ode_batch.rs:309)
+    det = np.array([[0.0], [0.1]], dtype=complex)
+    with pytest.raises(oracle.OracleError, match=r"^trajectory 0: Stopped at x="):
+        p.solve_batch(_opts(p, maxiters=1), d["rho0_packed"], [p.slot_names.index("delta")], det)
