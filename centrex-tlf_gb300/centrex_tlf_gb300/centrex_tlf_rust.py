@@ -1,0 +1,388 @@
+"""Drop-in replacement of the reference's native Lindblad entry points.
+
+The reference's Python surface imports four functions from its PyO3 extension
+``centrex_tlf.centrex_tlf_rust`` (centrex_tlf/lindblad/plan_static.py:180, solve.py:419,
+batch.py:235, batch.py:440).  This module provides the same four names, signatures, defaults,
+return tuples and error messages (rust/src/lindblad/python_api.rs:271-799), backed by the
+GB300 CUDA solver.  ``install()`` registers it under that import path so the reference's own
+``solve_lindblad``/``solve_lindblad_batch``/``parameter_scan``/``initial_condition_scan``/
+``grid_scan`` drive the GPU unchanged.
+
+Only ``mode="expanded_sparse"`` with the adaptive ``dopri5``/``tsit5`` solvers runs here; the
+reference's other execution modes and fixed-step solvers raise ``NotImplementedError``.
+"""
+
+from __future__ import annotations
+
+import math
+import sys
+from typing import Any
+
+import numpy as np
+
+from ._options import INTEGRAL_OUTPUTS, RATE_OUTPUTS, SolveOptions
+from .native import NativePlan
+
+__all__ = [
+    "PreparedLindbladPlan",
+    "install",
+    "prepare_lindblad_problem_py",
+    "solve_lindblad_batch_ode_py",
+    "solve_lindblad_grid_ode_py",
+    "solve_lindblad_ode_py",
+]
+
+_KNOWN_MODES = {
+    "reference",
+    "structured",
+    "structured_upper",
+    "expanded_sparse",
+    "experimental_expanded_sparse_baseline_packed",
+    "experimental_expanded_sparse_current_split_inputs",
+    "experimental_expanded_sparse_split_coefficients",
+    "experimental_expanded_sparse_split_inputs",
+    "experimental_expanded_sparse_precomputed_inputs",
+}
+_SOLVERS = ("dopri5", "tsit5", "fixed_dopri5", "fixed_rk2", "fixed_rk4")
+
+
+def _rust_repr(s: str) -> str:
+    return '"' + str(s).replace("\\", "\\\\").replace('"', '\\"') + '"'
+
+
+def _check_mode(mode: str) -> None:
+    # ExecutionMode::from_str (rust/src/lindblad/rhs.rs:41-65)
+    if mode not in _KNOWN_MODES:
+        raise ValueError(f"unsupported execution mode {_rust_repr(mode)}")
+    if mode != "expanded_sparse":
+        raise NotImplementedError(
+            f"execution_mode={mode!r} is not part of the GB300 solver; it implements 'expanded_sparse'"
+        )
+
+
+def _check_solver(solver: str) -> None:
+    # OdeSolver::from_str (rust/src/ode/batch.rs:17-29)
+    if solver not in _SOLVERS:
+        raise ValueError(
+            "solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4', "
+            f"got {_rust_repr(solver)}"
+        )
+    if solver not in ("dopri5", "tsit5"):
+        raise NotImplementedError(f"solver={solver!r} is not part of the GB300 solver; use 'dopri5' or 'tsit5'")
+
+
+def _time_tol(t: float) -> float:
+    return 10.0 * np.finfo(np.float64).eps * max(abs(t), 1.0)
+
+
+def _fmt(v: float) -> str:
+    """Rust's Display for f64 (shortest round-trip, positional)."""
+    if math.isnan(v):
+        return "NaN"
+    if math.isinf(v):
+        return "inf" if v > 0 else "-inf"
+    r = repr(float(v))
+    if "e" not in r and "E" not in r:
+        return r[:-2] if r.endswith(".0") else r
+    mant, exp = r.lower().split("e")
+    exp = int(exp)
+    neg = mant.startswith("-")
+    mant = mant.lstrip("-")
+    digits = mant.replace(".", "")
+    point = (mant.index(".") if "." in mant else len(mant)) + exp
+    if point <= 0:
+        out = "0." + "0" * (-point) + digits
+    elif point >= len(digits):
+        out = digits + "0" * (point - len(digits))
+    else:
+        out = digits[:point] + "." + digits[point:]
+    out = out.rstrip("0").rstrip(".") if "." in out else out
+    return ("-" if neg else "") + out
+
+
+def _save_plan(saveat: np.ndarray | None, t0: float, t1: float, save_start: bool) -> list[float] | None:
+    """build_save_plan (rust/src/ode/common.rs:124-151)."""
+    if saveat is None:
+        return None
+    times: list[float] = []
+    if save_start:
+        times.append(t0)
+    for t in np.asarray(saveat, dtype=np.float64).reshape(-1):
+        t = float(t)
+        if save_start and abs(t - t0) <= _time_tol(t0):
+            continue
+        if not math.isfinite(t):
+            raise ValueError("saveat contains non-finite value")
+        if t < t0 - _time_tol(t0) or t > t1 + _time_tol(t1):
+            raise ValueError(f"saveat value {_fmt(t)} is outside [{_fmt(t0)}, {_fmt(t1)}]")
+        times.append(t)
+    return times
+
+
+class PreparedLindbladPlan:
+    """Opaque prepared plan (the reference's ``PreparedLindbladPlan`` pyclass)."""
+
+    def __init__(self, payload: dict) -> None:
+        self.native = NativePlan(payload)
+
+    def n_states(self) -> int:
+        return self.native.n_states
+
+    def __repr__(self) -> str:
+        return f"PreparedLindbladPlan(n_states={self.native.n_states}, backend='gb300')"
+
+
+def prepare_lindblad_problem_py(payload: dict) -> PreparedLindbladPlan:
+    """rust/src/lindblad/python_api.rs:271-274 -> plan.rs:1155-1308."""
+    return PreparedLindbladPlan(payload)
+
+
+def _native(plan: Any) -> NativePlan:
+    if isinstance(plan, PreparedLindbladPlan):
+        return plan.native
+    if isinstance(plan, NativePlan):
+        return plan
+    raise TypeError("plan must be a PreparedLindbladPlan from prepare_lindblad_problem_py")
+
+
+def _output_kind(output: str, output_indices, integral_weights) -> None:
+    if output == "selected" and output_indices is None:
+        raise ValueError("output='selected' requires output_indices")
+    if (output in INTEGRAL_OUTPUTS or output in RATE_OUTPUTS) and integral_weights is None:
+        raise ValueError(f"output='{output}' requires integral_weights")
+
+
+def _opts(native: NativePlan, *, t0, t1, abstol, reltol, dt, saveat, save_start, maxiters, solver, output,
+          output_indices, output_when, integral_weights, stop_event, precision) -> SolveOptions:
+    return native.options(
+        t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=saveat, save_start=save_start,
+        maxiters=maxiters, solver=solver, output=output, output_indices=output_indices,
+        output_when=output_when, integral_weights=integral_weights, stop_event=stop_event,
+        precision=precision,
+    )
+
+
+def solve_lindblad_ode_py(
+    plan,
+    packed_rho0,
+    t0,
+    t1,
+    abstol,
+    reltol,
+    dt,
+    saveat=None,
+    save_start=True,
+    maxiters=100000,
+    mode="expanded_sparse",
+    solver="dopri5",
+    output="full",
+    output_indices=None,
+    output_when="saveat",
+    integral_weights=None,
+    stop_event=None,
+    use_split_input_rhs=True,
+    precision="fp64",
+):
+    """One trajectory (rust/src/lindblad/python_api.rs:422-528).
+
+    Returns ``(times, values, width, stats)``; ``values`` is flat (complex for 'selected').
+    ``use_split_input_rhs`` selects a CPU kernel variant in the reference and is accepted for
+    compatibility.  ``precision="mixed"`` runs the FP32-RHS / FP64-accumulate form.
+    """
+    native = _native(plan)
+    _check_mode(mode)
+    _check_solver(solver)
+    _output_kind(output, output_indices, integral_weights)
+    kind = output if output in ("populations", "selected") or output in INTEGRAL_OUTPUTS or output in RATE_OUTPUTS else "full"
+    rho0 = np.ascontiguousarray(np.asarray(packed_rho0, dtype=np.float64).reshape(-1))
+    if rho0.size != native.packed_len:
+        raise ValueError(f"expected {native.packed_len}, got {rho0.size}")
+    opts = _opts(native, t0=float(t0), t1=float(t1), abstol=abstol, reltol=reltol, dt=dt,
+                 saveat=None if saveat is None else np.asarray(saveat, dtype=np.float64), save_start=save_start,
+                 maxiters=maxiters, solver=solver, output=kind, output_indices=output_indices,
+                 output_when=output_when, integral_weights=integral_weights, stop_event=stop_event,
+                 precision=precision)
+    times, values, width, st = native.solve_single(opts, rho0)
+    stats = {
+        "solver": solver,
+        "accepted_steps": st["accepted_steps"],
+        "rejected_steps": st["rejected_steps"],
+        "rhs_calls": st["rhs_calls"],
+        "event_triggered": st["event_triggered"],
+    }
+    if st["event_triggered"]:
+        stats["event_time"] = st["event_time"]
+        stats["event_index"] = 0
+    return np.asarray(times, dtype=np.float64), values, int(width), stats
+
+
+def _batch_common(native, t0, t1, saveat, save_start, output, output_when, integral_weights, output_indices, stop_event):
+    """Option mapping of python_api.rs:589-617 / 723-746 and the point count per trajectory."""
+    if output not in ("populations", "selected", "full") and output not in INTEGRAL_OUTPUTS and output not in RATE_OUTPUTS:
+        raise ValueError(f"unknown output mode: {_rust_repr(output)}")
+    _output_kind(output, output_indices, integral_weights)
+    final_integral = output_when == "final" and output in INTEGRAL_OUTPUTS
+    saveat_vec = None if saveat is None else np.asarray(saveat, dtype=np.float64).reshape(-1)
+    if output_when == "final" and not final_integral:
+        saveat_vec = np.array([t1], dtype=np.float64)
+    eff_save_start = bool((output_when != "final" or final_integral) and save_start)
+    plan_times = _save_plan(saveat_vec, t0, t1, eff_save_start)
+    if t1 == t0:
+        raise NotImplementedError("a zero-length time span is not supported by the GB300 batch solver")
+    if plan_times is not None:
+        if output in INTEGRAL_OUTPUTS and output_when != "saveat":
+            time_count, ref_times = 1, [plan_times[-1] if plan_times else t1]
+        else:
+            time_count, ref_times = len(plan_times), list(plan_times)
+    elif output in INTEGRAL_OUTPUTS and output_when != "saveat":
+        time_count, ref_times = 1, [t1]
+    else:
+        raise NotImplementedError(
+            "batch outputs at every accepted step (saveat=None with output_when='saveat') are not "
+            "supported by the GB300 solver; pass explicit saveat values"
+        )
+    return saveat_vec, eff_save_start, time_count, ref_times
+
+
+def _batch_result(values, stats_arr, width, time_count, ref_times, t1, solver, stop_event, is_complex):
+    triggered = [bool(x) for x in stats_arr["event_triggered"]]
+    last_t = ref_times[-1] if ref_times else t1
+    event_times = [float(stats_arr["event_time"][i]) if triggered[i] else float(last_t) for i in range(len(triggered))]
+    times = np.asarray(event_times if stop_event is not None else ref_times, dtype=np.float64)
+    flat = np.ascontiguousarray(values).reshape(-1)
+    stats = {
+        "solver": solver,
+        "accepted_steps": int(stats_arr["accepted_steps"].sum()),
+        "rejected_steps": int(stats_arr["rejected_steps"].sum()),
+        "rhs_calls": int(stats_arr["rhs_calls"].sum()),
+        "event_triggered": any(triggered),
+        "event_triggered_by_trajectory": triggered,
+        "event_times": event_times,
+        "event_count": sum(triggered),
+    }
+    return times, flat, int(width), int(time_count), stats
+
+
+def solve_lindblad_batch_ode_py(
+    plan,
+    packed_rho0_batch,
+    t0,
+    t1,
+    abstol,
+    reltol,
+    dt,
+    saveat=None,
+    save_start=True,
+    maxiters=100000,
+    mode="expanded_sparse",
+    solver="dopri5",
+    output="populations",
+    output_indices=None,
+    output_when="final",
+    integral_weights=None,
+    parameter_slot_indices=None,
+    parameter_batch=None,
+    parallel=True,
+    threads=None,
+    stop_event=None,
+    use_split_input_rhs=True,
+    precision="fp64",
+):
+    """B trajectories, one GPU launch (rust/src/lindblad/python_api.rs:530-669 ->
+    rust/src/lindblad/ode_batch.rs:176-351).  ``parallel``/``threads`` choose the reference's
+    CPU thread pool and are accepted for compatibility.
+
+    Returns ``(times, values, width, time_count, stats)``."""
+    native = _native(plan)
+    _check_mode(mode)
+    _check_solver(solver)
+    batch = np.asarray(packed_rho0_batch, dtype=np.float64)
+    if batch.ndim != 2:
+        raise ValueError("packed_rho0_batch must be 2D")
+    if batch.shape[1] != native.packed_len:
+        raise ValueError(f"rho0 dim mismatch: {batch.shape[1]} vs {native.packed_len}")
+    t0, t1 = float(t0), float(t1)
+    slots = list(parameter_slot_indices or [])
+    if parameter_batch is not None:
+        pv = np.asarray(parameter_batch, dtype=np.complex128)
+        if pv.ndim != 2 or pv.shape[0] != batch.shape[0] or pv.shape[1] != len(slots):
+            raise ValueError("parameter_batch shape mismatch")
+    else:
+        pv = None
+    if batch.shape[0] == 0:
+        return np.zeros(0), np.zeros(0), 0, 0, {
+            "solver": solver, "accepted_steps": 0, "rejected_steps": 0, "rhs_calls": 0, "event_triggered": False,
+            "event_triggered_by_trajectory": [], "event_times": [], "event_count": 0}
+    saveat_vec, eff_ss, time_count, ref_times = _batch_common(
+        native, t0, t1, saveat, save_start, output, output_when, integral_weights, output_indices, stop_event
+    )
+    opts = _opts(native, t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=saveat_vec, save_start=eff_ss,
+                 maxiters=maxiters, solver=solver, output=output, output_indices=output_indices,
+                 output_when=output_when, integral_weights=integral_weights, stop_event=stop_event,
+                 precision=precision)
+    use = pv is not None and len(slots) > 0
+    values, st = native.solve_batch(opts, batch, slots if use else None, pv if use else None, time_count)
+    return _batch_result(values, st, opts.width, time_count, ref_times, t1, solver, stop_event, opts.is_complex)
+
+
+def solve_lindblad_grid_ode_py(
+    plan,
+    packed_rho0,
+    t0,
+    t1,
+    abstol,
+    reltol,
+    dt,
+    parameter_slot_indices,
+    parameter_axes,
+    parameter_axis_lengths,
+    saveat=None,
+    save_start=True,
+    maxiters=100000,
+    mode="expanded_sparse",
+    solver="dopri5",
+    output="populations",
+    output_indices=None,
+    output_when="final",
+    integral_weights=None,
+    parallel=True,
+    threads=None,
+    stop_event=None,
+    use_split_input_rhs=True,
+    precision="fp64",
+):
+    """A row-major parameter grid from one rho0 (rust/src/lindblad/python_api.rs:671-799 ->
+    rust/src/lindblad/ode_batch.rs:571-1040); last axis fastest."""
+    native = _native(plan)
+    _check_mode(mode)
+    _check_solver(solver)
+    lengths = [int(x) for x in parameter_axis_lengths]
+    if not lengths:
+        raise ValueError("parameter grid must contain at least one axis")
+    if any(x == 0 for x in lengths):
+        raise ValueError("parameter grid axes must be non-empty")
+    rho0 = np.asarray(packed_rho0, dtype=np.float64).reshape(-1)
+    t0, t1 = float(t0), float(t1)
+    axes_flat = np.asarray(parameter_axes, dtype=np.complex128).reshape(-1)
+    axes = []
+    off = 0
+    for n in lengths:
+        axes.append(axes_flat[off: off + n])
+        off += n
+    saveat_vec, eff_ss, time_count, ref_times = _batch_common(
+        native, t0, t1, saveat, save_start, output, output_when, integral_weights, output_indices, stop_event
+    )
+    opts = _opts(native, t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=saveat_vec, save_start=eff_ss,
+                 maxiters=maxiters, solver=solver, output=output, output_indices=output_indices,
+                 output_when=output_when, integral_weights=integral_weights, stop_event=stop_event,
+                 precision=precision)
+    values, st = native.solve_grid(opts, rho0, list(parameter_slot_indices), axes, time_count)
+    return _batch_result(values, st, opts.width, time_count, ref_times, t1, solver, stop_event, opts.is_complex)
+
+
+def install() -> None:
+    """Register this module as ``centrex_tlf.centrex_tlf_rust`` so the reference's Python
+    surface calls the GB300 solver.  The builder helpers of the reference's extension are
+    absent on purpose: the reference falls back to its Python builders
+    (centrex_tlf/hamiltonian/generate_hamiltonian.py:18-30)."""
+    sys.modules["centrex_tlf.centrex_tlf_rust"] = sys.modules[__name__]

@@ -1,0 +1,144 @@
+// obe_internal.h -- layouts shared by the host packer (obe_plan.cpp) and the CUDA solver
+// (obe_solver.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/obe_gb300.h"
+
+namespace obe {
+
+// Expression VM opcodes (centrex_tlf/lindblad/ir.py:28-47; rust/src/lindblad/eval.rs:11-57).
+enum : int32_t {
+    OP_CONST = 1, OP_SLOT = 2, OP_TEMP = 3, OP_TIME = 4, OP_ADD = 5, OP_SUB = 6, OP_MUL = 7,
+    OP_DIV = 8, OP_POW = 9, OP_NEG = 10, OP_CONJ = 11, OP_BUILTIN = 12, OP_HELPER = 13,
+    OP_GT = 14, OP_GE = 15, OP_LT = 16, OP_LE = 17, OP_EQ = 18, OP_NE = 19,
+    // device-only opcode: helper 16 resolved on the host to a PCHIP table (index in `fn`)
+    OP_PCHIP_TABLE = 32
+};
+
+constexpr int kMaxStack = 48;      // device VM stack depth (host rejects deeper programs)
+constexpr int kMaxSlots = 96;      // per-lane slot storage of the device VM
+constexpr int kMaxDynCoeff = 16;   // time-dependent Hamiltonian coefficients per plan
+constexpr int kMaxHelperArgs = 12;
+
+// One expression in the device instruction pool.
+struct DevExpr {
+    int32_t start;
+    int32_t len;
+};
+
+// A record of the RHS gather stream.  Bits:
+//   [0, 14)  packed index of the input (its real part; the imaginary part is the next slot)
+//   14       complex input (off-diagonal) -- otherwise a real diagonal input
+//   15       input conjugated (negate the imaginary part)
+//   16       last record of the current output: flush the accumulator
+//   [17, 32) index of the coefficient formula in the per-trajectory table
+constexpr uint32_t kRecIndexMask = 0x3FFFu;
+constexpr uint32_t kRecComplex = 1u << 14;
+constexpr uint32_t kRecConj = 1u << 15;
+constexpr uint32_t kRecFlush = 1u << 16;
+constexpr int kRecCoefShift = 17;
+constexpr uint32_t kMaxFormulas = (1u << 15) - 1;
+constexpr uint32_t kNoImag = 0xFFFFu;
+
+// Device view of a packed plan.  All pointers point into one device allocation.
+struct DevPlan {
+    int32_t n, N, U;
+    // expression pool
+    const int32_t* ins_op;
+    const int32_t* ins_arg;      // slot index (SLOT) / argc (BUILTIN, HELPER)
+    const int32_t* ins_fn;       // function id / PCHIP table index
+    const double* ins_val;       // [2 * n_ins]
+    // parameter graph
+    int32_t n_slots, n_base;
+    const double* base_val;      // [2 * n_base]
+    const int32_t* base_tuple;   // [n_base] tuple id or -1
+    const int32_t* tuple_ptr;    // [n_tuples + 1]
+    const double* tuple_items;   // [2 * items]
+    int32_t n_comp;
+    const int32_t* comp_slot;
+    const DevExpr* comp_expr;
+    const uint8_t* comp_dynamic;
+    int32_t n_coeff;
+    const DevExpr* coeff_expr;
+    const uint8_t* coeff_dynamic;
+    int32_t n_dyn;               // time-dependent coefficients
+    const int32_t* dyn_ids;      // [n_dyn] coefficient index
+    const int32_t* coeff_dyn_pos;// [n_coeff] position in dyn_ids or -1
+    int32_t time_dependent;
+    // PCHIP tables (plan.rs:27-116)
+    int32_t n_pchip;
+    const int32_t* pchip_ptr;
+    const double* pchip_grid;
+    const double* pchip_coef;    // [4 * segments]
+    const int32_t* pchip_cptr;   // [n_pchip] offset of each table's coefficients
+    // coefficient formulas: table entry f = sum over its products of factor * c(class)
+    int32_t n_formula;           // entries 1..n_formula (entry 0 is the zero coefficient)
+    int32_t n_static_formula;    // entries 1..n_static_formula are time independent
+    const int32_t* formula_ptr;  // [n_formula + 1] into the product lists
+    const double* prod_factor;   // [2 * n_prod]
+    const int32_t* prod_class;   // [n_prod] -1 = constant 1, else coeff * 2 + conj
+    const float* prod_factor32;  // [2 * n_prod] single-precision copy (mixed form)
+    // gather stream, lane interleaved for `tpt` threads per trajectory
+    int32_t tpt;
+    int32_t n_iter;              // records per thread (padded)
+    const uint32_t* rec;         // [n_iter * tpt]
+    int32_t n_out;               // outputs per thread (padded)
+    const uint32_t* lane_out;    // [n_out * tpt]: re | im << 16 (im = kNoImag on the diagonal)
+};
+
+// Host-side result of packing (owned by obe_plan).
+struct HostPacked {
+    std::vector<int32_t> ins_op, ins_arg, ins_fn;
+    std::vector<double> ins_val;
+    std::vector<double> base_val;
+    std::vector<int32_t> base_tuple, tuple_ptr;
+    std::vector<double> tuple_items;
+    std::vector<int32_t> comp_slot;
+    std::vector<DevExpr> comp_expr;
+    std::vector<uint8_t> comp_dynamic;
+    std::vector<DevExpr> coeff_expr;
+    std::vector<uint8_t> coeff_dynamic;
+    std::vector<int32_t> dyn_ids, coeff_dyn_pos;
+    std::vector<int32_t> pchip_ptr;
+    std::vector<double> pchip_grid, pchip_coef;
+    std::vector<int32_t> pchip_cptr;
+    std::vector<int32_t> formula_ptr, prod_class;
+    std::vector<double> prod_factor;
+    std::vector<float> prod_factor32;
+    std::vector<uint32_t> rec, lane_out;
+    int32_t n_iter = 0, n_out = 0, tpt = 32;
+    int32_t n_formula = 0, n_static_formula = 0;
+    int32_t max_stack = 0;
+};
+
+}  // namespace obe
+
+// Opaque handle of the public ABI.
+struct obe_plan {
+    int32_t n = 0;
+    int64_t N = 0, U = 0;
+    int32_t n_slots = 0, n_base = 0, n_coeff = 0;
+    int32_t has_expanded = 0;
+    int32_t time_dependent = 0;
+    std::vector<int32_t> base_is_tuple;
+    obe::HostPacked packed;
+    // device copy (uploaded on first use, per device)
+    void* d_blob = nullptr;
+    int d_device = -1;
+    obe::DevPlan dev{};
+    // reusable device scratch of the host-pointer entry points
+    void* d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    void* d_counter = nullptr;
+};
+
+namespace obe {
+void set_error(const std::string& msg);
+std::string fmt_f64(double v);  // Rust Display of f64
+obe_status pack_plan(const obe_plan_desc* d, obe_plan* p);
+int threads_per_trajectory_for(int32_t n);
+}  // namespace obe

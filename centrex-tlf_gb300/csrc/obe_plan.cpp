@@ -1,0 +1,500 @@
+// obe_plan.cpp -- host side of prepare_lindblad_problem_py: payload validation and the
+// coefficient packer that lays the expanded_sparse term list out for the GPU.
+//
+// Reference behaviour: rust/src/lindblad/plan.rs:1069-1308 (validation, dynamic-coefficient
+// detection) and rust/src/lindblad/rhs.rs:151-384 (upper-to-packed map, term partitioning).
+// The GPU layout is this project's own: terms are merged per (output, input, conjugation) into
+// records whose coefficient is a *formula* (a sum of factor x coefficient products) kept in a
+// per-trajectory table; records are bin-packed onto the threads of a trajectory and stored
+// thread-interleaved so that each step of the gather loop is one conflict-free shared-memory
+// word per thread.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "obe_internal.h"
+
+namespace obe {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+std::string fmt_f64(double v) {
+    // Rust's Display for f64: shortest round-trip digits, positional notation.
+    if (std::isnan(v)) return "NaN";
+    if (std::isinf(v)) return v > 0 ? "inf" : "-inf";
+    if (v == 0.0) return std::signbit(v) ? "-0" : "0";
+    char buf[64];
+    int prec;
+    for (prec = 1; prec <= 17; ++prec) {
+        std::snprintf(buf, sizeof buf, "%.*e", prec - 1, v);
+        if (std::strtod(buf, nullptr) == v) break;
+    }
+    std::string digits;
+    bool neg = false;
+    const char* p = buf;
+    if (*p == '-') { neg = true; ++p; }
+    for (; *p && *p != 'e'; ++p)
+        if (*p != '.') digits.push_back(*p);
+    int exp10 = std::atoi(p + 1);
+    while (digits.size() > 1 && digits.back() == '0') digits.pop_back();
+    std::string out = neg ? "-" : "";
+    int nd = static_cast<int>(digits.size());
+    if (exp10 >= 0) {
+        for (int i = 0; i <= exp10 || i < nd; ++i) {
+            if (i == exp10 + 1) out.push_back('.');
+            out.push_back(i < nd ? digits[i] : '0');
+            if (i >= exp10 && i >= nd - 1) break;
+        }
+    } else {
+        out += "0.";
+        for (int i = 0; i < -exp10 - 1; ++i) out.push_back('0');
+        out += digits;
+    }
+    return out;
+}
+
+int threads_per_trajectory_for(int32_t n) {
+    int64_t N = static_cast<int64_t>(n) * n;
+    if (N <= 512) return 32;
+    if (N <= 1024) return 64;
+    if (N <= 2048) return 128;
+    if (N <= 4096) return 256;
+    return 512;
+}
+
+namespace {
+
+struct Fail {
+    obe_status code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(obe_status code, const std::string& msg) { throw Fail{code, msg}; }
+
+std::string strf(const char* fmt, long long a = 0, long long b = 0) {
+    char buf[512];
+    std::snprintf(buf, sizeof buf, fmt, a, b);
+    return buf;
+}
+
+// Kind-check one expression by simulating its stack (scalar vs tuple values), the way the
+// reference's compiler tracks them (ir.py:210-326), and append it to the device pool.
+// Tuples may only come from tuple base slots and may only feed helpers 8, 10, 14 and 16.
+DevExpr append_expr(HostPacked& hp, const obe_expr& e, int32_t n_slots, const std::vector<int32_t>& slot_is_tuple,
+                    const std::vector<std::vector<double>>& tuple_grid, const std::vector<int32_t>& pchip_of_grid_slot,
+                    bool allow_pchip_tables, const char* what) {
+    DevExpr out{static_cast<int32_t>(hp.ins_op.size()), static_cast<int32_t>(e.n_instr)};
+    std::vector<int> kinds;  // 0 scalar, 1 tuple
+    std::vector<int32_t> src_slot;  // slot a stack value was loaded from (-1 otherwise)
+    for (int64_t k = 0; k < e.n_instr; ++k) {
+        int32_t op = e.op[k];
+        int64_t idx = e.index ? e.index[k] : 0;
+        int32_t argc = e.argc ? e.argc[k] : 0;
+        int32_t fn = e.function ? e.function[k] : 0;
+        double re = e.value ? e.value[2 * k] : 0.0, im = e.value ? e.value[2 * k + 1] : 0.0;
+        int32_t dev_op = op, dev_arg = 0, dev_fn = fn;
+        if (op < 1 || op > 19) fail(OBE_ERR_INVALID, strf("unknown instruction op %lld", op));
+        switch (op) {
+        case OP_CONST: kinds.push_back(0); src_slot.push_back(-1); break;
+        case OP_SLOT:
+            if (idx < 0 || idx >= n_slots)
+                fail(OBE_ERR_INVALID, strf("slot index %lld out of bounds for %lld slots", idx, n_slots));
+            kinds.push_back(slot_is_tuple[idx]);
+            src_slot.push_back(static_cast<int32_t>(idx));
+            dev_arg = static_cast<int32_t>(idx);
+            break;
+        case OP_TEMP: fail(OBE_ERR_UNSUPPORTED, "temporary values belong to entrywise Hamiltonian plans, which the GPU solver does not run");
+        case OP_TIME: kinds.push_back(0); src_slot.push_back(-1); break;
+        case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW:
+        case OP_GT: case OP_GE: case OP_LT: case OP_LE: case OP_EQ: case OP_NE: {
+            if (kinds.size() < 2) fail(OBE_ERR_INVALID, std::string("stack underflow in ") + what);
+            if (kinds.back() || kinds[kinds.size() - 2])
+                fail(OBE_ERR_UNSUPPORTED, std::string("elementwise tuple arithmetic is not supported by the GPU solver (") + what + ")");
+            kinds.pop_back(); src_slot.pop_back();
+            src_slot.back() = -1;
+            break;
+        }
+        case OP_NEG: case OP_CONJ:
+            if (kinds.empty()) fail(OBE_ERR_INVALID, std::string("stack underflow in ") + what);
+            if (kinds.back()) fail(OBE_ERR_UNSUPPORTED, std::string("tuple negation/conjugation is not supported by the GPU solver (") + what + ")");
+            src_slot.back() = -1;
+            break;
+        case OP_BUILTIN: {
+            if (argc < 1 || static_cast<size_t>(argc) > kinds.size()) fail(OBE_ERR_INVALID, std::string("stack underflow in ") + what);
+            if (fn < 1 || fn > 7) fail(OBE_ERR_INVALID, strf("unknown builtin function id %lld", fn));
+            if (kinds[kinds.size() - argc]) fail(OBE_ERR_UNSUPPORTED, "builtin applied to a tuple");
+            kinds.resize(kinds.size() - argc); src_slot.resize(src_slot.size() - argc);
+            kinds.push_back(0); src_slot.push_back(-1);
+            dev_arg = argc;
+            break;
+        }
+        case OP_HELPER: {
+            if (argc < 0 || static_cast<size_t>(argc) > kinds.size()) fail(OBE_ERR_INVALID, std::string("stack underflow in ") + what);
+            if (argc > kMaxHelperArgs) fail(OBE_ERR_UNSUPPORTED, "helper with too many arguments");
+            if (fn < 1 || fn > 16) fail(OBE_ERR_INVALID, strf("unknown helper function id %lld", fn));
+            size_t base = kinds.size() - argc;
+            std::vector<int> want(argc, 0);
+            if (fn == 8 || fn == 10) { if (argc < 7) fail(OBE_ERR_INVALID, "multipass helper needs 7 arguments"); want[2] = want[3] = want[4] = 1; }
+            if (fn == 14 || fn == 16) { if (argc < 3) fail(OBE_ERR_INVALID, "interpolation helper needs 3 arguments"); want[1] = want[2] = 1; }
+            for (int32_t a = 0; a < argc; ++a)
+                if (kinds[base + a] != want[a])
+                    fail(OBE_ERR_UNSUPPORTED, std::string("helper argument kinds not supported by the GPU solver (") + what + ")");
+            dev_arg = argc;
+            if (fn == 16 && allow_pchip_tables) {
+                int32_t gs = src_slot[base + 1];
+                if (gs >= 0 && pchip_of_grid_slot[gs] >= 0) {
+                    dev_op = OP_PCHIP_TABLE;
+                    dev_fn = pchip_of_grid_slot[gs];
+                }
+            }
+            kinds.resize(base); src_slot.resize(base);
+            kinds.push_back(0); src_slot.push_back(-1);
+            break;
+        }
+        }
+        if (static_cast<int>(kinds.size()) > hp.max_stack) hp.max_stack = static_cast<int>(kinds.size());
+        hp.ins_op.push_back(dev_op);
+        hp.ins_arg.push_back(dev_arg);
+        hp.ins_fn.push_back(dev_fn);
+        hp.ins_val.push_back(re);
+        hp.ins_val.push_back(im);
+    }
+    (void)tuple_grid;
+    if (kinds.size() != 1) fail(OBE_ERR_INVALID, "expression evaluation did not end with a single stack value");
+    if (kinds[0]) fail(OBE_ERR_UNSUPPORTED, std::string("tuple-valued expressions are not supported by the GPU solver (") + what + ")");
+    if (hp.max_stack > kMaxStack) fail(OBE_ERR_UNSUPPORTED, "expression too deep for the GPU solver");
+    return out;
+}
+
+bool uses_time(const obe_expr& e) {
+    for (int64_t k = 0; k < e.n_instr; ++k)
+        if (e.op[k] == OP_TIME) return true;
+    return false;
+}
+
+bool uses_dynamic_slot(const obe_expr& e, const std::vector<uint8_t>& dyn_slot) {
+    for (int64_t k = 0; k < e.n_instr; ++k)
+        if (e.op[k] == OP_SLOT) {
+            int64_t s = e.index ? e.index[k] : 0;
+            if (s >= 0 && s < static_cast<int64_t>(dyn_slot.size()) && dyn_slot[s]) return true;
+        }
+    return false;
+}
+
+// PchipTable::from_grid_values (plan.rs:34-80)
+void build_pchip(const double* grid, const double* values, int64_t n, std::vector<double>& coef) {
+    if (n < 2) return;
+    std::vector<double> h(n - 1), delta(n - 1), d(n);
+    for (int64_t i = 0; i < n - 1; ++i) {
+        h[i] = grid[i + 1] - grid[i];
+        if (h[i] <= 0.0) fail(OBE_ERR_INVALID, "pchip grid must be strictly increasing");
+        delta[i] = (values[i + 1] - values[i]) / h[i];
+    }
+    d[0] = delta[0];
+    d[n - 1] = delta[n - 2];
+    for (int64_t i = 1; i < n - 1; ++i) {
+        bool s0 = std::signbit(delta[i - 1]), s1 = std::signbit(delta[i]);
+        if (s0 != s1 || delta[i - 1] == 0.0 || delta[i] == 0.0) {
+            d[i] = 0.0;
+        } else {
+            double w1 = 2.0 * h[i] + h[i - 1], w2 = h[i] + 2.0 * h[i - 1];
+            d[i] = (w1 + w2) / (w1 / delta[i - 1] + w2 / delta[i]);
+        }
+    }
+    for (int64_t i = 0; i < n - 1; ++i) {
+        coef.push_back(values[i]);
+        coef.push_back(d[i]);
+        coef.push_back((3.0 * delta[i] - 2.0 * d[i] - d[i + 1]) / h[i]);
+        coef.push_back((d[i] + d[i + 1] - 2.0 * delta[i]) / (h[i] * h[i]));
+    }
+}
+
+int64_t upper_index(int32_t n, int32_t i, int32_t j) {
+    int64_t off = 0;
+    for (int32_t r = 0; r < i; ++r) off += n - r;
+    return off + (j - i);
+}
+
+}  // namespace
+
+obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
+    try {
+        if (!d) fail(OBE_ERR_INVALID, "null plan descriptor");
+        if (d->n_states <= 0) fail(OBE_ERR_INVALID, "layout dimension must be positive");
+        const int32_t n = d->n_states;
+        p->n = n;
+        p->N = static_cast<int64_t>(n) * n;
+        p->U = static_cast<int64_t>(n) * (n + 1) / 2;
+        p->n_slots = d->n_slots;
+        p->n_base = d->n_base;
+        p->n_coeff = d->n_coefficients;
+        p->has_expanded = d->has_expanded;
+        if (d->n_base < 0 || d->n_slots < d->n_base) fail(OBE_ERR_INVALID, "more base values than slots");
+        HostPacked& hp = p->packed;
+
+        // ---- parameter graph --------------------------------------------------------------
+        std::vector<int32_t> slot_is_tuple(d->n_slots, 0);
+        std::vector<std::vector<double>> tuple_grid(d->n_slots);
+        hp.tuple_ptr.push_back(0);
+        p->base_is_tuple.assign(d->n_base, 0);
+        for (int32_t i = 0; i < d->n_base; ++i) {
+            bool is_tuple = d->base_is_tuple && d->base_is_tuple[i];
+            p->base_is_tuple[i] = is_tuple;
+            slot_is_tuple[i] = is_tuple;
+            hp.base_val.push_back(is_tuple ? 0.0 : d->base_scalar[2 * i]);
+            hp.base_val.push_back(is_tuple ? 0.0 : d->base_scalar[2 * i + 1]);
+            if (is_tuple) {
+                hp.base_tuple.push_back(static_cast<int32_t>(hp.tuple_ptr.size()) - 1);
+                for (int64_t k = d->base_tuple_ptr[i]; k < d->base_tuple_ptr[i + 1]; ++k) {
+                    hp.tuple_items.push_back(d->base_tuple_items[2 * k]);
+                    hp.tuple_items.push_back(d->base_tuple_items[2 * k + 1]);
+                    tuple_grid[i].push_back(d->base_tuple_items[2 * k]);
+                }
+                hp.tuple_ptr.push_back(static_cast<int32_t>(hp.tuple_items.size() / 2));
+            } else {
+                hp.base_tuple.push_back(-1);
+            }
+        }
+        // PCHIP tables and the tuple slot whose values match each table's grid exactly enough
+        // for the reference's runtime match (|a - b| < 1e-15, eval.rs:590-606)
+        hp.pchip_ptr.push_back(0);
+        for (int32_t t = 0; t < d->n_pchip; ++t) {
+            int64_t a = d->pchip_ptr[t], b = d->pchip_ptr[t + 1];
+            hp.pchip_grid.insert(hp.pchip_grid.end(), d->pchip_grid + a, d->pchip_grid + b);
+            hp.pchip_cptr.push_back(static_cast<int32_t>(hp.pchip_coef.size()));
+            if (b - a >= 2) build_pchip(d->pchip_grid + a, d->pchip_values + a, b - a, hp.pchip_coef);
+            hp.pchip_ptr.push_back(static_cast<int32_t>(hp.pchip_grid.size()));
+        }
+        std::vector<int32_t> pchip_of_grid_slot(d->n_slots, -1);
+        for (int32_t s = 0; s < d->n_base; ++s) {
+            if (!slot_is_tuple[s]) continue;
+            for (int32_t t = 0; t < d->n_pchip; ++t) {
+                int64_t a = d->pchip_ptr[t], b = d->pchip_ptr[t + 1];
+                if (b - a != static_cast<int64_t>(tuple_grid[s].size())) continue;
+                bool match = true;
+                for (int64_t k = 0; k < b - a; ++k)
+                    if (!(std::fabs(d->pchip_grid[a + k] - tuple_grid[s][k]) < 1e-15)) { match = false; break; }
+                if (match) {
+                    if (b - a < 2) break;  // a one-point table evaluates to zero; keep the direct form
+                    pchip_of_grid_slot[s] = t;
+                    break;
+                }
+            }
+        }
+        std::vector<uint8_t> dyn_slot(d->n_slots, 0);
+        bool params_use_time = false;
+        for (int32_t i = 0; i < d->n_compounds; ++i) {
+            int32_t slot = d->compound_slot[i];
+            if (slot < 0 || slot >= d->n_slots) fail(OBE_ERR_INVALID, strf("compound slot %lld out of bounds", slot));
+            const obe_expr& e = d->compound_expr[i];
+            hp.comp_slot.push_back(slot);
+            hp.comp_expr.push_back(append_expr(hp, e, d->n_slots, slot_is_tuple, tuple_grid, pchip_of_grid_slot, true, "compound parameter"));
+            bool dyn = uses_time(e) || uses_dynamic_slot(e, dyn_slot);
+            dyn_slot[slot] = dyn;
+            hp.comp_dynamic.push_back(dyn);
+            params_use_time = params_use_time || uses_time(e);
+        }
+        if (d->n_slots > kMaxSlots) fail(OBE_ERR_UNSUPPORTED, "too many parameter slots for the GPU solver");
+
+        // ---- decomposed coefficients (plan.rs:242-276, 1240-1291) ---------------------------
+        bool ham_uses_time = false;
+        for (int32_t k = 0; k < d->n_coefficients; ++k) {
+            const obe_expr& e = d->coefficient_expr[k];
+            hp.coeff_expr.push_back(append_expr(hp, e, d->n_slots, slot_is_tuple, tuple_grid, pchip_of_grid_slot, false, "Hamiltonian coefficient"));
+            bool dyn = uses_time(e) || uses_dynamic_slot(e, dyn_slot);
+            hp.coeff_dynamic.push_back(dyn);
+            hp.coeff_dyn_pos.push_back(dyn ? static_cast<int32_t>(hp.dyn_ids.size()) : -1);
+            if (dyn) hp.dyn_ids.push_back(k);
+            ham_uses_time = ham_uses_time || uses_time(e);
+        }
+        p->time_dependent = params_use_time || ham_uses_time;
+        if (static_cast<int>(hp.dyn_ids.size()) > kMaxDynCoeff)
+            fail(OBE_ERR_UNSUPPORTED, "too many time-dependent Hamiltonian coefficients for the GPU solver");
+
+        if (!d->has_expanded) return OBE_OK;  // solves report the missing plan
+
+        // ---- expanded RHS validation (plan.rs:1069-1153) -----------------------------------
+        const int64_t U = p->U;
+        const int64_t T = d->n_terms;
+        if (d->output_ptrs[0] != 0 || d->output_ptrs[U] != T)
+            fail(OBE_ERR_INVALID, "expanded RHS output_ptrs must start at 0 and end at term count");
+        for (int64_t u = 0; u < U; ++u)
+            if (d->output_ptrs[u] > d->output_ptrs[u + 1]) fail(OBE_ERR_INVALID, "expanded RHS output_ptrs must be monotonic");
+        for (int64_t t = 0; t < T; ++t) {
+            if (d->input_indices[t] < 0 || d->input_indices[t] >= U)
+                fail(OBE_ERR_INVALID, strf("expanded RHS input index %lld out of bounds for upper length %lld", d->input_indices[t], U));
+            if (d->coeff_indices[t] >= d->n_coefficients)
+                fail(OBE_ERR_INVALID, strf("expanded RHS coefficient index %lld out of bounds for %lld coefficients", d->coeff_indices[t], d->n_coefficients));
+        }
+        if (p->N > static_cast<int64_t>(kRecIndexMask))
+            fail(OBE_ERR_UNSUPPORTED, "state too large for the GPU solver's record format (n_states <= 127)");
+
+        // ---- upper -> packed map (rhs.rs:151-176) -------------------------------------------
+        std::vector<int64_t> u_re(U), u_im(U);
+        for (int32_t i = 0; i < n; ++i) { u_re[upper_index(n, i, i)] = i; u_im[upper_index(n, i, i)] = -1; }
+        int64_t cursor = n;
+        for (int32_t i = 0; i < n; ++i)
+            for (int32_t j = i + 1; j < n; ++j) {
+                int64_t u = upper_index(n, i, j);
+                u_re[u] = cursor; u_im[u] = cursor + 1;
+                cursor += 2;
+            }
+
+        // ---- records and formulas -----------------------------------------------------------
+        // A formula is the exact list of (factor, class) products of the terms merged into one
+        // record; identical lists share one table entry.
+        using Product = std::tuple<int32_t, double, double>;  // class, factor re, factor im
+        using Formula = std::vector<Product>;
+        std::map<Formula, int32_t> static_ids, dyn_ids;
+        std::vector<Formula> static_list, dyn_list;
+        struct Rec { int64_t in_re; bool cplx, conj; Formula f; bool dynamic; };
+        std::vector<std::vector<Rec>> out_recs(U);
+        for (int64_t u = 0; u < U; ++u) {
+            // group the output's terms by (input, input conjugation), in input order
+            std::map<std::pair<int64_t, int>, std::vector<int64_t>> groups;
+            for (int64_t t = d->output_ptrs[u]; t < d->output_ptrs[u + 1]; ++t) {
+                int64_t in = d->input_indices[t];
+                bool diag = u_im[in] < 0;
+                int conj = diag ? 0 : (d->input_conj[t] ? 1 : 0);
+                groups[{u_re[in], conj}].push_back(t);
+            }
+            for (auto& kv : groups) {
+                Rec r;
+                r.in_re = kv.first.first;
+                r.conj = kv.first.second != 0;
+                int64_t in_upper = d->input_indices[kv.second[0]];
+                r.cplx = u_im[in_upper] >= 0;
+                r.dynamic = false;
+                for (int64_t t : kv.second) {
+                    int64_t k = d->coeff_indices[t];
+                    int32_t cls = k < 0 ? -1 : static_cast<int32_t>(2 * k + (d->coeff_conj[t] ? 1 : 0));
+                    r.f.emplace_back(cls, d->factors_re[t], d->factors_im[t]);
+                    if (k >= 0 && hp.coeff_dynamic[k]) r.dynamic = true;
+                }
+                auto& ids = r.dynamic ? dyn_ids : static_ids;
+                auto& lst = r.dynamic ? dyn_list : static_list;
+                if (!ids.count(r.f)) { ids[r.f] = static_cast<int32_t>(lst.size()); lst.push_back(r.f); }
+                out_recs[u].push_back(std::move(r));
+            }
+        }
+        const int32_t S = static_cast<int32_t>(static_list.size());
+        const int32_t D = static_cast<int32_t>(dyn_list.size());
+        if (static_cast<uint32_t>(S + D) > kMaxFormulas) fail(OBE_ERR_UNSUPPORTED, "too many coefficient formulas for the GPU solver");
+        hp.n_static_formula = S;
+        hp.n_formula = S + D;
+        hp.formula_ptr.push_back(0);
+        for (int pass = 0; pass < 2; ++pass)
+            for (const Formula& f : pass == 0 ? static_list : dyn_list) {
+                for (const Product& pr : f) {
+                    hp.prod_class.push_back(std::get<0>(pr));
+                    hp.prod_factor.push_back(std::get<1>(pr));
+                    hp.prod_factor.push_back(std::get<2>(pr));
+                    hp.prod_factor32.push_back(static_cast<float>(std::get<1>(pr)));
+                    hp.prod_factor32.push_back(static_cast<float>(std::get<2>(pr)));
+                }
+                hp.formula_ptr.push_back(static_cast<int32_t>(hp.prod_class.size()));
+            }
+
+        // ---- bin-pack outputs onto the threads of one trajectory (longest first) -----------
+        const int tpt = threads_per_trajectory_for(n);
+        hp.tpt = tpt;
+        std::vector<int64_t> order(U);
+        std::iota(order.begin(), order.end(), 0);
+        auto cost = [&](int64_t u) { return std::max<int64_t>(1, static_cast<int64_t>(out_recs[u].size())); };
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cost(a) > cost(b); });
+        std::vector<int64_t> load(tpt, 0);
+        std::vector<std::vector<int64_t>> lane_outputs(tpt);
+        for (int64_t u : order) {
+            int lane = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+            lane_outputs[lane].push_back(u);
+            load[lane] += cost(u);
+        }
+        int64_t n_iter = *std::max_element(load.begin(), load.end());
+        size_t n_out = 0;
+        for (auto& v : lane_outputs) {
+            std::sort(v.begin(), v.end());
+            n_out = std::max(n_out, v.size());
+        }
+        hp.n_iter = static_cast<int32_t>(n_iter);
+        hp.n_out = static_cast<int32_t>(n_out);
+        hp.rec.assign(static_cast<size_t>(n_iter) * tpt, 0u);  // padding: input 0, formula 0 (zero)
+        hp.lane_out.assign(n_out * tpt, 0u);
+        for (int lane = 0; lane < tpt; ++lane) {
+            int64_t it = 0;
+            for (size_t o = 0; o < lane_outputs[lane].size(); ++o) {
+                int64_t u = lane_outputs[lane][o];
+                uint32_t im = u_im[u] < 0 ? kNoImag : static_cast<uint32_t>(u_im[u]);
+                hp.lane_out[o * tpt + lane] = static_cast<uint32_t>(u_re[u]) | (im << 16);
+                const auto& recs = out_recs[u];
+                if (recs.empty()) {
+                    hp.rec[it * tpt + lane] = kRecFlush;  // an output with no terms stays 0
+                    ++it;
+                    continue;
+                }
+                for (size_t r = 0; r < recs.size(); ++r) {
+                    const Rec& rc = recs[r];
+                    uint32_t fid = rc.dynamic ? static_cast<uint32_t>(1 + S + dyn_ids[rc.f]) : static_cast<uint32_t>(1 + static_ids[rc.f]);
+                    uint32_t w = static_cast<uint32_t>(rc.in_re) | (fid << kRecCoefShift);
+                    if (rc.cplx) w |= kRecComplex;
+                    if (rc.conj) w |= kRecConj;
+                    if (r + 1 == recs.size()) w |= kRecFlush;
+                    hp.rec[it * tpt + lane] = w;
+                    ++it;
+                }
+            }
+        }
+        return OBE_OK;
+    } catch (const Fail& f) {
+        set_error(f.msg);
+        return f.code;
+    } catch (const std::exception& ex) {
+        set_error(std::string("plan packing failed: ") + ex.what());
+        return OBE_ERR_INVALID;
+    }
+}
+
+}  // namespace obe
+
+extern "C" {
+
+const char* obe_last_error(void);
+
+obe_status obe_plan_create(const obe_plan_desc* desc, obe_plan** out_plan) {
+    if (!out_plan) {
+        obe::set_error("null output pointer");
+        return OBE_ERR_INVALID;
+    }
+    *out_plan = nullptr;
+    obe_plan* p = new obe_plan();
+    obe_status st = obe::pack_plan(desc, p);
+    if (st != OBE_OK) {
+        delete p;
+        return st;
+    }
+    *out_plan = p;
+    obe::set_error("");
+    return OBE_OK;
+}
+
+int64_t obe_plan_packed_len(const obe_plan* plan) { return plan ? plan->N : 0; }
+int32_t obe_plan_n_states(const obe_plan* plan) { return plan ? plan->n : 0; }
+
+int32_t obe_abi_version(void) { return OBE_ABI_VERSION; }
+
+}  // extern "C"
+
+namespace obe {
+const char* last_error_cstr() { return g_last_error.c_str(); }
+}
+
+extern "C" const char* obe_last_error(void) { return obe::last_error_cstr(); }

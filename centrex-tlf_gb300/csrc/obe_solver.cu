@@ -1,0 +1,1601 @@
+// obe_solver.cu -- the GB300 Lindblad expanded_sparse solver: a persistent kernel that owns
+// whole trajectories (one trajectory per warp, or per group of warps for larger systems) and
+// runs the Dopri5/Tsit5 loop, the packed-Hermitian RHS, the step controller, terminal events,
+// saveat dense output and the observables on the device.
+//
+// Reference behaviour (CPU, Rust): rust/src/ode/dopri5.rs:160-379, rust/src/ode/tsit5.rs:159-363,
+// rust/src/ode/common.rs (controller, hinit, save plan), rust/src/ode/output.rs (observables),
+// rust/src/lindblad/rhs.rs:815-876 and 1789-1867 (the expanded_sparse RHS),
+// rust/src/lindblad/ode_batch.rs (batch/grid drivers), rust/src/lindblad/python_api.rs.
+//
+// Layout of one trajectory group in shared memory:
+//   coefficient-formula table (1 + n_formula complex; entry 0 = 0), the gather buffer (the stage
+//   input, n^2 reals), seven stage derivatives K1..K7 (7 n^2 reals), a double push buffer,
+//   coefficient values and reduction scratch.  The plan's gather stream is staged once per CTA.
+// The state y and the candidate yn stay in registers (EPT elements per thread, element
+// i = lane + e * TPT), so stage combinations, the error norm and dense output never leave the
+// SM.  In the mixed form the gather buffer, the formula table and K are single precision; the
+// state, stage combination, error norm, controller and observables stay double.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "obe_internal.h"
+#include "obe_vm.cuh"
+
+namespace obe {
+
+// ------------------------------------------------------------------------------------------
+// tableaus (rust/src/ode/dopri5.rs:5-43, rust/src/ode/tsit5.rs:5-60)
+
+// kA[m][s][j]: stage s+2 input = y + h * sum_j kA[m][s][j] K_{j+1}; row 5 is the solution.
+__constant__ double kA[2][6][6] = {
+    {{1.0 / 5.0, 0, 0, 0, 0, 0},
+     {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+     {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0},
+     {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0},
+     {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0},
+     {35.0 / 384.0, 0.0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}},
+    {{0.161, 0, 0, 0, 0, 0},
+     {-0.008480655492356989, 0.335480655492357, 0, 0, 0, 0},
+     {2.8971530571054935, -6.359448489975075, 4.3622954328695815, 0, 0, 0},
+     {5.325864828439257, -11.748883564062828, 7.4955393428898365, -0.09249506636175525, 0, 0},
+     {5.86145544294642, -12.92096931784711, 8.159367898576159, -0.071584973281401, -0.028269050394068383, 0},
+     {0.09646076681806523, 0.01, 0.4798896504144996, 1.379008574103742, -3.290069515436081, 2.324710524099774}}};
+// stage times c2..c5 (c6 = c7 = 1)
+__constant__ double kC[2][4] = {{1.0 / 5.0, 3.0 / 10.0, 4.0 / 5.0, 8.0 / 9.0},
+                                {0.161, 0.327, 0.9, 0.9800255409045097}};
+// error weights e1..e7 (Dopri5 has no e2)
+__constant__ double kE[2][7] = {
+    {71.0 / 57600.0, 0.0, -71.0 / 16695.0, 71.0 / 1920.0, -17253.0 / 339200.0, 22.0 / 525.0, -1.0 / 40.0},
+    {-0.0017800110522257771, -0.0008164344596567469, 0.007880878010261995, -0.1447110071732629,
+     0.5823571654525552, -0.458082105929187, 1.0 / 66.0}};
+// Dopri5 dense output d1, d3..d7 (dopri5.rs:38-43)
+__constant__ double kDd[7] = {-12715105075.0 / 11282082432.0, 0.0, 87487479700.0 / 32700410799.0,
+                              -10690763975.0 / 1880347072.0, 701980252875.0 / 199316789632.0,
+                              -1453857185.0 / 822651844.0, 69997945.0 / 29380423.0};
+// Tsit5 dense output r[i][1..4] (tsit5.rs:41-60)
+__constant__ double kR[7][4] = {{1.0, -2.763706197274826, 2.9132554618219126, -1.0530884977290216},
+                                {0.0, 0.1317, -0.2234, 0.1017},
+                                {0.0, 3.9302962368947516, -5.941033872131505, 2.490627285651253},
+                                {0.0, -12.411077166933676, 30.33818863028232, -16.548102889244902},
+                                {0.0, 37.50931341651104, -88.1789048947664, 47.37952196281928},
+                                {0.0, -27.896526289197286, 65.09189467479366, -34.87065786149661},
+                                {0.0, 1.5, -4.0, 2.5}};
+
+constexpr int kMaxWeights = 64;
+constexpr int kMaxSelected = 64;
+constexpr int kMaxEventIdx = 32;
+constexpr int kMaxParams = 16;
+
+enum TrajCode : int32_t {
+    ST_OK = 0,
+    ST_MAXITERS = 1,
+    ST_UNDERFLOW = 2,
+    ST_STIFF = 3,
+    ST_SAVEAT = 4,
+    ST_EVENT_COMPLEX = 5,
+    ST_EVENT_INDEX = 6,
+    ST_POINTS = 7,
+    ST_BAD_MAXITERS = 8,
+    ST_BACKWARD = 9
+};
+
+struct TrajErr {
+    double x;
+    long long a, b;
+};
+
+// Per-call arguments (passed by value).  Pointers are device memory.
+struct CallArgs {
+    long long n_traj;
+    double t0, t1, atol, rtol, dt;
+    long long maxiters;
+    int save_start, has_saveat, n_save;
+    const double* save_times;
+    int output, store_trace;
+    int n_weights;
+    const int* w_idx;
+    const double* w_val;
+    int n_sel;
+    const int* sel_re;
+    const int* sel_im;
+    const int* sel_kind;
+    int ev_kind, n_ev;
+    const int* ev_idx;
+    double ev_thr;
+    int ev_len;  // event program in the call blob
+    const int32_t* ev_op;
+    const int32_t* ev_arg;
+    const int32_t* ev_fn;
+    const double* ev_val;
+    const double* rho0;
+    long long rho0_stride;
+    int n_param;
+    int param_slot[kMaxParams];
+    const double* param_values;  // [traj][n_param] complex, or NULL (grid mode)
+    int n_axes;
+    long long axis_len[kMaxParams], axis_off[kMaxParams], axis_stride[kMaxParams];
+    const double* axes;          // complex
+    long long cap;               // output points per trajectory
+    long long out_stride;        // doubles per trajectory in values
+    double* values;
+    double* times;               // [traj][cap] or NULL
+    obe_traj_stats* stats;
+    TrajErr* errs;
+    unsigned long long* counter;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+struct GroupLayout {
+    size_t tab, yg, K, ybuf, cstat, cdyn, red, traj, bytes;
+};
+
+__host__ __device__ inline GroupLayout group_layout(int N, int n_formula, int n_coeff, int n_dyn, int tpt, bool mixed) {
+    size_t rs = mixed ? 4 : 8;
+    GroupLayout L;
+    size_t o = 0;
+    L.tab = o; o = align16(o + (1 + n_formula) * 2 * rs);
+    L.yg = o; o = align16(o + static_cast<size_t>(N) * rs);
+    L.K = o; o = align16(o + 7 * static_cast<size_t>(N) * rs);
+    L.ybuf = o; o = align16(o + static_cast<size_t>(N) * 8);
+    L.cstat = o; o = align16(o + static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
+    L.cdyn = o; o = align16(o + 6 * static_cast<size_t>(n_dyn > 0 ? n_dyn : 1) * 16);
+    L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
+    L.traj = o; o = align16(o + 16);
+    L.bytes = o;
+    return L;
+}
+
+__host__ __device__ inline size_t plan_smem_bytes(int n_iter, int n_out, int tpt) {
+    return align16(static_cast<size_t>(n_iter + n_out) * tpt * 4);
+}
+
+template <int TPT>
+__device__ __forceinline__ void gsync(int g) {
+    if constexpr (TPT == 32) {
+        __syncwarp();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(TPT) : "memory");
+    }
+}
+
+// Sum over the group; every thread returns the same value (fixed reduction order).
+template <int TPT>
+__device__ __forceinline__ double group_sum(double v, double* red, int lt, int g) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if constexpr (TPT == 32) {
+        return __shfl_sync(0xffffffffu, v, 0);
+    } else {
+        if ((lt & 31) == 0) red[lt >> 5] = v;
+        gsync<TPT>(g);
+        double tot = 0.0;
+#pragma unroll
+        for (int w = 0; w < TPT / 32; ++w) tot += red[w];
+        gsync<TPT>(g);
+        return tot;
+    }
+}
+
+__device__ __forceinline__ double time_tol(double t) { return 10.0 * 2.220446049250313e-16 * fmax(fabs(t), 1.0); }
+
+// ------------------------------------------------------------------------------------------
+// the VM side of a trajectory: slot values of one lane and coefficient evaluation
+
+struct LaneSlots {
+    double2 s[kMaxSlots];
+};
+
+__device__ __noinline__ void init_slots(const DevPlan& P, const CallArgs& A, long long traj, LaneSlots& L) {
+    for (int i = 0; i < P.n_slots; ++i)
+        L.s[i] = i < P.n_base ? make_double2(P.base_val[2 * i], P.base_val[2 * i + 1]) : make_double2(0.0, 0.0);
+    if (A.param_values) {
+        for (int k = 0; k < A.n_param; ++k) {
+            const double* v = A.param_values + 2 * (traj * A.n_param + k);
+            L.s[A.param_slot[k]] = make_double2(v[0], v[1]);
+        }
+    } else if (A.n_axes > 0) {
+        // row-major grid decode, last axis fastest (ode_batch.rs:353-391)
+        for (int k = 0; k < A.n_axes; ++k) {
+            long long idx = (traj / A.axis_stride[k]) % A.axis_len[k];
+            const double* v = A.axes + 2 * (A.axis_off[k] + idx);
+            L.s[A.param_slot[k]] = make_double2(v[0], v[1]);
+        }
+    }
+}
+
+__device__ __forceinline__ double2 eval_expr(const DevPlan& P, DevExpr e, const LaneSlots& L, double t) {
+    return vm_eval(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, e.start, e.len, L.s, t);
+}
+
+// Evaluate the compounds (all of them, or only the time-dependent ones) at time t.
+__device__ __noinline__ void eval_compounds(const DevPlan& P, LaneSlots& L, double t, bool only_dynamic) {
+    for (int c = 0; c < P.n_comp; ++c)
+        if (!only_dynamic || P.comp_dynamic[c]) L.s[P.comp_slot[c]] = eval_expr(P, P.comp_expr[c], L, t);
+}
+
+__device__ __forceinline__ double2 coeff_value(const DevPlan& P, int cls, const double2* cstat, const double2* crow) {
+    int k = cls >> 1;
+    int pos = P.coeff_dyn_pos[k];
+    double2 c = pos >= 0 ? crow[pos] : cstat[k];
+    if (cls & 1) c.y = -c.y;
+    return c;
+}
+
+// table entries [lo, hi) of the formula table from coefficient values (cstat static, crow the
+// time-dependent ones at the current stage time)
+template <int TPT, bool MIXED>
+__device__ __forceinline__ void fill_formulas(const DevPlan& P, int lo, int hi, const double2* cstat, const double2* crow,
+                                              void* tab_raw, int lt) {
+    for (int f = lo + lt; f < hi; f += TPT) {
+        int a = P.formula_ptr[f - 1], b = P.formula_ptr[f];
+        if constexpr (MIXED) {
+            float2 acc = make_float2(0.f, 0.f);
+            for (int p = a; p < b; ++p) {
+                float fr = P.prod_factor32[2 * p], fi = P.prod_factor32[2 * p + 1];
+                int cls = P.prod_class[p];
+                if (cls < 0) {
+                    acc.x += fr;
+                    acc.y += fi;
+                } else {
+                    double2 c = coeff_value(P, cls, cstat, crow);
+                    float cr = static_cast<float>(c.x), ci = static_cast<float>(c.y);
+                    acc.x += fr * cr - fi * ci;
+                    acc.y += fr * ci + fi * cr;
+                }
+            }
+            reinterpret_cast<float2*>(tab_raw)[f] = acc;
+        } else {
+            double2 acc = make_double2(0.0, 0.0);
+            for (int p = a; p < b; ++p) {
+                double2 fac = make_double2(P.prod_factor[2 * p], P.prod_factor[2 * p + 1]);
+                int cls = P.prod_class[p];
+                double2 c = cls < 0 ? make_double2(1.0, 0.0) : coeff_value(P, cls, cstat, crow);
+                double2 v = cmul(fac, c);
+                acc.x += v.x;
+                acc.y += v.y;
+            }
+            reinterpret_cast<double2*>(tab_raw)[f] = acc;
+        }
+    }
+}
+
+// The packed expanded_sparse RHS of one stage: gather from yg, write K (the stage derivative).
+template <int TPT, bool MIXED>
+__device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
+                                           const void* tab_raw, const void* yg_raw, void* K_raw, int lt) {
+    using RT = std::conditional_t<MIXED, float, double>;
+    using RT2 = std::conditional_t<MIXED, float2, double2>;
+    const RT2* tab = reinterpret_cast<const RT2*>(tab_raw);
+    const RT* yg = reinterpret_cast<const RT*>(yg_raw);
+    RT* K = reinterpret_cast<RT*>(K_raw);
+    RT ar = 0, ai = 0;
+    int o = 0;
+    const int n_iter = P.n_iter;
+#pragma unroll 4
+    for (int it = 0; it < n_iter; ++it) {
+        uint32_t w = s_rec[it * TPT + lt];
+        int in = static_cast<int>(w & kRecIndexMask);
+        RT2 c = tab[w >> kRecCoefShift];
+        RT vr = yg[in];
+        RT vi = (w & kRecComplex) ? yg[in + 1] : RT(0);
+        if (w & kRecConj) vi = -vi;
+        ar = fma(c.x, vr, ar);
+        ar = fma(-c.y, vi, ar);
+        ai = fma(c.x, vi, ai);
+        ai = fma(c.y, vr, ai);
+        if (w & kRecFlush) {
+            uint32_t d = s_out[o * TPT + lt];
+            K[d & 0xFFFFu] = ar;
+            uint32_t im = d >> 16;
+            if (im != kNoImag) K[im] = ai;
+            ar = 0;
+            ai = 0;
+            ++o;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// the integrator kernel
+
+template <int TPT, int EPT, bool MIXED>
+__global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
+    using RT = std::conditional_t<MIXED, float, double>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int g = static_cast<int>(threadIdx.x) / TPT;
+    const int lt = static_cast<int>(threadIdx.x) % TPT;
+    const int N = P.N;
+
+    // stage the plan's gather stream once per CTA
+    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* s_out = s_rec + static_cast<size_t>(P.n_iter) * TPT;
+    {
+        const int total = (P.n_iter + P.n_out) * TPT;
+        for (int i = threadIdx.x; i < total; i += blockDim.x)
+            s_rec[i] = i < P.n_iter * TPT ? P.rec[i] : P.lane_out[i - P.n_iter * TPT];
+    }
+    __syncthreads();
+    if (g >= gpb) return;
+
+    const GroupLayout Lay = group_layout(N, P.n_formula, P.n_coeff, P.n_dyn, TPT, MIXED);
+    unsigned char* gb = smem + plan_smem_bytes(P.n_iter, P.n_out, TPT) + static_cast<size_t>(g) * group_bytes;
+    void* s_tab = gb + Lay.tab;
+    RT* s_yg = reinterpret_cast<RT*>(gb + Lay.yg);
+    RT* s_K = reinterpret_cast<RT*>(gb + Lay.K);
+    double* s_ybuf = reinterpret_cast<double*>(gb + Lay.ybuf);
+    double2* s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
+    double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
+    double* s_red = reinterpret_cast<double*>(gb + Lay.red);
+    long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
+    const int nd = P.n_dyn > 0 ? P.n_dyn : 1;
+
+    LaneSlots L;  // meaningful in lanes 0..5 (the VM lanes)
+
+    while (true) {
+        if (lt == 0) *s_traj = static_cast<long long>(atomicAdd(A.counter, 1ull));
+        gsync<TPT>(g);
+        const long long traj = *s_traj;
+        gsync<TPT>(g);
+        if (traj >= A.n_traj) break;
+
+        // ---------------- per-trajectory setup ----------------
+        const double t0 = A.t0, t1 = A.t1;
+        if (lt < 6) {
+            init_slots(P, A, traj, L);
+            eval_compounds(P, L, t0, false);
+        }
+        if (lt == 0) {
+            for (int k = 0; k < P.n_coeff; ++k)
+                s_cstat[k] = P.coeff_dynamic[k] ? make_double2(0.0, 0.0) : eval_expr(P, P.coeff_expr[k], L, t0);
+            for (int j = 0; j < P.n_dyn; ++j) s_cdyn[5 * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t0);
+        }
+        if (lt == 0) {
+            if constexpr (MIXED) reinterpret_cast<float2*>(s_tab)[0] = make_float2(0.f, 0.f);
+            else reinterpret_cast<double2*>(s_tab)[0] = make_double2(0.0, 0.0);
+        }
+        gsync<TPT>(g);
+        fill_formulas<TPT, MIXED>(P, 1, 1 + P.n_static_formula, s_cstat, s_cdyn + 5 * nd, s_tab, lt);
+
+        double y[EPT], yn[EPT];
+        const double* r0 = A.rho0 + traj * A.rho0_stride;
+#pragma unroll
+        for (int e = 0; e < EPT; ++e) {
+            int i = lt + e * TPT;
+            y[e] = i < N ? r0[i] : 0.0;
+            yn[e] = 0.0;
+            if (i < N) s_yg[i] = static_cast<RT>(y[e]);
+        }
+
+        long long accepted = 0, rejected = 0, rhs_calls = 0, count = 0;
+        int status = ST_OK;
+        double err_x = 0.0;
+        long long err_a = 0, err_b = 0;
+        int ev_triggered = 0;
+        double ev_time = CUDART_NAN;
+        double integral = 0.0, last_t = CUDART_NAN, last_value = 0.0, last_time = 0.0;
+        bool has_last_time = false;
+        double* out_vals = A.values + traj * A.out_stride;
+        double* out_times = A.times ? A.times + traj * A.cap : nullptr;
+
+        // push the group's state in s_ybuf (already written and synced) as one output point
+        auto push = [&](double t) {
+            last_time = t;
+            has_last_time = true;
+            const long long pt = count;
+            const bool store = pt < A.cap;
+            switch (A.output) {
+            case OBE_OUTPUT_POPULATIONS:
+                if (store)
+                    for (int i = lt; i < P.n; i += TPT) out_vals[pt * P.n + i] = s_ybuf[i];
+                break;
+            case OBE_OUTPUT_FULL:
+                if (store)
+                    for (int i = lt; i < N; i += TPT) out_vals[pt * N + i] = s_ybuf[i];
+                break;
+            case OBE_OUTPUT_SELECTED:
+                if (store)
+                    for (int k = lt; k < A.n_sel; k += TPT) {
+                        double re = s_ybuf[A.sel_re[k]];
+                        double im = A.sel_kind[k] == 0 ? 0.0 : (A.sel_kind[k] == 1 ? s_ybuf[A.sel_im[k]] : -s_ybuf[A.sel_im[k]]);
+                        out_vals[2 * (pt * A.n_sel + k)] = re;
+                        out_vals[2 * (pt * A.n_sel + k) + 1] = im;
+                    }
+                break;
+            default: {
+                if (lt == 0) {
+                    double value = 0.0;
+                    for (int k = 0; k < A.n_weights; ++k) value += A.w_val[k] * s_ybuf[A.w_idx[k]];
+                    if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL) {
+                        if (isfinite(last_t)) integral += 0.5 * (last_value + value) * (t - last_t);
+                        last_t = t;
+                        last_value = value;
+                        if (A.store_trace && store) out_vals[pt] = integral;
+                    } else if (store) {
+                        out_vals[pt] = value;
+                    }
+                }
+                break;
+            }
+            }
+            if (lt == 0 && out_times && store && !(A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace)) out_times[pt] = t;
+            if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace) count = 1;
+            else ++count;
+            gsync<TPT>(g);
+        };
+        auto stage_registers_to_buf = [&](const double* v) {
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                int i = lt + e * TPT;
+                if (i < N) s_ybuf[i] = v[e];
+            }
+            gsync<TPT>(g);
+        };
+        auto points = [&]() -> long long { return count; };
+
+        // event function g(t, y) for the state in s_ybuf (synced); uniform result
+        auto event_value = [&](double t, bool& has, double& gv) {
+            has = false;
+            if (A.ev_kind == OBE_EVENT_NONE) return;
+            if (lt == 0) {
+                double v = 0.0;
+                int bad = 0;
+                if (A.ev_kind == OBE_EVENT_POPULATION) {
+                    for (int k = 0; k < A.n_ev; ++k) {
+                        int idx = A.ev_idx[k];
+                        if (idx < 0 || idx >= P.n) { bad = ST_EVENT_INDEX; break; }
+                        v += s_ybuf[idx];
+                    }
+                    v -= A.ev_thr;
+                } else {
+                    eval_compounds(P, L, t, true);
+                    double2 r = vm_eval(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, L.s, t);
+                    if (fabs(r.y) > 1e-12) bad = ST_EVENT_COMPLEX;
+                    v = r.x;
+                }
+                s_red[TPT / 32] = v;
+                s_red[TPT / 32 + 1] = static_cast<double>(bad);
+            }
+            gsync<TPT>(g);
+            gv = s_red[TPT / 32];
+            int bad = static_cast<int>(s_red[TPT / 32 + 1]);
+            gsync<TPT>(g);
+            if (bad) {
+                status = bad;
+                return;
+            }
+            has = true;
+        };
+
+        // evaluate the time-dependent coefficients at t into row `row` of s_cdyn by lane `lane`
+        auto dyn_coeffs_at = [&](double t, int row) {
+            if (P.n_dyn > 0 && lt == 0) {
+                eval_compounds(P, L, t, true);
+                for (int j = 0; j < P.n_dyn; ++j) s_cdyn[row * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t);
+            }
+        };
+        // one RHS: formulas for the stage row, then the gather into K slot `ks`
+        auto rhs = [&](int row, int ks) {
+            gsync<TPT>(g);  // yg written, coefficient row ready
+            if (P.n_formula > P.n_static_formula)
+                fill_formulas<TPT, MIXED>(P, 1 + P.n_static_formula, 1 + P.n_formula, s_cstat, s_cdyn + row * nd, s_tab, lt);
+            gsync<TPT>(g);
+            gather_rhs<TPT, MIXED>(P, s_rec, s_out, s_tab, s_yg, s_K + static_cast<size_t>(ks) * N, lt);
+            gsync<TPT>(g);  // K complete, yg free
+        };
+        auto Kat = [&](int j, int i) -> double { return static_cast<double>(s_K[static_cast<size_t>(j) * N + i]); };
+
+        bool done = false;
+        if (A.maxiters <= 0) {
+            status = ST_BAD_MAXITERS;
+            done = true;
+        } else if (t1 < t0) {
+            status = ST_BACKWARD;
+            done = true;
+        } else if (t1 == t0) {
+            if (A.save_start) {
+                stage_registers_to_buf(y);
+                push(t0);
+            }
+            done = true;
+        }
+
+        double x = t0, h = 0.0;
+        if (!done) {
+            // initial step (dopri5.rs:199-206)
+            if (isfinite(A.dt) && A.dt > 0.0) {
+                h = fmin(A.dt, t1 - t0);
+            } else {
+                // hinit (common.rs:72-118): f0 = f(x, y) into K slot 0, f1 into slot 1
+                dyn_coeffs_at(x, 5);
+                rhs(5, 0);
+                double d0 = 0.0, d1 = 0.0;
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) {
+                        double sci = A.atol + fabs(y[e]) * A.rtol;
+                        double f0 = Kat(0, i);
+                        d0 += (y[e] / sci) * (y[e] / sci);
+                        d1 += (f0 / sci) * (f0 / sci);
+                    }
+                }
+                d0 = group_sum<TPT>(d0, s_red, lt, g);
+                d1 = group_sum<TPT>(d1, s_red, lt, g);
+                double posneg = (t1 - x) >= 0.0 ? 1.0 : -1.0;
+                double h_max = fabs(t1 - x);
+                double h0 = (d0 < 1.0e-10 || d1 < 1.0e-10) ? 1.0e-6 : 0.01 * sqrt(d0 / d1);
+                h0 = fmin(h0, h_max);
+                h0 = posneg * fabs(h0);
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) s_yg[i] = static_cast<RT>(y[e] + Kat(0, i) * h0);
+                }
+                dyn_coeffs_at(x + h0, 4);
+                rhs(4, 1);
+                double d2 = 0.0;
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) {
+                        double sci = A.atol + fabs(y[e]) * A.rtol;
+                        double df = Kat(1, i) - Kat(0, i);
+                        d2 += (df / sci) * (df / sci);
+                    }
+                }
+                d2 = sqrt(group_sum<TPT>(d2, s_red, lt, g)) / h0;
+                double h1 = fmax(sqrt(d1), fabs(d2)) <= 1.0e-15 ? fmax(1.0e-6, fabs(h0) * 1.0e-3)
+                                                                 : pow(0.01 / fmax(sqrt(d1), d2), 1.0 / 5.0);
+                h = posneg * fabs(fmin(100.0 * fabs(h0), fmin(h1, h_max)));
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) s_yg[i] = static_cast<RT>(y[e]);
+                }
+            }
+        }
+
+        // controller state (common.rs:20-46)
+        const double beta = 0.04, alpha = 0.2 - beta * 0.75, facc1 = 1.0 / 0.2, facc2 = 1.0 / 10.0, safety = 0.9;
+        double fac_old = 1.0e-4;
+        const double h_maxc = fabs(t1 - t0);
+        const double posneg = (t1 - t0) >= 0.0 ? 1.0 : -1.0;
+        bool reject = false;
+        bool ev_old_has = false;
+        double ev_old = 0.0;
+        int si = 0;
+
+        if (!done) {
+            dyn_coeffs_at(x, 5);
+            rhs(5, 0);  // K1 = f(t0, y0)
+            rhs_calls = 1;
+            if (A.ev_kind != OBE_EVENT_NONE) {
+                stage_registers_to_buf(y);
+                event_value(x, ev_old_has, ev_old);
+                if (status) done = true;
+            }
+        }
+        if (!done) {
+            if (A.has_saveat) {
+                bool buffered = false;
+                while (si < A.n_save && fabs(A.save_times[si] - t0) <= time_tol(t0)) {
+                    if (!buffered) { stage_registers_to_buf(y); buffered = true; }
+                    push(A.save_times[si]);
+                    ++si;
+                }
+            } else if (A.save_start) {
+                stage_registers_to_buf(y);
+                push(x);
+            }
+        }
+
+        long long ns = 0, nst = 0, ia = 0;
+        bool last = false;
+        while (!done && !last) {
+            if (ns > A.maxiters) { status = ST_MAXITERS; err_x = x; err_a = ns; break; }
+            if (0.1 * fabs(h) <= 2.220446049250313e-16 * fabs(x)) { status = ST_UNDERFLOW; err_x = x; break; }
+            if ((x + 1.01 * h - t1) * posneg > 0.0) {
+                h = t1 - x;
+                last = true;
+            }
+            ++ns;
+            // coefficients at the five distinct stage times, one VM lane each
+            if (P.n_dyn > 0 && lt < 5) {
+                double c = lt < 4 ? kC[M][lt] : 1.0;
+                double ts = x + h * c;
+                eval_compounds(P, L, ts, true);
+                for (int j = 0; j < P.n_dyn; ++j) s_cdyn[lt * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, ts);
+            }
+            // stages 2..7 (stage 7 input is the solution yn)
+#pragma unroll 1
+            for (int s = 0; s < 6; ++s) {
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) {
+                        double acc = 0.0;
+#pragma unroll
+                        for (int j = 0; j < 6; ++j)
+                            if (j <= s) acc += kA[M][s][j] * Kat(j, i);
+                        double v = y[e] + h * acc;
+                        if (s == 5) yn[e] = v;
+                        s_yg[i] = static_cast<RT>(v);
+                    }
+                }
+                rhs(s < 4 ? s : 4, s + 1);
+            }
+            rhs_calls += 6;
+            // error norm (dopri5.rs:88-102, tsit5.rs:104-119)
+            double err = 0.0;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e) {
+                int i = lt + e * TPT;
+                if (i < N) {
+                    double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int j = 0; j < 7; ++j)
+                        if (M == 1 || j != 1) acc += kE[M][j] * Kat(j, i);
+                    double ei = h * acc;
+                    double q = ei / sc;
+                    err += q * q;
+                }
+            }
+            err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
+            // controller (common.rs:48-69)
+            double fac11 = pow(err, alpha);
+            double fac = fac11 * pow(fac_old, -beta);
+            fac = fmax(facc2, fmin(facc1, fac / safety));
+            double hn = h / fac;
+            if (err <= 1.0) {
+                fac_old = fmax(err, 1.0e-4);
+                if (fabs(hn) > h_maxc) hn = posneg * h_maxc;
+                if (reject) hn = posneg * fmin(fabs(hn), fabs(h));
+                reject = false;
+                ++accepted;
+                // stiffness detection (dopri5.rs:255-277)
+                if (accepted % 1000 == 0 || ia > 0) {
+                    double n2 = 0.0, dd2 = 0.0;
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        if (i < N) {
+                            // the stage-6 input, recomputed exactly as in the stage loop
+                            double acc6 = 0.0;
+#pragma unroll
+                            for (int j = 0; j < 6; ++j)
+                                if (j <= 4) acc6 += kA[M][4][j] * Kat(j, i);
+                            double ys6 = y[e] + h * acc6;
+                            double dk = Kat(6, i) - Kat(5, i);
+                            double dy = yn[e] - ys6;
+                            n2 += dk * dk;
+                            dd2 += dy * dy;
+                        }
+                    }
+                    n2 = group_sum<TPT>(n2, s_red, lt, g);
+                    dd2 = group_sum<TPT>(dd2, s_red, lt, g);
+                    double hl = dd2 > 0.0 ? h * sqrt(n2 / dd2) : 0.0;
+                    if (hl > 3.25) {
+                        ++ia;
+                        nst = 0;
+                        if (ia == 15) { status = ST_STIFF; err_x = x; break; }
+                    } else {
+                        ++nst;
+                        if (nst == 6) ia = 0;
+                    }
+                }
+                const double xo = x;
+                x += h;
+                // dense output of own elements at theta, written to the push buffer (synced)
+                auto dense_to_buf = [&](double th) {
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        if (i >= N) continue;
+                        double v;
+                        if (M == 0) {
+                            double r4 = 0.0;
+#pragma unroll
+                            for (int j = 0; j < 7; ++j)
+                                if (j != 1) r4 += kDd[j] * Kat(j, i);
+                            r4 *= h;
+                            double dd = yn[e] - y[e];
+                            double bb = Kat(0, i) * h - dd;
+                            double r3 = -Kat(6, i) * h + dd - bb;
+                            double th1 = 1.0 - th;
+                            v = y[e] + (dd + (bb + (r3 + r4 * th1) * th) * th1) * th;
+                        } else {
+                            double t2 = th * th, t3 = t2 * th, t4 = t3 * th;
+                            double acc = 0.0;
+#pragma unroll
+                            for (int j = 0; j < 7; ++j) {
+                                double bj = kR[j][0] * th + kR[j][1] * t2 + kR[j][2] * t3 + kR[j][3] * t4;
+                                acc += bj * Kat(j, i);
+                            }
+                            v = y[e] + h * acc;
+                        }
+                        s_ybuf[i] = v;
+                    }
+                    gsync<TPT>(g);
+                };
+                // which state the event point carries: 0 = y, 1 = yn, 2 = dense at ev_theta
+                int ev_state = 0;
+                double ev_theta = 0.0;
+                bool ev_new_has = false;
+                double ev_new = 0.0;
+                bool hit = false;
+                double te = 0.0;
+                if (A.ev_kind != OBE_EVENT_NONE) {
+                    stage_registers_to_buf(yn);
+                    event_value(x, ev_new_has, ev_new);
+                    if (status) { err_x = x; break; }
+                    if (ev_old_has && ev_new_has &&
+                        (ev_old == 0.0 || ev_new == 0.0 || (ev_old < 0.0 && ev_new > 0.0) || (ev_old > 0.0 && ev_new < 0.0))) {
+                        hit = true;
+                        if (ev_old == 0.0) {
+                            te = xo;
+                            ev_state = 0;
+                        } else if (ev_new == 0.0) {
+                            te = x;
+                            ev_state = 1;
+                        } else {
+                            // 60-step bisection on the dense interpolant (dopri5.rs:289-315)
+                            double lo = 0.0, hi = 1.0, glo = ev_old;
+                            for (int itb = 0; itb < 60; ++itb) {
+                                double mid = 0.5 * (lo + hi);
+                                dense_to_buf(mid);
+                                bool hs;
+                                double gm;
+                                event_value(xo + mid * h, hs, gm);
+                                if (status) break;
+                                if (gm == 0.0) { lo = mid; hi = mid; break; }
+                                if ((glo < 0.0 && gm > 0.0) || (glo > 0.0 && gm < 0.0)) hi = mid;
+                                else { lo = mid; glo = gm; }
+                            }
+                            if (status) { err_x = x; break; }
+                            ev_theta = 0.5 * (lo + hi);
+                            ev_state = 2;
+                            te = xo + ev_theta * h;
+                        }
+                    }
+                }
+                if (A.has_saveat) {
+                    double event_time = hit ? te : x;
+                    while (si < A.n_save && A.save_times[si] <= event_time + time_tol(event_time)) {
+                        double ts = A.save_times[si];
+                        if (ts >= xo - time_tol(xo)) {
+                            if (fabs(ts - xo) <= time_tol(xo)) stage_registers_to_buf(y);
+                            else if (fabs(ts - x) <= time_tol(x)) stage_registers_to_buf(yn);
+                            else dense_to_buf((ts - xo) / h);
+                            push(ts);
+                        }
+                        ++si;
+                    }
+                } else if (!hit) {
+                    stage_registers_to_buf(yn);
+                    push(x);
+                }
+                if (hit) {
+                    // push_unique (dopri5.rs:150-158)
+                    if (!(points() > 0 && fabs(last_time - te) <= time_tol(te))) {
+                        if (ev_state == 0) stage_registers_to_buf(y);
+                        else if (ev_state == 1) stage_registers_to_buf(yn);
+                        else dense_to_buf(ev_theta);
+                        push(te);
+                    }
+                    ev_triggered = 1;
+                    ev_time = te;
+                    break;
+                }
+                // accept: y <- yn, K1 <- K7 (own elements; K7 is complete after the last sync)
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    y[e] = yn[e];
+                    if (i < N) {
+                        s_K[i] = s_K[static_cast<size_t>(6) * N + i];
+                        s_yg[i] = static_cast<RT>(y[e]);
+                    }
+                }
+                ev_old_has = ev_new_has;
+                ev_old = ev_new;
+                h = hn;
+                if (last) break;
+            } else {
+                hn = h / fmin(facc1, fac11 / safety);
+                reject = true;
+                last = false;
+                if (accepted >= 1) ++rejected;
+                h = hn;
+                // restore the gather buffer to the step's start state
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) s_yg[i] = static_cast<RT>(y[e]);
+                }
+            }
+            gsync<TPT>(g);
+        }
+        if (status == ST_OK && A.has_saveat && si != A.n_save && !ev_triggered && !done) {
+            status = ST_SAVEAT;
+            err_a = si;
+            err_b = A.n_save;
+        }
+
+        // ---------------- finalise ----------------
+        if (lt == 0) {
+            if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace && has_last_time && A.cap > 0) {
+                out_vals[0] = integral;
+                if (out_times) out_times[0] = last_time;
+            }
+            obe_traj_stats st;
+            st.accepted_steps = accepted;
+            st.rejected_steps = rejected;
+            st.rhs_calls = rhs_calls;
+            st.event_triggered = ev_triggered;
+            st.status = status;
+            st.event_time = ev_time;
+            st.n_points = (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace) ? (has_last_time ? 1 : 0) : count;
+            A.stats[traj] = st;
+            TrajErr te;
+            te.x = err_x;
+            te.a = err_a;
+            te.b = err_b;
+            A.errs[traj] = te;
+        }
+        gsync<TPT>(g);
+    }
+}
+
+// One RHS evaluation per state (lindblad_rhs_py), batched; overrides per state.
+template <int TPT, bool MIXED>
+__global__ void __launch_bounds__(256) rhs_kernel(const DevPlan P, long long count, const double* ts, const double* ys,
+                                                  int n_ov, const int* ov_slots, const double* ov_vals, double* dys,
+                                                  int gpb, size_t group_bytes) {
+    using RT = std::conditional_t<MIXED, float, double>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int g = static_cast<int>(threadIdx.x) / TPT;
+    const int lt = static_cast<int>(threadIdx.x) % TPT;
+    const int N = P.N;
+    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* s_out = s_rec + static_cast<size_t>(P.n_iter) * TPT;
+    for (int i = threadIdx.x; i < (P.n_iter + P.n_out) * TPT; i += blockDim.x)
+        s_rec[i] = i < P.n_iter * TPT ? P.rec[i] : P.lane_out[i - P.n_iter * TPT];
+    __syncthreads();
+    if (g >= gpb) return;
+    const GroupLayout Lay = group_layout(N, P.n_formula, P.n_coeff, P.n_dyn, TPT, MIXED);
+    unsigned char* gb = smem + plan_smem_bytes(P.n_iter, P.n_out, TPT) + static_cast<size_t>(g) * group_bytes;
+    void* s_tab = gb + Lay.tab;
+    RT* s_yg = reinterpret_cast<RT*>(gb + Lay.yg);
+    RT* s_K = reinterpret_cast<RT*>(gb + Lay.K);
+    double2* s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
+    double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
+    LaneSlots L;
+    for (long long st = static_cast<long long>(blockIdx.x) * gpb + g; st < count; st += static_cast<long long>(gridDim.x) * gpb) {
+        const double t = ts[st];
+        if (lt == 0) {
+            for (int i = 0; i < P.n_slots; ++i)
+                L.s[i] = i < P.n_base ? make_double2(P.base_val[2 * i], P.base_val[2 * i + 1]) : make_double2(0.0, 0.0);
+            for (int k = 0; k < n_ov; ++k) L.s[ov_slots[k]] = make_double2(ov_vals[2 * (st * n_ov + k)], ov_vals[2 * (st * n_ov + k) + 1]);
+            eval_compounds(P, L, t, false);
+            for (int k = 0; k < P.n_coeff; ++k) {
+                double2 c = eval_expr(P, P.coeff_expr[k], L, t);
+                s_cstat[k] = c;
+                if (P.coeff_dyn_pos[k] >= 0) s_cdyn[P.coeff_dyn_pos[k]] = c;
+            }
+            if constexpr (MIXED) reinterpret_cast<float2*>(s_tab)[0] = make_float2(0.f, 0.f);
+            else reinterpret_cast<double2*>(s_tab)[0] = make_double2(0.0, 0.0);
+        }
+        for (int i = lt; i < N; i += TPT) s_yg[i] = static_cast<RT>(ys[st * N + i]);
+        gsync<TPT>(g);
+        fill_formulas<TPT, MIXED>(P, 1, 1 + P.n_formula, s_cstat, s_cdyn, s_tab, lt);
+        gsync<TPT>(g);
+        gather_rhs<TPT, MIXED>(P, s_rec, s_out, s_tab, s_yg, s_K, lt);
+        gsync<TPT>(g);
+        for (int i = lt; i < N; i += TPT) dys[st * N + i] = static_cast<double>(s_K[i]);
+        gsync<TPT>(g);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// host side
+
+namespace {
+
+thread_local long long g_launches = 0;
+
+bool cuda_ok(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+template <typename T>
+size_t put(std::vector<unsigned char>& blob, const std::vector<T>& v) {
+    size_t off = align16(blob.size());
+    blob.resize(off + std::max<size_t>(v.size() * sizeof(T), 16));
+    if (!v.empty()) std::memcpy(blob.data() + off, v.data(), v.size() * sizeof(T));
+    return off;
+}
+
+obe_status upload_plan(obe_plan* p) {
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
+    if (p->d_blob && p->d_device == dev) return OBE_OK;
+    if (p->d_blob) {
+        cudaFree(p->d_blob);
+        p->d_blob = nullptr;
+    }
+    const HostPacked& h = p->packed;
+    std::vector<unsigned char> blob;
+    size_t o_op = put(blob, h.ins_op), o_arg = put(blob, h.ins_arg), o_fn = put(blob, h.ins_fn), o_val = put(blob, h.ins_val);
+    size_t o_bv = put(blob, h.base_val), o_bt = put(blob, h.base_tuple), o_tp = put(blob, h.tuple_ptr), o_ti = put(blob, h.tuple_items);
+    size_t o_cs = put(blob, h.comp_slot), o_ce = put(blob, h.comp_expr), o_cd = put(blob, h.comp_dynamic);
+    size_t o_ke = put(blob, h.coeff_expr), o_kd = put(blob, h.coeff_dynamic), o_di = put(blob, h.dyn_ids), o_dp = put(blob, h.coeff_dyn_pos);
+    size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
+    size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
+    size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out);
+    void* d = nullptr;
+    if (!cuda_ok(cudaMalloc(&d, blob.size()), "cudaMalloc(plan)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpy(d, blob.data(), blob.size(), cudaMemcpyHostToDevice), "cudaMemcpy(plan)")) {
+        cudaFree(d);
+        return OBE_ERR_CUDA;
+    }
+    auto* b = static_cast<unsigned char*>(d);
+    DevPlan& P = p->dev;
+    P.n = p->n;
+    P.N = static_cast<int32_t>(p->N);
+    P.U = static_cast<int32_t>(p->U);
+    P.ins_op = reinterpret_cast<const int32_t*>(b + o_op);
+    P.ins_arg = reinterpret_cast<const int32_t*>(b + o_arg);
+    P.ins_fn = reinterpret_cast<const int32_t*>(b + o_fn);
+    P.ins_val = reinterpret_cast<const double*>(b + o_val);
+    P.n_slots = p->n_slots;
+    P.n_base = p->n_base;
+    P.base_val = reinterpret_cast<const double*>(b + o_bv);
+    P.base_tuple = reinterpret_cast<const int32_t*>(b + o_bt);
+    P.tuple_ptr = reinterpret_cast<const int32_t*>(b + o_tp);
+    P.tuple_items = reinterpret_cast<const double*>(b + o_ti);
+    P.n_comp = static_cast<int32_t>(h.comp_slot.size());
+    P.comp_slot = reinterpret_cast<const int32_t*>(b + o_cs);
+    P.comp_expr = reinterpret_cast<const DevExpr*>(b + o_ce);
+    P.comp_dynamic = reinterpret_cast<const uint8_t*>(b + o_cd);
+    P.n_coeff = p->n_coeff;
+    P.coeff_expr = reinterpret_cast<const DevExpr*>(b + o_ke);
+    P.coeff_dynamic = reinterpret_cast<const uint8_t*>(b + o_kd);
+    P.n_dyn = static_cast<int32_t>(h.dyn_ids.size());
+    P.dyn_ids = reinterpret_cast<const int32_t*>(b + o_di);
+    P.coeff_dyn_pos = reinterpret_cast<const int32_t*>(b + o_dp);
+    P.time_dependent = p->time_dependent;
+    P.n_pchip = static_cast<int32_t>(h.pchip_cptr.size());
+    P.pchip_ptr = reinterpret_cast<const int32_t*>(b + o_pp);
+    P.pchip_grid = reinterpret_cast<const double*>(b + o_pg);
+    P.pchip_coef = reinterpret_cast<const double*>(b + o_pc);
+    P.pchip_cptr = reinterpret_cast<const int32_t*>(b + o_pcp);
+    P.n_formula = h.n_formula;
+    P.n_static_formula = h.n_static_formula;
+    P.formula_ptr = reinterpret_cast<const int32_t*>(b + o_fp);
+    P.prod_factor = reinterpret_cast<const double*>(b + o_pf);
+    P.prod_class = reinterpret_cast<const int32_t*>(b + o_pcl);
+    P.prod_factor32 = reinterpret_cast<const float*>(b + o_pf32);
+    P.tpt = h.tpt;
+    P.n_iter = h.n_iter;
+    P.rec = reinterpret_cast<const uint32_t*>(b + o_rec);
+    P.n_out = h.n_out;
+    P.lane_out = reinterpret_cast<const uint32_t*>(b + o_lo);
+    p->d_blob = d;
+    p->d_device = dev;
+    return OBE_OK;
+}
+
+// grow-only device scratch of a plan
+obe_status scratch(obe_plan* p, size_t bytes, unsigned char** out) {
+    if (p->scratch_bytes < bytes) {
+        if (p->d_scratch) cudaFree(p->d_scratch);
+        p->d_scratch = nullptr;
+        p->scratch_bytes = 0;
+        size_t want = std::max<size_t>(bytes, 1 << 20);
+        if (!cuda_ok(cudaMalloc(&p->d_scratch, want), "cudaMalloc(scratch)")) return OBE_ERR_CUDA;
+        p->scratch_bytes = want;
+    }
+    *out = static_cast<unsigned char*>(p->d_scratch);
+    return OBE_OK;
+}
+
+int ept_for(int N, int tpt) {
+    int need = (N + tpt - 1) / tpt;
+    return need <= 8 ? 8 : 16;
+}
+
+struct LaunchShape {
+    int tpt, ept, gpb, blocks;
+    size_t group_bytes, smem;
+};
+
+template <int TPT, int EPT, bool MIXED>
+cudaError_t launch_one(const DevPlan& P, const CallArgs& A, const LaunchShape& s, int method, cudaStream_t stream) {
+    auto k = integrate_kernel<TPT, EPT, MIXED>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s.smem));
+    if (e != cudaSuccess) return e;
+    k<<<s.blocks, s.gpb * TPT, s.smem, stream>>>(P, A, s.gpb, s.group_bytes, method);
+    return cudaGetLastError();
+}
+
+template <bool MIXED>
+cudaError_t dispatch_shape(const DevPlan& P, const CallArgs& A, const LaunchShape& s, int method, cudaStream_t st) {
+    if (s.tpt == 32) {
+        if (s.ept == 8) return launch_one<32, 8, MIXED>(P, A, s, method, st);
+        return launch_one<32, 16, MIXED>(P, A, s, method, st);
+    }
+    if (s.tpt == 64) return launch_one<64, 16, MIXED>(P, A, s, method, st);
+    return launch_one<128, 16, MIXED>(P, A, s, method, st);
+}
+
+int sm_count() {
+    static int count = 0;
+    if (!count) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+        if (count <= 0) count = 1;
+    }
+    return count;
+}
+
+obe_status plan_launch(const obe_plan* p, bool mixed, long long n_traj, LaunchShape* s) {
+    const DevPlan& P = p->dev;
+    s->tpt = P.tpt;
+    if (s->tpt > 128) {
+        set_error("systems with more than 45 states are not supported by this build of the GPU solver");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    s->ept = ept_for(P.N, s->tpt);
+    GroupLayout L = group_layout(P.N, P.n_formula, P.n_coeff, P.n_dyn, s->tpt, mixed);
+    s->group_bytes = L.bytes;
+    size_t plan_bytes = plan_smem_bytes(P.n_iter, P.n_out, s->tpt);
+    const size_t limit = 227 * 1024;
+    int gpb = std::max(1, 256 / s->tpt);
+    while (gpb > 1 && plan_bytes + gpb * L.bytes > limit) --gpb;
+    if (plan_bytes + gpb * L.bytes > limit) {
+        set_error("system too large for the GPU solver's shared-memory layout");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    // fewer groups per CTA when the batch is small, so that every SM gets work
+    long long per_sm = (n_traj + sm_count() - 1) / sm_count();
+    while (gpb > 1 && gpb > per_sm) --gpb;
+    s->gpb = gpb;
+    s->smem = plan_bytes + gpb * L.bytes;
+    int blocks_per_sm = std::max<int>(1, static_cast<int>(limit / s->smem));
+    long long want = (n_traj + gpb - 1) / gpb;
+    long long cap = static_cast<long long>(sm_count()) * blocks_per_sm;
+    s->blocks = static_cast<int>(std::max<long long>(1, std::min(want, cap)));
+    return OBE_OK;
+}
+
+// Host-side save plan (common.rs:124-151).
+obe_status save_plan(const obe_solve_options* o, std::vector<double>& times) {
+    times.clear();
+    if (!o->has_saveat) return OBE_OK;
+    auto tol = [](double t) { return 10.0 * 2.220446049250313e-16 * std::fmax(std::fabs(t), 1.0); };
+    if (o->save_start) times.push_back(o->t0);
+    for (int64_t i = 0; i < o->n_saveat; ++i) {
+        double t = o->saveat[i];
+        if (o->save_start && std::fabs(t - o->t0) <= tol(o->t0)) continue;
+        if (!std::isfinite(t)) {
+            set_error("saveat contains non-finite value");
+            return OBE_ERR_INVALID;
+        }
+        if (t < o->t0 - tol(o->t0) || t > o->t1 + tol(o->t1)) {
+            set_error("saveat value " + fmt_f64(t) + " is outside [" + fmt_f64(o->t0) + ", " + fmt_f64(o->t1) + "]");
+            return OBE_ERR_INVALID;
+        }
+        times.push_back(t);
+    }
+    return OBE_OK;
+}
+
+int64_t packed_upper_real_index(int32_t n, int64_t i, int64_t j) {
+    int64_t off = 0;
+    for (int64_t r = 0; r < i; ++r) off += n - r - 1;
+    return n + 2 * (off + (j - i - 1));
+}
+
+std::string traj_message(int code, const TrajErr& e) {
+    switch (code) {
+    case ST_MAXITERS: return "Stopped at x=" + fmt_f64(e.x) + ". Need more than " + std::to_string(e.a) + " steps.";
+    case ST_UNDERFLOW: return "Stopped at x=" + fmt_f64(e.x) + ". Step size underflow.";
+    case ST_STIFF: return "Stiff at x=" + fmt_f64(e.x) + ".";
+    case ST_SAVEAT: return "ended before all saveat: " + std::to_string(e.a) + " of " + std::to_string(e.b);
+    case ST_EVENT_COMPLEX: return "event expression evaluated to a complex value";
+    case ST_EVENT_INDEX: return "population event index out of bounds";
+    case ST_POINTS: return "expected " + std::to_string(e.a) + " output points, got " + std::to_string(e.b);
+    case ST_BAD_MAXITERS: return "maxiters must be positive";
+    case ST_BACKWARD: return "only forward integration";
+    default: return "trajectory failed with status " + std::to_string(code);
+    }
+}
+
+// Everything a solve needs on the device besides the plan: the per-call blob of small arrays.
+struct CallBlob {
+    std::vector<unsigned char> bytes;
+    size_t o_save = 0, o_widx = 0, o_wval = 0, o_sre = 0, o_sim = 0, o_skind = 0, o_evidx = 0, o_evop = 0, o_evarg = 0, o_evfn = 0, o_evval = 0;
+    int ev_len = 0;
+};
+
+obe_status validate_options(const obe_plan* p, const obe_solve_options* o, std::vector<double>& save_times, CallBlob& cb,
+                            int64_t* width_out, int* is_complex) {
+    if (!p->has_expanded) {
+        set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan");
+        return OBE_ERR_INVALID;
+    }
+    if (o->solver != OBE_SOLVER_DOPRI5 && o->solver != OBE_SOLVER_TSIT5) {
+        set_error("solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4'");
+        return OBE_ERR_INVALID;
+    }
+    obe_status st = save_plan(o, save_times);
+    if (st != OBE_OK) return st;
+    int64_t width = 0;
+    *is_complex = 0;
+    std::vector<int32_t> widx, sre, sim, skind, evidx;
+    std::vector<double> wval;
+    switch (o->output) {
+    case OBE_OUTPUT_POPULATIONS: width = p->n; break;
+    case OBE_OUTPUT_FULL: width = p->N; break;
+    case OBE_OUTPUT_SELECTED:
+        width = o->n_selected;
+        *is_complex = 1;
+        if (o->n_selected > kMaxSelected) { set_error("too many selected outputs for the GPU solver"); return OBE_ERR_UNSUPPORTED; }
+        for (int k = 0; k < o->n_selected; ++k) {
+            int64_t i = o->selected_i[k], j = o->selected_j[k];
+            if (i < 0 || j < 0 || i >= p->n || j >= p->n) { set_error("selected output index out of bounds"); return OBE_ERR_INVALID; }
+            if (i == j) { sre.push_back(static_cast<int32_t>(i)); sim.push_back(static_cast<int32_t>(i)); skind.push_back(0); }
+            else if (i < j) { int64_t r = packed_upper_real_index(p->n, i, j); sre.push_back(static_cast<int32_t>(r)); sim.push_back(static_cast<int32_t>(r + 1)); skind.push_back(1); }
+            else { int64_t r = packed_upper_real_index(p->n, j, i); sre.push_back(static_cast<int32_t>(r)); sim.push_back(static_cast<int32_t>(r + 1)); skind.push_back(2); }
+        }
+        break;
+    case OBE_OUTPUT_WEIGHTED_INTEGRAL:
+    case OBE_OUTPUT_WEIGHTED_RATE:
+        width = 1;
+        if (o->n_weights > kMaxWeights) { set_error("too many integral weights for the GPU solver"); return OBE_ERR_UNSUPPORTED; }
+        for (int k = 0; k < o->n_weights; ++k) {
+            if (o->weight_index[k] < 0 || o->weight_index[k] >= p->N) { set_error("integral weight index out of bounds"); return OBE_ERR_INVALID; }
+            widx.push_back(static_cast<int32_t>(o->weight_index[k]));
+            wval.push_back(o->weight_value[k]);
+        }
+        break;
+    default: set_error("unknown output mode"); return OBE_ERR_INVALID;
+    }
+    *width_out = width;
+    std::vector<int32_t> evop, evarg, evfn;
+    std::vector<double> evval;
+    if (o->event_kind == OBE_EVENT_POPULATION) {
+        if (o->n_event_indices > kMaxEventIdx) { set_error("too many population event indices"); return OBE_ERR_UNSUPPORTED; }
+        for (int k = 0; k < o->n_event_indices; ++k) evidx.push_back(static_cast<int32_t>(o->event_indices[k]));
+    } else if (o->event_kind == OBE_EVENT_EXPRESSION) {
+        // kind-check the event program with the plan's slot kinds and keep it in the call blob
+        HostPacked tmp;
+        obe_plan_desc dd{};
+        (void)dd;
+        const obe_expr& e = o->event_expr;
+        for (int64_t k = 0; k < e.n_instr; ++k) {
+            int32_t op = e.op[k];
+            if (op == OP_TEMP || op < 1 || op > 19) { set_error("unsupported instruction in stop_event expression"); return OBE_ERR_UNSUPPORTED; }
+            if (op == OP_SLOT && (e.index[k] < 0 || e.index[k] >= p->n_slots)) { set_error("stop_event slot index out of bounds"); return OBE_ERR_INVALID; }
+            if (op == OP_SLOT && e.index[k] < p->n_base && p->base_is_tuple[e.index[k]]) {
+                set_error("tuple-valued stop_event operands are not supported by the GPU solver");
+                return OBE_ERR_UNSUPPORTED;
+            }
+            if (op == OP_HELPER && (e.function[k] == 8 || e.function[k] == 10 || e.function[k] == 14 || e.function[k] == 16)) {
+                set_error("tuple helpers in stop_event expressions are not supported by the GPU solver");
+                return OBE_ERR_UNSUPPORTED;
+            }
+            evop.push_back(op);
+            evarg.push_back(op == OP_SLOT ? static_cast<int32_t>(e.index[k]) : (e.argc ? e.argc[k] : 0));
+            evfn.push_back(e.function ? e.function[k] : 0);
+            evval.push_back(e.value ? e.value[2 * k] : 0.0);
+            evval.push_back(e.value ? e.value[2 * k + 1] : 0.0);
+        }
+        if (e.n_instr > kMaxStack) { set_error("stop_event expression too long for the GPU solver"); return OBE_ERR_UNSUPPORTED; }
+        cb.ev_len = static_cast<int>(e.n_instr);
+    }
+    cb.o_save = put(cb.bytes, save_times);
+    cb.o_widx = put(cb.bytes, widx);
+    cb.o_wval = put(cb.bytes, wval);
+    cb.o_sre = put(cb.bytes, sre);
+    cb.o_sim = put(cb.bytes, sim);
+    cb.o_skind = put(cb.bytes, skind);
+    cb.o_evidx = put(cb.bytes, evidx);
+    cb.o_evop = put(cb.bytes, evop);
+    cb.o_evarg = put(cb.bytes, evarg);
+    cb.o_evfn = put(cb.bytes, evfn);
+    cb.o_evval = put(cb.bytes, evval);
+    return OBE_OK;
+}
+
+void fill_call_args(CallArgs& A, const obe_solve_options* o, const std::vector<double>& save_times, const CallBlob& cb,
+                    const unsigned char* d_blob) {
+    std::memset(&A, 0, sizeof A);
+    A.t0 = o->t0;
+    A.t1 = o->t1;
+    A.atol = o->abstol;
+    A.rtol = o->reltol;
+    A.dt = o->dt;
+    A.maxiters = o->maxiters;
+    A.save_start = o->save_start;
+    A.has_saveat = o->has_saveat;
+    A.n_save = static_cast<int>(save_times.size());
+    A.save_times = reinterpret_cast<const double*>(d_blob + cb.o_save);
+    A.output = o->output;
+    A.store_trace = o->store_trace;
+    A.n_weights = o->output == OBE_OUTPUT_WEIGHTED_INTEGRAL || o->output == OBE_OUTPUT_WEIGHTED_RATE ? o->n_weights : 0;
+    A.w_idx = reinterpret_cast<const int*>(d_blob + cb.o_widx);
+    A.w_val = reinterpret_cast<const double*>(d_blob + cb.o_wval);
+    A.n_sel = o->output == OBE_OUTPUT_SELECTED ? o->n_selected : 0;
+    A.sel_re = reinterpret_cast<const int*>(d_blob + cb.o_sre);
+    A.sel_im = reinterpret_cast<const int*>(d_blob + cb.o_sim);
+    A.sel_kind = reinterpret_cast<const int*>(d_blob + cb.o_skind);
+    A.ev_kind = o->event_kind;
+    A.n_ev = o->event_kind == OBE_EVENT_POPULATION ? o->n_event_indices : 0;
+    A.ev_idx = reinterpret_cast<const int*>(d_blob + cb.o_evidx);
+    A.ev_thr = o->event_threshold;
+    A.ev_len = cb.ev_len;
+    A.ev_op = reinterpret_cast<const int32_t*>(d_blob + cb.o_evop);
+    A.ev_arg = reinterpret_cast<const int32_t*>(d_blob + cb.o_evarg);
+    A.ev_fn = reinterpret_cast<const int32_t*>(d_blob + cb.o_evfn);
+    A.ev_val = reinterpret_cast<const double*>(d_blob + cb.o_evval);
+}
+
+cudaError_t launch_integrate(const obe_plan* p, const CallArgs& A, bool mixed, int solver, const LaunchShape& s, cudaStream_t st) {
+    const int method = solver == OBE_SOLVER_TSIT5 ? 1 : 0;
+    return mixed ? dispatch_shape<true>(p->dev, A, s, method, st) : dispatch_shape<false>(p->dev, A, s, method, st);
+}
+
+obe_status check_params(const obe_plan* p, int32_t n_param, const int64_t* slots) {
+    if (n_param > kMaxParams) {
+        set_error("too many scanned parameter slots for the GPU solver");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    for (int k = 0; k < n_param; ++k) {
+        if (slots[k] < 0 || slots[k] >= p->n_base) {
+            set_error("parameter override slot " + std::to_string(slots[k]) + " is not a base parameter slot");
+            return OBE_ERR_TRAJECTORY;
+        }
+        if (p->base_is_tuple[slots[k]]) {
+            set_error("scanning a tuple-valued parameter is not supported by the GPU solver");
+            return OBE_ERR_UNSUPPORTED;
+        }
+    }
+    return OBE_OK;
+}
+
+// Common device path: everything already on the device except the call blob, which goes into
+// the front of the plan's scratch.  Stats and errors land in d_stats / d_errs.
+obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_traj, const double* d_rho0, long long rho0_stride,
+                        int32_t n_param, const int64_t* param_slots, const double* d_param_values, int n_axes,
+                        const int64_t* axis_len, const double* d_axes, long long cap, long long out_stride, double* d_values,
+                        double* d_times, obe_traj_stats* d_stats, TrajErr* d_errs, unsigned char* d_blob_area,
+                        const CallBlob& cb, const std::vector<double>& save_times, unsigned long long* d_counter,
+                        cudaStream_t stream) {
+    CallArgs A;
+    fill_call_args(A, o, save_times, cb, d_blob_area);
+    A.n_traj = n_traj;
+    A.rho0 = d_rho0;
+    A.rho0_stride = rho0_stride;
+    A.n_param = n_param;
+    for (int k = 0; k < n_param; ++k) A.param_slot[k] = static_cast<int>(param_slots[k]);
+    A.param_values = d_param_values;
+    A.n_axes = n_axes;
+    if (n_axes > 0) {
+        long long off = 0, stride = 1;
+        for (int k = n_axes - 1; k >= 0; --k) { A.axis_stride[k] = stride; stride *= axis_len[k]; }
+        for (int k = 0; k < n_axes; ++k) { A.axis_len[k] = axis_len[k]; A.axis_off[k] = off; off += axis_len[k]; }
+    }
+    A.axes = d_axes;
+    A.cap = cap;
+    A.out_stride = out_stride;
+    A.values = d_values;
+    A.times = d_times;
+    A.stats = d_stats;
+    A.errs = d_errs;
+    A.counter = d_counter;
+    LaunchShape s;
+    obe_status st = plan_launch(p, o->precision == OBE_PRECISION_MIXED, n_traj, &s);
+    if (st != OBE_OK) return st;
+    if (!cuda_ok(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync")) return OBE_ERR_CUDA;
+    if (!cuda_ok(launch_integrate(p, A, o->precision == OBE_PRECISION_MIXED, o->solver, s, stream), "kernel launch")) return OBE_ERR_CUDA;
+    g_launches += 1;
+    return OBE_OK;
+}
+
+std::mutex g_plan_mutex;  // a plan's scratch is shared by the host-pointer entry points
+
+}  // namespace
+}  // namespace obe
+
+using namespace obe;
+
+struct obe_result {
+    std::vector<double> times, values;
+    int64_t width = 0;
+    int32_t is_complex = 0;
+    obe_traj_stats stats{};
+};
+
+extern "C" {
+
+int32_t obe_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+int64_t obe_last_launch_count(void) { return g_launches; }
+
+void obe_plan_destroy(obe_plan* plan) {
+    if (!plan) return;
+    if (plan->d_blob) cudaFree(plan->d_blob);
+    if (plan->d_scratch) cudaFree(plan->d_scratch);
+    if (plan->d_counter) cudaFree(plan->d_counter);
+    delete plan;
+}
+
+static obe_status ensure_ready(obe_plan* p) {
+    if (obe_device_count() <= 0) {
+        set_error("no CUDA device is available: the GB300 solver has no CPU fallback");
+        return OBE_ERR_CUDA;
+    }
+    obe_status st = upload_plan(p);
+    if (st != OBE_OK) return st;
+    if (!p->d_counter && !cuda_ok(cudaMalloc(&p->d_counter, 64), "cudaMalloc(counter)")) return OBE_ERR_CUDA;
+    return OBE_OK;
+}
+
+obe_status obe_solve_batch_device(const obe_plan* plan_c, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
+                                  int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values,
+                                  int64_t time_count, int64_t width, double* d_values, obe_traj_stats* d_stats, void* stream) {
+    g_launches = 0;
+    obe_plan* p = const_cast<obe_plan*>(plan_c);
+    if (!p || !opt) { set_error("null argument"); return OBE_ERR_INVALID; }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    obe_status st = ensure_ready(p);
+    if (st != OBE_OK) return st;
+    if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
+    std::vector<double> save_times;
+    CallBlob cb;
+    int64_t w = 0;
+    int cplx = 0;
+    if ((st = validate_options(p, opt, save_times, cb, &w, &cplx)) != OBE_OK) return st;
+    if (w != width) { set_error("output width mismatch"); return OBE_ERR_INVALID; }
+    size_t errs_off = align16(cb.bytes.size());
+    size_t need = errs_off + sizeof(TrajErr) * static_cast<size_t>(std::max<int64_t>(n_traj, 1));
+    unsigned char* d = nullptr;
+    if ((st = scratch(p, need, &d)) != OBE_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!cuda_ok(cudaMemcpyAsync(d, cb.bytes.data(), cb.bytes.size(), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(args)")) return OBE_ERR_CUDA;
+    return solve_device(p, opt, n_traj, d_rho0, p->N, n_param_slots, param_slots, d_param_values, 0, nullptr, nullptr, time_count,
+                        time_count * width * (cplx ? 2 : 1), d_values, nullptr, d_stats, reinterpret_cast<TrajErr*>(d + errs_off), d,
+                        cb, save_times, static_cast<unsigned long long*>(p->d_counter), s);
+}
+
+// Host-pointer batch/grid/single driver.
+static obe_status solve_host(obe_plan* p, const obe_solve_options* o, long long n_traj, const double* rho0, long long rho0_stride,
+                             int32_t n_param, const int64_t* param_slots, const double* param_values, int n_axes,
+                             const int64_t* axis_slots, const int64_t* axis_len, const double* axes, long long time_count,
+                             int64_t width, double* values, obe_traj_stats* stats_out, double* times_out, bool single,
+                             std::vector<obe_traj_stats>* stats_vec) {
+    g_launches = 0;
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    obe_status st = ensure_ready(p);
+    if (st != OBE_OK) return st;
+    if (n_axes > 0) {
+        if ((st = check_params(p, n_axes, axis_slots)) != OBE_OK) return st;
+    } else if ((st = check_params(p, n_param, param_slots)) != OBE_OK) {
+        return st;
+    }
+    std::vector<double> save_times;
+    CallBlob cb;
+    int64_t w = 0;
+    int cplx = 0;
+    if ((st = validate_options(p, o, save_times, cb, &w, &cplx)) != OBE_OK) return st;
+    if (w != width) { set_error("output width mismatch"); return OBE_ERR_INVALID; }
+    if (o->maxiters <= 0) {
+        set_error(single ? "maxiters must be positive" : "trajectory 0: maxiters must be positive");
+        return single ? OBE_ERR_INVALID : OBE_ERR_TRAJECTORY;
+    }
+    if (o->t1 < o->t0) {
+        set_error(single ? "only forward integration" : "trajectory 0: only forward integration");
+        return single ? OBE_ERR_INVALID : OBE_ERR_TRAJECTORY;
+    }
+    const long long per = time_count * width * (cplx ? 2 : 1);
+    const size_t n_rho = static_cast<size_t>(rho0_stride ? n_traj * p->N : p->N);
+    const size_t n_pv = param_values ? static_cast<size_t>(n_traj * n_param * 2) : 0;
+    size_t n_ax = 0;
+    for (int k = 0; k < n_axes; ++k) n_ax += static_cast<size_t>(axis_len[k]);
+    // scratch layout: call blob | errs | stats | rho0 | params | axes | values | times
+    size_t off = align16(cb.bytes.size());
+    size_t o_errs = off; off = align16(off + sizeof(TrajErr) * n_traj);
+    size_t o_stats = off; off = align16(off + sizeof(obe_traj_stats) * n_traj);
+    size_t o_rho = off; off = align16(off + 8 * n_rho);
+    size_t o_pv = off; off = align16(off + 8 * n_pv);
+    size_t o_ax = off; off = align16(off + 16 * n_ax);
+    size_t o_val = off; off = align16(off + 8 * static_cast<size_t>(n_traj * per));
+    size_t o_tim = off; off = align16(off + (single ? 8 * static_cast<size_t>(time_count) : 0));
+    unsigned char* d = nullptr;
+    if ((st = scratch(p, off, &d)) != OBE_OK) return st;
+    cudaStream_t s = nullptr;
+    if (!cuda_ok(cudaMemcpyAsync(d, cb.bytes.data(), cb.bytes.size(), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(args)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyAsync(d + o_rho, rho0, 8 * n_rho, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(rho0)")) return OBE_ERR_CUDA;
+    if (n_pv && !cuda_ok(cudaMemcpyAsync(d + o_pv, param_values, 8 * n_pv, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(params)")) return OBE_ERR_CUDA;
+    if (n_ax && !cuda_ok(cudaMemcpyAsync(d + o_ax, axes, 16 * n_ax, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(axes)")) return OBE_ERR_CUDA;
+    std::vector<int64_t> slots_v;
+    if (n_axes > 0) slots_v.assign(axis_slots, axis_slots + n_axes);
+    else if (n_param > 0) slots_v.assign(param_slots, param_slots + n_param);
+    st = solve_device(p, o, n_traj, reinterpret_cast<double*>(d + o_rho), rho0_stride ? p->N : 0,
+                      n_axes > 0 ? n_axes : n_param, slots_v.data(), n_pv ? reinterpret_cast<double*>(d + o_pv) : nullptr,
+                      n_axes, axis_len, n_ax ? reinterpret_cast<double*>(d + o_ax) : nullptr, time_count, per,
+                      reinterpret_cast<double*>(d + o_val), single ? reinterpret_cast<double*>(d + o_tim) : nullptr,
+                      reinterpret_cast<obe_traj_stats*>(d + o_stats), reinterpret_cast<TrajErr*>(d + o_errs), d, cb, save_times,
+                      static_cast<unsigned long long*>(p->d_counter), s);
+    if (st != OBE_OK) return st;
+    std::vector<obe_traj_stats> stats(static_cast<size_t>(n_traj));
+    std::vector<TrajErr> errs(static_cast<size_t>(n_traj));
+    if (!cuda_ok(cudaMemcpyAsync(values, d + o_val, 8 * static_cast<size_t>(n_traj * per), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(values)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyAsync(stats.data(), d + o_stats, sizeof(obe_traj_stats) * n_traj, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(stats)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyAsync(errs.data(), d + o_errs, sizeof(TrajErr) * n_traj, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(errs)")) return OBE_ERR_CUDA;
+    if (single && times_out && !cuda_ok(cudaMemcpyAsync(times_out, d + o_tim, 8 * static_cast<size_t>(time_count), cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync(times)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaStreamSynchronize(s), "kernel execution")) return OBE_ERR_CUDA;
+    for (long long b = 0; b < n_traj; ++b) {
+        int code = stats[b].status;
+        if (code == ST_OK && !single && stats[b].n_points != time_count) {
+            code = ST_POINTS;
+            errs[b].a = time_count;
+            errs[b].b = stats[b].n_points;
+        }
+        if (code != ST_OK) {
+            set_error(single ? traj_message(code, errs[b]) : "trajectory " + std::to_string(b) + ": " + traj_message(code, errs[b]));
+            return single ? OBE_ERR_INVALID : OBE_ERR_TRAJECTORY;
+        }
+    }
+    if (stats_out) std::memcpy(stats_out, stats.data(), sizeof(obe_traj_stats) * n_traj);
+    if (stats_vec) *stats_vec = std::move(stats);
+    set_error("");
+    return OBE_OK;
+}
+
+obe_status obe_solve_batch(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj, const double* rho0,
+                           int32_t n_param_slots, const int64_t* param_slots, const double* param_values, int64_t time_count,
+                           int64_t width, double* values, obe_traj_stats* stats) {
+    if (!plan || !opt || !rho0 || !values || n_traj <= 0) { set_error("invalid batch arguments"); return OBE_ERR_INVALID; }
+    return solve_host(const_cast<obe_plan*>(plan), opt, n_traj, rho0, 1, n_param_slots, param_slots, param_values, 0, nullptr,
+                      nullptr, nullptr, time_count, width, values, stats, nullptr, false, nullptr);
+}
+
+obe_status obe_solve_grid(const obe_plan* plan, const obe_solve_options* opt, const double* rho0, int32_t n_axes,
+                          const int64_t* axis_slots, const int64_t* axis_lengths, const double* axes, int64_t time_count,
+                          int64_t width, double* values, obe_traj_stats* stats) {
+    if (!plan || !opt || !rho0 || !values) { set_error("invalid grid arguments"); return OBE_ERR_INVALID; }
+    if (n_axes <= 0) { set_error("parameter grid must contain at least one axis"); return OBE_ERR_INVALID; }
+    if (n_axes > kMaxParams) { set_error("too many grid axes for the GPU solver"); return OBE_ERR_UNSUPPORTED; }
+    long long count = 1;
+    for (int k = 0; k < n_axes; ++k) {
+        if (axis_lengths[k] <= 0) { set_error("parameter grid axes must be non-empty"); return OBE_ERR_INVALID; }
+        count *= axis_lengths[k];
+    }
+    return solve_host(const_cast<obe_plan*>(plan), opt, count, rho0, 0, 0, nullptr, nullptr, n_axes, axis_slots, axis_lengths,
+                      axes, time_count, width, values, stats, nullptr, false, nullptr);
+}
+
+obe_status obe_solve_single(const obe_plan* plan, const obe_solve_options* opt, const double* rho0, obe_result** out_result) {
+    if (!plan || !opt || !rho0 || !out_result) { set_error("invalid single-solve arguments"); return OBE_ERR_INVALID; }
+    *out_result = nullptr;
+    obe_plan* p = const_cast<obe_plan*>(plan);
+    int32_t cplx = opt->output == OBE_OUTPUT_SELECTED;
+    int64_t width = opt->output == OBE_OUTPUT_POPULATIONS ? p->n : opt->output == OBE_OUTPUT_FULL ? p->N
+                  : opt->output == OBE_OUTPUT_SELECTED ? opt->n_selected : 1;
+    long long cap = opt->has_saveat ? opt->n_saveat + 2 : 4096;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        auto* r = new obe_result();
+        r->width = width;
+        r->is_complex = cplx;
+        r->values.assign(static_cast<size_t>(cap * width * (cplx ? 2 : 1)), 0.0);
+        r->times.assign(static_cast<size_t>(cap), 0.0);
+        std::vector<obe_traj_stats> stv;
+        // single solves run with time_count = capacity and accept any point count up to it
+        obe_solve_options o = *opt;
+        obe_status st = solve_host(p, &o, 1, rho0, 0, 0, nullptr, nullptr, 0, nullptr, nullptr, nullptr, cap, width,
+                                   r->values.data(), nullptr, r->times.data(), true, &stv);
+        if (st != OBE_OK) {
+            delete r;
+            return st;
+        }
+        long long pts = stv[0].n_points;
+        if (pts <= cap) {
+            r->times.resize(static_cast<size_t>(pts));
+            r->values.resize(static_cast<size_t>(pts * width * (cplx ? 2 : 1)));
+            r->stats = stv[0];
+            *out_result = r;
+            return OBE_OK;
+        }
+        delete r;
+        cap = pts + 1;
+    }
+    set_error("single solve output did not fit after repeated growth");
+    return OBE_ERR_INVALID;
+}
+
+void obe_result_shape(const obe_result* res, int64_t* n_times, int64_t* width, int32_t* is_complex) {
+    if (n_times) *n_times = res ? static_cast<int64_t>(res->times.size()) : 0;
+    if (width) *width = res ? res->width : 0;
+    if (is_complex) *is_complex = res ? res->is_complex : 0;
+}
+
+void obe_result_stats(const obe_result* res, obe_traj_stats* stats) {
+    if (res && stats) *stats = res->stats;
+}
+
+void obe_result_copy(const obe_result* res, double* times, double* values) {
+    if (!res) return;
+    if (times && !res->times.empty()) std::memcpy(times, res->times.data(), res->times.size() * 8);
+    if (values && !res->values.empty()) std::memcpy(values, res->values.data(), res->values.size() * 8);
+}
+
+void obe_result_destroy(obe_result* res) { delete res; }
+
+obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, const double* y, int32_t n_override_slots,
+                        const int64_t* override_slots, const double* override_values, int32_t precision, double* dy) {
+    g_launches = 0;
+    obe_plan* p = const_cast<obe_plan*>(plan);
+    if (!p || !t || !y || !dy || count <= 0) { set_error("invalid RHS arguments"); return OBE_ERR_INVALID; }
+    if (!p->has_expanded) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    obe_status st = ensure_ready(p);
+    if (st != OBE_OK) return st;
+    if ((st = check_params(p, n_override_slots, override_slots)) != OBE_OK) return st;
+    const bool mixed = precision == OBE_PRECISION_MIXED;
+    LaunchShape s;
+    if ((st = plan_launch(p, mixed, count, &s)) != OBE_OK) return st;
+    std::vector<int32_t> slots(override_slots, override_slots + n_override_slots);
+    size_t off = 0;
+    size_t o_t = off; off = align16(off + 8 * count);
+    size_t o_y = off; off = align16(off + 8 * count * p->N);
+    size_t o_dy = off; off = align16(off + 8 * count * p->N);
+    size_t o_sl = off; off = align16(off + 4 * std::max<size_t>(slots.size(), 1));
+    size_t o_ov = off; off = align16(off + 16 * count * std::max<int32_t>(n_override_slots, 1));
+    unsigned char* d = nullptr;
+    if ((st = scratch(p, off, &d)) != OBE_OK) return st;
+    cudaMemcpy(d + o_t, t, 8 * count, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + o_y, y, 8 * count * p->N, cudaMemcpyHostToDevice);
+    if (n_override_slots > 0) {
+        cudaMemcpy(d + o_sl, slots.data(), 4 * slots.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(d + o_ov, override_values, 16 * count * n_override_slots, cudaMemcpyHostToDevice);
+    }
+    auto run = [&](auto kernel) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s.smem));
+        kernel<<<s.blocks, s.gpb * s.tpt, s.smem>>>(p->dev, count, reinterpret_cast<double*>(d + o_t), reinterpret_cast<double*>(d + o_y),
+                                                    n_override_slots, reinterpret_cast<int*>(d + o_sl), reinterpret_cast<double*>(d + o_ov),
+                                                    reinterpret_cast<double*>(d + o_dy), s.gpb, s.group_bytes);
+    };
+    if (s.tpt == 32) mixed ? run(rhs_kernel<32, true>) : run(rhs_kernel<32, false>);
+    else if (s.tpt == 64) mixed ? run(rhs_kernel<64, true>) : run(rhs_kernel<64, false>);
+    else mixed ? run(rhs_kernel<128, true>) : run(rhs_kernel<128, false>);
+    g_launches += 1;
+    if (!cuda_ok(cudaGetLastError(), "rhs kernel launch")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpy(dy, d + o_dy, 8 * count * p->N, cudaMemcpyDeviceToHost), "rhs kernel")) return OBE_ERR_CUDA;
+    set_error("");
+    return OBE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+"""The C-ABI library loads, exports every entry point include/obe_gb300.h declares, and packs
+plans on the host (no GPU needed for any of this)."""
+
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from centrex_tlf_gb300 import _abi
+from centrex_tlf_gb300 import centrex_tlf_rust as api
+from centrex_tlf_gb300.native import NativePlan
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "obe_gb300.h"
+
+
+def declared_functions() -> list[str]:
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(obe_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _abi.load_library()
+    names = declared_functions()
+    assert "obe_solve_batch" in names and "obe_plan_create" in names
+    for name in names:
+        assert hasattr(lib, name), f"{name} is declared in include/obe_gb300.h but not exported"
+    assert lib.obe_abi_version() == 1
+
+
+def test_struct_layouts_match_header_sizes():
+    # obe_traj_stats: 3*i64 + 2*i32 + f64 + i64
+    assert ctypes.sizeof(_abi.ObeTrajStats) == 48
+    assert _abi.TRAJ_STATS_DTYPE.itemsize == 48
+
+
+@pytest.mark.parametrize("name", ["two_level", "two_level_td", "chain3", "chain45", "q1_16"])
+def test_plans_pack_on_host(golden, name):
+    payload = golden(f"plan_{name}")["payload"]
+    plan = NativePlan(payload)
+    n = payload["n_states"]
+    assert plan.n_states == n
+    assert plan.lib.obe_plan_packed_len(plan.handle) == n * n
+
+
+def _payload(golden):
+    import copy
+
+    return copy.deepcopy(golden("plan_two_level")["payload"])
+
+
+def test_payload_validation_messages_match_reference(golden):
+    """plan.rs:1096-1150 messages."""
+    p = _payload(golden)
+    p["expanded_rhs_plan"]["output_ptrs"] = list(p["expanded_rhs_plan"]["output_ptrs"])[:-1]
+    with pytest.raises(ValueError, match="expanded RHS output_ptrs must have length 4, got 3"):
+        api.prepare_lindblad_problem_py(p)
+    p = _payload(golden)
+    p["expanded_rhs_plan"]["input_indices"] = [7] + list(p["expanded_rhs_plan"]["input_indices"])[1:]
+    with pytest.raises(ValueError, match="expanded RHS input index 7 out of bounds for upper length 3"):
+        api.prepare_lindblad_problem_py(p)
+    p = _payload(golden)
+    p["expanded_rhs_plan"]["n"] = 5
+    with pytest.raises(ValueError, match="expanded RHS dimension 5 does not match n_states 2"):
+        api.prepare_lindblad_problem_py(p)
+    p = _payload(golden)
+    p["expanded_rhs_plan"]["kind"] = "dense"
+    with pytest.raises(ValueError, match="unknown expanded RHS plan kind: dense"):
+        api.prepare_lindblad_problem_py(p)
+    p = _payload(golden)
+    del p["parameter_graph"]
+    with pytest.raises(KeyError, match='missing key "parameter_graph"'):
+        api.prepare_lindblad_problem_py(p)
+    p = _payload(golden)
+    p["hamiltonian_plan"]["kind"] = "magic"
+    with pytest.raises(ValueError, match="unknown hamiltonian kind: magic"):
+        api.prepare_lindblad_problem_py(p)
+    p = _payload(golden)
+    p["expanded_rhs_plan"]["coeff_indices"] = [3] * len(p["expanded_rhs_plan"]["coeff_indices"])
+    with pytest.raises(ValueError, match="expanded RHS coefficient index 3 out of bounds for 2 coefficients"):
+        api.prepare_lindblad_problem_py(p)
+
+
+def test_argument_validation_before_any_device_work(golden):
+    d = golden("plan_two_level")
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    rho0 = d["rho0_packed"]
+    with pytest.raises(ValueError, match='unsupported execution mode "nope"'):
+        api.solve_lindblad_ode_py(plan, rho0, 0.0, 1.0, 1e-8, 1e-6, 1e-3, mode="nope")
+    with pytest.raises(NotImplementedError):
+        api.solve_lindblad_ode_py(plan, rho0, 0.0, 1.0, 1e-8, 1e-6, 1e-3, mode="structured")
+    with pytest.raises(ValueError, match=r"solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4', got \"rk45\""):
+        api.solve_lindblad_ode_py(plan, rho0, 0.0, 1.0, 1e-8, 1e-6, 1e-3, solver="rk45")
+    with pytest.raises(ValueError, match="output='selected' requires output_indices"):
+        api.solve_lindblad_ode_py(plan, rho0, 0.0, 1.0, 1e-8, 1e-6, 1e-3, output="selected")
+    with pytest.raises(ValueError, match="output='photon_integral' requires integral_weights"):
+        api.solve_lindblad_ode_py(plan, rho0, 0.0, 1.0, 1e-8, 1e-6, 1e-3, output="photon_integral")
+    with pytest.raises(ValueError, match="packed_rho0_batch must be 2D"):
+        api.solve_lindblad_batch_ode_py(plan, rho0, 0.0, 1.0, 1e-8, 1e-6, 1e-3)
+    with pytest.raises(ValueError, match="rho0 dim mismatch: 3 vs 4"):
+        api.solve_lindblad_batch_ode_py(plan, np.zeros((2, 3)), 0.0, 1.0, 1e-8, 1e-6, 1e-3)
+    with pytest.raises(ValueError, match="parameter_batch shape mismatch"):
+        api.solve_lindblad_batch_ode_py(plan, np.zeros((2, 4)), 0.0, 1.0, 1e-8, 1e-6, 1e-3,
+                                        parameter_slot_indices=[0], parameter_batch=np.zeros((3, 1), complex))
+    with pytest.raises(ValueError, match="parameter grid axes must be non-empty"):
+        api.solve_lindblad_grid_ode_py(plan, rho0, 0.0, 1.0, 1e-8, 1e-6, 1e-3, [0], np.zeros(0, complex), [0])
+    with pytest.raises(ValueError, match=r"saveat value 2 is outside \[0, 1\]"):
+        api.solve_lindblad_batch_ode_py(plan, np.zeros((1, 4)), 0.0, 1.0, 1e-8, 1e-6, 1e-3,
+                                        saveat=np.array([0.5, 2.0]), output_when="saveat")
+
+
+def test_no_cpu_fallback_without_gpu(golden):
+    """Without a CUDA device the solver refuses instead of computing on the CPU."""
+    if _abi.load_library().obe_device_count() > 0:
+        pytest.skip("a GPU is present")
+    d = golden("plan_two_level")
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    with pytest.raises(RuntimeError, match="no CUDA device"):
+        api.solve_lindblad_ode_py(plan, d["rho0_packed"], 0.0, 0.5, 1e-10, 1e-8, 1e-3)
+
+
+def test_layout_roundtrip():
+    from centrex_tlf_gb300.lindblad import PackedHermitianLayout
+
+    layout = PackedHermitianLayout(3)
+    rho = np.array([[0.2, 0.1 + 0.3j, -0.4j], [0.1 - 0.3j, 0.5, 0.2 - 0.1j], [0.4j, 0.2 + 0.1j, 0.3]])
+    packed = layout.pack(rho)
+    assert packed[3] == 0.1 and packed[4] == 0.3 and packed[5] == 0.0 and packed[6] == -0.4
+    np.testing.assert_allclose(layout.unpack(packed), rho)
