@@ -305,12 +305,118 @@ __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __r
     }
 }
 
+// Mixed (deviation) form layout of one trajectory group: the stage derivatives are kept as
+// deviations d_j = k_j - k_1 in single precision, k_1 in double.  Both the stage inputs and the
+// embedded error estimate are then sums of the d_j (the k_1 parts cancel exactly, because the
+// tableau's error weights sum to zero and a_sj sums to c_s), so single-precision rounding of
+// the RHS no longer feeds noise into the step-size controller.
+struct DevLayout {
+    size_t tab64, tab32, dtab32, Df, Yf, yg64, K32, k1, k1f, ybuf, cstat, cdyn, red, traj, bytes;
+};
+
+__host__ __device__ inline DevLayout group_layout_dev(int N, int n_formula, int n_coeff, int n_dyn, int tpt) {
+    DevLayout L;
+    size_t o = 0;
+    L.tab64 = o; o = align16(o + (1 + n_formula) * 16);
+    L.tab32 = o; o = align16(o + (1 + n_formula) * 8);
+    L.dtab32 = o; o = align16(o + (1 + n_formula) * 8);
+    L.Df = o; o = align16(o + static_cast<size_t>(N) * 4);
+    L.Yf = o; o = align16(o + static_cast<size_t>(N) * 4);
+    L.yg64 = o; o = align16(o + static_cast<size_t>(N) * 8);
+    L.K32 = o; o = align16(o + 6 * static_cast<size_t>(N) * 4);
+    L.k1 = o; o = align16(o + static_cast<size_t>(N) * 8);
+    L.k1f = o; o = align16(o + static_cast<size_t>(N) * 4);
+    L.ybuf = o; o = align16(o + static_cast<size_t>(N) * 8);
+    L.cstat = o; o = align16(o + static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
+    L.cdyn = o; o = align16(o + 6 * static_cast<size_t>(n_dyn > 0 ? n_dyn : 1) * 16);
+    L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
+    L.traj = o; o = align16(o + 16);
+    L.bytes = o;
+    return L;
+}
+
+// Single-precision formula values at a stage time (tab32) and their change since the step's
+// start time (dtab32, from coefficient *differences*, so it keeps its relative precision).
+template <int TPT>
+__device__ __forceinline__ void fill_formulas_dev(const DevPlan& P, int lo, int hi, const double2* cstat, const double2* crow,
+                                                  const double2* crow0, float2* tab32, float2* dtab32, int lt) {
+    for (int f = lo + lt; f < hi; f += TPT) {
+        int a = P.formula_ptr[f - 1], b = P.formula_ptr[f];
+        float2 acc = make_float2(0.f, 0.f), dacc = make_float2(0.f, 0.f);
+        for (int p = a; p < b; ++p) {
+            float fr = P.prod_factor32[2 * p], fi = P.prod_factor32[2 * p + 1];
+            int cls = P.prod_class[p];
+            if (cls < 0) {
+                acc.x += fr;
+                acc.y += fi;
+                continue;
+            }
+            int k = cls >> 1;
+            int pos = P.coeff_dyn_pos[k];
+            double2 c = pos >= 0 ? crow[pos] : cstat[k];
+            double2 c0 = pos >= 0 ? crow0[pos] : c;
+            double dre = c.x - c0.x, dim = c.y - c0.y;
+            if (cls & 1) { c.y = -c.y; dim = -dim; }
+            float cr = static_cast<float>(c.x), ci = static_cast<float>(c.y);
+            float dr = static_cast<float>(dre), di = static_cast<float>(dim);
+            acc.x += fr * cr - fi * ci;
+            acc.y += fr * ci + fi * cr;
+            dacc.x += fr * dr - fi * di;
+            dacc.y += fr * di + fi * dr;
+        }
+        tab32[f] = acc;
+        dtab32[f] = dacc;
+    }
+}
+
+// Stage deviation d_s = L(t_s) (y_s - y_n) + (L(t_s) - L(t_n)) y_n, all in single precision.
+template <int TPT>
+__device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
+                                           const float2* tab32, const float2* dtab32, const float* Df, const float* Yf,
+                                           float* K, int lt) {
+    float ar = 0.f, ai = 0.f;
+    int o = 0;
+    const int n_iter = P.n_iter;
+#pragma unroll 4
+    for (int it = 0; it < n_iter; ++it) {
+        uint32_t w = s_rec[it * TPT + lt];
+        int in = static_cast<int>(w & kRecIndexMask);
+        int f = static_cast<int>(w >> kRecCoefShift);
+        float2 c = tab32[f];
+        float2 dc = dtab32[f];
+        float dr = Df[in], yr = Yf[in];
+        float di = 0.f, yi = 0.f;
+        if (w & kRecComplex) { di = Df[in + 1]; yi = Yf[in + 1]; }
+        if (w & kRecConj) { di = -di; yi = -yi; }
+        ar = fmaf(c.x, dr, ar);
+        ar = fmaf(-c.y, di, ar);
+        ar = fmaf(dc.x, yr, ar);
+        ar = fmaf(-dc.y, yi, ar);
+        ai = fmaf(c.x, di, ai);
+        ai = fmaf(c.y, dr, ai);
+        ai = fmaf(dc.x, yi, ai);
+        ai = fmaf(dc.y, yr, ai);
+        if (w & kRecFlush) {
+            uint32_t d = s_out[o * TPT + lt];
+            K[d & 0xFFFFu] = ar;
+            uint32_t im = d >> 16;
+            if (im != kNoImag) K[im] = ai;
+            ar = 0.f;
+            ai = 0.f;
+            ++o;
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // the integrator kernel
+//
+// FP64 form: K_1..K_7 in double, each stage a full double RHS.
+// Mixed form: k_1 = f(t_n, y_n) in double (recomputed at every accepted step, which equals
+// the reference's FSAL k_7 up to rounding), stage deviations d_2..d_7 in single precision.
 
 template <int TPT, int EPT, bool MIXED>
 __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
-    using RT = std::conditional_t<MIXED, float, double>;
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
@@ -327,17 +433,53 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
     __syncthreads();
     if (g >= gpb) return;
 
-    const GroupLayout Lay = group_layout(N, P.n_formula, P.n_coeff, P.n_dyn, TPT, MIXED);
     unsigned char* gb = smem + plan_smem_bytes(P.n_iter, P.n_out, TPT) + static_cast<size_t>(g) * group_bytes;
-    void* s_tab = gb + Lay.tab;
-    RT* s_yg = reinterpret_cast<RT*>(gb + Lay.yg);
-    RT* s_K = reinterpret_cast<RT*>(gb + Lay.K);
-    double* s_ybuf = reinterpret_cast<double*>(gb + Lay.ybuf);
-    double2* s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
-    double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
-    double* s_red = reinterpret_cast<double*>(gb + Lay.red);
-    long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
+    // FP64-form buffers
+    double2* s_tab = nullptr;  // formula table (double)
+    double* s_yg = nullptr;    // gather input (double)
+    double* s_K = nullptr;     // K_1..K_7
+    // mixed-form buffers
+    float2* s_tab32 = nullptr;
+    float2* s_dtab32 = nullptr;
+    float* s_Df = nullptr;
+    float* s_Yf = nullptr;
+    float* s_K32 = nullptr;    // d_2..d_7 in slots 0..5
+    double* s_k1 = nullptr;
+    float* s_k1f = nullptr;
+    double* s_ybuf;
+    double2* s_cstat;
+    double2* s_cdyn;
+    double* s_red;
+    long long* s_traj;
+    if constexpr (MIXED) {
+        const DevLayout Lay = group_layout_dev(N, P.n_formula, P.n_coeff, P.n_dyn, TPT);
+        s_tab = reinterpret_cast<double2*>(gb + Lay.tab64);
+        s_yg = reinterpret_cast<double*>(gb + Lay.yg64);
+        s_tab32 = reinterpret_cast<float2*>(gb + Lay.tab32);
+        s_dtab32 = reinterpret_cast<float2*>(gb + Lay.dtab32);
+        s_Df = reinterpret_cast<float*>(gb + Lay.Df);
+        s_Yf = reinterpret_cast<float*>(gb + Lay.Yf);
+        s_K32 = reinterpret_cast<float*>(gb + Lay.K32);
+        s_k1 = reinterpret_cast<double*>(gb + Lay.k1);
+        s_k1f = reinterpret_cast<float*>(gb + Lay.k1f);
+        s_ybuf = reinterpret_cast<double*>(gb + Lay.ybuf);
+        s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
+        s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
+        s_red = reinterpret_cast<double*>(gb + Lay.red);
+        s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
+    } else {
+        const GroupLayout Lay = group_layout(N, P.n_formula, P.n_coeff, P.n_dyn, TPT, false);
+        s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
+        s_yg = reinterpret_cast<double*>(gb + Lay.yg);
+        s_K = reinterpret_cast<double*>(gb + Lay.K);
+        s_ybuf = reinterpret_cast<double*>(gb + Lay.ybuf);
+        s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
+        s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
+        s_red = reinterpret_cast<double*>(gb + Lay.red);
+        s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
+    }
     const int nd = P.n_dyn > 0 ? P.n_dyn : 1;
+    const int S = P.n_static_formula, F = P.n_formula;
 
     LaneSlots L;  // meaningful in lanes 0..5 (the VM lanes)
 
@@ -358,13 +500,22 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             for (int k = 0; k < P.n_coeff; ++k)
                 s_cstat[k] = P.coeff_dynamic[k] ? make_double2(0.0, 0.0) : eval_expr(P, P.coeff_expr[k], L, t0);
             for (int j = 0; j < P.n_dyn; ++j) s_cdyn[5 * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t0);
-        }
-        if (lt == 0) {
-            if constexpr (MIXED) reinterpret_cast<float2*>(s_tab)[0] = make_float2(0.f, 0.f);
-            else reinterpret_cast<double2*>(s_tab)[0] = make_double2(0.0, 0.0);
+            s_tab[0] = make_double2(0.0, 0.0);
+            if constexpr (MIXED) {
+                s_tab32[0] = make_float2(0.f, 0.f);
+                s_dtab32[0] = make_float2(0.f, 0.f);
+            }
         }
         gsync<TPT>(g);
-        fill_formulas<TPT, MIXED>(P, 1, 1 + P.n_static_formula, s_cstat, s_cdyn + 5 * nd, s_tab, lt);
+        // time-independent formulas: once per trajectory
+        fill_formulas<TPT, false>(P, 1, 1 + S, s_cstat, s_cdyn + 5 * nd, s_tab, lt);
+        if constexpr (MIXED) {
+            for (int f = 1 + lt; f < 1 + S; f += TPT) {
+                double2 v = s_tab[f];
+                s_tab32[f] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+                s_dtab32[f] = make_float2(0.f, 0.f);
+            }
+        }
 
         double y[EPT], yn[EPT];
         const double* r0 = A.rho0 + traj * A.rho0_stride;
@@ -373,7 +524,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             int i = lt + e * TPT;
             y[e] = i < N ? r0[i] : 0.0;
             yn[e] = 0.0;
-            if (i < N) s_yg[i] = static_cast<RT>(y[e]);
+            if (i < N) s_yg[i] = y[e];
         }
 
         long long accepted = 0, rejected = 0, rhs_calls = 0, count = 0;
@@ -476,23 +627,27 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             has = true;
         };
 
-        // evaluate the time-dependent coefficients at t into row `row` of s_cdyn by lane `lane`
+        // evaluate the time-dependent coefficients at t into row `row` of s_cdyn (lane 0)
         auto dyn_coeffs_at = [&](double t, int row) {
             if (P.n_dyn > 0 && lt == 0) {
                 eval_compounds(P, L, t, true);
                 for (int j = 0; j < P.n_dyn; ++j) s_cdyn[row * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t);
             }
         };
-        // one RHS: formulas for the stage row, then the gather into K slot `ks`
-        auto rhs = [&](int row, int ks) {
+        // one double-precision RHS from s_yg: formulas for coefficient row `row`, gather into out
+        auto rhs64 = [&](int row, double* out) {
             gsync<TPT>(g);  // yg written, coefficient row ready
-            if (P.n_formula > P.n_static_formula)
-                fill_formulas<TPT, MIXED>(P, 1 + P.n_static_formula, 1 + P.n_formula, s_cstat, s_cdyn + row * nd, s_tab, lt);
+            if (F > S) fill_formulas<TPT, false>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
             gsync<TPT>(g);
-            gather_rhs<TPT, MIXED>(P, s_rec, s_out, s_tab, s_yg, s_K + static_cast<size_t>(ks) * N, lt);
-            gsync<TPT>(g);  // K complete, yg free
+            gather_rhs<TPT, false>(P, s_rec, s_out, s_tab, s_yg, out, lt);
+            gsync<TPT>(g);  // out complete, yg free
         };
-        auto Kat = [&](int j, int i) -> double { return static_cast<double>(s_K[static_cast<size_t>(j) * N + i]); };
+        // stage derivative j (0-based: K_1..K_7) at own element i, as double
+        auto Kat = [&](int j, int i) -> double {
+            if constexpr (MIXED) return j == 0 ? s_k1[i] : s_k1[i] + static_cast<double>(s_K32[static_cast<size_t>(j - 1) * N + i]);
+            else return s_K[static_cast<size_t>(j) * N + i];
+        };
+        double* k1_out = MIXED ? s_k1 : s_K;  // where a full double RHS for K_1 goes
 
         bool done = false;
         if (A.maxiters <= 0) {
@@ -515,16 +670,16 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             if (isfinite(A.dt) && A.dt > 0.0) {
                 h = fmin(A.dt, t1 - t0);
             } else {
-                // hinit (common.rs:72-118): f0 = f(x, y) into K slot 0, f1 into slot 1
+                // hinit (common.rs:72-118), in double: f0 into K_1's buffer, f1 into s_ybuf
                 dyn_coeffs_at(x, 5);
-                rhs(5, 0);
+                rhs64(5, k1_out);
                 double d0 = 0.0, d1 = 0.0;
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
                     if (i < N) {
                         double sci = A.atol + fabs(y[e]) * A.rtol;
-                        double f0 = Kat(0, i);
+                        double f0 = k1_out[i];
                         d0 += (y[e] / sci) * (y[e] / sci);
                         d1 += (f0 / sci) * (f0 / sci);
                     }
@@ -539,17 +694,17 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
-                    if (i < N) s_yg[i] = static_cast<RT>(y[e] + Kat(0, i) * h0);
+                    if (i < N) s_yg[i] = y[e] + k1_out[i] * h0;
                 }
                 dyn_coeffs_at(x + h0, 4);
-                rhs(4, 1);
+                rhs64(4, s_ybuf);
                 double d2 = 0.0;
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
                     if (i < N) {
                         double sci = A.atol + fabs(y[e]) * A.rtol;
-                        double df = Kat(1, i) - Kat(0, i);
+                        double df = s_ybuf[i] - k1_out[i];
                         d2 += (df / sci) * (df / sci);
                     }
                 }
@@ -560,7 +715,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
-                    if (i < N) s_yg[i] = static_cast<RT>(y[e]);
+                    if (i < N) s_yg[i] = y[e];
                 }
             }
         }
@@ -575,9 +730,23 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
         double ev_old = 0.0;
         int si = 0;
 
+        // K_1 = f(t0, y0) in double
+        auto refresh_k1 = [&](int row) {
+            rhs64(row, k1_out);
+            if constexpr (MIXED) {
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) {
+                        s_k1f[i] = static_cast<float>(s_k1[i]);
+                        s_Yf[i] = static_cast<float>(y[e]);
+                    }
+                }
+            }
+        };
         if (!done) {
             dyn_coeffs_at(x, 5);
-            rhs(5, 0);  // K1 = f(t0, y0)
+            refresh_k1(5);
             rhs_calls = 1;
             if (A.ev_kind != OBE_EVENT_NONE) {
                 stage_registers_to_buf(y);
@@ -616,41 +785,91 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                 eval_compounds(P, L, ts, true);
                 for (int j = 0; j < P.n_dyn; ++j) s_cdyn[lt * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, ts);
             }
-            // stages 2..7 (stage 7 input is the solution yn)
+            double err = 0.0;
+            if constexpr (!MIXED) {
+                // stages 2..7 (stage 7 input is the solution yn)
 #pragma unroll 1
-            for (int s = 0; s < 6; ++s) {
+                for (int s = 0; s < 6; ++s) {
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        if (i < N) {
+                            double acc = 0.0;
+#pragma unroll
+                            for (int j = 0; j < 6; ++j)
+                                if (j <= s) acc += kA[M][s][j] * Kat(j, i);
+                            double v = y[e] + h * acc;
+                            if (s == 5) yn[e] = v;
+                            s_yg[i] = v;
+                        }
+                    }
+                    rhs64(s < 4 ? s : 4, s_K + static_cast<size_t>(s + 1) * N);
+                }
+                // error norm (dopri5.rs:88-102, tsit5.rs:104-119)
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
                     if (i < N) {
+                        double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
                         double acc = 0.0;
 #pragma unroll
-                        for (int j = 0; j < 6; ++j)
-                            if (j <= s) acc += kA[M][s][j] * Kat(j, i);
-                        double v = y[e] + h * acc;
-                        if (s == 5) yn[e] = v;
-                        s_yg[i] = static_cast<RT>(v);
+                        for (int j = 0; j < 7; ++j)
+                            if (M == 1 || j != 1) acc += kE[M][j] * Kat(j, i);
+                        double ei = h * acc;
+                        double q = ei / sc;
+                        err += q * q;
                     }
                 }
-                rhs(s < 4 ? s : 4, s + 1);
-            }
-            rhs_calls += 6;
-            // error norm (dopri5.rs:88-102, tsit5.rs:104-119)
-            double err = 0.0;
+            } else {
+                const float hf = static_cast<float>(h);
+#pragma unroll 1
+                for (int s = 0; s < 6; ++s) {
+                    // stage input deviation y_s - y_n = h (c_s k_1 + sum_j a_sj d_j), in single
+                    // precision (small next to y_n); the solution y_{n+1} itself in double
+                    float csum = 0.f;
 #pragma unroll
-            for (int e = 0; e < EPT; ++e) {
-                int i = lt + e * TPT;
-                if (i < N) {
-                    double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
-                    double acc = 0.0;
+                    for (int j = 0; j < 6; ++j)
+                        if (j <= s) csum += static_cast<float>(kA[M][s][j]);
 #pragma unroll
-                    for (int j = 0; j < 7; ++j)
-                        if (M == 1 || j != 1) acc += kE[M][j] * Kat(j, i);
-                    double ei = h * acc;
-                    double q = ei / sc;
-                    err += q * q;
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        if (i < N) {
+                            float acc = 0.f;
+#pragma unroll
+                            for (int j = 1; j < 6; ++j)
+                                if (j <= s) acc += static_cast<float>(kA[M][s][j]) * s_K32[static_cast<size_t>(j - 1) * N + i];
+                            if (s == 5) {
+                                yn[e] = y[e] + h * s_k1[i] + h * static_cast<double>(acc);
+                                s_Df[i] = static_cast<float>(yn[e] - y[e]);
+                            } else {
+                                s_Df[i] = hf * (csum * s_k1f[i] + acc);
+                            }
+                        }
+                    }
+                    const int row = s < 4 ? s : 4;
+                    gsync<TPT>(g);
+                    fill_formulas_dev<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_cdyn + 5 * nd, s_tab32, s_dtab32, lt);
+                    gsync<TPT>(g);
+                    gather_dev<TPT>(P, s_rec, s_out, s_tab32, s_dtab32, s_Df, s_Yf, s_K32 + static_cast<size_t>(s) * N, lt);
+                    gsync<TPT>(g);
+                }
+                // error estimate from the deviations alone (the error weights sum to zero)
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    int i = lt + e * TPT;
+                    if (i < N) {
+                        float acc = 0.f;
+#pragma unroll
+                        for (int j = 1; j < 7; ++j)
+                            if (M == 1 || j != 1) acc += static_cast<float>(kE[M][j]) * s_K32[static_cast<size_t>(j - 1) * N + i];
+                        double ei = h * static_cast<double>(acc);
+                        double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
+                        double q = ei / sc;
+                        err += q * q;
+                    }
                 }
             }
+            rhs_calls += 6;
             err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
             // controller (common.rs:48-69)
             double fac11 = pow(err, alpha);
@@ -670,7 +889,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
                         if (i < N) {
-                            // the stage-6 input, recomputed exactly as in the stage loop
+                            // the stage-6 input, recomputed as in the stage loop
                             double acc6 = 0.0;
 #pragma unroll
                             for (int j = 0; j < 6; ++j)
@@ -797,15 +1016,24 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                     ev_time = te;
                     break;
                 }
-                // accept: y <- yn, K1 <- K7 (own elements; K7 is complete after the last sync)
+                // accept: y <- yn; K_1 <- f(t_{n+1}, y_{n+1})
+                if constexpr (!MIXED) {
 #pragma unroll
-                for (int e = 0; e < EPT; ++e) {
-                    int i = lt + e * TPT;
-                    y[e] = yn[e];
-                    if (i < N) {
-                        s_K[i] = s_K[static_cast<size_t>(6) * N + i];
-                        s_yg[i] = static_cast<RT>(y[e]);
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        y[e] = yn[e];
+                        if (i < N) s_K[i] = s_K[static_cast<size_t>(6) * N + i];
                     }
+                } else {
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        y[e] = yn[e];
+                        if (i < N) s_yg[i] = y[e];
+                    }
+                    // the coefficients at t_{n+1} = x + h are row 4; they become the step-start row
+                    if (lt < P.n_dyn) s_cdyn[5 * nd + lt] = s_cdyn[4 * nd + lt];
+                    if (!last) refresh_k1(4);
                 }
                 ev_old_has = ev_new_has;
                 ev_old = ev_new;
@@ -817,12 +1045,6 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                 last = false;
                 if (accepted >= 1) ++rejected;
                 h = hn;
-                // restore the gather buffer to the step's start state
-#pragma unroll
-                for (int e = 0; e < EPT; ++e) {
-                    int i = lt + e * TPT;
-                    if (i < N) s_yg[i] = static_cast<RT>(y[e]);
-                }
             }
             gsync<TPT>(g);
         }
@@ -1060,7 +1282,9 @@ obe_status plan_launch(const obe_plan* p, bool mixed, long long n_traj, LaunchSh
         return OBE_ERR_UNSUPPORTED;
     }
     s->ept = ept_for(P.N, s->tpt);
-    GroupLayout L = group_layout(P.N, P.n_formula, P.n_coeff, P.n_dyn, s->tpt, mixed);
+    struct { size_t bytes; } L;
+    L.bytes = mixed ? group_layout_dev(P.N, P.n_formula, P.n_coeff, P.n_dyn, s->tpt).bytes
+                    : group_layout(P.N, P.n_formula, P.n_coeff, P.n_dyn, s->tpt, false).bytes;
     s->group_bytes = L.bytes;
     size_t plan_bytes = plan_smem_bytes(P.n_iter, P.n_out, s->tpt);
     const size_t limit = 227 * 1024;
