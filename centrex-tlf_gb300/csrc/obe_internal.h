@@ -31,7 +31,7 @@ struct DevExpr {
 };
 
 // A record of the RHS gather stream.  Bits:
-//   [0, 14)  packed index of the input (its real part; the imaginary part is the next slot)
+//   [0, 14)  input slot: i for the diagonal entry rho_ii, n + m for the m-th upper pair
 //   14       complex input (off-diagonal) -- otherwise a real diagonal input
 //   15       input conjugated (negate the imaginary part)
 //   16       last record of the current output: flush the accumulator
@@ -69,6 +69,7 @@ struct DevPlan {
     const int32_t* dyn_ids;      // [n_dyn] coefficient index
     const int32_t* coeff_dyn_pos;// [n_coeff] position in dyn_ids or -1
     int32_t time_dependent;
+    int32_t max_stack;           // deepest VM stack of the plan's programs
     // PCHIP tables (plan.rs:27-116)
     int32_t n_pchip;
     const int32_t* pchip_ptr;

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <map>
 #include <numeric>
 #include <string>
@@ -65,11 +66,13 @@ std::string fmt_f64(double v) {
 
 int threads_per_trajectory_for(int32_t n) {
     int64_t N = static_cast<int64_t>(n) * n;
-    if (N <= 512) return 32;
-    if (N <= 1024) return 64;
-    if (N <= 2048) return 128;
-    if (N <= 4096) return 256;
-    return 512;
+    int t = N <= 512 ? 32 : N <= 1024 ? 64 : N <= 2048 ? 128 : N <= 4096 ? 256 : 512;
+    // OBE_TPT widens the group (64 or 128 threads per trajectory) for tuning runs
+    if (const char* env = std::getenv("OBE_TPT")) {
+        int v = std::atoi(env);
+        if ((v == 64 || v == 128) && v > t) t = v;
+    }
+    return t;
 }
 
 namespace {
@@ -444,7 +447,10 @@ obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
                 for (size_t r = 0; r < recs.size(); ++r) {
                     const Rec& rc = recs[r];
                     uint32_t fid = rc.dynamic ? static_cast<uint32_t>(1 + S + dyn_ids[rc.f]) : static_cast<uint32_t>(1 + static_ids[rc.f]);
-                    uint32_t w = static_cast<uint32_t>(rc.in_re) | (fid << kRecCoefShift);
+                    // the gather reads 16-byte input slots: diagonal i -> slot i, the (re, im)
+                    // pair at packed index r >= n -> slot n + (r - n) / 2
+                    uint32_t slot = rc.cplx ? static_cast<uint32_t>(n + (rc.in_re - n) / 2) : static_cast<uint32_t>(rc.in_re);
+                    uint32_t w = slot | (fid << kRecCoefShift);
                     if (rc.cplx) w |= kRecComplex;
                     if (rc.conj) w |= kRecConj;
                     if (r + 1 == recs.size()) w |= kRecFlush;

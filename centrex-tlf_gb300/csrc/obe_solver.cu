@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -69,6 +70,11 @@ __constant__ double kR[7][4] = {{1.0, -2.763706197274826, 2.9132554618219126, -1
                                 {0.0, 37.50931341651104, -88.1789048947664, 47.37952196281928},
                                 {0.0, -27.896526289197286, 65.09189467479366, -34.87065786149661},
                                 {0.0, 1.5, -4.0, 2.5}};
+
+// single-precision copies for the mixed form's stage and error sums
+__constant__ float kAf[2][6][6];
+__constant__ float kCsumf[2][6];  // row sums of kA (= c_s up to rounding)
+__constant__ float kEf[2][7];
 
 constexpr int kMaxWeights = 64;
 constexpr int kMaxSelected = 64;
@@ -131,22 +137,45 @@ struct CallArgs {
     obe_traj_stats* stats;
     TrajErr* errs;
     unsigned long long* counter;
+    int k1_refresh;  // mixed form: recompute k_1 in double every this many accepted steps
+    int vm_depth;    // VM stack depth of the plan's and the event's programs
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// Shared-memory layout of one trajectory group.  Gather inputs live in 16-byte slots (slot i:
+// rho_ii, slot n + m: the m-th upper pair), so one record reads one input and one coefficient.
+//   FP64 form: tab double2[1+F], G double2[U], K double[7][N]
+//   mixed form: tab double2[1+F] (k_1 refreshes), T4 float4[1+F] = (c, dc), G double2[U] (k_1
+//               refreshes), G4 float4[U] = (y_s - y_n, y_n), K32 float[6][N] (d_2..d_7),
+//               k1 double[N], k1f float[N]
+//   both: ybuf double[N] (outputs, events), VM slot and stack storage for the six VM lanes,
+//   coefficient rows, reduction scratch.
 struct GroupLayout {
-    size_t tab, yg, K, ybuf, cstat, cdyn, red, traj, bytes;
+    size_t tab, T4, cv, G, G4, K, k1, k1f, ybuf, vm_slots, vm_stack, vm_tup, cstat, cdyn, red, traj, bytes;
 };
 
-__host__ __device__ inline GroupLayout group_layout(int N, int n_formula, int n_coeff, int n_dyn, int tpt, bool mixed) {
-    size_t rs = mixed ? 4 : 8;
-    GroupLayout L;
+__host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula, int n_coeff, int n_dyn, int n_slots,
+                                                    int vm_depth, int tpt, bool mixed) {
+    const size_t U = static_cast<size_t>(n) * (n + 1) / 2;
+    GroupLayout L{};
     size_t o = 0;
-    L.tab = o; o = align16(o + (1 + n_formula) * 2 * rs);
-    L.yg = o; o = align16(o + static_cast<size_t>(N) * rs);
-    L.K = o; o = align16(o + 7 * static_cast<size_t>(N) * rs);
+    L.tab = o; o = align16(o + (1 + n_formula) * 16);
+    if (mixed) {
+        L.T4 = o; o = align16(o + (1 + n_formula) * 16);
+        L.cv = o; o = align16(o + 2 * static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
+    }
+    L.G = o; o = align16(o + U * 16);
+    if (mixed) { L.G4 = o; o = align16(o + U * 16); }
+    L.K = o; o = align16(o + (mixed ? 6 * 4 : 7 * 8) * static_cast<size_t>(N));
+    if (mixed) {
+        L.k1 = o; o = align16(o + static_cast<size_t>(N) * 8);
+        L.k1f = o; o = align16(o + static_cast<size_t>(N) * 4);
+    }
     L.ybuf = o; o = align16(o + static_cast<size_t>(N) * 8);
+    L.vm_slots = o; o = align16(o + 6 * static_cast<size_t>(n_slots > 0 ? n_slots : 1) * 16);
+    L.vm_stack = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 16);
+    L.vm_tup = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 4);
     L.cstat = o; o = align16(o + static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
     L.cdyn = o; o = align16(o + 6 * static_cast<size_t>(n_dyn > 0 ? n_dyn : 1) * 16);
     L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
@@ -188,39 +217,46 @@ __device__ __forceinline__ double group_sum(double v, double* red, int lt, int g
 
 __device__ __forceinline__ double time_tol(double t) { return 10.0 * 2.220446049250313e-16 * fmax(fabs(t), 1.0); }
 
-// ------------------------------------------------------------------------------------------
-// the VM side of a trajectory: slot values of one lane and coefficient evaluation
+// double index of packed element i inside the slot buffer G (double2[U]) of the group
+__device__ __forceinline__ int gslot64(int i, int n) { return i < n ? 2 * i : n + i; }
+// float index of packed element i's deviation inside G4 (float4[U]); + 2 for y_n
+__device__ __forceinline__ int gslot32(int i, int n) { return i < n ? 4 * i : 4 * (n + ((i - n) >> 1)) + ((i - n) & 1); }
 
-struct LaneSlots {
-    double2 s[kMaxSlots];
+// ------------------------------------------------------------------------------------------
+// the VM side of a trajectory: six VM lanes, each with its own slot values and stack in
+// shared memory
+
+struct VMLane {
+    double2* slots;
+    VStack stack;
 };
 
-__device__ __noinline__ void init_slots(const DevPlan& P, const CallArgs& A, long long traj, LaneSlots& L) {
+__device__ __noinline__ void init_slots(const DevPlan& P, const CallArgs& A, long long traj, double2* slots) {
     for (int i = 0; i < P.n_slots; ++i)
-        L.s[i] = i < P.n_base ? make_double2(P.base_val[2 * i], P.base_val[2 * i + 1]) : make_double2(0.0, 0.0);
+        slots[i] = i < P.n_base ? make_double2(P.base_val[2 * i], P.base_val[2 * i + 1]) : make_double2(0.0, 0.0);
     if (A.param_values) {
         for (int k = 0; k < A.n_param; ++k) {
             const double* v = A.param_values + 2 * (traj * A.n_param + k);
-            L.s[A.param_slot[k]] = make_double2(v[0], v[1]);
+            slots[A.param_slot[k]] = make_double2(v[0], v[1]);
         }
     } else if (A.n_axes > 0) {
         // row-major grid decode, last axis fastest (ode_batch.rs:353-391)
         for (int k = 0; k < A.n_axes; ++k) {
             long long idx = (traj / A.axis_stride[k]) % A.axis_len[k];
             const double* v = A.axes + 2 * (A.axis_off[k] + idx);
-            L.s[A.param_slot[k]] = make_double2(v[0], v[1]);
+            slots[A.param_slot[k]] = make_double2(v[0], v[1]);
         }
     }
 }
 
-__device__ __forceinline__ double2 eval_expr(const DevPlan& P, DevExpr e, const LaneSlots& L, double t) {
-    return vm_eval(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, e.start, e.len, L.s, t);
+__device__ __forceinline__ double2 eval_expr(const DevPlan& P, DevExpr e, const VMLane& L, double t) {
+    return vm_eval(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, e.start, e.len, L.slots, t, L.stack);
 }
 
 // Evaluate the compounds (all of them, or only the time-dependent ones) at time t.
-__device__ __noinline__ void eval_compounds(const DevPlan& P, LaneSlots& L, double t, bool only_dynamic) {
+__device__ __noinline__ void eval_compounds(const DevPlan& P, VMLane L, double t, bool only_dynamic) {
     for (int c = 0; c < P.n_comp; ++c)
-        if (!only_dynamic || P.comp_dynamic[c]) L.s[P.comp_slot[c]] = eval_expr(P, P.comp_expr[c], L, t);
+        if (!only_dynamic || P.comp_dynamic[c]) L.slots[P.comp_slot[c]] = eval_expr(P, P.comp_expr[c], L, t);
 }
 
 __device__ __forceinline__ double2 coeff_value(const DevPlan& P, int cls, const double2* cstat, const double2* crow) {
@@ -231,68 +267,84 @@ __device__ __forceinline__ double2 coeff_value(const DevPlan& P, int cls, const 
     return c;
 }
 
-// table entries [lo, hi) of the formula table from coefficient values (cstat static, crow the
-// time-dependent ones at the current stage time)
-template <int TPT, bool MIXED>
+// formula table entries [lo, hi) in double from coefficient values (cstat: time-independent
+// coefficients, crow: the time-dependent ones at the current time)
+template <int TPT>
 __device__ __forceinline__ void fill_formulas(const DevPlan& P, int lo, int hi, const double2* cstat, const double2* crow,
-                                              void* tab_raw, int lt) {
+                                              double2* tab, int lt) {
     for (int f = lo + lt; f < hi; f += TPT) {
         int a = P.formula_ptr[f - 1], b = P.formula_ptr[f];
-        if constexpr (MIXED) {
-            float2 acc = make_float2(0.f, 0.f);
-            for (int p = a; p < b; ++p) {
-                float fr = P.prod_factor32[2 * p], fi = P.prod_factor32[2 * p + 1];
-                int cls = P.prod_class[p];
-                if (cls < 0) {
-                    acc.x += fr;
-                    acc.y += fi;
-                } else {
-                    double2 c = coeff_value(P, cls, cstat, crow);
-                    float cr = static_cast<float>(c.x), ci = static_cast<float>(c.y);
-                    acc.x += fr * cr - fi * ci;
-                    acc.y += fr * ci + fi * cr;
-                }
-            }
-            reinterpret_cast<float2*>(tab_raw)[f] = acc;
-        } else {
-            double2 acc = make_double2(0.0, 0.0);
-            for (int p = a; p < b; ++p) {
-                double2 fac = make_double2(P.prod_factor[2 * p], P.prod_factor[2 * p + 1]);
-                int cls = P.prod_class[p];
-                double2 c = cls < 0 ? make_double2(1.0, 0.0) : coeff_value(P, cls, cstat, crow);
-                double2 v = cmul(fac, c);
-                acc.x += v.x;
-                acc.y += v.y;
-            }
-            reinterpret_cast<double2*>(tab_raw)[f] = acc;
+        double2 acc = make_double2(0.0, 0.0);
+        for (int p = a; p < b; ++p) {
+            double2 fac = make_double2(P.prod_factor[2 * p], P.prod_factor[2 * p + 1]);
+            int cls = P.prod_class[p];
+            double2 c = cls < 0 ? make_double2(1.0, 0.0) : coeff_value(P, cls, cstat, crow);
+            double2 v = cmul(fac, c);
+            acc.x += v.x;
+            acc.y += v.y;
         }
+        tab[f] = acc;
     }
 }
 
-// The packed expanded_sparse RHS of one stage: gather from yg, write K (the stage derivative).
-template <int TPT, bool MIXED>
+// Single-precision formula values at a stage time (.xy) and their change since the step's
+// start time (.zw).  cv holds, per coefficient class (k, conj), the value and the change as
+// float4; the changes were taken in double before rounding, so they keep their relative
+// precision.  Pure single-precision work per product.
+template <int TPT>
+__device__ __forceinline__ void fill_formulas_dev(const DevPlan& P, int lo, int hi, const float4* cv, float4* T4, int lt) {
+    for (int f = lo + lt; f < hi; f += TPT) {
+        int a = P.formula_ptr[f - 1], b = P.formula_ptr[f];
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int p = a; p < b; ++p) {
+            float fr = P.prod_factor32[2 * p], fi = P.prod_factor32[2 * p + 1];
+            int cls = P.prod_class[p];
+            if (cls < 0) {
+                acc.x += fr;
+                acc.y += fi;
+                continue;
+            }
+            float4 c = cv[cls];
+            acc.x += fr * c.x - fi * c.y;
+            acc.y += fr * c.y + fi * c.x;
+            acc.z += fr * c.z - fi * c.w;
+            acc.w += fr * c.w + fi * c.z;
+        }
+        T4[f] = acc;
+    }
+}
+
+// per-class single-precision values and changes for the stage row (threads < 2 * n_coeff)
+__device__ __forceinline__ void stage_classes(const DevPlan& P, const double2* cstat, const double2* crow, const double2* crow0,
+                                              float4* cv, int lt) {
+    if (lt < 2 * P.n_coeff) {
+        int k = lt >> 1;
+        int pos = P.coeff_dyn_pos[k];
+        double2 c = pos >= 0 ? crow[pos] : cstat[k];
+        double2 c0 = pos >= 0 ? crow0[pos] : c;
+        double dre = c.x - c0.x, dim = c.y - c0.y;
+        if (lt & 1) { c.y = -c.y; dim = -dim; }
+        cv[lt] = make_float4(static_cast<float>(c.x), static_cast<float>(c.y), static_cast<float>(dre), static_cast<float>(dim));
+    }
+}
+
+// The packed expanded_sparse RHS: one record = one 16-byte coefficient and one 16-byte input.
+template <int TPT, typename T, typename T2>
 __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
-                                           const void* tab_raw, const void* yg_raw, void* K_raw, int lt) {
-    using RT = std::conditional_t<MIXED, float, double>;
-    using RT2 = std::conditional_t<MIXED, float2, double2>;
-    const RT2* tab = reinterpret_cast<const RT2*>(tab_raw);
-    const RT* yg = reinterpret_cast<const RT*>(yg_raw);
-    RT* K = reinterpret_cast<RT*>(K_raw);
-    RT ar = 0, ai = 0;
+                                           const T2* tab, const T2* G, T* K, int lt) {
+    T ar = 0, ai = 0;
     int o = 0;
     const int n_iter = P.n_iter;
 #pragma unroll 4
     for (int it = 0; it < n_iter; ++it) {
         uint32_t w = s_rec[it * TPT + lt];
-        int in = static_cast<int>(w & kRecIndexMask);
-        RT2 c = tab[w >> kRecCoefShift];
-        RT vr = yg[in];
-        RT vi = (w & kRecComplex) ? yg[in + 1] : RT(0);
-        if (w & kRecConj) vi = -vi;
-        ar = fma(c.x, vr, ar);
-        ar = fma(-c.y, vi, ar);
-        ai = fma(c.x, vi, ai);
-        ai = fma(c.y, vr, ai);
+        T2 c = tab[w >> kRecCoefShift];
+        T2 v = G[w & kRecIndexMask];
+        if (w & kRecConj) v.y = -v.y;
+        ar = fma(c.x, v.x, ar);
+        ar = fma(-c.y, v.y, ar);
+        ai = fma(c.x, v.y, ai);
+        ai = fma(c.y, v.x, ai);
         if (w & kRecFlush) {
             uint32_t d = s_out[o * TPT + lt];
             K[d & 0xFFFFu] = ar;
@@ -305,97 +357,27 @@ __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __r
     }
 }
 
-// Mixed (deviation) form layout of one trajectory group: the stage derivatives are kept as
-// deviations d_j = k_j - k_1 in single precision, k_1 in double.  Both the stage inputs and the
-// embedded error estimate are then sums of the d_j (the k_1 parts cancel exactly, because the
-// tableau's error weights sum to zero and a_sj sums to c_s), so single-precision rounding of
-// the RHS no longer feeds noise into the step-size controller.
-struct DevLayout {
-    size_t tab64, tab32, dtab32, Df, Yf, yg64, K32, k1, k1f, ybuf, cstat, cdyn, red, traj, bytes;
-};
-
-__host__ __device__ inline DevLayout group_layout_dev(int N, int n_formula, int n_coeff, int n_dyn, int tpt) {
-    DevLayout L;
-    size_t o = 0;
-    L.tab64 = o; o = align16(o + (1 + n_formula) * 16);
-    L.tab32 = o; o = align16(o + (1 + n_formula) * 8);
-    L.dtab32 = o; o = align16(o + (1 + n_formula) * 8);
-    L.Df = o; o = align16(o + static_cast<size_t>(N) * 4);
-    L.Yf = o; o = align16(o + static_cast<size_t>(N) * 4);
-    L.yg64 = o; o = align16(o + static_cast<size_t>(N) * 8);
-    L.K32 = o; o = align16(o + 6 * static_cast<size_t>(N) * 4);
-    L.k1 = o; o = align16(o + static_cast<size_t>(N) * 8);
-    L.k1f = o; o = align16(o + static_cast<size_t>(N) * 4);
-    L.ybuf = o; o = align16(o + static_cast<size_t>(N) * 8);
-    L.cstat = o; o = align16(o + static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
-    L.cdyn = o; o = align16(o + 6 * static_cast<size_t>(n_dyn > 0 ? n_dyn : 1) * 16);
-    L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
-    L.traj = o; o = align16(o + 16);
-    L.bytes = o;
-    return L;
-}
-
-// Single-precision formula values at a stage time (tab32) and their change since the step's
-// start time (dtab32, from coefficient *differences*, so it keeps its relative precision).
-template <int TPT>
-__device__ __forceinline__ void fill_formulas_dev(const DevPlan& P, int lo, int hi, const double2* cstat, const double2* crow,
-                                                  const double2* crow0, float2* tab32, float2* dtab32, int lt) {
-    for (int f = lo + lt; f < hi; f += TPT) {
-        int a = P.formula_ptr[f - 1], b = P.formula_ptr[f];
-        float2 acc = make_float2(0.f, 0.f), dacc = make_float2(0.f, 0.f);
-        for (int p = a; p < b; ++p) {
-            float fr = P.prod_factor32[2 * p], fi = P.prod_factor32[2 * p + 1];
-            int cls = P.prod_class[p];
-            if (cls < 0) {
-                acc.x += fr;
-                acc.y += fi;
-                continue;
-            }
-            int k = cls >> 1;
-            int pos = P.coeff_dyn_pos[k];
-            double2 c = pos >= 0 ? crow[pos] : cstat[k];
-            double2 c0 = pos >= 0 ? crow0[pos] : c;
-            double dre = c.x - c0.x, dim = c.y - c0.y;
-            if (cls & 1) { c.y = -c.y; dim = -dim; }
-            float cr = static_cast<float>(c.x), ci = static_cast<float>(c.y);
-            float dr = static_cast<float>(dre), di = static_cast<float>(dim);
-            acc.x += fr * cr - fi * ci;
-            acc.y += fr * ci + fi * cr;
-            dacc.x += fr * dr - fi * di;
-            dacc.y += fr * di + fi * dr;
-        }
-        tab32[f] = acc;
-        dtab32[f] = dacc;
-    }
-}
-
 // Stage deviation d_s = L(t_s) (y_s - y_n) + (L(t_s) - L(t_n)) y_n, all in single precision.
 template <int TPT>
 __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
-                                           const float2* tab32, const float2* dtab32, const float* Df, const float* Yf,
-                                           float* K, int lt) {
+                                           const float4* T4, const float4* G4, float* K, int lt) {
     float ar = 0.f, ai = 0.f;
     int o = 0;
     const int n_iter = P.n_iter;
 #pragma unroll 4
     for (int it = 0; it < n_iter; ++it) {
         uint32_t w = s_rec[it * TPT + lt];
-        int in = static_cast<int>(w & kRecIndexMask);
-        int f = static_cast<int>(w >> kRecCoefShift);
-        float2 c = tab32[f];
-        float2 dc = dtab32[f];
-        float dr = Df[in], yr = Yf[in];
-        float di = 0.f, yi = 0.f;
-        if (w & kRecComplex) { di = Df[in + 1]; yi = Yf[in + 1]; }
-        if (w & kRecConj) { di = -di; yi = -yi; }
-        ar = fmaf(c.x, dr, ar);
-        ar = fmaf(-c.y, di, ar);
-        ar = fmaf(dc.x, yr, ar);
-        ar = fmaf(-dc.y, yi, ar);
-        ai = fmaf(c.x, di, ai);
-        ai = fmaf(c.y, dr, ai);
-        ai = fmaf(dc.x, yi, ai);
-        ai = fmaf(dc.y, yr, ai);
+        float4 c = T4[w >> kRecCoefShift];
+        float4 v = G4[w & kRecIndexMask];
+        if (w & kRecConj) { v.y = -v.y; v.w = -v.w; }
+        ar = fmaf(c.x, v.x, ar);
+        ar = fmaf(-c.y, v.y, ar);
+        ar = fmaf(c.z, v.z, ar);
+        ar = fmaf(-c.w, v.w, ar);
+        ai = fmaf(c.x, v.y, ai);
+        ai = fmaf(c.y, v.x, ai);
+        ai = fmaf(c.z, v.w, ai);
+        ai = fmaf(c.w, v.z, ai);
         if (w & kRecFlush) {
             uint32_t d = s_out[o * TPT + lt];
             K[d & 0xFFFFu] = ar;
@@ -412,15 +394,18 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
 // the integrator kernel
 //
 // FP64 form: K_1..K_7 in double, each stage a full double RHS.
-// Mixed form: k_1 = f(t_n, y_n) in double (recomputed at every accepted step, which equals
-// the reference's FSAL k_7 up to rounding), stage deviations d_2..d_7 in single precision.
+// Mixed form: k_1 = f(t_n, y_n) in double, stage deviations d_2..d_7 in single precision.  The
+// stage inputs and the embedded error estimate are sums of the d_j only (a_sj sums to c_s and
+// the error weights to zero), so single-precision rounding does not reach the step-size
+// controller.  k_1 of the next step is k_1 + d_7 (first-same-as-last), recomputed in double
+// every k1_refresh accepted steps.
 
 template <int TPT, int EPT, bool MIXED>
 __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
-    const int N = P.N;
+    const int n = P.n, N = P.N, U = P.U;
 
     // stage the plan's gather stream once per CTA
     uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
@@ -433,55 +418,36 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
     __syncthreads();
     if (g >= gpb) return;
 
+    const int vm_depth = A.vm_depth;
+    const GroupLayout Lay = group_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, vm_depth, TPT, MIXED);
     unsigned char* gb = smem + plan_smem_bytes(P.n_iter, P.n_out, TPT) + static_cast<size_t>(g) * group_bytes;
-    // FP64-form buffers
-    double2* s_tab = nullptr;  // formula table (double)
-    double* s_yg = nullptr;    // gather input (double)
-    double* s_K = nullptr;     // K_1..K_7
-    // mixed-form buffers
-    float2* s_tab32 = nullptr;
-    float2* s_dtab32 = nullptr;
-    float* s_Df = nullptr;
-    float* s_Yf = nullptr;
-    float* s_K32 = nullptr;    // d_2..d_7 in slots 0..5
-    double* s_k1 = nullptr;
-    float* s_k1f = nullptr;
-    double* s_ybuf;
-    double2* s_cstat;
-    double2* s_cdyn;
-    double* s_red;
-    long long* s_traj;
-    if constexpr (MIXED) {
-        const DevLayout Lay = group_layout_dev(N, P.n_formula, P.n_coeff, P.n_dyn, TPT);
-        s_tab = reinterpret_cast<double2*>(gb + Lay.tab64);
-        s_yg = reinterpret_cast<double*>(gb + Lay.yg64);
-        s_tab32 = reinterpret_cast<float2*>(gb + Lay.tab32);
-        s_dtab32 = reinterpret_cast<float2*>(gb + Lay.dtab32);
-        s_Df = reinterpret_cast<float*>(gb + Lay.Df);
-        s_Yf = reinterpret_cast<float*>(gb + Lay.Yf);
-        s_K32 = reinterpret_cast<float*>(gb + Lay.K32);
-        s_k1 = reinterpret_cast<double*>(gb + Lay.k1);
-        s_k1f = reinterpret_cast<float*>(gb + Lay.k1f);
-        s_ybuf = reinterpret_cast<double*>(gb + Lay.ybuf);
-        s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
-        s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
-        s_red = reinterpret_cast<double*>(gb + Lay.red);
-        s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
-    } else {
-        const GroupLayout Lay = group_layout(N, P.n_formula, P.n_coeff, P.n_dyn, TPT, false);
-        s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
-        s_yg = reinterpret_cast<double*>(gb + Lay.yg);
-        s_K = reinterpret_cast<double*>(gb + Lay.K);
-        s_ybuf = reinterpret_cast<double*>(gb + Lay.ybuf);
-        s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
-        s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
-        s_red = reinterpret_cast<double*>(gb + Lay.red);
-        s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
-    }
+    double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
+    double2* s_G = reinterpret_cast<double2*>(gb + Lay.G);
+    double* s_G64 = reinterpret_cast<double*>(gb + Lay.G);
+    double* s_K = reinterpret_cast<double*>(gb + Lay.K);      // FP64 form
+    float* s_K32 = reinterpret_cast<float*>(gb + Lay.K);      // mixed form
+    float4* s_T4 = reinterpret_cast<float4*>(gb + Lay.T4);
+    float4* s_cv = reinterpret_cast<float4*>(gb + Lay.cv);
+    float4* s_G4 = reinterpret_cast<float4*>(gb + Lay.G4);
+    float* s_G4f = reinterpret_cast<float*>(gb + Lay.G4);
+    double* s_k1 = reinterpret_cast<double*>(gb + Lay.k1);
+    float* s_k1f = reinterpret_cast<float*>(gb + Lay.k1f);
+    double* s_ybuf = reinterpret_cast<double*>(gb + Lay.ybuf);
+    double2* s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
+    double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
+    double* s_red = reinterpret_cast<double*>(gb + Lay.red);
+    long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
     const int nd = P.n_dyn > 0 ? P.n_dyn : 1;
     const int S = P.n_static_formula, F = P.n_formula;
 
-    LaneSlots L;  // meaningful in lanes 0..5 (the VM lanes)
+    // this thread's VM lane (lanes 0..5 only)
+    VMLane L;
+    {
+        int vl = lt < 6 ? lt : 0;
+        L.slots = reinterpret_cast<double2*>(gb + Lay.vm_slots) + vl * (P.n_slots > 0 ? P.n_slots : 1);
+        L.stack.v = reinterpret_cast<double2*>(gb + Lay.vm_stack) + vl * vm_depth;
+        L.stack.tup = reinterpret_cast<int32_t*>(gb + Lay.vm_tup) + vl * vm_depth;
+    }
 
     while (true) {
         if (lt == 0) *s_traj = static_cast<long long>(atomicAdd(A.counter, 1ull));
@@ -493,7 +459,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
         // ---------------- per-trajectory setup ----------------
         const double t0 = A.t0, t1 = A.t1;
         if (lt < 6) {
-            init_slots(P, A, traj, L);
+            init_slots(P, A, traj, L.slots);
             eval_compounds(P, L, t0, false);
         }
         if (lt == 0) {
@@ -501,19 +467,20 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                 s_cstat[k] = P.coeff_dynamic[k] ? make_double2(0.0, 0.0) : eval_expr(P, P.coeff_expr[k], L, t0);
             for (int j = 0; j < P.n_dyn; ++j) s_cdyn[5 * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t0);
             s_tab[0] = make_double2(0.0, 0.0);
-            if constexpr (MIXED) {
-                s_tab32[0] = make_float2(0.f, 0.f);
-                s_dtab32[0] = make_float2(0.f, 0.f);
-            }
+            if constexpr (MIXED) s_T4[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        // slot buffers start at zero (the imaginary halves of diagonal slots stay zero)
+        for (int i = lt; i < U; i += TPT) {
+            s_G[i] = make_double2(0.0, 0.0);
+            if constexpr (MIXED) s_G4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         gsync<TPT>(g);
         // time-independent formulas: once per trajectory
-        fill_formulas<TPT, false>(P, 1, 1 + S, s_cstat, s_cdyn + 5 * nd, s_tab, lt);
+        fill_formulas<TPT>(P, 1, 1 + S, s_cstat, s_cdyn + 5 * nd, s_tab, lt);
         if constexpr (MIXED) {
             for (int f = 1 + lt; f < 1 + S; f += TPT) {
                 double2 v = s_tab[f];
-                s_tab32[f] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
-                s_dtab32[f] = make_float2(0.f, 0.f);
+                s_T4[f] = make_float4(static_cast<float>(v.x), static_cast<float>(v.y), 0.f, 0.f);
             }
         }
 
@@ -524,7 +491,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             int i = lt + e * TPT;
             y[e] = i < N ? r0[i] : 0.0;
             yn[e] = 0.0;
-            if (i < N) s_yg[i] = y[e];
+            if (i < N) s_G64[gslot64(i, n)] = y[e];
         }
 
         long long accepted = 0, rejected = 0, rhs_calls = 0, count = 0;
@@ -547,7 +514,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             switch (A.output) {
             case OBE_OUTPUT_POPULATIONS:
                 if (store)
-                    for (int i = lt; i < P.n; i += TPT) out_vals[pt * P.n + i] = s_ybuf[i];
+                    for (int i = lt; i < n; i += TPT) out_vals[pt * n + i] = s_ybuf[i];
                 break;
             case OBE_OUTPUT_FULL:
                 if (store)
@@ -591,7 +558,6 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             }
             gsync<TPT>(g);
         };
-        auto points = [&]() -> long long { return count; };
 
         // event function g(t, y) for the state in s_ybuf (synced); uniform result
         auto event_value = [&](double t, bool& has, double& gv) {
@@ -603,13 +569,13 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                 if (A.ev_kind == OBE_EVENT_POPULATION) {
                     for (int k = 0; k < A.n_ev; ++k) {
                         int idx = A.ev_idx[k];
-                        if (idx < 0 || idx >= P.n) { bad = ST_EVENT_INDEX; break; }
+                        if (idx < 0 || idx >= n) { bad = ST_EVENT_INDEX; break; }
                         v += s_ybuf[idx];
                     }
                     v -= A.ev_thr;
                 } else {
                     eval_compounds(P, L, t, true);
-                    double2 r = vm_eval(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, L.s, t);
+                    double2 r = vm_eval(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, L.slots, t, L.stack);
                     if (fabs(r.y) > 1e-12) bad = ST_EVENT_COMPLEX;
                     v = r.x;
                 }
@@ -634,13 +600,13 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                 for (int j = 0; j < P.n_dyn; ++j) s_cdyn[row * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t);
             }
         };
-        // one double-precision RHS from s_yg: formulas for coefficient row `row`, gather into out
+        // one double-precision RHS from the slot buffer: formulas for coefficient row `row`, gather into out
         auto rhs64 = [&](int row, double* out) {
-            gsync<TPT>(g);  // yg written, coefficient row ready
-            if (F > S) fill_formulas<TPT, false>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
+            gsync<TPT>(g);  // G written, coefficient row ready
+            if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
             gsync<TPT>(g);
-            gather_rhs<TPT, false>(P, s_rec, s_out, s_tab, s_yg, out, lt);
-            gsync<TPT>(g);  // out complete, yg free
+            gather_rhs<TPT, double, double2>(P, s_rec, s_out, s_tab, s_G, out, lt);
+            gsync<TPT>(g);  // out complete, G free
         };
         // stage derivative j (0-based: K_1..K_7) at own element i, as double
         auto Kat = [&](int j, int i) -> double {
@@ -694,7 +660,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
-                    if (i < N) s_yg[i] = y[e] + k1_out[i] * h0;
+                    if (i < N) s_G64[gslot64(i, n)] = y[e] + k1_out[i] * h0;
                 }
                 dyn_coeffs_at(x + h0, 4);
                 rhs64(4, s_ybuf);
@@ -715,7 +681,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
-                    if (i < N) s_yg[i] = y[e];
+                    if (i < N) s_G64[gslot64(i, n)] = y[e];
                 }
             }
         }
@@ -730,7 +696,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
         double ev_old = 0.0;
         int si = 0;
 
-        // K_1 = f(t0, y0) in double
+        // K_1 = f(t, y) in double from the slot buffer (which holds y)
         auto refresh_k1 = [&](int row) {
             rhs64(row, k1_out);
             if constexpr (MIXED) {
@@ -739,7 +705,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                     int i = lt + e * TPT;
                     if (i < N) {
                         s_k1f[i] = static_cast<float>(s_k1[i]);
-                        s_Yf[i] = static_cast<float>(y[e]);
+                        s_G4f[gslot32(i, n) + 2] = static_cast<float>(y[e]);
                     }
                 }
             }
@@ -769,6 +735,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
         }
 
         long long ns = 0, nst = 0, ia = 0;
+        int since_refresh = 0;
         bool last = false;
         while (!done && !last) {
             if (ns > A.maxiters) { status = ST_MAXITERS; err_x = x; err_a = ns; break; }
@@ -800,7 +767,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                                 if (j <= s) acc += kA[M][s][j] * Kat(j, i);
                             double v = y[e] + h * acc;
                             if (s == 5) yn[e] = v;
-                            s_yg[i] = v;
+                            s_G64[gslot64(i, n)] = v;
                         }
                     }
                     rhs64(s < 4 ? s : 4, s_K + static_cast<size_t>(s + 1) * N);
@@ -826,10 +793,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                 for (int s = 0; s < 6; ++s) {
                     // stage input deviation y_s - y_n = h (c_s k_1 + sum_j a_sj d_j), in single
                     // precision (small next to y_n); the solution y_{n+1} itself in double
-                    float csum = 0.f;
-#pragma unroll
-                    for (int j = 0; j < 6; ++j)
-                        if (j <= s) csum += static_cast<float>(kA[M][s][j]);
+                    const float csum = kCsumf[M][s];
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
@@ -837,23 +801,27 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                             float acc = 0.f;
 #pragma unroll
                             for (int j = 1; j < 6; ++j)
-                                if (j <= s) acc += static_cast<float>(kA[M][s][j]) * s_K32[static_cast<size_t>(j - 1) * N + i];
-                            if (s == 5) {
-                                yn[e] = y[e] + h * s_k1[i] + h * static_cast<double>(acc);
-                                s_Df[i] = static_cast<float>(yn[e] - y[e]);
-                            } else {
-                                s_Df[i] = hf * (csum * s_k1f[i] + acc);
-                            }
+                                if (j <= s) acc = fmaf(kAf[M][s][j], s_K32[static_cast<size_t>(j - 1) * N + i], acc);
+                            const float k1f = s_k1f[i];
+                            if (s == 5) yn[e] = y[e] + h * (s_k1[i] + static_cast<double>(acc));
+                            s_G4f[gslot32(i, n)] = hf * fmaf(csum, k1f, acc);
                         }
                     }
                     const int row = s < 4 ? s : 4;
+                    if (s < 5) {  // stage 7 shares stage 6's time
+                        gsync<TPT>(g);
+                        stage_classes(P, s_cstat, s_cdyn + row * nd, s_cdyn + 5 * nd, s_cv, lt);
+                        gsync<TPT>(g);
+                        fill_formulas_dev<TPT>(P, 1 + S, 1 + F, s_cv, s_T4, lt);
+                    }
                     gsync<TPT>(g);
-                    fill_formulas_dev<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_cdyn + 5 * nd, s_tab32, s_dtab32, lt);
-                    gsync<TPT>(g);
-                    gather_dev<TPT>(P, s_rec, s_out, s_tab32, s_dtab32, s_Df, s_Yf, s_K32 + static_cast<size_t>(s) * N, lt);
+                    gather_dev<TPT>(P, s_rec, s_out, s_T4, s_G4, s_K32 + static_cast<size_t>(s) * N, lt);
                     gsync<TPT>(g);
                 }
-                // error estimate from the deviations alone (the error weights sum to zero)
+                // error estimate from the deviations alone (the error weights sum to zero); the
+                // per-element ratios in single precision, their sum and the controller in double
+                const float atolf = static_cast<float>(A.atol), rtolf = static_cast<float>(A.rtol);
+                float errf = 0.f;
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
@@ -861,17 +829,35 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                         float acc = 0.f;
 #pragma unroll
                         for (int j = 1; j < 7; ++j)
-                            if (M == 1 || j != 1) acc += static_cast<float>(kE[M][j]) * s_K32[static_cast<size_t>(j - 1) * N + i];
-                        double ei = h * static_cast<double>(acc);
-                        double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
-                        double q = ei / sc;
-                        err += q * q;
+                            if (M == 1 || j != 1) acc = fmaf(kEf[M][j], s_K32[static_cast<size_t>(j - 1) * N + i], acc);
+                        const int gi = gslot32(i, n);
+                        const float yf = s_G4f[gi + 2];
+                        const float ynf = yf + s_G4f[gi];
+                        const float sc = fmaf(fmaxf(fabsf(yf), fabsf(ynf)), rtolf, atolf);
+                        const float q = __fdividef(hf * acc, sc);
+                        errf = fmaf(q, q, errf);
                     }
                 }
+                // warp-level sum in single precision, broadcast from lane 0 (fixed order)
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) errf += __shfl_down_sync(0xffffffffu, errf, off);
+                if constexpr (TPT == 32) {
+                    errf = __shfl_sync(0xffffffffu, errf, 0);
+                } else {
+                    float* redf = reinterpret_cast<float*>(s_red);
+                    if ((lt & 31) == 0) redf[lt >> 5] = errf;
+                    gsync<TPT>(g);
+                    errf = 0.f;
+#pragma unroll
+                    for (int w = 0; w < TPT / 32; ++w) errf += redf[w];
+                    gsync<TPT>(g);
+                }
+                err = static_cast<double>(sqrtf(errf / static_cast<float>(N)));
             }
             rhs_calls += 6;
-            err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
-            // controller (common.rs:48-69)
+            if constexpr (!MIXED) err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
+            // controller (common.rs:48-69), in double for both forms (single-precision powers
+            // here made the controller choose ~18% smaller steps)
             double fac11 = pow(err, alpha);
             double fac = fac11 * pow(fac_old, -beta);
             fac = fmax(facc2, fmin(facc1, fac / safety));
@@ -1006,7 +992,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                 }
                 if (hit) {
                     // push_unique (dopri5.rs:150-158)
-                    if (!(points() > 0 && fabs(last_time - te) <= time_tol(te))) {
+                    if (!(count > 0 && fabs(last_time - te) <= time_tol(te))) {
                         if (ev_state == 0) stage_registers_to_buf(y);
                         else if (ev_state == 1) stage_registers_to_buf(yn);
                         else dense_to_buf(ev_theta);
@@ -1016,7 +1002,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                     ev_time = te;
                     break;
                 }
-                // accept: y <- yn; K_1 <- f(t_{n+1}, y_{n+1})
+                // accept: y <- yn; K_1 <- K_7
                 if constexpr (!MIXED) {
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
@@ -1025,15 +1011,29 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                         if (i < N) s_K[i] = s_K[static_cast<size_t>(6) * N + i];
                     }
                 } else {
+                    // the coefficients at t_{n+1} = x + h are row 4; they become the step-start row
+                    if (lt < P.n_dyn) s_cdyn[5 * nd + lt] = s_cdyn[4 * nd + lt];
+                    const bool refresh = !last && ++since_refresh >= A.k1_refresh;
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
                         y[e] = yn[e];
-                        if (i < N) s_yg[i] = y[e];
+                        if (i < N) {
+                            if (refresh) {
+                                s_G64[gslot64(i, n)] = y[e];
+                            } else {
+                                // first-same-as-last: k_1 of the next step is k_7 = k_1 + d_7
+                                double k = s_k1[i] + static_cast<double>(s_K32[static_cast<size_t>(5) * N + i]);
+                                s_k1[i] = k;
+                                s_k1f[i] = static_cast<float>(k);
+                                s_G4f[gslot32(i, n) + 2] = static_cast<float>(y[e]);
+                            }
+                        }
                     }
-                    // the coefficients at t_{n+1} = x + h are row 4; they become the step-start row
-                    if (lt < P.n_dyn) s_cdyn[5 * nd + lt] = s_cdyn[4 * nd + lt];
-                    if (!last) refresh_k1(4);
+                    if (refresh) {
+                        since_refresh = 0;
+                        refresh_k1(4);
+                    }
                 }
                 ev_old_has = ev_new_has;
                 ev_old = ev_new;
@@ -1079,52 +1079,68 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
     }
 }
 
-// One RHS evaluation per state (lindblad_rhs_py), batched; overrides per state.
+// One RHS evaluation per state (lindblad_rhs_py), batched; overrides per state.  The mixed
+// form evaluates the products in single precision.
 template <int TPT, bool MIXED>
 __global__ void __launch_bounds__(256) rhs_kernel(const DevPlan P, long long count, const double* ts, const double* ys,
                                                   int n_ov, const int* ov_slots, const double* ov_vals, double* dys,
-                                                  int gpb, size_t group_bytes) {
-    using RT = std::conditional_t<MIXED, float, double>;
+                                                  int gpb, size_t group_bytes, int vm_depth) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
-    const int N = P.N;
+    const int n = P.n, N = P.N, U = P.U;
     uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
     uint32_t* s_out = s_rec + static_cast<size_t>(P.n_iter) * TPT;
     for (int i = threadIdx.x; i < (P.n_iter + P.n_out) * TPT; i += blockDim.x)
         s_rec[i] = i < P.n_iter * TPT ? P.rec[i] : P.lane_out[i - P.n_iter * TPT];
     __syncthreads();
     if (g >= gpb) return;
-    const GroupLayout Lay = group_layout(N, P.n_formula, P.n_coeff, P.n_dyn, TPT, MIXED);
+    const GroupLayout Lay = group_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, vm_depth, TPT, false);
     unsigned char* gb = smem + plan_smem_bytes(P.n_iter, P.n_out, TPT) + static_cast<size_t>(g) * group_bytes;
-    void* s_tab = gb + Lay.tab;
-    RT* s_yg = reinterpret_cast<RT*>(gb + Lay.yg);
-    RT* s_K = reinterpret_cast<RT*>(gb + Lay.K);
+    double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
+    double2* s_G = reinterpret_cast<double2*>(gb + Lay.G);
+    double* s_K = reinterpret_cast<double*>(gb + Lay.K);
     double2* s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
     double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
-    LaneSlots L;
+    // single-precision views for the mixed form (inside the double buffers)
+    float2* s_tab32 = reinterpret_cast<float2*>(gb + Lay.K);
+    float2* s_G32 = s_tab32 + (1 + P.n_formula);
+    float* s_K32 = reinterpret_cast<float*>(gb + Lay.ybuf);
+    VMLane L;
+    L.slots = reinterpret_cast<double2*>(gb + Lay.vm_slots);
+    L.stack.v = reinterpret_cast<double2*>(gb + Lay.vm_stack);
+    L.stack.tup = reinterpret_cast<int32_t*>(gb + Lay.vm_tup);
+    CallArgs none{};
     for (long long st = static_cast<long long>(blockIdx.x) * gpb + g; st < count; st += static_cast<long long>(gridDim.x) * gpb) {
         const double t = ts[st];
         if (lt == 0) {
-            for (int i = 0; i < P.n_slots; ++i)
-                L.s[i] = i < P.n_base ? make_double2(P.base_val[2 * i], P.base_val[2 * i + 1]) : make_double2(0.0, 0.0);
-            for (int k = 0; k < n_ov; ++k) L.s[ov_slots[k]] = make_double2(ov_vals[2 * (st * n_ov + k)], ov_vals[2 * (st * n_ov + k) + 1]);
+            init_slots(P, none, 0, L.slots);
+            for (int k = 0; k < n_ov; ++k) L.slots[ov_slots[k]] = make_double2(ov_vals[2 * (st * n_ov + k)], ov_vals[2 * (st * n_ov + k) + 1]);
             eval_compounds(P, L, t, false);
             for (int k = 0; k < P.n_coeff; ++k) {
                 double2 c = eval_expr(P, P.coeff_expr[k], L, t);
                 s_cstat[k] = c;
                 if (P.coeff_dyn_pos[k] >= 0) s_cdyn[P.coeff_dyn_pos[k]] = c;
             }
-            if constexpr (MIXED) reinterpret_cast<float2*>(s_tab)[0] = make_float2(0.f, 0.f);
-            else reinterpret_cast<double2*>(s_tab)[0] = make_double2(0.0, 0.0);
+            s_tab[0] = make_double2(0.0, 0.0);
         }
-        for (int i = lt; i < N; i += TPT) s_yg[i] = static_cast<RT>(ys[st * N + i]);
+        for (int i = lt; i < U; i += TPT) s_G[i] = make_double2(0.0, 0.0);
         gsync<TPT>(g);
-        fill_formulas<TPT, MIXED>(P, 1, 1 + P.n_formula, s_cstat, s_cdyn, s_tab, lt);
+        for (int i = lt; i < N; i += TPT) reinterpret_cast<double*>(s_G)[gslot64(i, n)] = ys[st * N + i];
+        fill_formulas<TPT>(P, 1, 1 + P.n_formula, s_cstat, s_cdyn, s_tab, lt);
         gsync<TPT>(g);
-        gather_rhs<TPT, MIXED>(P, s_rec, s_out, s_tab, s_yg, s_K, lt);
-        gsync<TPT>(g);
-        for (int i = lt; i < N; i += TPT) dys[st * N + i] = static_cast<double>(s_K[i]);
+        if constexpr (MIXED) {
+            for (int f = lt; f < 1 + P.n_formula; f += TPT) s_tab32[f] = make_float2(static_cast<float>(s_tab[f].x), static_cast<float>(s_tab[f].y));
+            for (int i = lt; i < U; i += TPT) s_G32[i] = make_float2(static_cast<float>(s_G[i].x), static_cast<float>(s_G[i].y));
+            gsync<TPT>(g);
+            gather_rhs<TPT, float, float2>(P, s_rec, s_out, s_tab32, s_G32, s_K32, lt);
+            gsync<TPT>(g);
+            for (int i = lt; i < N; i += TPT) dys[st * N + i] = static_cast<double>(s_K32[i]);
+        } else {
+            gather_rhs<TPT, double, double2>(P, s_rec, s_out, s_tab, s_G, s_K, lt);
+            gsync<TPT>(g);
+            for (int i = lt; i < N; i += TPT) dys[st * N + i] = s_K[i];
+        }
         gsync<TPT>(g);
     }
 }
@@ -1150,9 +1166,50 @@ size_t put(std::vector<unsigned char>& blob, const std::vector<T>& v) {
     return off;
 }
 
+// single-precision tableau copies, once per device
+obe_status init_constants() {
+    static bool done_dev[64] = {false};
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
+    if (dev < 64 && done_dev[dev]) return OBE_OK;
+    double a[2][6][6], e[2][7];
+    if (!cuda_ok(cudaMemcpyFromSymbol(a, kA, sizeof a), "cudaMemcpyFromSymbol(kA)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyFromSymbol(e, kE, sizeof e), "cudaMemcpyFromSymbol(kE)")) return OBE_ERR_CUDA;
+    float af[2][6][6], cs[2][6], ef[2][7];
+    for (int m = 0; m < 2; ++m) {
+        for (int r = 0; r < 6; ++r) {
+            double sum = 0.0;
+            for (int j = 0; j < 6; ++j) {
+                af[m][r][j] = static_cast<float>(a[m][r][j]);
+                sum += a[m][r][j];
+            }
+            cs[m][r] = static_cast<float>(sum);
+        }
+        for (int j = 0; j < 7; ++j) ef[m][j] = static_cast<float>(e[m][j]);
+    }
+    if (!cuda_ok(cudaMemcpyToSymbol(kAf, af, sizeof af), "cudaMemcpyToSymbol(kAf)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyToSymbol(kCsumf, cs, sizeof cs), "cudaMemcpyToSymbol(kCsumf)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyToSymbol(kEf, ef, sizeof ef), "cudaMemcpyToSymbol(kEf)")) return OBE_ERR_CUDA;
+    if (dev < 64) done_dev[dev] = true;
+    return OBE_OK;
+}
+
+int k1_refresh_interval() {
+    static int v = 0;
+    if (!v) {
+        const char* env = std::getenv("OBE_K1_REFRESH");
+        v = env ? std::max(1, std::atoi(env)) : 8;
+    }
+    return v;
+}
+
 obe_status upload_plan(obe_plan* p) {
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
+    {
+        obe_status cst = init_constants();
+        if (cst != OBE_OK) return cst;
+    }
     if (p->d_blob && p->d_device == dev) return OBE_OK;
     if (p->d_blob) {
         cudaFree(p->d_blob);
@@ -1199,6 +1256,7 @@ obe_status upload_plan(obe_plan* p) {
     P.dyn_ids = reinterpret_cast<const int32_t*>(b + o_di);
     P.coeff_dyn_pos = reinterpret_cast<const int32_t*>(b + o_dp);
     P.time_dependent = p->time_dependent;
+    P.max_stack = std::max(1, h.max_stack);
     P.n_pchip = static_cast<int32_t>(h.pchip_cptr.size());
     P.pchip_ptr = reinterpret_cast<const int32_t*>(b + o_pp);
     P.pchip_grid = reinterpret_cast<const double*>(b + o_pg);
@@ -1274,7 +1332,7 @@ int sm_count() {
     return count;
 }
 
-obe_status plan_launch(const obe_plan* p, bool mixed, long long n_traj, LaunchShape* s) {
+obe_status plan_launch(const obe_plan* p, bool mixed, long long n_traj, int vm_depth, LaunchShape* s) {
     const DevPlan& P = p->dev;
     s->tpt = P.tpt;
     if (s->tpt > 128) {
@@ -1283,8 +1341,7 @@ obe_status plan_launch(const obe_plan* p, bool mixed, long long n_traj, LaunchSh
     }
     s->ept = ept_for(P.N, s->tpt);
     struct { size_t bytes; } L;
-    L.bytes = mixed ? group_layout_dev(P.N, P.n_formula, P.n_coeff, P.n_dyn, s->tpt).bytes
-                    : group_layout(P.N, P.n_formula, P.n_coeff, P.n_dyn, s->tpt, false).bytes;
+    L.bytes = group_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, vm_depth, s->tpt, mixed).bytes;
     s->group_bytes = L.bytes;
     size_t plan_bytes = plan_smem_bytes(P.n_iter, P.n_out, s->tpt);
     const size_t limit = 227 * 1024;
@@ -1532,8 +1589,10 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
     A.stats = d_stats;
     A.errs = d_errs;
     A.counter = d_counter;
+    A.k1_refresh = k1_refresh_interval();
+    A.vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
     LaunchShape s;
-    obe_status st = plan_launch(p, o->precision == OBE_PRECISION_MIXED, n_traj, &s);
+    obe_status st = plan_launch(p, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s);
     if (st != OBE_OK) return st;
     if (!cuda_ok(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync")) return OBE_ERR_CUDA;
     if (!cuda_ok(launch_integrate(p, A, o->precision == OBE_PRECISION_MIXED, o->solver, s, stream), "kernel launch")) return OBE_ERR_CUDA;
@@ -1790,7 +1849,8 @@ obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, co
     if ((st = check_params(p, n_override_slots, override_slots)) != OBE_OK) return st;
     const bool mixed = precision == OBE_PRECISION_MIXED;
     LaunchShape s;
-    if ((st = plan_launch(p, mixed, count, &s)) != OBE_OK) return st;
+    const int vm_depth = std::max(p->dev.max_stack, 1);
+    if ((st = plan_launch(p, false, count, vm_depth, &s)) != OBE_OK) return st;
     std::vector<int32_t> slots(override_slots, override_slots + n_override_slots);
     size_t off = 0;
     size_t o_t = off; off = align16(off + 8 * count);
@@ -1810,7 +1870,7 @@ obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, co
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(s.smem));
         kernel<<<s.blocks, s.gpb * s.tpt, s.smem>>>(p->dev, count, reinterpret_cast<double*>(d + o_t), reinterpret_cast<double*>(d + o_y),
                                                     n_override_slots, reinterpret_cast<int*>(d + o_sl), reinterpret_cast<double*>(d + o_ov),
-                                                    reinterpret_cast<double*>(d + o_dy), s.gpb, s.group_bytes);
+                                                    reinterpret_cast<double*>(d + o_dy), s.gpb, s.group_bytes, vm_depth);
     };
     if (s.tpt == 32) mixed ? run(rhs_kernel<32, true>) : run(rhs_kernel<32, false>);
     else if (s.tpt == 64) mixed ? run(rhs_kernel<64, true>) : run(rhs_kernel<64, false>);

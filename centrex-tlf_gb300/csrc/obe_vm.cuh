@@ -16,9 +16,11 @@
 
 namespace obe {
 
-struct VVal {
-    double re, im;
-    int32_t tup;  // >= 0: tuple id (tuples are base-slot constants)
+// A VM value: (re, im) in `v`, tuple id (>= 0, tuples are base-slot constants) in `tup`.
+// The stack lives in memory the caller provides (shared memory in the integrator).
+struct VStack {
+    double2* v;
+    int32_t* tup;
 };
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
@@ -42,7 +44,9 @@ __device__ __forceinline__ double2 cexp(double2 z) {
     } else if (isnan(re) && im == 0.0) {
         return z;
     }
-    double e = exp(re), s, c;
+    double e = exp(re);
+    if (im == 0.0) return make_double2(e, e * 0.0);
+    double s, c;
     sincos(im, &s, &c);
     return make_double2(e * c, e * s);
 }
@@ -88,8 +92,8 @@ __device__ __forceinline__ double rabi_from_intensity(double intensity, double c
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kEdXtB = 0.315 * 1.602176634e-19 * 5.29177210544e-11;
 
-__device__ __noinline__ double2 helper_scalar(int fid, const VVal* a, int argc) {
-    auto S = [&](int i) { return i < argc ? a[i].re : 0.0; };
+__device__ __noinline__ double2 helper_scalar(int fid, const double2* a, int argc) {
+    auto S = [&](int i) { return i < argc ? a[i].x : 0.0; };
     switch (fid) {
     case 1: return make_double2(g2d(S(0), S(1), S(2), S(3), S(4), S(5), S(6)), 0.0);
     case 2: {
@@ -154,33 +158,28 @@ __device__ double pchip_d(const double2* g, const double2* v, int n, int i) {
     return (w1 + w2) / (w1 / d0 + w2 / d1);
 }
 
-struct VMEnv {
-    const DevPlan* P;
-    const double2* slots;  // per-lane slot values (scalar slots)
-};
-
 __device__ __forceinline__ const double2* tuple_items(const DevPlan& P, int32_t id, int* len) {
     *len = P.tuple_ptr[id + 1] - P.tuple_ptr[id];
     return reinterpret_cast<const double2*>(P.tuple_items) + P.tuple_ptr[id];
 }
 
-__device__ __noinline__ double2 helper_general(const DevPlan& P, int fid, const VVal* a, int argc) {
+__device__ __noinline__ double2 helper_general(const DevPlan& P, int fid, const double2* a, const int32_t* tup, int argc) {
     if (fid == 8 || fid == 10) {
         int la, lx, ly;
-        const double2* amp = tuple_items(P, a[2].tup, &la);
-        const double2* xl = tuple_items(P, a[3].tup, &lx);
-        const double2* yl = tuple_items(P, a[4].tup, &ly);
+        const double2* amp = tuple_items(P, tup[2], &la);
+        const double2* xl = tuple_items(P, tup[3], &lx);
+        const double2* yl = tuple_items(P, tup[4], &ly);
         double acc = 0.0;
         int m = min(la, min(lx, ly));
-        for (int i = 0; i < m; ++i) acc += g2d(a[0].re, a[1].re, amp[i].x, xl[i].x, yl[i].x, a[5].re, a[6].re);
+        for (int i = 0; i < m; ++i) acc += g2d(a[0].x, a[1].x, amp[i].x, xl[i].x, yl[i].x, a[5].x, a[6].x);
         if (fid == 8) return make_double2(acc, 0.0);
-        return make_double2(rabi_from_intensity(acc, a[7].re, argc > 8 ? a[8].re : kEdXtB), 0.0);
+        return make_double2(rabi_from_intensity(acc, a[7].x, argc > 8 ? a[8].x : kEdXtB), 0.0);
     }
     if (fid == 14) {
         int lg, lv;
-        const double2* g = tuple_items(P, a[1].tup, &lg);
-        const double2* v = tuple_items(P, a[2].tup, &lv);
-        double x = a[0].re;
+        const double2* g = tuple_items(P, tup[1], &lg);
+        const double2* v = tuple_items(P, tup[2], &lv);
+        double x = a[0].x;
         if (lg == 1) return make_double2(v[0].x, 0.0);
         if (x <= g[0].x) return make_double2(v[0].x, 0.0);
         for (int i = 0; i < lg - 1; ++i) {
@@ -194,9 +193,9 @@ __device__ __noinline__ double2 helper_general(const DevPlan& P, int fid, const 
     }
     if (fid == 16) {  // direct PCHIP (eval.rs:305-351)
         int n, lv;
-        const double2* g = tuple_items(P, a[1].tup, &n);
-        const double2* v = tuple_items(P, a[2].tup, &lv);
-        double x = a[0].re;
+        const double2* g = tuple_items(P, tup[1], &n);
+        const double2* v = tuple_items(P, tup[2], &lv);
+        double x = a[0].x;
         if (n == 1) return make_double2(v[0].x, 0.0);
         if (x <= g[0].x) return make_double2(v[0].x, 0.0);
         if (x >= g[n - 1].x) return make_double2(v[n - 1].x, 0.0);
@@ -238,42 +237,49 @@ __device__ __noinline__ double pchip_table_eval(const DevPlan& P, int table, dou
 // Evaluate one program.  Programs were kind-checked on the host, so tuples only reach the
 // helpers that accept them and the result is a scalar.
 __device__ __noinline__ double2 vm_eval(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
-                           const double* val, int32_t start, int32_t len, const double2* slots, double t) {
-    VVal st[kMaxStack];
+                                        const double* val, int32_t start, int32_t len, const double2* slots, double t,
+                                        VStack S) {
+    double2* st = S.v;
+    int32_t* tp = S.tup;
     int sp = 0;
     for (int32_t k = start; k < start + len; ++k) {
         int32_t o = op[k];
         switch (o) {
-        case OP_CONST: st[sp++] = VVal{val[2 * k], val[2 * k + 1], -1}; break;
+        case OP_CONST: st[sp] = make_double2(val[2 * k], val[2 * k + 1]); tp[sp++] = -1; break;
         case OP_SLOT: {
             int32_t s = arg[k];
             int32_t tid = s < P.n_base ? P.base_tuple[s] : -1;
-            if (tid >= 0) st[sp++] = VVal{0.0, 0.0, tid};
-            else st[sp++] = VVal{slots[s].x, slots[s].y, -1};
+            st[sp] = tid >= 0 ? make_double2(0.0, 0.0) : slots[s];
+            tp[sp++] = tid;
             break;
         }
-        case OP_TIME: st[sp++] = VVal{t, 0.0, -1}; break;
+        case OP_TIME: st[sp] = make_double2(t, 0.0); tp[sp++] = -1; break;
         case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW: {
-            VVal r = st[--sp], l = st[sp - 1];
-            double2 a = make_double2(l.re, l.im), b = make_double2(r.re, r.im), c;
+            double2 b = st[--sp], a = st[sp - 1], c;
             if (o == OP_ADD) c = make_double2(a.x + b.x, a.y + b.y);
             else if (o == OP_SUB) c = make_double2(a.x - b.x, a.y - b.y);
             else if (o == OP_MUL) c = cmul(a, b);
             else if (o == OP_DIV) c = cdiv(a, b);
             else c = cpow(a, b);
-            st[sp - 1] = VVal{c.x, c.y, -1};
+            st[sp - 1] = c;
+            tp[sp - 1] = -1;
             break;
         }
-        case OP_NEG: st[sp - 1].re = -st[sp - 1].re; st[sp - 1].im = -st[sp - 1].im; break;
-        case OP_CONJ: st[sp - 1].im = -st[sp - 1].im; break;
+        case OP_NEG: st[sp - 1] = make_double2(-st[sp - 1].x, -st[sp - 1].y); break;
+        case OP_CONJ: st[sp - 1].y = -st[sp - 1].y; break;
         case OP_BUILTIN: {
             int argc = arg[k];
-            VVal x = st[sp - argc];
+            double2 z = st[sp - argc], r;
             sp -= argc;
-            double2 z = make_double2(x.re, x.im), r;
             switch (fn[k]) {
-            case 1: r = make_double2(sin(z.x) * cosh(z.y), cos(z.x) * sinh(z.y)); break;
-            case 2: r = make_double2(cos(z.x) * cosh(z.y), -sin(z.x) * sinh(z.y)); break;
+            case 1:
+            case 2: {
+                double sn, cs;
+                sincos(z.x, &sn, &cs);
+                double ch = z.y == 0.0 ? 1.0 : cosh(z.y), sh = z.y == 0.0 ? z.y : sinh(z.y);
+                r = fn[k] == 1 ? make_double2(sn * ch, cs * sh) : make_double2(cs * ch, -sn * sh);
+                break;
+            }
             case 3: {
                 double tr = z.x + z.x, ti = z.y + z.y, dd = cos(tr) + cosh(ti);
                 r = make_double2(sin(tr) / dd, sinh(ti) / dd);
@@ -284,33 +290,36 @@ __device__ __noinline__ double2 vm_eval(const DevPlan& P, const int32_t* op, con
             case 6: r = make_double2(z.x, 0.0); break;
             default: r = make_double2(z.y, 0.0); break;
             }
-            st[sp++] = VVal{r.x, r.y, -1};
+            st[sp] = r;
+            tp[sp++] = -1;
             break;
         }
         case OP_HELPER: {
             int argc = arg[k];
             sp -= argc;
-            double2 r = helper_general(P, fn[k], st + sp, argc);
-            st[sp++] = VVal{r.x, r.y, -1};
+            double2 r = helper_general(P, fn[k], st + sp, tp + sp, argc);
+            st[sp] = r;
+            tp[sp++] = -1;
             break;
         }
         case OP_PCHIP_TABLE: {
             sp -= 3;
-            double x = st[sp].re;
-            st[sp] = VVal{pchip_table_eval(P, fn[k], x), 0.0, -1};
-            ++sp;
+            double x = st[sp].x;
+            st[sp] = make_double2(pchip_table_eval(P, fn[k], x), 0.0);
+            tp[sp++] = -1;
             break;
         }
         default: {  // comparisons
-            double r = st[sp - 1].re, l = st[sp - 2].re;
+            double r = st[sp - 1].x, l = st[sp - 2].x;
             sp -= 2;
             bool res = o == OP_GT ? l > r : o == OP_GE ? l >= r : o == OP_LT ? l < r : o == OP_LE ? l <= r : o == OP_EQ ? l == r : l != r;
-            st[sp++] = VVal{res ? 1.0 : 0.0, 0.0, -1};
+            st[sp] = make_double2(res ? 1.0 : 0.0, 0.0);
+            tp[sp++] = -1;
             break;
         }
         }
     }
-    return make_double2(st[0].re, st[0].im);
+    return st[0];
 }
 
 }  // namespace obe
