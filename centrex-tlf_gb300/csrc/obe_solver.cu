@@ -1883,3 +1883,191 @@ obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, co
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free batch solve.
+//
+// For callers that must not allocate device memory while they solve (a caller that owns all
+// device memory up front through its own arena or a fixed memory budget, or that records its
+// work into a CUDA graph, cannot let a library call cudaMalloc underneath it): the same
+// integrator kernel as obe_solve_batch_device, but every byte of scratch it needs -- the
+// plan's device image, the per-call argument block, the per-trajectory error records and the
+// work-queue counter -- lives in one fixed, file-scope device array.  Every GPU that loads
+// this library holds the array until the process exits.
+
+namespace obe {
+namespace {
+
+constexpr size_t kNoAllocPlanBytes = 1u << 20;       // plan device image
+constexpr size_t kNoAllocArgBytes = 64u << 10;       // per-call argument block
+constexpr long long kNoAllocMaxTrajectories = 65536; // per-trajectory error records
+constexpr size_t kNoAllocCounterOff = 0;
+constexpr size_t kNoAllocPlanOff = 256;
+constexpr size_t kNoAllocArgOff = kNoAllocPlanOff + kNoAllocPlanBytes;
+constexpr size_t kNoAllocErrOff = kNoAllocArgOff + kNoAllocArgBytes;
+constexpr size_t kNoAllocBytes = kNoAllocErrOff + sizeof(TrajErr) * static_cast<size_t>(kNoAllocMaxTrajectories);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_base[64] = {nullptr};  // device address of g_noalloc_scratch, per device
+
+// The plan's device image laid out as upload_plan lays it out, with its pointers relative to
+// `base` (a device address), serialised into `blob` on the host.
+void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, unsigned char* base, DevPlan& P) {
+    const HostPacked& h = p->packed;
+    size_t o_op = put(blob, h.ins_op), o_arg = put(blob, h.ins_arg), o_fn = put(blob, h.ins_fn), o_val = put(blob, h.ins_val);
+    size_t o_bv = put(blob, h.base_val), o_bt = put(blob, h.base_tuple), o_tp = put(blob, h.tuple_ptr), o_ti = put(blob, h.tuple_items);
+    size_t o_cs = put(blob, h.comp_slot), o_ce = put(blob, h.comp_expr), o_cd = put(blob, h.comp_dynamic);
+    size_t o_ke = put(blob, h.coeff_expr), o_kd = put(blob, h.coeff_dynamic), o_di = put(blob, h.dyn_ids), o_dp = put(blob, h.coeff_dyn_pos);
+    size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
+    size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
+    size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out);
+    P = DevPlan{};
+    P.n = p->n;
+    P.N = static_cast<int32_t>(p->N);
+    P.U = static_cast<int32_t>(p->U);
+    P.ins_op = reinterpret_cast<const int32_t*>(base + o_op);
+    P.ins_arg = reinterpret_cast<const int32_t*>(base + o_arg);
+    P.ins_fn = reinterpret_cast<const int32_t*>(base + o_fn);
+    P.ins_val = reinterpret_cast<const double*>(base + o_val);
+    P.n_slots = p->n_slots;
+    P.n_base = p->n_base;
+    P.base_val = reinterpret_cast<const double*>(base + o_bv);
+    P.base_tuple = reinterpret_cast<const int32_t*>(base + o_bt);
+    P.tuple_ptr = reinterpret_cast<const int32_t*>(base + o_tp);
+    P.tuple_items = reinterpret_cast<const double*>(base + o_ti);
+    P.n_comp = static_cast<int32_t>(h.comp_slot.size());
+    P.comp_slot = reinterpret_cast<const int32_t*>(base + o_cs);
+    P.comp_expr = reinterpret_cast<const DevExpr*>(base + o_ce);
+    P.comp_dynamic = reinterpret_cast<const uint8_t*>(base + o_cd);
+    P.n_coeff = p->n_coeff;
+    P.coeff_expr = reinterpret_cast<const DevExpr*>(base + o_ke);
+    P.coeff_dynamic = reinterpret_cast<const uint8_t*>(base + o_kd);
+    P.n_dyn = static_cast<int32_t>(h.dyn_ids.size());
+    P.dyn_ids = reinterpret_cast<const int32_t*>(base + o_di);
+    P.coeff_dyn_pos = reinterpret_cast<const int32_t*>(base + o_dp);
+    P.time_dependent = p->time_dependent;
+    P.max_stack = std::max(1, h.max_stack);
+    P.n_pchip = static_cast<int32_t>(h.pchip_cptr.size());
+    P.pchip_ptr = reinterpret_cast<const int32_t*>(base + o_pp);
+    P.pchip_grid = reinterpret_cast<const double*>(base + o_pg);
+    P.pchip_coef = reinterpret_cast<const double*>(base + o_pc);
+    P.pchip_cptr = reinterpret_cast<const int32_t*>(base + o_pcp);
+    P.n_formula = h.n_formula;
+    P.n_static_formula = h.n_static_formula;
+    P.formula_ptr = reinterpret_cast<const int32_t*>(base + o_fp);
+    P.prod_factor = reinterpret_cast<const double*>(base + o_pf);
+    P.prod_class = reinterpret_cast<const int32_t*>(base + o_pcl);
+    P.prod_factor32 = reinterpret_cast<const float*>(base + o_pf32);
+    P.tpt = h.tpt;
+    P.n_iter = h.n_iter;
+    P.rec = reinterpret_cast<const uint32_t*>(base + o_rec);
+    P.n_out = h.n_out;
+    P.lane_out = reinterpret_cast<const uint32_t*>(base + o_lo);
+}
+
+}  // namespace
+}  // namespace obe
+
+extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
+                                                     const double* d_rho0, int32_t n_param_slots, const int64_t* param_slots,
+                                                     const double* d_param_values, int64_t time_count, int64_t width,
+                                                     double* d_values, obe_traj_stats* d_stats, void* stream) {
+    using namespace obe;
+    g_launches = 0;
+    obe_plan* p = const_cast<obe_plan*>(plan);
+    if (!p || !opt || !d_rho0 || !d_values || !d_stats) { set_error("null argument"); return OBE_ERR_INVALID; }
+    if (n_traj <= 0) { set_error("n_traj must be positive"); return OBE_ERR_INVALID; }
+    if (n_traj > kNoAllocMaxTrajectories) {
+        set_error("obe_solve_batch_device_noalloc handles at most " + std::to_string(kNoAllocMaxTrajectories) +
+                  " trajectories per call, got " + std::to_string(n_traj));
+        return OBE_ERR_INVALID;
+    }
+    if (!p->has_expanded) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
+    if (obe_device_count() <= 0) { set_error("no CUDA device is available: the GB300 solver has no CPU fallback"); return OBE_ERR_CUDA; }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
+    if (dev < 0 || dev >= 64) { set_error("device index out of range for the allocation-free entry point"); return OBE_ERR_UNSUPPORTED; }
+    // once per device, with that device current: the device address of the scratch array
+    if (!g_noalloc_base[dev]) {
+        void* base = nullptr;
+        if (!cuda_ok(cudaGetSymbolAddress(&base, g_noalloc_scratch), "cudaGetSymbolAddress(scratch)")) return OBE_ERR_CUDA;
+        g_noalloc_base[dev] = base;
+    }
+    obe_status st = init_constants();
+    if (st != OBE_OK) return st;
+    if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
+    std::vector<double> save_times;
+    CallBlob cb;
+    int64_t w = 0;
+    int cplx = 0;
+    if ((st = validate_options(p, opt, save_times, cb, &w, &cplx)) != OBE_OK) return st;
+    if (w != width) { set_error("output width mismatch"); return OBE_ERR_INVALID; }
+    if (cb.bytes.size() > kNoAllocArgBytes) {
+        set_error("per-call arguments (saveat, weights, selections, event program) exceed the " +
+                  std::to_string(kNoAllocArgBytes) + "-byte block of the allocation-free entry point");
+        return OBE_ERR_INVALID;
+    }
+    unsigned char* base = static_cast<unsigned char*>(g_noalloc_base[dev]);
+    std::vector<unsigned char> image;
+    DevPlan P;
+    build_plan_image(p, image, base + kNoAllocPlanOff, P);
+    if (image.size() > kNoAllocPlanBytes) {
+        set_error("plan device image (" + std::to_string(image.size()) + " bytes) exceeds the " +
+                  std::to_string(kNoAllocPlanBytes) + "-byte plan block of the allocation-free entry point");
+        return OBE_ERR_INVALID;
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!cuda_ok(cudaMemcpyAsync(base + kNoAllocPlanOff, image.data(), image.size(), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(plan image)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyAsync(base + kNoAllocArgOff, cb.bytes.data(), cb.bytes.size(), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(arguments)")) return OBE_ERR_CUDA;
+    // the work-queue counter must start at zero on every call
+    if (!cuda_ok(cudaMemsetAsync(base + kNoAllocCounterOff, 0, sizeof(unsigned long long), s), "cudaMemsetAsync(counter)")) return OBE_ERR_CUDA;
+
+    CallArgs A;
+    fill_call_args(A, opt, save_times, cb, base + kNoAllocArgOff);
+    A.n_traj = n_traj;
+    A.rho0 = d_rho0;
+    A.rho0_stride = p->N;
+    A.n_param = d_param_values ? n_param_slots : 0;
+    for (int k = 0; k < A.n_param; ++k) A.param_slot[k] = static_cast<int>(param_slots[k]);
+    A.param_values = d_param_values;
+    A.n_axes = 0;
+    A.axes = nullptr;
+    A.cap = time_count;
+    A.out_stride = time_count * width * (cplx ? 2 : 1);
+    A.values = d_values;
+    A.times = nullptr;
+    A.stats = d_stats;
+    A.errs = reinterpret_cast<TrajErr*>(base + kNoAllocErrOff);
+    A.counter = reinterpret_cast<unsigned long long*>(base + kNoAllocCounterOff);
+    A.k1_refresh = k1_refresh_interval();
+    A.vm_depth = std::max(P.max_stack, std::max(cb.ev_len, 1));
+
+    // launch shape, as for the allocating entry points
+    const bool mixed = opt->precision == OBE_PRECISION_MIXED;
+    LaunchShape shape;
+    shape.tpt = P.tpt;
+    if (shape.tpt > 128) { set_error("systems with more than 45 states are not supported by this build of the GPU solver"); return OBE_ERR_UNSUPPORTED; }
+    shape.ept = ept_for(P.N, shape.tpt);
+    shape.group_bytes = group_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, shape.tpt, mixed).bytes;
+    const size_t plan_bytes = plan_smem_bytes(P.n_iter, P.n_out, shape.tpt);
+    const size_t limit = 227 * 1024;
+    int gpb = std::max(1, 256 / shape.tpt);
+    while (gpb > 1 && plan_bytes + gpb * shape.group_bytes > limit) --gpb;
+    if (plan_bytes + gpb * shape.group_bytes > limit) { set_error("system too large for the GPU solver's shared-memory layout"); return OBE_ERR_UNSUPPORTED; }
+    const long long per_sm = (n_traj + sm_count() - 1) / sm_count();
+    while (gpb > 1 && gpb > per_sm) --gpb;
+    shape.gpb = gpb;
+    shape.smem = plan_bytes + gpb * shape.group_bytes;
+    const int blocks_per_sm = std::max<int>(1, static_cast<int>(limit / shape.smem));
+    shape.blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n_traj + gpb - 1) / gpb, static_cast<long long>(sm_count()) * blocks_per_sm)));
+    const int method = opt->solver == OBE_SOLVER_TSIT5 ? 1 : 0;
+    cudaError_t e = mixed ? dispatch_shape<true>(P, A, shape, method, s) : dispatch_shape<false>(P, A, shape, method, s);
+    if (!cuda_ok(e, "kernel launch")) return OBE_ERR_CUDA;
+    g_launches += 1;
+    // the host copy of the plan image may go: cudaMemcpyAsync from pageable memory returns only
+    // once the source has been staged
+    return OBE_OK;
+}

@@ -230,6 +230,31 @@ obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options*
                                   int64_t time_count, int64_t width, double* d_values,
                                   obe_traj_stats* d_stats, void* stream);
 
+/*
+ * Allocation-free form of obe_solve_batch_device (no counterpart in the reference).  Some
+ * callers cannot let a library allocate device memory while they solve: a caller that owns all
+ * device memory up front through its own arena or a fixed memory budget, or one that records
+ * its GPU work into a CUDA graph.  This entry point calls no cudaMalloc/cudaFree (and no
+ * allocating library routine); the caller passes every input and output in device memory.  All
+ * scratch the integrator needs -- the plan's device image, the per-call argument block, the
+ * per-trajectory error records and the work-queue counter -- lives in one fixed file-scope
+ * device array of 2,687,232 bytes (about 2.6 MiB) that every GPU which loads this library holds until the process
+ * exits.
+ * Limits: at most 65,536 trajectories per call, a plan device image of at most 1 MiB and at
+ * most 64 KiB of per-call arguments (saveat, weights, selections, event program); larger
+ * requests are rejected with OBE_ERR_INVALID and a message saying which limit was hit.
+ * The first call on a device looks up the array's device address (once per device, with that
+ * device current); make that first call before any stream capture begins.
+ * Every call shares the one array and leaves its contents behind: calls whose GPU work overlaps
+ * (other streams, other host threads) race on it and must be serialised by the caller.
+ * Per-trajectory statuses land in d_stats as with obe_solve_batch_device.
+ */
+obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const obe_solve_options* opt,
+                                          int64_t n_traj, const double* d_rho0, int32_t n_param_slots,
+                                          const int64_t* param_slots, const double* d_param_values,
+                                          int64_t time_count, int64_t width, double* d_values,
+                                          obe_traj_stats* d_stats, void* stream);
+
 /* Number of kernel launches issued by the last solve in this thread (for accounting). */
 int64_t obe_last_launch_count(void);
 

@@ -1,0 +1,107 @@
+"""The allocation-free batch entry point (obe_solve_batch_device_noalloc).
+
+It exists for callers that cannot let a library allocate device memory while they solve -- a
+caller that owns all device memory up front (its own arena, a fixed budget) or that records its
+GPU work into a CUDA graph.  It must produce exactly what the allocating device entry point
+produces, call after call, although every call reuses the same fixed device scratch array.
+
+This file is collected last, so that a run that stops at the first failure has already run
+every other test; it also passes on its own in a fresh process.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from centrex_tlf_gb300 import _abi
+from centrex_tlf_gb300 import centrex_tlf_rust as api
+
+pytestmark = pytest.mark.gpu
+
+W_EXCITED = [(13, 1.0), (14, 1.0), (15, 1.0)]
+
+
+def _noalloc(lib):
+    fn = lib.obe_solve_batch_device_noalloc
+    fn.argtypes = [
+        ctypes.c_void_p, ctypes.POINTER(_abi.ObeSolveOptions), ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32,
+        _abi.c_i64p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+    ]
+    fn.restype = ctypes.c_int
+    return fn
+
+
+@pytest.mark.parametrize("precision,output", [("fp64", "populations"), ("mixed", "excited_population")])
+def test_noalloc_matches_allocating_entry_point_on_consecutive_calls(golden, precision, output):
+    torch = pytest.importorskip("torch")
+    d = golden("plan_q1_16")
+    gamma, (t0, t1) = d["gamma"], d["t_span"]
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    native = plan.native
+    slot_names = d["payload"]["parameter_graph"]["slot_names"]
+    slots = [slot_names.index(s) for s in ("rabi", "detuning", "theta")]
+    rng = np.random.default_rng(5)
+    b = 48
+    params = np.stack([gamma * 10 ** rng.uniform(-1, 1, b), rng.uniform(-5, 5, b) * gamma, rng.uniform(0, np.pi, b)],
+                      axis=1).astype(np.complex128)
+    final_pops = output == "populations"
+    opts = native.options(
+        t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma,
+        saveat=np.array([t1]) if final_pops else None, save_start=not final_pops, maxiters=100000, solver="tsit5",
+        output=output, output_indices=None, output_when="final",
+        integral_weights=None if final_pops else W_EXCITED, stop_event=None, precision=precision,
+    )
+    width = opts.width
+    dev = torch.device("cuda:0")
+    d_rho = torch.from_numpy(np.repeat(d["rho0_packed"].reshape(1, -1), b, axis=0)).to(dev)
+    d_par = torch.from_numpy(np.ascontiguousarray(params).view(np.float64).reshape(-1)).to(dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    slots_arr = np.asarray(slots, dtype=np.int64)
+
+    # the allocating device entry point: the expected result
+    ref_vals = torch.zeros(b * width, dtype=torch.float64, device=dev)
+    ref_stats = torch.zeros(b * 6, dtype=torch.int64, device=dev)
+    native.solve_batch_device(opts, b, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, ref_vals.data_ptr(),
+                              ref_stats.data_ptr(), stream)
+    torch.cuda.synchronize()
+
+    lib = _abi.load_library()
+    fn = _noalloc(lib)
+    for call in range(2):
+        vals = torch.full((b * width,), float("nan"), dtype=torch.float64, device=dev)
+        stats = torch.full((b * 6,), -1, dtype=torch.int64, device=dev)
+        st = fn(native.handle, ctypes.byref(opts.opts), b, d_rho.data_ptr(), len(slots),
+                slots_arr.ctypes.data_as(_abi.c_i64p), d_par.data_ptr(), 1, width, vals.data_ptr(), stats.data_ptr(),
+                ctypes.c_void_p(stream))
+        assert st == _abi.OBE_OK, _abi.last_error(lib)
+        torch.cuda.synchronize()
+        # same kernel, same inputs: the tolerance of the FP64 parity tests, met exactly here
+        np.testing.assert_allclose(vals.cpu().numpy(), ref_vals.cpu().numpy(), rtol=1e-12, atol=0.0,
+                                   err_msg=f"call {call}")
+        np.testing.assert_array_equal(stats.cpu().numpy(), ref_stats.cpu().numpy())
+        status = stats.view(b, 6)[:, 3].cpu().numpy() >> 32
+        assert np.all(status == 0)
+
+
+def test_noalloc_rejects_sizes_beyond_its_limit(golden):
+    torch = pytest.importorskip("torch")
+    d = golden("plan_two_level")
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    native = plan.native
+    opts = native.options(t0=0.0, t1=0.5, abstol=1e-10, reltol=1e-8, dt=1e-3, saveat=np.array([0.5]), save_start=False,
+                          maxiters=100000, solver="dopri5", output="populations", output_indices=None,
+                          output_when="final", integral_weights=None, stop_event=None)
+    lib = _abi.load_library()
+    fn = _noalloc(lib)
+    dev = torch.device("cuda:0")
+    too_many = 65537
+    rho = torch.zeros(4, dtype=torch.float64, device=dev)
+    out = torch.zeros(2, dtype=torch.float64, device=dev)
+    st_buf = torch.zeros(6, dtype=torch.int64, device=dev)
+    st = fn(native.handle, ctypes.byref(opts.opts), too_many, rho.data_ptr(), 0, None, None, 1, 2, out.data_ptr(),
+            st_buf.data_ptr(), None)
+    assert st == _abi.OBE_ERR_INVALID
+    assert "at most 65536 trajectories" in _abi.last_error(lib)
