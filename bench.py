@@ -6,7 +6,10 @@ J'=1 F'=1 (+ lumped X J=3) system, Gaussian Rabi pulse (peak Γ·10^U[-1,1], σ 
 rtol 1e-8 / atol 1e-11 over [0, 200/Γ], observable = time-integrated excited population.  The
 plan payload is the reference builders' own output (tests/golden/plan_q1_16.json).
 
-A "step" is one solve of the whole 4096-point batch.  `value` times the device-resident entry
+A "step" is one solve of the whole 4096-point batch.  The default precision is the mixed form
+(single-precision RHS products, double-precision state, error norm and controller); its final
+populations are compared with the plain FP64 path on every point, and the FP64 path is timed on
+the same batch beside it (`fp64_gpu`).  `value` times the device-resident entry
 point (obe_solve_batch_device) with CUDA events on its stream and the L2 flushed between steps;
 `e2e` times the reference-facing call solve_lindblad_batch_ode_py with host arrays (copies in
 the timed region).  `--impl reference` times the CPU path of the reference restated in C
@@ -16,6 +19,7 @@ the timed region).  `--impl reference` times the CPU path of the reference resta
 from __future__ import annotations
 
 import argparse
+import contextlib
 import json
 import os
 import subprocess
@@ -203,40 +207,53 @@ def run_gpu(args) -> None:
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
     stream = torch.cuda.current_stream(dev)
 
-    def step():
-        native.solve_batch_device(opts, b, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, d_val.data_ptr(), d_st.data_ptr(),
-                                  stream.cuda_stream)
+    def timed(o, steps, sampler=None):
+        """Warm-up, then `steps` device-resident solves of the batch, L2 flushed before each;
+        returns (per-step ms, attempted steps of the last solve)."""
+        def step():
+            native.solve_batch_device(o, b, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, d_val.data_ptr(),
+                                      d_st.data_ptr(), stream.cuda_stream)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    attempted = 0
-    clock_path = Path(tempfile.gettempdir()) / f"obe_clocks_{os.getpid()}.csv"
-    with ClockSampler(clock_path) as sampler:
-        torch.cuda.synchronize()
-        for i in range(args.steps):
-            flush.zero_()
-            starts[i].record(stream)
+        for _ in range(args.warmup):
             step()
-            ends[i].record(stream)
         torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    st = d_st.view(b, 6).cpu().numpy()
-    status = st[:, 3] >> 32
-    if np.any(status != 0):
-        raise RuntimeError(f"{int(np.count_nonzero(status))} trajectories failed on the GPU")
-    attempted = int(st[:, 0].sum() + st[:, 1].sum())
-    ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        if world > 1:
+            torch.distributed.barrier()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        with sampler if sampler is not None else contextlib.nullcontext():
+            torch.cuda.synchronize()
+            for i in range(steps):
+                flush.zero_()
+                starts[i].record(stream)
+                step()
+                ends[i].record(stream)
+            torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        st = d_st.view(b, 6).cpu().numpy()
+        status = st[:, 3] >> 32
+        if np.any(status != 0):
+            raise RuntimeError(f"{int(np.count_nonzero(status))} trajectories failed on the GPU")
+        return [s.elapsed_time(e) for s, e in zip(starts, ends)], int(st[:, 0].sum() + st[:, 1].sum())
+
+    clock_path = Path(tempfile.gettempdir()) / f"obe_clocks_{os.getpid()}.csv"
+    sampler = ClockSampler(clock_path)
+    ms, attempted = timed(opts, args.steps, sampler)
+    # the plain FP64 GPU path on the same batch, for the mixed/FP64 speed ratio
+    other = None
+    if args.precision != "fp64" and not args.no_fp64_compare:
+        o64 = native.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=None, save_start=True,
+                             maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
+                             output_when="final", integral_weights=W_EXCITED, stop_event=None, precision="fp64")
+        ms64, att64 = timed(o64, args.steps)
+        other = (ms64, att64)
     total_s = sum(ms) * 1e-3
+    total64_s = sum(other[0]) * 1e-3 if other else 0.0
     if world > 1:
-        t = torch.tensor([total_s], device=dev, dtype=torch.float64)
+        t = torch.tensor([total_s, total64_s], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
+        total_s, total64_s = float(t[0].item()), float(t[1].item())
     value = b * world * args.steps / total_s
     launches = args.steps  # one integrator launch per solve (obe_last_launch_count agrees)
 
@@ -300,6 +317,10 @@ def run_gpu(args) -> None:
                              f"{f_rhs}) / mean launch time; peak = cuBLAS DGEMM measured in this run (no FP64 entry in "
                              "the driver's peak file)"},
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "fp64_gpu": ({"value": b * world * args.steps / total64_s, "unit": "trajectories/s",
+                      "ms_per_step": sum(other[0]) / len(other[0]), "attempted_steps_per_launch": other[1],
+                      "speedup_of_this_precision": (b * world * args.steps / total_s) / (b * world * args.steps / total64_s)}
+                     if other else None),
         "accuracy": {"max_population_error_vs_fp64_gpu": max_pop_err, "observable_max_rel_err_vs_cpu_oracle": obs_rel},
         "clocks": clocks,
     }
@@ -314,7 +335,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 path beside mixed")
     ap.add_argument("--points", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--ref-sample", type=int, default=256)

@@ -23,7 +23,7 @@ OBE_ERR_UNSUPPORTED = 3
 OBE_ERR_CUDA = 4
 OBE_ERR_TIMEOUT = 5
 
-SOLVERS = {"dopri5": 0, "tsit5": 1}
+SOLVERS = {"dopri5": 0, "tsit5": 1, "fixed_dopri5": 2, "fixed_rk2": 3, "fixed_rk4": 4}
 OUTPUT_POPULATIONS = 0
 OUTPUT_SELECTED = 1
 OUTPUT_FULL = 2

@@ -8,8 +8,10 @@ GB300 CUDA solver.  ``install()`` registers it under that import path so the ref
 ``solve_lindblad``/``solve_lindblad_batch``/``parameter_scan``/``initial_condition_scan``/
 ``grid_scan`` drive the GPU unchanged.
 
-Only ``mode="expanded_sparse"`` with the adaptive ``dopri5``/``tsit5`` solvers runs here; the
-reference's other execution modes and fixed-step solvers raise ``NotImplementedError``.
+Only ``mode="expanded_sparse"`` runs here (with every solver of the reference: ``dopri5``,
+``tsit5``, ``fixed_dopri5``, ``fixed_rk2``, ``fixed_rk4``); the reference's other execution modes
+raise ``NotImplementedError``.  The extra keyword ``precision="mixed"`` (adaptive solvers only)
+selects single-precision RHS products with double-precision state, error norm and controller.
 """
 
 from __future__ import annotations
@@ -67,8 +69,6 @@ def _check_solver(solver: str) -> None:
             "solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4', "
             f"got {_rust_repr(solver)}"
         )
-    if solver not in ("dopri5", "tsit5"):
-        raise NotImplementedError(f"solver={solver!r} is not part of the GB300 solver; use 'dopri5' or 'tsit5'")
 
 
 def _time_tol(t: float) -> float:

@@ -83,6 +83,7 @@ struct DevPlan {
     const double* prod_factor;   // [2 * n_prod]
     const int32_t* prod_class;   // [n_prod] -1 = constant 1, else coeff * 2 + conj
     const float* prod_factor32;  // [2 * n_prod] single-precision copy (mixed form)
+    int32_t dyn_prod0, n_dyn_prod;  // the time-dependent formulas' products: [dyn_prod0, dyn_prod0 + n_dyn_prod)
     // gather stream, lane interleaved for `tpt` threads per trajectory
     int32_t tpt;
     int32_t n_iter;              // records per thread (padded)

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
@@ -91,7 +92,8 @@ enum TrajCode : int32_t {
     ST_EVENT_INDEX = 6,
     ST_POINTS = 7,
     ST_BAD_MAXITERS = 8,
-    ST_BACKWARD = 9
+    ST_BACKWARD = 9,
+    ST_FIXED_DT = 10
 };
 
 struct TrajErr {
@@ -139,6 +141,7 @@ struct CallArgs {
     unsigned long long* counter;
     int k1_refresh;  // mixed form: recompute k_1 in double every this many accepted steps
     int vm_depth;    // VM stack depth of the plan's and the event's programs
+    int fixed;       // 0: adaptive; else the fixed-step obe_solver value (double-precision form only)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -184,8 +187,23 @@ __host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula,
     return L;
 }
 
-__host__ __device__ inline size_t plan_smem_bytes(int n_iter, int n_out, int tpt) {
-    return align16(static_cast<size_t>(n_iter + n_out) * tpt * 4);
+// Per-CTA shared copy of the plan: the gather stream (records, output slots) and, for the
+// time-dependent formulas, their product lists (offsets, coefficient classes, factors in the
+// precision of the form).
+struct PlanSmem {
+    size_t rec, out, fptr, fcls, ffac, bytes;
+};
+
+__host__ __device__ inline PlanSmem plan_smem(const DevPlan& P, int tpt, bool mixed) {
+    PlanSmem L{};
+    size_t o = 0;
+    L.rec = o; o += static_cast<size_t>(P.n_iter) * tpt * 4;
+    L.out = o; o = align16(o + static_cast<size_t>(P.n_out) * tpt * 4);
+    L.fptr = o; o = align16(o + static_cast<size_t>(P.n_formula - P.n_static_formula + 1) * 4);
+    L.fcls = o; o = align16(o + static_cast<size_t>(P.n_dyn_prod) * 4);
+    L.ffac = o; o = align16(o + static_cast<size_t>(P.n_dyn_prod) * (mixed ? 8 : 16));
+    L.bytes = o;
+    return L;
 }
 
 template <int TPT>
@@ -287,18 +305,45 @@ __device__ __forceinline__ void fill_formulas(const DevPlan& P, int lo, int hi, 
     }
 }
 
+// The time-dependent formulas in double from the CTA's shared copy of their product lists.
+template <int TPT>
+__device__ __forceinline__ void fill_formulas_dyn(const DevPlan& P, const int32_t* __restrict__ fptr,
+                                                  const int32_t* __restrict__ fcls, const double2* __restrict__ ffac,
+                                                  const double2* cstat, const double2* crow, double2* tab, int lt) {
+    const int S = P.n_static_formula;
+    for (int f = 1 + S + lt; f < 1 + P.n_formula; f += TPT) {
+        int a = fptr[f - 1 - S], b = fptr[f - S];
+        double2 acc = make_double2(0.0, 0.0);
+        for (int p = a; p < b; ++p) {
+            double2 fac = ffac[p];
+            int cls = fcls[p];
+            double2 c = cls < 0 ? make_double2(1.0, 0.0) : coeff_value(P, cls, cstat, crow);
+            double2 v = cmul(fac, c);
+            acc.x += v.x;
+            acc.y += v.y;
+        }
+        tab[f] = acc;
+    }
+}
+
 // Single-precision formula values at a stage time (.xy) and their change since the step's
 // start time (.zw).  cv holds, per coefficient class (k, conj), the value and the change as
 // float4; the changes were taken in double before rounding, so they keep their relative
 // precision.  Pure single-precision work per product.
+// The time-dependent formulas (entries 1 + n_static_formula .. n_formula) from the CTA's shared
+// copy of their product lists: fptr relative to the first such product.
 template <int TPT>
-__device__ __forceinline__ void fill_formulas_dev(const DevPlan& P, int lo, int hi, const float4* cv, float4* T4, int lt) {
-    for (int f = lo + lt; f < hi; f += TPT) {
-        int a = P.formula_ptr[f - 1], b = P.formula_ptr[f];
+__device__ __forceinline__ void fill_formulas_dev(const DevPlan& P, const int32_t* __restrict__ fptr,
+                                                  const int32_t* __restrict__ fcls, const float2* __restrict__ ffac,
+                                                  const float4* __restrict__ cv, float4* __restrict__ T4, int lt) {
+    const int S = P.n_static_formula;
+    for (int f = 1 + S + lt; f < 1 + P.n_formula; f += TPT) {
+        int a = fptr[f - 1 - S], b = fptr[f - S];
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int p = a; p < b; ++p) {
-            float fr = P.prod_factor32[2 * p], fi = P.prod_factor32[2 * p + 1];
-            int cls = P.prod_class[p];
+            const float2 fac = ffac[p];
+            const float fr = fac.x, fi = fac.y;
+            int cls = fcls[p];
             if (cls < 0) {
                 acc.x += fr;
                 acc.y += fi;
@@ -329,9 +374,11 @@ __device__ __forceinline__ void stage_classes(const DevPlan& P, const double2* c
 }
 
 // The packed expanded_sparse RHS: one record = one 16-byte coefficient and one 16-byte input.
+// The formula table, the slot buffer and the output are disjoint (restrict), so the operand
+// loads of later records can be issued ahead of the output stores of earlier ones.
 template <int TPT, typename T, typename T2>
 __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
-                                           const T2* tab, const T2* G, T* K, int lt) {
+                                           const T2* __restrict__ tab, const T2* __restrict__ G, T* __restrict__ K, int lt) {
     T ar = 0, ai = 0;
     int o = 0;
     const int n_iter = P.n_iter;
@@ -360,7 +407,8 @@ __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __r
 // Stage deviation d_s = L(t_s) (y_s - y_n) + (L(t_s) - L(t_n)) y_n, all in single precision.
 template <int TPT>
 __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
-                                           const float4* T4, const float4* G4, float* K, int lt) {
+                                           const float4* __restrict__ T4, const float4* __restrict__ G4, float* __restrict__ K,
+                                           int lt) {
     float ar = 0.f, ai = 0.f;
     int o = 0;
     const int n_iter = P.n_iter;
@@ -407,20 +455,32 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
     const int lt = static_cast<int>(threadIdx.x) % TPT;
     const int n = P.n, N = P.N, U = P.U;
 
-    // stage the plan's gather stream once per CTA
-    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
-    uint32_t* s_out = s_rec + static_cast<size_t>(P.n_iter) * TPT;
+    // stage the plan's gather stream and time-dependent formula products once per CTA
+    const PlanSmem PS = plan_smem(P, TPT, MIXED);
+    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem + PS.rec);
+    uint32_t* s_out = reinterpret_cast<uint32_t*>(smem + PS.out);
+    int32_t* s_fptr = reinterpret_cast<int32_t*>(smem + PS.fptr);
+    int32_t* s_fcls = reinterpret_cast<int32_t*>(smem + PS.fcls);
+    float2* s_ffac32 = reinterpret_cast<float2*>(smem + PS.ffac);
+    double2* s_ffac64 = reinterpret_cast<double2*>(smem + PS.ffac);
     {
-        const int total = (P.n_iter + P.n_out) * TPT;
-        for (int i = threadIdx.x; i < total; i += blockDim.x)
-            s_rec[i] = i < P.n_iter * TPT ? P.rec[i] : P.lane_out[i - P.n_iter * TPT];
+        for (int i = threadIdx.x; i < P.n_iter * TPT; i += blockDim.x) s_rec[i] = P.rec[i];
+        for (int i = threadIdx.x; i < P.n_out * TPT; i += blockDim.x) s_out[i] = P.lane_out[i];
+        const int nf = P.n_formula - P.n_static_formula;
+        for (int i = threadIdx.x; i <= nf; i += blockDim.x) s_fptr[i] = P.formula_ptr[P.n_static_formula + i] - P.dyn_prod0;
+        for (int i = threadIdx.x; i < P.n_dyn_prod; i += blockDim.x) {
+            const int q = P.dyn_prod0 + i;
+            s_fcls[i] = P.prod_class[q];
+            if constexpr (MIXED) s_ffac32[i] = make_float2(P.prod_factor32[2 * q], P.prod_factor32[2 * q + 1]);
+            else s_ffac64[i] = make_double2(P.prod_factor[2 * q], P.prod_factor[2 * q + 1]);
+        }
     }
     __syncthreads();
     if (g >= gpb) return;
 
     const int vm_depth = A.vm_depth;
     const GroupLayout Lay = group_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, vm_depth, TPT, MIXED);
-    unsigned char* gb = smem + plan_smem_bytes(P.n_iter, P.n_out, TPT) + static_cast<size_t>(g) * group_bytes;
+    unsigned char* gb = smem + PS.bytes + static_cast<size_t>(g) * group_bytes;
     double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
     double2* s_G = reinterpret_cast<double2*>(gb + Lay.G);
     double* s_G64 = reinterpret_cast<double*>(gb + Lay.G);
@@ -603,7 +663,10 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
         // one double-precision RHS from the slot buffer: formulas for coefficient row `row`, gather into out
         auto rhs64 = [&](int row, double* out) {
             gsync<TPT>(g);  // G written, coefficient row ready
-            if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
+            if (F > S) {
+                if constexpr (MIXED) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
+                else fill_formulas_dyn<TPT>(P, s_fptr, s_fcls, s_ffac64, s_cstat, s_cdyn + row * nd, s_tab, lt);
+            }
             gsync<TPT>(g);
             gather_rhs<TPT, double, double2>(P, s_rec, s_out, s_tab, s_G, out, lt);
             gsync<TPT>(g);  // out complete, G free
@@ -622,12 +685,165 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
         } else if (t1 < t0) {
             status = ST_BACKWARD;
             done = true;
+        } else if (A.fixed && !(isfinite(A.dt) && A.dt > 0.0)) {
+            status = ST_FIXED_DT;
+            done = true;
         } else if (t1 == t0) {
             if (A.save_start) {
                 stage_registers_to_buf(y);
                 push(t0);
             }
             done = true;
+        }
+
+        // ---------------- fixed-step solvers (fixed.rs:133-249), double precision ----------------
+        if constexpr (!MIXED) {
+            if (A.fixed && !done) {
+                done = true;
+                int fsi = 0;
+                if (A.has_saveat) {
+                    bool buffered = false;
+                    while (fsi < A.n_save && fabs(A.save_times[fsi] - t0) <= time_tol(t0)) {
+                        if (!buffered) { stage_registers_to_buf(y); buffered = true; }
+                        push(A.save_times[fsi]);
+                        ++fsi;
+                    }
+                } else if (A.save_start) {
+                    stage_registers_to_buf(y);
+                    push(t0);
+                }
+                bool ev_old_has = false;
+                double ev_old = 0.0;
+                if (A.ev_kind != OBE_EVENT_NONE) {
+                    stage_registers_to_buf(y);
+                    event_value(t0, ev_old_has, ev_old);
+                }
+                double x = t0;
+                long long steps = 0;
+                while (status == ST_OK && x < t1 - time_tol(t1)) {
+                    if (steps >= A.maxiters) { status = ST_MAXITERS; err_x = x; err_a = steps; break; }
+                    // next_step_limit (fixed.rs:16-26): dt, clipped to t1 and the next saveat time
+                    double target = fmin(x + A.dt, t1);
+                    if (A.has_saveat && fsi < A.n_save && A.save_times[fsi] > x + time_tol(x)) target = fmin(target, A.save_times[fsi]);
+                    const double h = target - x;
+                    if (h <= 0.0 || 0.1 * h <= 2.220446049250313e-16 * fmax(fabs(x), 1.0)) { status = ST_UNDERFLOW; err_x = x; break; }
+                    // coefficients at the stage times, one VM lane each: row 5 is the step start;
+                    // Dopri5 rows 0-4 are c_2..c_6, RK2/RK4 use row 0 (x + h/2) and row 4 (x + h)
+                    if (P.n_dyn > 0 && lt < 6) {
+                        const bool dp = A.fixed == OBE_SOLVER_FIXED_DOPRI5;
+                        if (lt == 5 || lt == 0 || lt == 4 || dp) {
+                            double ts = x;
+                            if (lt < 5) ts = dp ? x + h * (lt < 4 ? kC[0][lt] : 1.0) : (lt == 0 ? x + 0.5 * h : x + h);
+                            eval_compounds(P, L, ts, true);
+                            for (int j = 0; j < P.n_dyn; ++j) s_cdyn[lt * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, ts);
+                        }
+                    }
+                    // k_1 = f(x, y)
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        if (i < N) s_G64[gslot64(i, n)] = y[e];
+                    }
+                    rhs64(5, s_K);
+                    if (A.fixed == OBE_SOLVER_FIXED_RK2) {
+                        // rk2_step (fixed.rs:28-48)
+#pragma unroll
+                        for (int e = 0; e < EPT; ++e) {
+                            int i = lt + e * TPT;
+                            if (i < N) s_G64[gslot64(i, n)] = y[e] + 0.5 * h * s_K[i];
+                        }
+                        rhs64(0, s_K + N);
+#pragma unroll
+                        for (int e = 0; e < EPT; ++e) {
+                            int i = lt + e * TPT;
+                            if (i < N) yn[e] = y[e] + h * s_K[N + i];
+                        }
+                        rhs_calls += 2;
+                    } else if (A.fixed == OBE_SOLVER_FIXED_RK4) {
+                        // rk4_step (fixed.rs:103-131)
+#pragma unroll 1
+                        for (int s = 0; s < 3; ++s) {
+                            const double c = s < 2 ? 0.5 * h : h;
+#pragma unroll
+                            for (int e = 0; e < EPT; ++e) {
+                                int i = lt + e * TPT;
+                                if (i < N) s_G64[gslot64(i, n)] = y[e] + c * s_K[static_cast<size_t>(s) * N + i];
+                            }
+                            rhs64(s < 2 ? 0 : 4, s_K + static_cast<size_t>(s + 1) * N);
+                        }
+#pragma unroll
+                        for (int e = 0; e < EPT; ++e) {
+                            int i = lt + e * TPT;
+                            if (i < N)
+                                yn[e] = y[e] + h * (s_K[i] + 2.0 * s_K[N + i] + 2.0 * s_K[2 * N + i] + s_K[3 * N + i]) / 6.0;
+                        }
+                        rhs_calls += 4;
+                    } else {
+                        // dopri5_step (fixed.rs:50-101): the adaptive tableau without k_7
+#pragma unroll 1
+                        for (int s = 0; s < 6; ++s) {
+#pragma unroll
+                            for (int e = 0; e < EPT; ++e) {
+                                int i = lt + e * TPT;
+                                if (i < N) {
+                                    double acc = 0.0;
+#pragma unroll
+                                    for (int j = 0; j < 6; ++j)
+                                        if (j <= s) acc += kA[0][s][j] * s_K[static_cast<size_t>(j) * N + i];
+                                    double v = y[e] + h * acc;
+                                    if (s == 5) yn[e] = v;
+                                    else s_G64[gslot64(i, n)] = v;
+                                }
+                            }
+                            if (s < 5) rhs64(s, s_K + static_cast<size_t>(s + 1) * N);
+                        }
+                        rhs_calls += 6;
+                    }
+                    ++accepted;
+                    ++steps;
+                    const double xo = x;
+                    x += h;
+                    bool ev_new_has = false, hit = false;
+                    double ev_new = 0.0;
+                    if (A.ev_kind != OBE_EVENT_NONE) {
+                        stage_registers_to_buf(yn);
+                        event_value(x, ev_new_has, ev_new);
+                        if (status) { err_x = x; break; }
+                        if (ev_old_has && ev_new_has &&
+                            (ev_old == 0.0 || ev_new == 0.0 || (ev_old < 0.0 && ev_new > 0.0) || (ev_old > 0.0 && ev_new < 0.0))) {
+                            hit = true;
+                            ev_triggered = 1;
+                            ev_time = ev_old == 0.0 ? xo : x;
+                        }
+                    }
+                    if (A.has_saveat) {
+                        const double stop = hit ? ev_time : x;
+                        bool buffered = false;
+                        while (fsi < A.n_save && A.save_times[fsi] <= stop + time_tol(stop)) {
+                            if (!buffered) { stage_registers_to_buf(yn); buffered = true; }
+                            push(A.save_times[fsi]);
+                            ++fsi;
+                        }
+                    } else if (!hit) {
+                        stage_registers_to_buf(yn);
+                        push(x);
+                    }
+                    if (hit) {
+                        stage_registers_to_buf(yn);
+                        push(ev_time);
+                        break;
+                    }
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) y[e] = yn[e];
+                    ev_old_has = ev_new_has;
+                    ev_old = ev_new;
+                }
+                if (status == ST_OK && A.has_saveat && fsi != A.n_save && !ev_triggered) {
+                    status = ST_SAVEAT;
+                    err_a = fsi;
+                    err_b = A.n_save;
+                }
+            }
         }
 
         double x = t0, h = 0.0;
@@ -812,7 +1028,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                         gsync<TPT>(g);
                         stage_classes(P, s_cstat, s_cdyn + row * nd, s_cdyn + 5 * nd, s_cv, lt);
                         gsync<TPT>(g);
-                        fill_formulas_dev<TPT>(P, 1 + S, 1 + F, s_cv, s_T4, lt);
+                        fill_formulas_dev<TPT>(P, s_fptr, s_fcls, s_ffac32, s_cv, s_T4, lt);
                     }
                     gsync<TPT>(g);
                     gather_dev<TPT>(P, s_rec, s_out, s_T4, s_G4, s_K32 + static_cast<size_t>(s) * N, lt);
@@ -856,10 +1072,19 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
             }
             rhs_calls += 6;
             if constexpr (!MIXED) err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
-            // controller (common.rs:48-69), in double for both forms (single-precision powers
-            // here made the controller choose ~18% smaller steps)
-            double fac11 = pow(err, alpha);
-            double fac = fac11 * pow(fac_old, -beta);
+            // controller (common.rs:48-69).  The mixed form takes the two powers in single
+            // precision (its error norm is single precision already); the step sizes then differ
+            // from the double-precision powers' by ~1e-7 relative.
+            double fac11, fac;
+            if constexpr (MIXED) {
+                const float ef = static_cast<float>(err), fo = static_cast<float>(fac_old);
+                const float f11 = exp2f(static_cast<float>(alpha) * log2f(ef));
+                fac11 = f11;
+                fac = static_cast<double>(f11 * exp2f(static_cast<float>(-beta) * log2f(fo)));
+            } else {
+                fac11 = pow(err, alpha);
+                fac = fac11 * pow(fac_old, -beta);
+            }
             fac = fmax(facc2, fmin(facc1, fac / safety));
             double hn = h / fac;
             if (err <= 1.0) {
@@ -1089,14 +1314,15 @@ __global__ void __launch_bounds__(256) rhs_kernel(const DevPlan P, long long cou
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
     const int n = P.n, N = P.N, U = P.U;
-    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
-    uint32_t* s_out = s_rec + static_cast<size_t>(P.n_iter) * TPT;
-    for (int i = threadIdx.x; i < (P.n_iter + P.n_out) * TPT; i += blockDim.x)
-        s_rec[i] = i < P.n_iter * TPT ? P.rec[i] : P.lane_out[i - P.n_iter * TPT];
+    const PlanSmem PS = plan_smem(P, TPT, false);  // the layout the host sized (double-precision form)
+    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem + PS.rec);
+    uint32_t* s_out = reinterpret_cast<uint32_t*>(smem + PS.out);
+    for (int i = threadIdx.x; i < P.n_iter * TPT; i += blockDim.x) s_rec[i] = P.rec[i];
+    for (int i = threadIdx.x; i < P.n_out * TPT; i += blockDim.x) s_out[i] = P.lane_out[i];
     __syncthreads();
     if (g >= gpb) return;
     const GroupLayout Lay = group_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, vm_depth, TPT, false);
-    unsigned char* gb = smem + plan_smem_bytes(P.n_iter, P.n_out, TPT) + static_cast<size_t>(g) * group_bytes;
+    unsigned char* gb = smem + PS.bytes + static_cast<size_t>(g) * group_bytes;
     double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
     double2* s_G = reinterpret_cast<double2*>(gb + Lay.G);
     double* s_K = reinterpret_cast<double*>(gb + Lay.K);
@@ -1203,6 +1429,63 @@ int k1_refresh_interval() {
     return v;
 }
 
+// The plan's device image serialised into `blob` on the host, and the DevPlan whose pointers
+// address that image once it sits at device address `base`.
+void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintptr_t base, DevPlan& P) {
+    const HostPacked& h = p->packed;
+    size_t o_op = put(blob, h.ins_op), o_arg = put(blob, h.ins_arg), o_fn = put(blob, h.ins_fn), o_val = put(blob, h.ins_val);
+    size_t o_bv = put(blob, h.base_val), o_bt = put(blob, h.base_tuple), o_tp = put(blob, h.tuple_ptr), o_ti = put(blob, h.tuple_items);
+    size_t o_cs = put(blob, h.comp_slot), o_ce = put(blob, h.comp_expr), o_cd = put(blob, h.comp_dynamic);
+    size_t o_ke = put(blob, h.coeff_expr), o_kd = put(blob, h.coeff_dynamic), o_di = put(blob, h.dyn_ids), o_dp = put(blob, h.coeff_dyn_pos);
+    size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
+    size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
+    size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out);
+    P = DevPlan{};
+    P.n = p->n;
+    P.N = static_cast<int32_t>(p->N);
+    P.U = static_cast<int32_t>(p->U);
+    P.ins_op = reinterpret_cast<const int32_t*>(base + o_op);
+    P.ins_arg = reinterpret_cast<const int32_t*>(base + o_arg);
+    P.ins_fn = reinterpret_cast<const int32_t*>(base + o_fn);
+    P.ins_val = reinterpret_cast<const double*>(base + o_val);
+    P.n_slots = p->n_slots;
+    P.n_base = p->n_base;
+    P.base_val = reinterpret_cast<const double*>(base + o_bv);
+    P.base_tuple = reinterpret_cast<const int32_t*>(base + o_bt);
+    P.tuple_ptr = reinterpret_cast<const int32_t*>(base + o_tp);
+    P.tuple_items = reinterpret_cast<const double*>(base + o_ti);
+    P.n_comp = static_cast<int32_t>(h.comp_slot.size());
+    P.comp_slot = reinterpret_cast<const int32_t*>(base + o_cs);
+    P.comp_expr = reinterpret_cast<const DevExpr*>(base + o_ce);
+    P.comp_dynamic = reinterpret_cast<const uint8_t*>(base + o_cd);
+    P.n_coeff = p->n_coeff;
+    P.coeff_expr = reinterpret_cast<const DevExpr*>(base + o_ke);
+    P.coeff_dynamic = reinterpret_cast<const uint8_t*>(base + o_kd);
+    P.n_dyn = static_cast<int32_t>(h.dyn_ids.size());
+    P.dyn_ids = reinterpret_cast<const int32_t*>(base + o_di);
+    P.coeff_dyn_pos = reinterpret_cast<const int32_t*>(base + o_dp);
+    P.time_dependent = p->time_dependent;
+    P.max_stack = std::max(1, h.max_stack);
+    P.n_pchip = static_cast<int32_t>(h.pchip_cptr.size());
+    P.pchip_ptr = reinterpret_cast<const int32_t*>(base + o_pp);
+    P.pchip_grid = reinterpret_cast<const double*>(base + o_pg);
+    P.pchip_coef = reinterpret_cast<const double*>(base + o_pc);
+    P.pchip_cptr = reinterpret_cast<const int32_t*>(base + o_pcp);
+    P.n_formula = h.n_formula;
+    P.n_static_formula = h.n_static_formula;
+    P.formula_ptr = reinterpret_cast<const int32_t*>(base + o_fp);
+    P.prod_factor = reinterpret_cast<const double*>(base + o_pf);
+    P.prod_class = reinterpret_cast<const int32_t*>(base + o_pcl);
+    P.prod_factor32 = reinterpret_cast<const float*>(base + o_pf32);
+    P.dyn_prod0 = h.formula_ptr.empty() ? 0 : h.formula_ptr[h.n_static_formula];
+    P.n_dyn_prod = h.formula_ptr.empty() ? 0 : h.formula_ptr[h.n_formula] - P.dyn_prod0;
+    P.tpt = h.tpt;
+    P.n_iter = h.n_iter;
+    P.rec = reinterpret_cast<const uint32_t*>(base + o_rec);
+    P.n_out = h.n_out;
+    P.lane_out = reinterpret_cast<const uint32_t*>(base + o_lo);
+}
+
 obe_status upload_plan(obe_plan* p) {
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
@@ -1215,64 +1498,18 @@ obe_status upload_plan(obe_plan* p) {
         cudaFree(p->d_blob);
         p->d_blob = nullptr;
     }
-    const HostPacked& h = p->packed;
     std::vector<unsigned char> blob;
-    size_t o_op = put(blob, h.ins_op), o_arg = put(blob, h.ins_arg), o_fn = put(blob, h.ins_fn), o_val = put(blob, h.ins_val);
-    size_t o_bv = put(blob, h.base_val), o_bt = put(blob, h.base_tuple), o_tp = put(blob, h.tuple_ptr), o_ti = put(blob, h.tuple_items);
-    size_t o_cs = put(blob, h.comp_slot), o_ce = put(blob, h.comp_expr), o_cd = put(blob, h.comp_dynamic);
-    size_t o_ke = put(blob, h.coeff_expr), o_kd = put(blob, h.coeff_dynamic), o_di = put(blob, h.dyn_ids), o_dp = put(blob, h.coeff_dyn_pos);
-    size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
-    size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
-    size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out);
+    DevPlan P;
+    build_plan_image(p, blob, 0, P);  // sizes only
     void* d = nullptr;
     if (!cuda_ok(cudaMalloc(&d, blob.size()), "cudaMalloc(plan)")) return OBE_ERR_CUDA;
+    blob.clear();
+    build_plan_image(p, blob, reinterpret_cast<uintptr_t>(d), P);
     if (!cuda_ok(cudaMemcpy(d, blob.data(), blob.size(), cudaMemcpyHostToDevice), "cudaMemcpy(plan)")) {
         cudaFree(d);
         return OBE_ERR_CUDA;
     }
-    auto* b = static_cast<unsigned char*>(d);
-    DevPlan& P = p->dev;
-    P.n = p->n;
-    P.N = static_cast<int32_t>(p->N);
-    P.U = static_cast<int32_t>(p->U);
-    P.ins_op = reinterpret_cast<const int32_t*>(b + o_op);
-    P.ins_arg = reinterpret_cast<const int32_t*>(b + o_arg);
-    P.ins_fn = reinterpret_cast<const int32_t*>(b + o_fn);
-    P.ins_val = reinterpret_cast<const double*>(b + o_val);
-    P.n_slots = p->n_slots;
-    P.n_base = p->n_base;
-    P.base_val = reinterpret_cast<const double*>(b + o_bv);
-    P.base_tuple = reinterpret_cast<const int32_t*>(b + o_bt);
-    P.tuple_ptr = reinterpret_cast<const int32_t*>(b + o_tp);
-    P.tuple_items = reinterpret_cast<const double*>(b + o_ti);
-    P.n_comp = static_cast<int32_t>(h.comp_slot.size());
-    P.comp_slot = reinterpret_cast<const int32_t*>(b + o_cs);
-    P.comp_expr = reinterpret_cast<const DevExpr*>(b + o_ce);
-    P.comp_dynamic = reinterpret_cast<const uint8_t*>(b + o_cd);
-    P.n_coeff = p->n_coeff;
-    P.coeff_expr = reinterpret_cast<const DevExpr*>(b + o_ke);
-    P.coeff_dynamic = reinterpret_cast<const uint8_t*>(b + o_kd);
-    P.n_dyn = static_cast<int32_t>(h.dyn_ids.size());
-    P.dyn_ids = reinterpret_cast<const int32_t*>(b + o_di);
-    P.coeff_dyn_pos = reinterpret_cast<const int32_t*>(b + o_dp);
-    P.time_dependent = p->time_dependent;
-    P.max_stack = std::max(1, h.max_stack);
-    P.n_pchip = static_cast<int32_t>(h.pchip_cptr.size());
-    P.pchip_ptr = reinterpret_cast<const int32_t*>(b + o_pp);
-    P.pchip_grid = reinterpret_cast<const double*>(b + o_pg);
-    P.pchip_coef = reinterpret_cast<const double*>(b + o_pc);
-    P.pchip_cptr = reinterpret_cast<const int32_t*>(b + o_pcp);
-    P.n_formula = h.n_formula;
-    P.n_static_formula = h.n_static_formula;
-    P.formula_ptr = reinterpret_cast<const int32_t*>(b + o_fp);
-    P.prod_factor = reinterpret_cast<const double*>(b + o_pf);
-    P.prod_class = reinterpret_cast<const int32_t*>(b + o_pcl);
-    P.prod_factor32 = reinterpret_cast<const float*>(b + o_pf32);
-    P.tpt = h.tpt;
-    P.n_iter = h.n_iter;
-    P.rec = reinterpret_cast<const uint32_t*>(b + o_rec);
-    P.n_out = h.n_out;
-    P.lane_out = reinterpret_cast<const uint32_t*>(b + o_lo);
+    p->dev = P;
     p->d_blob = d;
     p->d_device = dev;
     return OBE_OK;
@@ -1332,8 +1569,7 @@ int sm_count() {
     return count;
 }
 
-obe_status plan_launch(const obe_plan* p, bool mixed, long long n_traj, int vm_depth, LaunchShape* s) {
-    const DevPlan& P = p->dev;
+obe_status plan_launch(const DevPlan& P, bool mixed, long long n_traj, int vm_depth, LaunchShape* s) {
     s->tpt = P.tpt;
     if (s->tpt > 128) {
         set_error("systems with more than 45 states are not supported by this build of the GPU solver");
@@ -1343,7 +1579,7 @@ obe_status plan_launch(const obe_plan* p, bool mixed, long long n_traj, int vm_d
     struct { size_t bytes; } L;
     L.bytes = group_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, vm_depth, s->tpt, mixed).bytes;
     s->group_bytes = L.bytes;
-    size_t plan_bytes = plan_smem_bytes(P.n_iter, P.n_out, s->tpt);
+    size_t plan_bytes = plan_smem(P, s->tpt, mixed).bytes;
     const size_t limit = 227 * 1024;
     int gpb = std::max(1, 256 / s->tpt);
     while (gpb > 1 && plan_bytes + gpb * L.bytes > limit) --gpb;
@@ -1402,6 +1638,7 @@ std::string traj_message(int code, const TrajErr& e) {
     case ST_POINTS: return "expected " + std::to_string(e.a) + " output points, got " + std::to_string(e.b);
     case ST_BAD_MAXITERS: return "maxiters must be positive";
     case ST_BACKWARD: return "only forward integration";
+    case ST_FIXED_DT: return "fixed-step solvers require positive finite dt";
     default: return "trajectory failed with status " + std::to_string(code);
     }
 }
@@ -1419,9 +1656,13 @@ obe_status validate_options(const obe_plan* p, const obe_solve_options* o, std::
         set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan");
         return OBE_ERR_INVALID;
     }
-    if (o->solver != OBE_SOLVER_DOPRI5 && o->solver != OBE_SOLVER_TSIT5) {
+    if (o->solver < OBE_SOLVER_DOPRI5 || o->solver > OBE_SOLVER_FIXED_RK4) {
         set_error("solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4'");
         return OBE_ERR_INVALID;
+    }
+    if (o->solver >= OBE_SOLVER_FIXED_DOPRI5 && o->precision == OBE_PRECISION_MIXED) {
+        set_error("precision='mixed' is implemented for the adaptive solvers 'dopri5' and 'tsit5'");
+        return OBE_ERR_UNSUPPORTED;
     }
     obe_status st = save_plan(o, save_times);
     if (st != OBE_OK) return st;
@@ -1534,6 +1775,7 @@ void fill_call_args(CallArgs& A, const obe_solve_options* o, const std::vector<d
     A.ev_arg = reinterpret_cast<const int32_t*>(d_blob + cb.o_evarg);
     A.ev_fn = reinterpret_cast<const int32_t*>(d_blob + cb.o_evfn);
     A.ev_val = reinterpret_cast<const double*>(d_blob + cb.o_evval);
+    A.fixed = o->solver >= OBE_SOLVER_FIXED_DOPRI5 ? o->solver : 0;
 }
 
 cudaError_t launch_integrate(const obe_plan* p, const CallArgs& A, bool mixed, int solver, const LaunchShape& s, cudaStream_t st) {
@@ -1592,7 +1834,7 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
     A.k1_refresh = k1_refresh_interval();
     A.vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
     LaunchShape s;
-    obe_status st = plan_launch(p, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s);
+    obe_status st = plan_launch(p->dev, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s);
     if (st != OBE_OK) return st;
     if (!cuda_ok(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync")) return OBE_ERR_CUDA;
     if (!cuda_ok(launch_integrate(p, A, o->precision == OBE_PRECISION_MIXED, o->solver, s, stream), "kernel launch")) return OBE_ERR_CUDA;
@@ -1850,7 +2092,8 @@ obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, co
     const bool mixed = precision == OBE_PRECISION_MIXED;
     LaunchShape s;
     const int vm_depth = std::max(p->dev.max_stack, 1);
-    if ((st = plan_launch(p, false, count, vm_depth, &s)) != OBE_OK) return st;
+    // the RHS kernel keeps both forms in the double-precision group layout
+    if ((st = plan_launch(p->dev, false, count, vm_depth, &s)) != OBE_OK) return st;
     std::vector<int32_t> slots(override_slots, override_slots + n_override_slots);
     size_t off = 0;
     size_t o_t = off; off = align16(off + 8 * count);
@@ -1912,61 +2155,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 std::mutex g_noalloc_mutex;
 void* g_noalloc_base[64] = {nullptr};  // device address of g_noalloc_scratch, per device
 
-// The plan's device image laid out as upload_plan lays it out, with its pointers relative to
-// `base` (a device address), serialised into `blob` on the host.
-void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, unsigned char* base, DevPlan& P) {
-    const HostPacked& h = p->packed;
-    size_t o_op = put(blob, h.ins_op), o_arg = put(blob, h.ins_arg), o_fn = put(blob, h.ins_fn), o_val = put(blob, h.ins_val);
-    size_t o_bv = put(blob, h.base_val), o_bt = put(blob, h.base_tuple), o_tp = put(blob, h.tuple_ptr), o_ti = put(blob, h.tuple_items);
-    size_t o_cs = put(blob, h.comp_slot), o_ce = put(blob, h.comp_expr), o_cd = put(blob, h.comp_dynamic);
-    size_t o_ke = put(blob, h.coeff_expr), o_kd = put(blob, h.coeff_dynamic), o_di = put(blob, h.dyn_ids), o_dp = put(blob, h.coeff_dyn_pos);
-    size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
-    size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
-    size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out);
-    P = DevPlan{};
-    P.n = p->n;
-    P.N = static_cast<int32_t>(p->N);
-    P.U = static_cast<int32_t>(p->U);
-    P.ins_op = reinterpret_cast<const int32_t*>(base + o_op);
-    P.ins_arg = reinterpret_cast<const int32_t*>(base + o_arg);
-    P.ins_fn = reinterpret_cast<const int32_t*>(base + o_fn);
-    P.ins_val = reinterpret_cast<const double*>(base + o_val);
-    P.n_slots = p->n_slots;
-    P.n_base = p->n_base;
-    P.base_val = reinterpret_cast<const double*>(base + o_bv);
-    P.base_tuple = reinterpret_cast<const int32_t*>(base + o_bt);
-    P.tuple_ptr = reinterpret_cast<const int32_t*>(base + o_tp);
-    P.tuple_items = reinterpret_cast<const double*>(base + o_ti);
-    P.n_comp = static_cast<int32_t>(h.comp_slot.size());
-    P.comp_slot = reinterpret_cast<const int32_t*>(base + o_cs);
-    P.comp_expr = reinterpret_cast<const DevExpr*>(base + o_ce);
-    P.comp_dynamic = reinterpret_cast<const uint8_t*>(base + o_cd);
-    P.n_coeff = p->n_coeff;
-    P.coeff_expr = reinterpret_cast<const DevExpr*>(base + o_ke);
-    P.coeff_dynamic = reinterpret_cast<const uint8_t*>(base + o_kd);
-    P.n_dyn = static_cast<int32_t>(h.dyn_ids.size());
-    P.dyn_ids = reinterpret_cast<const int32_t*>(base + o_di);
-    P.coeff_dyn_pos = reinterpret_cast<const int32_t*>(base + o_dp);
-    P.time_dependent = p->time_dependent;
-    P.max_stack = std::max(1, h.max_stack);
-    P.n_pchip = static_cast<int32_t>(h.pchip_cptr.size());
-    P.pchip_ptr = reinterpret_cast<const int32_t*>(base + o_pp);
-    P.pchip_grid = reinterpret_cast<const double*>(base + o_pg);
-    P.pchip_coef = reinterpret_cast<const double*>(base + o_pc);
-    P.pchip_cptr = reinterpret_cast<const int32_t*>(base + o_pcp);
-    P.n_formula = h.n_formula;
-    P.n_static_formula = h.n_static_formula;
-    P.formula_ptr = reinterpret_cast<const int32_t*>(base + o_fp);
-    P.prod_factor = reinterpret_cast<const double*>(base + o_pf);
-    P.prod_class = reinterpret_cast<const int32_t*>(base + o_pcl);
-    P.prod_factor32 = reinterpret_cast<const float*>(base + o_pf32);
-    P.tpt = h.tpt;
-    P.n_iter = h.n_iter;
-    P.rec = reinterpret_cast<const uint32_t*>(base + o_rec);
-    P.n_out = h.n_out;
-    P.lane_out = reinterpret_cast<const uint32_t*>(base + o_lo);
-}
-
 }  // namespace
 }  // namespace obe
 
@@ -2013,7 +2201,7 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
     unsigned char* base = static_cast<unsigned char*>(g_noalloc_base[dev]);
     std::vector<unsigned char> image;
     DevPlan P;
-    build_plan_image(p, image, base + kNoAllocPlanOff, P);
+    build_plan_image(p, image, reinterpret_cast<uintptr_t>(base + kNoAllocPlanOff), P);
     if (image.size() > kNoAllocPlanBytes) {
         set_error("plan device image (" + std::to_string(image.size()) + " bytes) exceeds the " +
                   std::to_string(kNoAllocPlanBytes) + "-byte plan block of the allocation-free entry point");
@@ -2045,24 +2233,9 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
     A.k1_refresh = k1_refresh_interval();
     A.vm_depth = std::max(P.max_stack, std::max(cb.ev_len, 1));
 
-    // launch shape, as for the allocating entry points
     const bool mixed = opt->precision == OBE_PRECISION_MIXED;
     LaunchShape shape;
-    shape.tpt = P.tpt;
-    if (shape.tpt > 128) { set_error("systems with more than 45 states are not supported by this build of the GPU solver"); return OBE_ERR_UNSUPPORTED; }
-    shape.ept = ept_for(P.N, shape.tpt);
-    shape.group_bytes = group_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, shape.tpt, mixed).bytes;
-    const size_t plan_bytes = plan_smem_bytes(P.n_iter, P.n_out, shape.tpt);
-    const size_t limit = 227 * 1024;
-    int gpb = std::max(1, 256 / shape.tpt);
-    while (gpb > 1 && plan_bytes + gpb * shape.group_bytes > limit) --gpb;
-    if (plan_bytes + gpb * shape.group_bytes > limit) { set_error("system too large for the GPU solver's shared-memory layout"); return OBE_ERR_UNSUPPORTED; }
-    const long long per_sm = (n_traj + sm_count() - 1) / sm_count();
-    while (gpb > 1 && gpb > per_sm) --gpb;
-    shape.gpb = gpb;
-    shape.smem = plan_bytes + gpb * shape.group_bytes;
-    const int blocks_per_sm = std::max<int>(1, static_cast<int>(limit / shape.smem));
-    shape.blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n_traj + gpb - 1) / gpb, static_cast<long long>(sm_count()) * blocks_per_sm)));
+    if ((st = plan_launch(P, mixed, n_traj, A.vm_depth, &shape)) != OBE_OK) return st;
     const int method = opt->solver == OBE_SOLVER_TSIT5 ? 1 : 0;
     cudaError_t e = mixed ? dispatch_shape<true>(P, A, shape, method, s) : dispatch_shape<false>(P, A, shape, method, s);
     if (!cuda_ok(e, "kernel launch")) return OBE_ERR_CUDA;

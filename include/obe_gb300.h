@@ -31,8 +31,15 @@ typedef enum {
     OBE_ERR_TIMEOUT = 5       /* a bounded device-side wait gave up                           */
 } obe_status;
 
-/* Solvers, rust/src/ode/batch.rs:8-30 (OdeSolver::from_str). */
-typedef enum { OBE_SOLVER_DOPRI5 = 0, OBE_SOLVER_TSIT5 = 1 } obe_solver;
+/* Solvers, rust/src/ode/batch.rs:8-30 (OdeSolver::from_str).  The fixed-step ones
+ * (rust/src/ode/fixed.rs) run in double precision only. */
+typedef enum {
+    OBE_SOLVER_DOPRI5 = 0,
+    OBE_SOLVER_TSIT5 = 1,
+    OBE_SOLVER_FIXED_DOPRI5 = 2,
+    OBE_SOLVER_FIXED_RK2 = 3,
+    OBE_SOLVER_FIXED_RK4 = 4
+} obe_solver;
 
 /* Observables, rust/src/lindblad/ode_batch.rs:103-163 (OutputSpec). */
 typedef enum {

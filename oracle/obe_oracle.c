@@ -1864,6 +1864,123 @@ done:
     return rc;
 }
 
+/* solve_fixed_step (fixed.rs:133-249): dopri5 (fixed.rs:50-101), rk2 (:28-48) and rk4
+ * (:103-131) steppers; the step is dt clipped to t1 and to the next saveat time
+ * (next_step_limit, fixed.rs:16-26); no dense output, events end on the step that crosses. */
+static int solve_fixed(workspace* w, int stepper, const double* y0, const obe_solve_options* o, sink* out, obe_traj_stats* st, errbuf* e) {
+    const orc_plan* p = w->p;
+    int64_t dim = p->N;
+    double t0 = o->t0, t1 = o->t1;
+    memset(st, 0, sizeof *st);
+    st->event_time = NAN;
+    if (o->maxiters <= 0) return fail(e, "maxiters must be positive");
+    if (t1 < t0) return fail(e, "only forward integration");
+    if (!isfinite(o->dt) || o->dt <= 0.0) return fail(e, "fixed-step solvers require positive finite dt");
+    if (t1 == t0) {
+        if (o->save_start) sink_push(out, t0, y0);
+        st->n_points = sink_points(out);
+        return 0;
+    }
+    double* sp = NULL;
+    int64_t n_sp = 0;
+    if (build_save_plan(o, t0, t1, &sp, &n_sp, e)) return 1;
+    int has_sp = o->has_saveat;
+    rk_buf b;
+    rkb_init(&b, dim);
+    int rc = 0;
+    double *k = b.k, *k1 = k, *k2 = k + dim, *k3 = k + 2 * dim, *k4 = k + 3 * dim, *k5 = k + 4 * dim, *k6 = k + 5 * dim;
+    memcpy(b.y, y0, sizeof(double) * (size_t)dim);
+    double x = t0;
+    int64_t si = 0;
+    if (has_sp) {
+        while (si < n_sp && close_to_start(sp[si], t0)) { sink_push(out, sp[si], b.y); ++si; }
+    } else if (o->save_start) {
+        sink_push(out, x, b.y);
+    }
+    int ev_old_has;
+    double ev_old;
+    if ((rc = ws_event(w, x, b.y, &ev_old_has, &ev_old, e))) goto done;
+    int64_t steps = 0;
+    char xs[64];
+    while (x < t1 - time_tol(t1)) {
+        if (steps >= o->maxiters) { fmt_f64(x, xs, sizeof xs); rc = fail(e, "Stopped at x=%s. Need more than %lld steps.", xs, (long long)steps); goto done; }
+        double target = fmin(x + o->dt, t1);
+        if (has_sp && si < n_sp && sp[si] > x + time_tol(x)) target = fmin(target, sp[si]);
+        double h = target - x;
+        if (h <= 0.0 || 0.1 * h <= 2.220446049250313e-16 * fmax(fabs(x), 1.0)) { fmt_f64(x, xs, sizeof xs); rc = fail(e, "Stopped at x=%s. Step size underflow.", xs); goto done; }
+        double *y = b.y, *yt = b.yt, *yn = b.yn;
+        if ((rc = ws_rhs(w, x, y, k1, e))) goto done;
+        if (stepper == OBE_SOLVER_FIXED_RK2) {
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + 0.5 * h * k1[i];
+            if ((rc = ws_rhs(w, x + 0.5 * h, yt, k2, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yn[i] = y[i] + h * k2[i];
+            st->rhs_calls += 2;
+        } else if (stepper == OBE_SOLVER_FIXED_RK4) {
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + 0.5 * h * k1[i];
+            if ((rc = ws_rhs(w, x + 0.5 * h, yt, k2, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + 0.5 * h * k2[i];
+            if ((rc = ws_rhs(w, x + 0.5 * h, yt, k3, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + h * k3[i];
+            if ((rc = ws_rhs(w, x + h, yt, k4, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yn[i] = y[i] + h * (k1[i] + 2.0 * k2[i] + 2.0 * k3[i] + k4[i]) / 6.0;
+            st->rhs_calls += 4;
+        } else {
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + h * D_A21 * k1[i];
+            if ((rc = ws_rhs(w, x + h * D_C2, yt, k2, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + h * (D_A31 * k1[i] + D_A32 * k2[i]);
+            if ((rc = ws_rhs(w, x + h * D_C3, yt, k3, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + h * (D_A41 * k1[i] + D_A42 * k2[i] + D_A43 * k3[i]);
+            if ((rc = ws_rhs(w, x + h * D_C4, yt, k4, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + h * (D_A51 * k1[i] + D_A52 * k2[i] + D_A53 * k3[i] + D_A54 * k4[i]);
+            if ((rc = ws_rhs(w, x + h * D_C5, yt, k5, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yt[i] = y[i] + h * (D_A61 * k1[i] + D_A62 * k2[i] + D_A63 * k3[i] + D_A64 * k4[i] + D_A65 * k5[i]);
+            if ((rc = ws_rhs(w, x + h, yt, k6, e))) goto done;
+            for (int64_t i = 0; i < dim; ++i) yn[i] = y[i] + h * (D_A71 * k1[i] + D_A73 * k3[i] + D_A74 * k4[i] + D_A75 * k5[i] + D_A76 * k6[i]);
+            st->rhs_calls += 6;
+        }
+        st->accepted_steps += 1;
+        ++steps;
+        double xo = x;
+        x += h;
+        int ev_new_has;
+        double ev_new;
+        if ((rc = ws_event(w, x, yn, &ev_new_has, &ev_new, e))) goto done;
+        int hit = 0;
+        if (ev_old_has && ev_new_has && crossed_zero(ev_old, ev_new)) {
+            hit = 1;
+            st->event_triggered = 1;
+            st->event_time = ev_old == 0.0 ? xo : x;
+        }
+        if (has_sp) {
+            double stop_time = hit ? st->event_time : x;
+            while (si < n_sp && sp[si] <= stop_time + time_tol(stop_time)) { sink_push(out, sp[si], yn); ++si; }
+        } else if (!hit) {
+            sink_push(out, x, yn);
+        }
+        if (hit) {
+            sink_push(out, st->event_time, yn);
+            break;
+        }
+        double* tmp = b.y; b.y = b.yn; b.yn = tmp;
+        ev_old_has = ev_new_has;
+        ev_old = ev_new;
+    }
+    if (has_sp && si != n_sp && !st->event_triggered) {
+        rc = fail(e, "ended before all saveat: %lld of %lld", (long long)si, (long long)n_sp);
+    }
+done:
+    st->n_points = sink_points(out);
+    rkb_free(&b);
+    free(sp);
+    return rc;
+}
+
+static int solve_any(workspace* w, const double* y0, const obe_solve_options* o, sink* out, obe_traj_stats* st, errbuf* e) {
+    if (o->solver == OBE_SOLVER_DOPRI5 || o->solver == OBE_SOLVER_TSIT5)
+        return solve_rk(w, o->solver == OBE_SOLVER_TSIT5, y0, o, out, st, e);
+    return solve_fixed(w, o->solver, y0, o, out, st, e);
+}
+
 static int setup_event(workspace* w, const obe_solve_options* o) {
     w->ev_kind = o->event_kind;
     if (o->event_kind == OBE_EVENT_POPULATION) {
@@ -1884,7 +2001,7 @@ static int setup_event(workspace* w, const obe_solve_options* o) {
 }
 
 static int check_solver(const obe_solve_options* o, errbuf* e) {
-    if (o->solver != OBE_SOLVER_DOPRI5 && o->solver != OBE_SOLVER_TSIT5)
+    if (o->solver < OBE_SOLVER_DOPRI5 || o->solver > OBE_SOLVER_FIXED_RK4)
         return fail(e, "solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4', got %d", o->solver);
     return 0;
 }
@@ -1927,7 +2044,7 @@ int orc_solve_single(const orc_plan* plan, const obe_solve_options* opt, const d
     setup_event(&w, opt);
     sink s;
     sink_init(&s, plan, opt, capacity, times, values);
-    int rc = solve_rk(&w, opt->solver == OBE_SOLVER_TSIT5, rho0, opt, &s, stats, &e);
+    int rc = solve_any(&w, rho0, opt, &s, stats, &e);
     sink_free(&s);
     ws_free(&w);
     if (rc) copy_err(&e, err, err_len);
@@ -1966,7 +2083,7 @@ int orc_solve_batch(const orc_plan* plan, const obe_solve_options* opt, int64_t 
             sink s;
             sink_init(&s, plan, opt, time_count, tbuf, values + b * per);
             obe_traj_stats st;
-            int rc = solve_rk(&w, opt->solver == OBE_SOLVER_TSIT5, rho0 + b * rho0_stride, opt, &s, &st, &e);
+            int rc = solve_any(&w, rho0 + b * rho0_stride, opt, &s, &st, &e);
             if (!rc && st.n_points != time_count)
                 rc = fail(&e, "expected %lld output points, got %lld", (long long)time_count, (long long)st.n_points);
             st.status = rc;

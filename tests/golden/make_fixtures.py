@@ -18,6 +18,10 @@ What it writes (all JSON through ``codec.py``):
 * ``rk45_<name>.json``: trajectories from the reference's SciPy RK45 solve
   (``solve_lindblad(..., backend="python")``, centrex_tlf/lindblad/solve.py:155-199):
   tolerance-level anchors for whole solves.
+* ``kat_fixed_step.json``: the reference's recorded fixed-step solver runs
+  (benchmarks/fixed_step_solver_results/fixed_step_solver_report.md and
+  fixed_step_solver_validation.csv): step and RHS counts per case, and the photon-integral
+  difference of each fixed-step run from the adaptive Dopri5 run.
 * ``ffi_calls.json``: the positional arguments the reference's Python surface
   (solve.py:419, batch.py:235, batch.py:440) passes across its native boundary, recorded by
   installing a recording stand-in module as ``centrex_tlf.centrex_tlf_rust``.
@@ -321,7 +325,45 @@ def record_ffi_calls(centrex_tlf, prepared, rho0):
     return {"slot_names": slots, "calls": calls}
 
 
+def fixed_step_kat() -> dict:
+    """Known answers of the reference's fixed-step benchmark (benchmarks/bench_fixed_step_solvers.py:
+    two-level system with Omega=0.8, delta=0, t in [0, 0.8], photon_integral with weights
+    [(1, 0.3)], output_when="final", saveat None; adaptive Dopri5 at rtol 1e-8, atol 1e-10,
+    dt 1e-3 as the reference run; the detuning grid is linspace(-2, 2, 201))."""
+    import csv
+
+    res = REFERENCE / "benchmarks" / "fixed_step_solver_results"
+    counts = {}
+    runtime_table = (res / "fixed_step_solver_report.md").read_text().split("## Validation")[0]
+    for line in runtime_table.splitlines():
+        cells = [c.strip() for c in line.strip().strip("|").split("|")]
+        if len(cells) == 7 and cells[1] in ("single", "grid") and cells[5].isdigit():
+            counts[(cells[0], cells[1], int(cells[2]))] = (int(cells[5]), int(cells[6]))
+    cases = {}
+    for label, mode, threads in counts:
+        if threads == 4:
+            continue
+        solver, dt = "dopri5", 1e-3
+        if label != "adaptive_dopri5":
+            solver = label.rsplit("_dt", 1)[0]
+            dt = float(label.rsplit("_dt", 1)[1].replace("p", "."))
+        c = cases.setdefault(label, {"solver": solver, "dt": dt})
+        c[f"{mode}_accepted_steps"], c[f"{mode}_rhs_calls"] = counts[(label, mode, threads)]
+    with open(res / "fixed_step_solver_validation.csv") as f:
+        for row in csv.DictReader(f):
+            if row["mode"] == "single":
+                cases[row["case"]]["abs_error_vs_adaptive"] = float(row["photon_integral_abs_error"])
+                cases[row["case"]]["rel_error_vs_adaptive"] = float(row["photon_integral_rel_error"])
+    return {
+        "omega": 0.8, "delta": 0.0, "t_span": [0.0, 0.8], "weights": [[1, 0.3]], "abstol": 1e-10, "reltol": 1e-8,
+        "grid_detuning": np.linspace(-2.0, 2.0, 201), "cases": cases,
+    }
+
+
 def main() -> None:
+    if "--kat-fixed-step" in sys.argv:
+        codec.save("kat_fixed_step", fixed_step_kat())
+        return
     centrex_tlf = _import_reference()
     started = time.perf_counter()
 
@@ -404,6 +446,8 @@ def main() -> None:
         rk[key]["override_slots"] = np.array(sorted(over), dtype=np.int64)
         rk[key]["override_values"] = np.array([over[k] for k in sorted(over)], dtype=np.complex128)
     codec.save("rk45_q1_16", rk)
+
+    codec.save("kat_fixed_step", fixed_step_kat())
 
     # --- the native-boundary call contract of the reference's Python surface ----------------
     codec.save("ffi_calls", record_ffi_calls(centrex_tlf, q1, rho_q))

@@ -188,3 +188,75 @@ def test_error_messages(golden):
     det = np.array([[0.0], [0.1]], dtype=complex)
     with pytest.raises(oracle.OracleError, match=r"^trajectory 0: Stopped at x="):
         p.solve_batch(_opts(p, maxiters=1), d["rho0_packed"], [p.slot_names.index("delta")], det)
+
+
+def _fixed_kat_solve(p, d, kat, case, grid=False):
+    """One run of the reference's fixed-step benchmark configuration
+    (benchmarks/bench_fixed_step_solvers.py:124-160) through the oracle."""
+    o = _opts(p, t0=kat["t_span"][0], t1=kat["t_span"][1], abstol=kat["abstol"], reltol=kat["reltol"],
+              dt=case["dt"], solver=case["solver"], output="photon_integral",
+              integral_weights=[tuple(w) for w in kat["weights"]])
+    slots = [p.slot_names.index("Omega"), p.slot_names.index("delta")]
+    det = kat["grid_detuning"] if grid else np.array([kat["delta"]])
+    params = np.stack([np.full(det.size, kat["omega"]), det], axis=1).astype(complex)
+    vals, _, st = p.solve_batch(o, d["rho0_packed"], slots, params)
+    return vals[:, 0, 0], st
+
+
+@pytest.mark.parametrize("label", ["fixed_dopri5_dt5e-2", "fixed_dopri5_dt2p5e-2", "fixed_dopri5_dt1e-3",
+                                   "fixed_rk4_dt5e-2", "fixed_rk4_dt2p5e-2", "fixed_rk4_dt1e-3", "fixed_rk4_dt2e-3",
+                                   "fixed_rk2_dt1e-2", "fixed_rk2_dt5e-4"])
+def test_fixed_step_known_answers(golden, label):
+    """Step and RHS counts of the reference's fixed-step runs, single and on the 201-point
+    detuning grid, and the photon-integral difference of each from the adaptive Dopri5 run
+    (benchmarks/fixed_step_solver_results/fixed_step_solver_report.md, fixed_step_solver_validation.csv)."""
+    d = golden("plan_two_level")
+    kat = golden("kat_fixed_step")
+    p = oracle.OraclePlan(d["payload"])
+    ref, st_ref = _fixed_kat_solve(p, d, kat, kat["cases"]["adaptive_dopri5"])
+    assert int(st_ref["accepted_steps"][0]) == kat["cases"]["adaptive_dopri5"]["single_accepted_steps"] == 15
+    assert int(st_ref["rhs_calls"][0]) == kat["cases"]["adaptive_dopri5"]["single_rhs_calls"] == 91
+    case = kat["cases"][label]
+    v, st = _fixed_kat_solve(p, d, kat, case)
+    assert int(st["accepted_steps"][0]) == case["single_accepted_steps"]
+    assert int(st["rhs_calls"][0]) == case["single_rhs_calls"]
+    assert int(st["rejected_steps"][0]) == 0
+    diff = abs(v[0] - ref[0])
+    assert abs(diff - case["abs_error_vs_adaptive"]) <= 1e-9 * case["abs_error_vs_adaptive"]
+    assert abs(diff / abs(ref[0]) - case["rel_error_vs_adaptive"]) <= 1e-9 * case["rel_error_vs_adaptive"]
+    # the reference's fixed-step value itself, rebuilt from its recorded abs and rel errors
+    # (adaptive = abs / rel, fixed = adaptive -/+ abs): the oracle matches it to the last bits
+    ref_adaptive = case["abs_error_vs_adaptive"] / case["rel_error_vs_adaptive"]
+    ref_fixed = ref_adaptive + np.sign(v[0] - ref[0]) * case["abs_error_vs_adaptive"]
+    assert abs(v[0] - ref_fixed) <= 5e-16 * abs(ref_fixed)
+    _, stg = _fixed_kat_solve(p, d, kat, case, grid=True)
+    assert int(stg["accepted_steps"].sum()) == case["grid_accepted_steps"]
+    assert int(stg["rhs_calls"].sum()) == case["grid_rhs_calls"]
+
+
+def test_adaptive_grid_known_answer_of_fixed_step_benchmark(golden):
+    d = golden("plan_two_level")
+    kat = golden("kat_fixed_step")
+    p = oracle.OraclePlan(d["payload"])
+    case = kat["cases"]["adaptive_dopri5"]
+    _, st = _fixed_kat_solve(p, d, kat, case, grid=True)
+    assert int(st["accepted_steps"].sum()) == case["grid_accepted_steps"] == 3845
+    assert int(st["rhs_calls"].sum()) == case["grid_rhs_calls"] == 23271
+
+
+def test_fixed_step_saveat_and_errors(golden):
+    d = golden("plan_two_level")
+    p = oracle.OraclePlan(d["payload"])
+    # steps shorten to land on saveat times (fixed.rs:16-26): 0.1 steps with saves at 0.25 and 0.5
+    saveat = np.array([0.0, 0.25, 0.5])
+    t, v, st = p.solve_single(_opts(p, t1=0.5, dt=0.1, solver="fixed_rk4", output="populations",
+                                    output_when="saveat", saveat=saveat), d["rho0_packed"])
+    np.testing.assert_array_equal(t, saveat)
+    assert st["accepted_steps"] == 6  # 0.1 0.2 0.25 0.35 0.45 0.5
+    full = _opts(p, t1=0.5, dt=0.1, solver="fixed_rk4", output="populations", output_when="saveat")
+    t2, v2, _ = p.solve_single(full, d["rho0_packed"])
+    np.testing.assert_allclose(t2, [0.0, 0.1, 0.2, 0.30000000000000004, 0.4, 0.5])
+    with pytest.raises(oracle.OracleError, match="^fixed-step solvers require positive finite dt$"):
+        p.solve_single(_opts(p, dt=0.0, solver="fixed_rk2"), d["rho0_packed"])
+    with pytest.raises(oracle.OracleError, match=r"^Stopped at x=0\.2\. Need more than 2 steps\.$"):
+        p.solve_single(_opts(p, dt=0.1, maxiters=2, solver="fixed_dopri5"), d["rho0_packed"])
