@@ -149,9 +149,10 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 // Shared-memory layout of one trajectory group.  Gather inputs live in 16-byte slots (slot i:
 // rho_ii, slot n + m: the m-th upper pair), so one record reads one input and one coefficient.
 //   FP64 form: tab double2[1+F], G double2[U], K double[7][N]
-//   mixed form: tab double2[1+F] (k_1 refreshes), T4 float4[1+F] = (c, dc), G double2[U] (k_1
-//               refreshes), G4 float4[U] = (y_s - y_n, y_n), K32 float[6][N] (d_2..d_7),
-//               k1 double[N], k1f float[N]
+//   mixed form: T4 float4[1+F] = (c, dc), G4 float4[U] = (y_s - y_n, y_n), K32 float[6][N]
+//               (d_2..d_7), k1f float[N], k1 double[N]; the double-precision tab double2[1+F]
+//               and G double2[U] serve only the k_1 refreshes, when K32 and k1f are dead, and
+//               share their storage
 //   both: ybuf double[N] (outputs, events), VM slot and stack storage for the six VM lanes,
 //   coefficient rows, reduction scratch.
 struct GroupLayout {
@@ -163,17 +164,22 @@ __host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula,
     const size_t U = static_cast<size_t>(n) * (n + 1) / 2;
     GroupLayout L{};
     size_t o = 0;
-    L.tab = o; o = align16(o + (1 + n_formula) * 16);
     if (mixed) {
         L.T4 = o; o = align16(o + (1 + n_formula) * 16);
         L.cv = o; o = align16(o + 2 * static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
-    }
-    L.G = o; o = align16(o + U * 16);
-    if (mixed) { L.G4 = o; o = align16(o + U * 16); }
-    L.K = o; o = align16(o + (mixed ? 6 * 4 : 7 * 8) * static_cast<size_t>(N));
-    if (mixed) {
+        L.G4 = o; o = align16(o + U * 16);
+        const size_t k32 = align16(6 * 4 * static_cast<size_t>(N)), k1f = align16(4 * static_cast<size_t>(N));
+        const size_t tab = align16((1 + n_formula) * 16), g = align16(U * 16);
+        L.K = o;
+        L.k1f = o + k32;
+        L.tab = o;
+        L.G = o + tab;
+        o += k32 + k1f > tab + g ? k32 + k1f : tab + g;
         L.k1 = o; o = align16(o + static_cast<size_t>(N) * 8);
-        L.k1f = o; o = align16(o + static_cast<size_t>(N) * 4);
+    } else {
+        L.tab = o; o = align16(o + (1 + n_formula) * 16);
+        L.G = o; o = align16(o + U * 16);
+        L.K = o; o = align16(o + 7 * 8 * static_cast<size_t>(N));
     }
     L.ybuf = o; o = align16(o + static_cast<size_t>(N) * 8);
     L.vm_slots = o; o = align16(o + 6 * static_cast<size_t>(n_slots > 0 ? n_slots : 1) * 16);
@@ -448,8 +454,13 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
 // controller.  k_1 of the next step is k_1 + d_7 (first-same-as-last), recomputed in double
 // every k1_refresh accepted steps.
 
+// Threads per CTA of the integrator: the mixed form's smaller per-trajectory footprint fits
+// more trajectory groups per SM (shared memory), at a register budget of 65536 / threads.
+constexpr int kThreadsFp64 = 256;
+constexpr int kThreadsMixed = 352;
+
 template <int TPT, int EPT, bool MIXED>
-__global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
+__global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
@@ -662,10 +673,16 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
         };
         // one double-precision RHS from the slot buffer: formulas for coefficient row `row`, gather into out
         auto rhs64 = [&](int row, double* out) {
-            gsync<TPT>(g);  // G written, coefficient row ready
-            if (F > S) {
-                if constexpr (MIXED) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
-                else fill_formulas_dyn<TPT>(P, s_fptr, s_fcls, s_ffac64, s_cstat, s_cdyn + row * nd, s_tab, lt);
+            if constexpr (MIXED) {
+                // the table and slot buffer share storage with the stage deviations: rebuild
+                // every entry, the zero coefficient and the diagonal slots' imaginary halves
+                for (int i = lt; i < n; i += TPT) s_G64[2 * i + 1] = 0.0;
+                if (lt == 0) s_tab[0] = make_double2(0.0, 0.0);
+                gsync<TPT>(g);  // G written, coefficient row ready
+                fill_formulas<TPT>(P, 1, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
+            } else {
+                gsync<TPT>(g);  // G written, coefficient row ready
+                if (F > S) fill_formulas_dyn<TPT>(P, s_fptr, s_fcls, s_ffac64, s_cstat, s_cdyn + row * nd, s_tab, lt);
             }
             gsync<TPT>(g);
             gather_rhs<TPT, double, double2>(P, s_rec, s_out, s_tab, s_G, out, lt);
@@ -1239,6 +1256,7 @@ __global__ void __launch_bounds__(256, 1) integrate_kernel(const DevPlan P, cons
                     // the coefficients at t_{n+1} = x + h are row 4; they become the step-start row
                     if (lt < P.n_dyn) s_cdyn[5 * nd + lt] = s_cdyn[4 * nd + lt];
                     const bool refresh = !last && ++since_refresh >= A.k1_refresh;
+                    if (refresh) gsync<TPT>(g);  // the slot buffer below overlays the stage deviations
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
@@ -1581,7 +1599,7 @@ obe_status plan_launch(const DevPlan& P, bool mixed, long long n_traj, int vm_de
     s->group_bytes = L.bytes;
     size_t plan_bytes = plan_smem(P, s->tpt, mixed).bytes;
     const size_t limit = 227 * 1024;
-    int gpb = std::max(1, 256 / s->tpt);
+    int gpb = std::max(1, (mixed ? kThreadsMixed : kThreadsFp64) / s->tpt);
     while (gpb > 1 && plan_bytes + gpb * L.bytes > limit) --gpb;
     if (plan_bytes + gpb * L.bytes > limit) {
         set_error("system too large for the GPU solver's shared-memory layout");
