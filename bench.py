@@ -35,6 +35,9 @@ for sub in ("centrex-tlf_gb300", "oracle", "tests/golden"):
     sys.path.insert(0, str(ROOT / sub))
 
 METRIC = "batched OBE trajectories/s at <=1e-6 pop. error vs plain FP64"
+# DRAM bytes (read + write) per trajectory of integrate_kernel, from ncu captures of this
+# workload at 1024 points (dram__bytes_read.sum + dram__bytes_write.sum / 1024); see profiles/.
+TRAFFIC_BYTES_PER_TRAJECTORY = {"mixed": 2_969_344 / 1024, "fp64": 2_841_088 / 1024}
 W_EXCITED = [(13, 1.0), (14, 1.0), (15, 1.0)]
 
 
@@ -157,21 +160,28 @@ def run_reference(args) -> None:
     print(json.dumps(line))
 
 
-def measure_dgemm_peak(torch, dev) -> float:
+def measure_gemm_peak(torch, dev, dtype) -> float:
+    """Best-of-3 dense GEMM rate in TFLOP/s: float64 (the FP64 pipe) or float32 with TF32 off
+    (the FP32 CUDA-core pipe)."""
     n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device=dev)
-    b = torch.randn(n, n, dtype=torch.float64, device=dev)
-    for _ in range(2):
-        torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = 0.0
-    for _ in range(3):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
-        torch.matmul(a, b)
-        e.record()
+    a = torch.randn(n, n, dtype=dtype, device=dev)
+    b = torch.randn(n, n, dtype=dtype, device=dev)
+    tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        for _ in range(2):
+            torch.matmul(a, b)
         torch.cuda.synchronize()
-        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+        best = 0.0
+        for _ in range(3):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            torch.matmul(a, b)
+            e.record()
+            torch.cuda.synchronize()
+            best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = tf32
     return best
 
 
@@ -297,7 +307,8 @@ def run_gpu(args) -> None:
     flops_per_launch = attempted * per_step
     kernel_s = (sum(ms) / len(ms)) * 1e-3
     achieved = flops_per_launch / kernel_s / 1e12
-    peak = measure_dgemm_peak(torch, dev)
+    mixed = args.precision != "fp64"
+    peak = measure_gemm_peak(torch, dev, torch.float32 if mixed else torch.float64)
     clocks = sampler.summary(local)
     line = {
         "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
@@ -311,11 +322,14 @@ def run_gpu(args) -> None:
         "e2e": {"value": e2e_value, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "api": "centrex_tlf_rust.solve_lindblad_batch_ode_py (host numpy in/out)"},
         "gpu_launches": launches,
-        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": None,
-                     "note": "algorithmic FP64-equivalent FLOPs (6*F_rhs + 60*N per attempted step, F_rhs = "
-                             f"{f_rhs}) / mean launch time; peak = cuBLAS DGEMM measured in this run (no FP64 entry in "
-                             "the driver's peak file)"},
+        "roofline": {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak,
+                     "traffic": TRAFFIC_BYTES_PER_TRAJECTORY[args.precision] * b,
+                     "note": "algorithmic FLOPs (6*F_rhs + 60*N per attempted step, F_rhs = "
+                             f"{f_rhs}) / mean launch time; peak = cuBLAS "
+                             + ("SGEMM (TF32 off: the FP32 pipe the mixed form's products run on)" if mixed else "DGEMM")
+                             + " measured in this run (the driver's peak file has HBM and bf16 only); traffic = ncu DRAM "
+                             "read+write bytes per trajectory of this kernel, scaled to the launch"},
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "fp64_gpu": ({"value": b * world * args.steps / total64_s, "unit": "trajectories/s",
                       "ms_per_step": sum(other[0]) / len(other[0]), "attempted_steps_per_launch": other[1],
