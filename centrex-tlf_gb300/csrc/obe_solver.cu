@@ -166,7 +166,7 @@ __host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula,
     size_t o = 0;
     if (mixed) {
         L.T4 = o; o = align16(o + (1 + n_formula) * 16);
-        L.cv = o; o = align16(o + 2 * static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
+        L.cv = o; o = align16(o + 5 * 2 * static_cast<size_t>(n_coeff > 0 ? n_coeff : 1) * 16);
         L.G4 = o; o = align16(o + U * 16);
         const size_t k32 = align16(6 * 4 * static_cast<size_t>(N)), k1f = align16(4 * static_cast<size_t>(N));
         const size_t tab = align16((1 + n_formula) * 16), g = align16(U * 16);
@@ -242,6 +242,35 @@ __device__ __forceinline__ double group_sum(double v, double* red, int lt, int g
 __device__ __forceinline__ double time_tol(double t) { return 10.0 * 2.220446049250313e-16 * fmax(fabs(t), 1.0); }
 
 // double index of packed element i inside the slot buffer G (double2[U]) of the group
+// binary32 <-> binary64 conversions by field arithmetic on the integer pipe.  On this GPU a
+// conversion instruction occupies the FP64 pipe like a double-precision FMA (one warp
+// instruction per ~20 SM cycles whatever its active lanes), so the mixed form's per-step
+// conversions go through these.  Normal numbers and zeros take the integer path; subnormals,
+// infinities and NaNs fall back to the hardware conversion.
+__device__ __forceinline__ double f2d(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    if ((b & 0x7FFFFFFFu) == 0u) return __hiloint2double(static_cast<int>(b), 0);
+    if (e == 0u || e == 0xFFu) return static_cast<double>(f);
+    // exponent rebias 127 -> 1023; the 23 fraction bits become the top of the 52
+    const uint32_t hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7FFFFFu) >> 3);
+    return __hiloint2double(static_cast<int>(hi), static_cast<int>(b << 29));
+}
+// round to nearest, ties to even
+__device__ __forceinline__ float d2f(double d) {
+    const uint32_t hi = static_cast<uint32_t>(__double2hiint(d)), lo = static_cast<uint32_t>(__double2loint(d));
+    const uint32_t sign = hi & 0x80000000u;
+    const uint32_t e = (hi >> 20) & 0x7FFu;
+    if ((hi & 0x7FFFFFFFu) == 0u && lo == 0u) return __uint_as_float(sign);
+    if (e < 897u || e > 1150u) return static_cast<float>(d);  // below the normal float range, overflow, inf, nan
+    // the 52 fraction bits: keep the top 23, round on the 29 dropped
+    const uint32_t keep = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const uint32_t rest = lo & 0x1FFFFFFFu;
+    uint32_t r = ((e - 896u) << 23) | keep;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (keep & 1u))) r += 1u;  // a carry bumps the exponent
+    return __uint_as_float(sign | r);
+}
+
 __device__ __forceinline__ int gslot64(int i, int n) { return i < n ? 2 * i : n + i; }
 // float index of packed element i's deviation inside G4 (float4[U]); + 2 for y_n
 __device__ __forceinline__ int gslot32(int i, int n) { return i < n ? 4 * i : 4 * (n + ((i - n) >> 1)) + ((i - n) & 1); }
@@ -365,17 +394,22 @@ __device__ __forceinline__ void fill_formulas_dev(const DevPlan& P, const int32_
     }
 }
 
-// per-class single-precision values and changes for the stage row (threads < 2 * n_coeff)
-__device__ __forceinline__ void stage_classes(const DevPlan& P, const double2* cstat, const double2* crow, const double2* crow0,
+// Per-class single-precision values and changes since the step start for the five stage rows
+// (cv[row * 2 n_coeff + class]); one pass over all rows so the double-precision differences and
+// conversions cost one warp instruction each.
+template <int TPT>
+__device__ __forceinline__ void stage_classes(const DevPlan& P, const double2* cstat, const double2* cdyn, int nd,
                                               float4* cv, int lt) {
-    if (lt < 2 * P.n_coeff) {
-        int k = lt >> 1;
-        int pos = P.coeff_dyn_pos[k];
-        double2 c = pos >= 0 ? crow[pos] : cstat[k];
-        double2 c0 = pos >= 0 ? crow0[pos] : c;
+    const int nc = 2 * P.n_coeff;
+    for (int q = lt; q < 5 * nc; q += TPT) {
+        const int row = q / nc, cls = q - row * nc;
+        const int k = cls >> 1;
+        const int pos = P.coeff_dyn_pos[k];
+        double2 c = pos >= 0 ? cdyn[row * nd + pos] : cstat[k];
+        double2 c0 = pos >= 0 ? cdyn[5 * nd + pos] : c;
         double dre = c.x - c0.x, dim = c.y - c0.y;
-        if (lt & 1) { c.y = -c.y; dim = -dim; }
-        cv[lt] = make_float4(static_cast<float>(c.x), static_cast<float>(c.y), static_cast<float>(dre), static_cast<float>(dim));
+        if (cls & 1) { c.y = -c.y; dim = -dim; }
+        cv[q] = make_float4(static_cast<float>(c.x), static_cast<float>(c.y), static_cast<float>(dre), static_cast<float>(dim));
     }
 }
 
@@ -922,6 +956,8 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
         // controller state (common.rs:20-46)
         const double beta = 0.04, alpha = 0.2 - beta * 0.75, facc1 = 1.0 / 0.2, facc2 = 1.0 / 10.0, safety = 0.9;
         double fac_old = 1.0e-4;
+        float fac_old32 = 1.0e-4f;
+        const float atolf = static_cast<float>(A.atol), rtolf = static_cast<float>(A.rtol);  // mixed error norm
         const double h_maxc = fabs(t1 - t0);
         const double posneg = (t1 - t0) >= 0.0 ? 1.0 : -1.0;
         bool reject = false;
@@ -937,8 +973,8 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
                     if (i < N) {
-                        s_k1f[i] = static_cast<float>(s_k1[i]);
-                        s_G4f[gslot32(i, n) + 2] = static_cast<float>(y[e]);
+                        s_k1f[i] = d2f(s_k1[i]);
+                        s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
                     }
                 }
             }
@@ -985,7 +1021,12 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                 eval_compounds(P, L, ts, true);
                 for (int j = 0; j < P.n_dyn; ++j) s_cdyn[lt * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, ts);
             }
+            if constexpr (MIXED) {
+                gsync<TPT>(g);
+                stage_classes<TPT>(P, s_cstat, s_cdyn, nd, s_cv, lt);
+            }
             double err = 0.0;
+            float err32 = 0.f;  // the mixed form's error norm
             if constexpr (!MIXED) {
                 // stages 2..7 (stage 7 input is the solution yn)
 #pragma unroll 1
@@ -1021,7 +1062,7 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                     }
                 }
             } else {
-                const float hf = static_cast<float>(h);
+                const float hf = d2f(h);
 #pragma unroll 1
                 for (int s = 0; s < 6; ++s) {
                     // stage input deviation y_s - y_n = h (c_s k_1 + sum_j a_sj d_j), in single
@@ -1036,16 +1077,13 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                             for (int j = 1; j < 6; ++j)
                                 if (j <= s) acc = fmaf(kAf[M][s][j], s_K32[static_cast<size_t>(j - 1) * N + i], acc);
                             const float k1f = s_k1f[i];
-                            if (s == 5) yn[e] = y[e] + h * (s_k1[i] + static_cast<double>(acc));
+                            if (s == 5) yn[e] = y[e] + h * (s_k1[i] + f2d(acc));
                             s_G4f[gslot32(i, n)] = hf * fmaf(csum, k1f, acc);
                         }
                     }
-                    const int row = s < 4 ? s : 4;
                     if (s < 5) {  // stage 7 shares stage 6's time
                         gsync<TPT>(g);
-                        stage_classes(P, s_cstat, s_cdyn + row * nd, s_cdyn + 5 * nd, s_cv, lt);
-                        gsync<TPT>(g);
-                        fill_formulas_dev<TPT>(P, s_fptr, s_fcls, s_ffac32, s_cv, s_T4, lt);
+                        fill_formulas_dev<TPT>(P, s_fptr, s_fcls, s_ffac32, s_cv + s * 2 * P.n_coeff, s_T4, lt);
                     }
                     gsync<TPT>(g);
                     gather_dev<TPT>(P, s_rec, s_out, s_T4, s_G4, s_K32 + static_cast<size_t>(s) * N, lt);
@@ -1053,7 +1091,6 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                 }
                 // error estimate from the deviations alone (the error weights sum to zero); the
                 // per-element ratios in single precision, their sum and the controller in double
-                const float atolf = static_cast<float>(A.atol), rtolf = static_cast<float>(A.rtol);
                 float errf = 0.f;
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
@@ -1085,27 +1122,32 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                     for (int w = 0; w < TPT / 32; ++w) errf += redf[w];
                     gsync<TPT>(g);
                 }
-                err = static_cast<double>(sqrtf(errf / static_cast<float>(N)));
+                err32 = sqrtf(errf / static_cast<float>(N));
             }
             rhs_calls += 6;
             if constexpr (!MIXED) err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
-            // controller (common.rs:48-69).  The mixed form takes the two powers in single
-            // precision (its error norm is single precision already); the step sizes then differ
-            // from the double-precision powers' by ~1e-7 relative.
-            double fac11, fac;
+            // controller (common.rs:48-69).  The mixed form runs it in single precision (its error
+            // norm is single precision already) and scales h by the rounded factor: its step sizes
+            // differ from a double-precision controller's by ~1e-7 relative.
+            double fac11 = 0.0, hn;
+            bool accept_step;
             if constexpr (MIXED) {
-                const float ef = static_cast<float>(err), fo = static_cast<float>(fac_old);
-                const float f11 = exp2f(static_cast<float>(alpha) * log2f(ef));
-                fac11 = f11;
-                fac = static_cast<double>(f11 * exp2f(static_cast<float>(-beta) * log2f(fo)));
+                const float f11 = exp2f(static_cast<float>(alpha) * log2f(err32));
+                float facf = f11 * exp2f(static_cast<float>(-beta) * log2f(fac_old32));
+                facf = fmaxf(static_cast<float>(facc2), fminf(static_cast<float>(facc1), facf / static_cast<float>(safety)));
+                hn = h * f2d(1.0f / facf);
+                accept_step = err32 <= 1.0f;
+                if (accept_step) fac_old32 = fmaxf(err32, 1.0e-4f);
+                else hn = h * f2d(1.0f / fminf(static_cast<float>(facc1), f11 / static_cast<float>(safety)));
             } else {
                 fac11 = pow(err, alpha);
-                fac = fac11 * pow(fac_old, -beta);
+                double fac = fac11 * pow(fac_old, -beta);
+                fac = fmax(facc2, fmin(facc1, fac / safety));
+                hn = h / fac;
+                accept_step = err <= 1.0;
+                if (accept_step) fac_old = fmax(err, 1.0e-4);
             }
-            fac = fmax(facc2, fmin(facc1, fac / safety));
-            double hn = h / fac;
-            if (err <= 1.0) {
-                fac_old = fmax(err, 1.0e-4);
+            if (accept_step) {
                 if (fabs(hn) > h_maxc) hn = posneg * h_maxc;
                 if (reject) hn = posneg * fmin(fabs(hn), fabs(h));
                 reject = false;
@@ -1266,10 +1308,10 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                                 s_G64[gslot64(i, n)] = y[e];
                             } else {
                                 // first-same-as-last: k_1 of the next step is k_7 = k_1 + d_7
-                                double k = s_k1[i] + static_cast<double>(s_K32[static_cast<size_t>(5) * N + i]);
+                                double k = s_k1[i] + f2d(s_K32[static_cast<size_t>(5) * N + i]);
                                 s_k1[i] = k;
-                                s_k1f[i] = static_cast<float>(k);
-                                s_G4f[gslot32(i, n) + 2] = static_cast<float>(y[e]);
+                                s_k1f[i] = d2f(k);
+                                s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
                             }
                         }
                     }
@@ -1283,7 +1325,7 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                 h = hn;
                 if (last) break;
             } else {
-                hn = h / fmin(facc1, fac11 / safety);
+                if constexpr (!MIXED) hn = h / fmin(facc1, fac11 / safety);
                 reject = true;
                 last = false;
                 if (accepted >= 1) ++rejected;
@@ -1723,9 +1765,6 @@ obe_status validate_options(const obe_plan* p, const obe_solve_options* o, std::
         for (int k = 0; k < o->n_event_indices; ++k) evidx.push_back(static_cast<int32_t>(o->event_indices[k]));
     } else if (o->event_kind == OBE_EVENT_EXPRESSION) {
         // kind-check the event program with the plan's slot kinds and keep it in the call blob
-        HostPacked tmp;
-        obe_plan_desc dd{};
-        (void)dd;
         const obe_expr& e = o->event_expr;
         for (int64_t k = 0; k < e.n_instr; ++k) {
             int32_t op = e.op[k];
