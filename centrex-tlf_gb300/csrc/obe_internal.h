@@ -41,6 +41,9 @@ constexpr uint32_t kRecComplex = 1u << 14;
 constexpr uint32_t kRecConj = 1u << 15;
 constexpr uint32_t kRecFlush = 1u << 16;
 constexpr int kRecCoefShift = 17;
+constexpr uint32_t kFStreamClassMask = 0xFFFu;
+constexpr uint32_t kFStreamFlush = 1u << 12;
+constexpr int kFStreamFormulaShift = 13;
 constexpr uint32_t kMaxFormulas = (1u << 15) - 1;
 constexpr uint32_t kNoImag = 0xFFFFu;
 
@@ -90,6 +93,11 @@ struct DevPlan {
     const uint32_t* rec;         // [n_iter * tpt]
     int32_t n_out;               // outputs per thread (padded)
     const uint32_t* lane_out;    // [n_out * tpt]: re | im << 16 (im = kNoImag on the diagonal)
+    // time-dependent formulas as a thread-interleaved product stream (mixed form):
+    // [n_fiter * tpt] of (factor re, factor im, meta, 0); meta = class + 1 (0: the constant 1)
+    // | kFStreamFlush (last product of the formula) | formula << kFStreamFormulaShift
+    int32_t n_fiter;
+    const uint32_t* fstream;     // [n_fiter * tpt * 4]
 };
 
 // Host-side result of packing (owned by obe_plan).
@@ -112,7 +120,8 @@ struct HostPacked {
     std::vector<double> prod_factor;
     std::vector<float> prod_factor32;
     std::vector<uint32_t> rec, lane_out;
-    int32_t n_iter = 0, n_out = 0, tpt = 32;
+    std::vector<uint32_t> fstream;  // 4 words per entry
+    int32_t n_iter = 0, n_out = 0, tpt = 32, n_fiter = 0;
     int32_t n_formula = 0, n_static_formula = 0;
     int32_t max_stack = 0;
 };

@@ -459,6 +459,48 @@ obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
                 }
             }
         }
+        // ---- time-dependent formulas as a thread-interleaved product stream -------------------
+        // (mixed form: each thread sums its formulas' products and stores the finished entries;
+        // formulas are dealt out longest first onto the least-loaded thread)
+        if (2 * static_cast<int64_t>(p->n_coeff) + 1 > static_cast<int64_t>(kFStreamClassMask))
+            fail(OBE_ERR_UNSUPPORTED, "too many Hamiltonian coefficients for the GPU solver");
+        {
+            std::vector<int32_t> forder(D);
+            std::iota(forder.begin(), forder.end(), 0);
+            std::stable_sort(forder.begin(), forder.end(), [&](int32_t a, int32_t b) { return dyn_list[a].size() > dyn_list[b].size(); });
+            std::vector<int64_t> fload(tpt, 0);
+            std::vector<std::vector<int32_t>> lane_f(tpt);
+            for (int32_t f : forder) {
+                int lane = static_cast<int>(std::min_element(fload.begin(), fload.end()) - fload.begin());
+                lane_f[lane].push_back(f);
+                fload[lane] += std::max<int64_t>(1, static_cast<int64_t>(dyn_list[f].size()));
+            }
+            const int64_t n_fiter = D > 0 ? *std::max_element(fload.begin(), fload.end()) : 0;
+            hp.n_fiter = static_cast<int32_t>(n_fiter);
+            hp.fstream.assign(static_cast<size_t>(n_fiter) * tpt * 4, 0u);  // padding: constant 0, no store
+            for (int lane = 0; lane < tpt; ++lane) {
+                int64_t it = 0;
+                for (int32_t f : lane_f[lane]) {
+                    const uint32_t fid = static_cast<uint32_t>(1 + S + f);
+                    const Formula& fl = dyn_list[f];
+                    for (size_t q = 0; q < std::max<size_t>(1, fl.size()); ++q) {
+                        uint32_t* e = &hp.fstream[(static_cast<size_t>(it) * tpt + lane) * 4];
+                        float fr = 0.f, fi = 0.f;
+                        uint32_t meta = 0u;
+                        if (q < fl.size()) {
+                            fr = static_cast<float>(std::get<1>(fl[q]));
+                            fi = static_cast<float>(std::get<2>(fl[q]));
+                            meta = static_cast<uint32_t>(std::get<0>(fl[q]) + 1);
+                        }
+                        if (q + 1 >= fl.size()) meta |= kFStreamFlush | (fid << kFStreamFormulaShift);
+                        std::memcpy(&e[0], &fr, 4);
+                        std::memcpy(&e[1], &fi, 4);
+                        e[2] = meta;
+                        ++it;
+                    }
+                }
+            }
+        }
         return OBE_OK;
     } catch (const Fail& f) {
         set_error(f.msg);

@@ -197,7 +197,7 @@ __host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula,
 // time-dependent formulas, their product lists (offsets, coefficient classes, factors in the
 // precision of the form).
 struct PlanSmem {
-    size_t rec, out, fptr, fcls, ffac, bytes;
+    size_t rec, out, fstream, fptr, fcls, ffac, bytes;
 };
 
 __host__ __device__ inline PlanSmem plan_smem(const DevPlan& P, int tpt, bool mixed) {
@@ -205,9 +205,13 @@ __host__ __device__ inline PlanSmem plan_smem(const DevPlan& P, int tpt, bool mi
     size_t o = 0;
     L.rec = o; o += static_cast<size_t>(P.n_iter) * tpt * 4;
     L.out = o; o = align16(o + static_cast<size_t>(P.n_out) * tpt * 4);
-    L.fptr = o; o = align16(o + static_cast<size_t>(P.n_formula - P.n_static_formula + 1) * 4);
-    L.fcls = o; o = align16(o + static_cast<size_t>(P.n_dyn_prod) * 4);
-    L.ffac = o; o = align16(o + static_cast<size_t>(P.n_dyn_prod) * (mixed ? 8 : 16));
+    if (mixed) {
+        L.fstream = o; o = align16(o + static_cast<size_t>(P.n_fiter) * tpt * 16);
+    } else {
+        L.fptr = o; o = align16(o + static_cast<size_t>(P.n_formula - P.n_static_formula + 1) * 4);
+        L.fcls = o; o = align16(o + static_cast<size_t>(P.n_dyn_prod) * 4);
+        L.ffac = o; o = align16(o + static_cast<size_t>(P.n_dyn_prod) * 16);
+    }
     L.bytes = o;
     return L;
 }
@@ -365,32 +369,33 @@ __device__ __forceinline__ void fill_formulas_dyn(const DevPlan& P, const int32_
 // start time (.zw).  cv holds, per coefficient class (k, conj), the value and the change as
 // float4; the changes were taken in double before rounding, so they keep their relative
 // precision.  Pure single-precision work per product.
-// The time-dependent formulas (entries 1 + n_static_formula .. n_formula) from the CTA's shared
-// copy of their product lists: fptr relative to the first such product.
+// The time-dependent formulas' single-precision values at a stage time (.xy) and their changes
+// since the step's start (.zw), from the CTA's shared thread-interleaved product stream: each
+// thread sums the products of its own formulas and stores each entry when its last product is
+// in.  cv holds the stage row's per-class values and changes.
 template <int TPT>
-__device__ __forceinline__ void fill_formulas_dev(const DevPlan& P, const int32_t* __restrict__ fptr,
-                                                  const int32_t* __restrict__ fcls, const float2* __restrict__ ffac,
-                                                  const float4* __restrict__ cv, float4* __restrict__ T4, int lt) {
-    const int S = P.n_static_formula;
-    for (int f = 1 + S + lt; f < 1 + P.n_formula; f += TPT) {
-        int a = fptr[f - 1 - S], b = fptr[f - S];
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int p = a; p < b; ++p) {
-            const float2 fac = ffac[p];
-            const float fr = fac.x, fi = fac.y;
-            int cls = fcls[p];
-            if (cls < 0) {
-                acc.x += fr;
-                acc.y += fi;
-                continue;
-            }
-            float4 c = cv[cls];
-            acc.x += fr * c.x - fi * c.y;
-            acc.y += fr * c.y + fi * c.x;
-            acc.z += fr * c.z - fi * c.w;
-            acc.w += fr * c.w + fi * c.z;
+__device__ __forceinline__ void fill_formulas_dev(int n_fiter, const float4* __restrict__ fs, const float4* __restrict__ cv,
+                                                  float4* __restrict__ T4, int lt) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 2
+    for (int it = 0; it < n_fiter; ++it) {
+        const float4 r = fs[it * TPT + lt];
+        const uint32_t meta = __float_as_uint(r.z);
+        const int cls = static_cast<int>(meta & kFStreamClassMask) - 1;
+        if (cls >= 0) {
+            const float4 c = cv[cls];
+            acc.x = fmaf(r.x, c.x, fmaf(-r.y, c.y, acc.x));
+            acc.y = fmaf(r.x, c.y, fmaf(r.y, c.x, acc.y));
+            acc.z = fmaf(r.x, c.z, fmaf(-r.y, c.w, acc.z));
+            acc.w = fmaf(r.x, c.w, fmaf(r.y, c.z, acc.w));
+        } else {
+            acc.x += r.x;
+            acc.y += r.y;
         }
-        T4[f] = acc;
+        if (meta & kFStreamFlush) {
+            T4[meta >> kFStreamFormulaShift] = acc;
+            acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
     }
 }
 
@@ -445,6 +450,8 @@ __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __r
 }
 
 // Stage deviation d_s = L(t_s) (y_s - y_n) + (L(t_s) - L(t_n)) y_n, all in single precision.
+// Software-pipelined: the record two iterations ahead and the operands of the next one are in
+// flight while the current record is summed (the loop is latency-bound otherwise).
 template <int TPT>
 __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
                                            const float4* __restrict__ T4, const float4* __restrict__ G4, float* __restrict__ K,
@@ -452,11 +459,14 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
     float ar = 0.f, ai = 0.f;
     int o = 0;
     const int n_iter = P.n_iter;
-#pragma unroll 4
+    uint32_t w = s_rec[lt];
+    uint32_t w1 = n_iter > 1 ? s_rec[TPT + lt] : 0u;
+    float4 c = T4[w >> kRecCoefShift];
+    float4 v = G4[w & kRecIndexMask];
     for (int it = 0; it < n_iter; ++it) {
-        uint32_t w = s_rec[it * TPT + lt];
-        float4 c = T4[w >> kRecCoefShift];
-        float4 v = G4[w & kRecIndexMask];
+        const uint32_t w2 = it + 2 < n_iter ? s_rec[(it + 2) * TPT + lt] : 0u;
+        const float4 cn = T4[w1 >> kRecCoefShift];
+        const float4 vn = G4[w1 & kRecIndexMask];
         if (w & kRecConj) { v.y = -v.y; v.w = -v.w; }
         ar = fmaf(c.x, v.x, ar);
         ar = fmaf(-c.y, v.y, ar);
@@ -475,6 +485,10 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
             ai = 0.f;
             ++o;
         }
+        w = w1;
+        w1 = w2;
+        c = cn;
+        v = vn;
     }
 }
 
@@ -506,18 +520,21 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
     uint32_t* s_out = reinterpret_cast<uint32_t*>(smem + PS.out);
     int32_t* s_fptr = reinterpret_cast<int32_t*>(smem + PS.fptr);
     int32_t* s_fcls = reinterpret_cast<int32_t*>(smem + PS.fcls);
-    float2* s_ffac32 = reinterpret_cast<float2*>(smem + PS.ffac);
     double2* s_ffac64 = reinterpret_cast<double2*>(smem + PS.ffac);
+    uint32_t* s_fstream = reinterpret_cast<uint32_t*>(smem + PS.fstream);
     {
         for (int i = threadIdx.x; i < P.n_iter * TPT; i += blockDim.x) s_rec[i] = P.rec[i];
         for (int i = threadIdx.x; i < P.n_out * TPT; i += blockDim.x) s_out[i] = P.lane_out[i];
-        const int nf = P.n_formula - P.n_static_formula;
-        for (int i = threadIdx.x; i <= nf; i += blockDim.x) s_fptr[i] = P.formula_ptr[P.n_static_formula + i] - P.dyn_prod0;
-        for (int i = threadIdx.x; i < P.n_dyn_prod; i += blockDim.x) {
-            const int q = P.dyn_prod0 + i;
-            s_fcls[i] = P.prod_class[q];
-            if constexpr (MIXED) s_ffac32[i] = make_float2(P.prod_factor32[2 * q], P.prod_factor32[2 * q + 1]);
-            else s_ffac64[i] = make_double2(P.prod_factor[2 * q], P.prod_factor[2 * q + 1]);
+        if constexpr (MIXED) {
+            for (int i = threadIdx.x; i < P.n_fiter * TPT * 4; i += blockDim.x) s_fstream[i] = P.fstream[i];
+        } else {
+            const int nf = P.n_formula - P.n_static_formula;
+            for (int i = threadIdx.x; i <= nf; i += blockDim.x) s_fptr[i] = P.formula_ptr[P.n_static_formula + i] - P.dyn_prod0;
+            for (int i = threadIdx.x; i < P.n_dyn_prod; i += blockDim.x) {
+                const int q = P.dyn_prod0 + i;
+                s_fcls[i] = P.prod_class[q];
+                s_ffac64[i] = make_double2(P.prod_factor[2 * q], P.prod_factor[2 * q + 1]);
+            }
         }
     }
     __syncthreads();
@@ -1083,7 +1100,8 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
                     }
                     if (s < 5) {  // stage 7 shares stage 6's time
                         gsync<TPT>(g);
-                        fill_formulas_dev<TPT>(P, s_fptr, s_fcls, s_ffac32, s_cv + s * 2 * P.n_coeff, s_T4, lt);
+                        fill_formulas_dev<TPT>(P.n_fiter, reinterpret_cast<const float4*>(s_fstream), s_cv + s * 2 * P.n_coeff,
+                                               s_T4, lt);
                     }
                     gsync<TPT>(g);
                     gather_dev<TPT>(P, s_rec, s_out, s_T4, s_G4, s_K32 + static_cast<size_t>(s) * N, lt);
@@ -1499,7 +1517,7 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     size_t o_ke = put(blob, h.coeff_expr), o_kd = put(blob, h.coeff_dynamic), o_di = put(blob, h.dyn_ids), o_dp = put(blob, h.coeff_dyn_pos);
     size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
     size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
-    size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out);
+    size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out), o_fs = put(blob, h.fstream);
     P = DevPlan{};
     P.n = p->n;
     P.N = static_cast<int32_t>(p->N);
@@ -1544,6 +1562,8 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     P.rec = reinterpret_cast<const uint32_t*>(base + o_rec);
     P.n_out = h.n_out;
     P.lane_out = reinterpret_cast<const uint32_t*>(base + o_lo);
+    P.n_fiter = h.n_fiter;
+    P.fstream = reinterpret_cast<const uint32_t*>(base + o_fs);
 }
 
 obe_status upload_plan(obe_plan* p) {
