@@ -28,6 +28,8 @@ constexpr int kMaxHelperArgs = 12;
 struct DevExpr {
     int32_t start;
     int32_t len;
+    int32_t real_ok;  // real operands give real results through every instruction (see vm_eval_real)
+    int32_t pad;
 };
 
 // A record of the RHS gather stream.  Bits:
@@ -73,6 +75,7 @@ struct DevPlan {
     const int32_t* coeff_dyn_pos;// [n_coeff] position in dyn_ids or -1
     int32_t time_dependent;
     int32_t max_stack;           // deepest VM stack of the plan's programs
+    int32_t dyn_real_closed;     // every time-dependent compound maps real slots to real values
     // PCHIP tables (plan.rs:27-116)
     int32_t n_pchip;
     const int32_t* pchip_ptr;
@@ -124,6 +127,8 @@ struct HostPacked {
     int32_t n_iter = 0, n_out = 0, tpt = 32, n_fiter = 0;
     int32_t n_formula = 0, n_static_formula = 0;
     int32_t max_stack = 0;
+    int32_t n_vm_slots = 0;     // parameter slots plus the hoisted static subexpressions
+    int32_t dyn_real_closed = 0;  // every time-dependent compound is real_ok
 };
 
 }  // namespace obe

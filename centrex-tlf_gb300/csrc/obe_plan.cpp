@@ -228,6 +228,122 @@ int64_t upper_index(int32_t n, int32_t i, int32_t j) {
     return off + (j - i);
 }
 
+// ---- static-subexpression hoisting and real closure --------------------------------------
+//
+// The time-dependent expressions are evaluated at five stage times per step; any subtree of
+// theirs that reads neither the time nor a time-dependent slot gives the same value every time.
+// Such subtrees (maximal, at least two instructions, no tuples or helpers) move into new static
+// compounds evaluated once per trajectory, and the expression reads them back from a new slot:
+// the same operations on the same values, so results are unchanged.
+
+struct Ins {
+    int32_t op, arg, fn;
+    double re, im;
+};
+
+int ins_arity(const Ins& x) {
+    switch (x.op) {
+    case OP_CONST: case OP_SLOT: case OP_TIME: return 0;
+    case OP_NEG: case OP_CONJ: return 1;
+    case OP_BUILTIN: case OP_HELPER: return x.arg;
+    case OP_PCHIP_TABLE: return 3;
+    default: return 2;  // arithmetic and comparisons
+    }
+}
+
+std::vector<Ins> read_expr(const HostPacked& hp, const DevExpr& e) {
+    std::vector<Ins> v;
+    for (int32_t k = e.start; k < e.start + e.len; ++k)
+        v.push_back(Ins{hp.ins_op[k], hp.ins_arg[k], hp.ins_fn[k], hp.ins_val[2 * k], hp.ins_val[2 * k + 1]});
+    return v;
+}
+
+// real_ok: every instruction maps real operands to a real result in the complex VM, and the
+// real-only VM reproduces that result exactly (integer powers by repeated multiplication only).
+bool expr_real_closed(const std::vector<Ins>& v, const std::vector<int32_t>& slot_is_tuple) {
+    for (size_t k = 0; k < v.size(); ++k) {
+        const Ins& x = v[k];
+        switch (x.op) {
+        case OP_CONST: if (x.im != 0.0) return false; break;
+        case OP_SLOT: if (x.arg < static_cast<int32_t>(slot_is_tuple.size()) && slot_is_tuple[x.arg]) return false; break;
+        case OP_TIME: case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_NEG: case OP_CONJ:
+        case OP_GT: case OP_GE: case OP_LT: case OP_LE: case OP_EQ: case OP_NE: break;
+        case OP_POW:
+            if (k == 0 || v[k - 1].op != OP_CONST || v[k - 1].im != 0.0 || v[k - 1].re != std::rint(v[k - 1].re) ||
+                std::fabs(v[k - 1].re) > 64.0)
+                return false;
+            break;
+        case OP_BUILTIN: if (x.fn < 1 || x.fn > 7 || x.arg != 1) return false; break;
+        default: return false;  // helpers, tables
+        }
+    }
+    return true;
+}
+
+DevExpr write_expr(HostPacked& hp, const std::vector<Ins>& v, const std::vector<int32_t>& slot_is_tuple) {
+    DevExpr e{static_cast<int32_t>(hp.ins_op.size()), static_cast<int32_t>(v.size()), 0, 0};
+    for (const Ins& x : v) {
+        hp.ins_op.push_back(x.op);
+        hp.ins_arg.push_back(x.arg);
+        hp.ins_fn.push_back(x.fn);
+        hp.ins_val.push_back(x.re);
+        hp.ins_val.push_back(x.im);
+    }
+    e.real_ok = expr_real_closed(v, slot_is_tuple) ? 1 : 0;
+    return e;
+}
+
+// Split the hoistable subtrees out of v: returns the rewritten program and appends each
+// hoisted subtree (with its new slot, numbered from next_slot) to `hoisted`.
+std::vector<Ins> hoist_expr(const std::vector<Ins>& v, const std::vector<uint8_t>& dyn_slot, const std::vector<int32_t>& slot_is_tuple,
+                            int32_t& next_slot, std::vector<std::pair<int32_t, std::vector<Ins>>>& hoisted) {
+    const int m = static_cast<int>(v.size());
+    std::vector<int> start(m), parent(m, -1);
+    std::vector<uint8_t> stat(m), ok(m);
+    std::vector<int> stack;
+    for (int k = 0; k < m; ++k) {
+        const Ins& x = v[k];
+        const int a = ins_arity(x);
+        bool st = x.op != OP_TIME && !(x.op == OP_SLOT && x.arg < static_cast<int32_t>(dyn_slot.size()) && dyn_slot[x.arg]);
+        bool good = x.op != OP_HELPER && x.op != OP_PCHIP_TABLE &&
+                    !(x.op == OP_SLOT && x.arg < static_cast<int32_t>(slot_is_tuple.size()) && slot_is_tuple[x.arg]);
+        int s0 = k;
+        if (a > static_cast<int>(stack.size())) return v;  // malformed: leave it alone
+        for (int c = 0; c < a; ++c) {
+            int ch = stack[stack.size() - a + c];
+            if (c == 0) s0 = start[ch];
+            st = st && stat[ch];
+            good = good && ok[ch];
+            parent[ch] = k;
+        }
+        stack.resize(stack.size() - a);
+        start[k] = s0;
+        stat[k] = st;
+        ok[k] = good;
+        stack.push_back(k);
+    }
+    std::vector<int> root_at(m, -1);  // subtree start -> hoisted root
+    for (int k = 0; k < m; ++k) {
+        const bool hoistable = stat[k] && ok[k] && k - start[k] + 1 >= 2;
+        const int par = parent[k];
+        if (hoistable && par >= 0 && !(stat[par] && ok[par])) root_at[start[k]] = k;
+    }
+    std::vector<Ins> out;
+    for (int k = 0; k < m;) {
+        const int r = root_at[k];
+        if (r >= 0) {
+            hoisted.emplace_back(next_slot, std::vector<Ins>(v.begin() + k, v.begin() + r + 1));
+            out.push_back(Ins{OP_SLOT, next_slot, 0, 0.0, 0.0});
+            ++next_slot;
+            k = r + 1;
+        } else {
+            out.push_back(v[k]);
+            ++k;
+        }
+    }
+    return out;
+}
+
 }  // namespace
 
 obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
@@ -321,6 +437,59 @@ obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
             ham_uses_time = ham_uses_time || uses_time(e);
         }
         p->time_dependent = params_use_time || ham_uses_time;
+
+        // ---- hoist the static parts of the time-dependent programs -----------------------------
+        {
+            int32_t next_slot = d->n_slots;
+            std::vector<int32_t> tuple_of(slot_is_tuple);
+            std::vector<int32_t> n_comp_slot;
+            std::vector<DevExpr> n_comp_expr;
+            std::vector<uint8_t> n_comp_dyn;
+            std::vector<std::vector<Ins>> comp_prog, coeff_prog;
+            for (size_t i = 0; i < hp.comp_expr.size(); ++i) comp_prog.push_back(read_expr(hp, hp.comp_expr[i]));
+            for (size_t k = 0; k < hp.coeff_expr.size(); ++k) coeff_prog.push_back(read_expr(hp, hp.coeff_expr[k]));
+            hp.ins_op.clear(); hp.ins_arg.clear(); hp.ins_fn.clear(); hp.ins_val.clear();
+            std::vector<std::pair<int32_t, std::vector<Ins>>> hoisted;
+            for (size_t i = 0; i < comp_prog.size(); ++i) {
+                std::vector<Ins> prog = comp_prog[i];
+                if (hp.comp_dynamic[i]) {
+                    hoisted.clear();
+                    prog = hoist_expr(prog, dyn_slot, slot_is_tuple, next_slot, hoisted);
+                    for (auto& hsub : hoisted) {
+                        tuple_of.push_back(0);
+                        n_comp_slot.push_back(hsub.first);
+                        n_comp_expr.push_back(write_expr(hp, hsub.second, tuple_of));
+                        n_comp_dyn.push_back(0);
+                    }
+                }
+                n_comp_slot.push_back(hp.comp_slot[i]);
+                n_comp_expr.push_back(write_expr(hp, prog, tuple_of));
+                n_comp_dyn.push_back(hp.comp_dynamic[i]);
+            }
+            for (size_t k = 0; k < coeff_prog.size(); ++k) {
+                std::vector<Ins> prog = coeff_prog[k];
+                if (hp.coeff_dynamic[k]) {
+                    hoisted.clear();
+                    prog = hoist_expr(prog, dyn_slot, slot_is_tuple, next_slot, hoisted);
+                    for (auto& hsub : hoisted) {
+                        tuple_of.push_back(0);
+                        n_comp_slot.push_back(hsub.first);
+                        n_comp_expr.push_back(write_expr(hp, hsub.second, tuple_of));
+                        n_comp_dyn.push_back(0);
+                    }
+                }
+                coeff_prog[k] = prog;
+            }
+            for (size_t k = 0; k < coeff_prog.size(); ++k) hp.coeff_expr[k] = write_expr(hp, coeff_prog[k], tuple_of);
+            hp.comp_slot = n_comp_slot;
+            hp.comp_expr = n_comp_expr;
+            hp.comp_dynamic = n_comp_dyn;
+            hp.n_vm_slots = next_slot;
+            hp.dyn_real_closed = 1;
+            for (size_t i = 0; i < hp.comp_expr.size(); ++i)
+                if (hp.comp_dynamic[i] && !hp.comp_expr[i].real_ok) hp.dyn_real_closed = 0;
+            if (hp.n_vm_slots > kMaxSlots) fail(OBE_ERR_UNSUPPORTED, "too many parameter slots for the GPU solver");
+        }
         if (static_cast<int>(hp.dyn_ids.size()) > kMaxDynCoeff)
             fail(OBE_ERR_UNSUPPORTED, "too many time-dependent Hamiltonian coefficients for the GPU solver");
 

@@ -286,6 +286,7 @@ __device__ __forceinline__ int gslot32(int i, int n) { return i < n ? 4 * i : 4 
 struct VMLane {
     double2* slots;
     VStack stack;
+    bool real;  // every slot is real and the time-dependent compounds keep it so: real-only VM
 };
 
 __device__ __noinline__ void init_slots(const DevPlan& P, const CallArgs& A, long long traj, double2* slots) {
@@ -307,6 +308,10 @@ __device__ __noinline__ void init_slots(const DevPlan& P, const CallArgs& A, lon
 }
 
 __device__ __forceinline__ double2 eval_expr(const DevPlan& P, DevExpr e, const VMLane& L, double t) {
+    if (L.real && e.real_ok)
+        return make_double2(vm_eval_real(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, e.start, e.len, L.slots, t,
+                                         reinterpret_cast<double*>(L.stack.v)),
+                            0.0);
     return vm_eval(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, e.start, e.len, L.slots, t, L.stack);
 }
 
@@ -564,6 +569,7 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
 
     // this thread's VM lane (lanes 0..5 only)
     VMLane L;
+    L.real = false;
     {
         int vl = lt < 6 ? lt : 0;
         L.slots = reinterpret_cast<double2*>(gb + Lay.vm_slots) + vl * (P.n_slots > 0 ? P.n_slots : 1);
@@ -582,7 +588,11 @@ __global__ void __launch_bounds__(MIXED ? kThreadsMixed : kThreadsFp64, 1) integ
         const double t0 = A.t0, t1 = A.t1;
         if (lt < 6) {
             init_slots(P, A, traj, L.slots);
+            L.real = false;
             eval_compounds(P, L, t0, false);
+            bool real = P.dyn_real_closed != 0;
+            for (int i = 0; i < P.n_slots && real; ++i) real = L.slots[i].y == 0.0;
+            L.real = real;
         }
         if (lt == 0) {
             for (int k = 0; k < P.n_coeff; ++k)
@@ -1414,6 +1424,7 @@ __global__ void __launch_bounds__(256) rhs_kernel(const DevPlan P, long long cou
     L.slots = reinterpret_cast<double2*>(gb + Lay.vm_slots);
     L.stack.v = reinterpret_cast<double2*>(gb + Lay.vm_stack);
     L.stack.tup = reinterpret_cast<int32_t*>(gb + Lay.vm_tup);
+    L.real = false;
     CallArgs none{};
     for (long long st = static_cast<long long>(blockIdx.x) * gpb + g; st < count; st += static_cast<long long>(gridDim.x) * gpb) {
         const double t = ts[st];
@@ -1526,8 +1537,9 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     P.ins_arg = reinterpret_cast<const int32_t*>(base + o_arg);
     P.ins_fn = reinterpret_cast<const int32_t*>(base + o_fn);
     P.ins_val = reinterpret_cast<const double*>(base + o_val);
-    P.n_slots = p->n_slots;
+    P.n_slots = std::max(p->n_slots, h.n_vm_slots);
     P.n_base = p->n_base;
+    P.dyn_real_closed = h.dyn_real_closed;
     P.base_val = reinterpret_cast<const double*>(base + o_bv);
     P.base_tuple = reinterpret_cast<const int32_t*>(base + o_bt);
     P.tuple_ptr = reinterpret_cast<const int32_t*>(base + o_tp);

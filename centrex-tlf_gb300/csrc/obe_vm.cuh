@@ -322,4 +322,80 @@ __device__ __noinline__ double2 vm_eval(const DevPlan& P, const int32_t* op, con
     return st[0];
 }
 
+// The same programs on real values only, for expressions marked real_ok (obe_plan.cpp:
+// expr_real_closed) when every slot of the trajectory is real.  Each case computes exactly what
+// the complex case above yields for operands with zero imaginary parts -- the quotient as
+// (a b) / (b b), tan(z) as sin(2z) / (cos(2z) + 1), integer powers by the same repeated
+// multiplication -- so the two paths agree bit for bit while the real one issues a fraction of
+// the double-precision instructions.  The stack is the caller's VM stack storage.
+__device__ __noinline__ double vm_eval_real(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
+                                            const double* val, int32_t start, int32_t len, const double2* slots, double t,
+                                            double* st) {
+    int sp = 0;
+    for (int32_t k = start; k < start + len; ++k) {
+        const int32_t o = op[k];
+        switch (o) {
+        case OP_CONST: st[sp++] = val[2 * k]; break;
+        case OP_SLOT: st[sp++] = slots[arg[k]].x; break;
+        case OP_TIME: st[sp++] = t; break;
+        case OP_ADD: { double b = st[--sp]; st[sp - 1] = st[sp - 1] + b; break; }
+        case OP_SUB: { double b = st[--sp]; st[sp - 1] = st[sp - 1] - b; break; }
+        case OP_MUL: { double b = st[--sp]; st[sp - 1] = st[sp - 1] * b; break; }
+        case OP_DIV: { double b = st[--sp], a = st[sp - 1]; st[sp - 1] = (a * b) / (b * b); break; }
+        case OP_POW: {
+            const double y = st[--sp], x = st[sp - 1];
+            double r;
+            if (y == 0.0) {
+                r = 1.0;
+            } else {
+                int kk = static_cast<int>(fabs(y));
+                double acc = 1.0, b = x;
+                bool first = true;
+                while (kk) {
+                    if (kk & 1) {
+                        acc = first ? b : acc * b;
+                        first = false;
+                    }
+                    kk >>= 1;
+                    if (kk) b = b * b;
+                }
+                r = y < 0.0 ? 1.0 / acc : acc;
+            }
+            st[sp - 1] = r;
+            break;
+        }
+        case OP_NEG: st[sp - 1] = -st[sp - 1]; break;
+        case OP_CONJ: break;
+        case OP_BUILTIN: {
+            const double z = st[sp - 1];
+            double r;
+            switch (fn[k]) {
+            case 1:
+            case 2: {
+                double sn, cs;
+                sincos(z, &sn, &cs);  // as the complex case computes them
+                r = fn[k] == 1 ? sn : cs;
+                break;
+            }
+            case 3: { double tr = z + z; r = sin(tr) / (cos(tr) + 1.0); break; }
+            case 4: r = exp(z); break;
+            case 5: r = hypot(z, 0.0); break;
+            case 6: r = z; break;
+            default: r = 0.0; break;
+            }
+            st[sp - 1] = r;
+            break;
+        }
+        default: {  // comparisons
+            const double r = st[sp - 1], l = st[sp - 2];
+            sp -= 2;
+            const bool res = o == OP_GT ? l > r : o == OP_GE ? l >= r : o == OP_LT ? l < r : o == OP_LE ? l <= r : o == OP_EQ ? l == r : l != r;
+            st[sp++] = res ? 1.0 : 0.0;
+            break;
+        }
+        }
+    }
+    return st[0];
+}
+
 }  // namespace obe
