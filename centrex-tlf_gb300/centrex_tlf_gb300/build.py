@@ -1,8 +1,8 @@
 """Build the in-tree CUDA solver library ``_lib/libobe_gb300.so`` for sm_103a.
 
-Two translation units compiled in parallel: the host packer (g++) and the CUDA solver
-(nvcc, ``-gencode arch=compute_103a,code=sm_103a``), linked with nvcc into one shared library
-with the C ABI of include/obe_gb300.h.
+Translation units compiled in parallel: the host packer (g++), the host side of the CUDA solver
+and one object per integrator kernel shape (nvcc, ``-gencode arch=compute_103a,code=sm_103a``),
+linked with nvcc into one shared library with the C ABI of include/obe_gb300.h.
 """
 
 from __future__ import annotations
@@ -21,6 +21,10 @@ CSRC = ROOT / "csrc"
 INCLUDE = ROOT.parent / "include"
 OUT = PKG / "_lib" / "libobe_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# integrator shapes (threads per trajectory, elements per thread); the RHS kernel is built with
+# the first shape of each width.  Must match OBE_FOR_EACH_SHAPE / OBE_FOR_EACH_RHS in obe_kernels.cuh.
+SHAPES = [(32, 8), (32, 16), (64, 16), (128, 16), (256, 32)]
+RHS_SHAPES = [(32, 8), (64, 16), (128, 16), (256, 32)]
 
 
 def _nvcc() -> str:
@@ -48,12 +52,18 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     OUT.parent.mkdir(parents=True, exist_ok=True)
     with tempfile.TemporaryDirectory(prefix="obe_build_") as tmp:
         tmp = Path(tmp)
+        common = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}"]
+        objs = [tmp / "obe_solver.o", tmp / "obe_plan.o"]
         cmds = [
-            [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}",
-             "-c", str(CSRC / "obe_solver.cu"), "-o", str(tmp / "obe_solver.o")],
-            ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}", "-c", str(CSRC / "obe_plan.cpp"),
-             "-o", str(tmp / "obe_plan.o")],
+            common + ["-c", str(CSRC / "obe_solver.cu"), "-o", str(objs[0])],
+            ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}", "-c", str(CSRC / "obe_plan.cpp"), "-o", str(objs[1])],
         ]
+        # one object per kernel shape (threads per trajectory, elements per thread), compiled in parallel
+        for tpt, ept in SHAPES:
+            obj = tmp / f"obe_instance_{tpt}_{ept}.o"
+            defs = [f"-DOBE_TPT={tpt}", f"-DOBE_EPT={ept}"] + (["-DOBE_RHS"] if (tpt, ept) in RHS_SHAPES else [])
+            cmds.append(common + defs + ["-c", str(CSRC / "obe_instance.cu"), "-o", str(obj)])
+            objs.append(obj)
 
         def run(cmd):
             res = subprocess.run(cmd, capture_output=True, text=True)
@@ -62,10 +72,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             if verbose:
                 sys.stdout.write(res.stdout + res.stderr)
 
-        with ThreadPoolExecutor(max_workers=2) as pool:
+        with ThreadPoolExecutor(max_workers=min(len(cmds), os.cpu_count() or 4)) as pool:
             list(pool.map(run, cmds))
         tmp_out = tmp / "libobe_gb300.so"
-        run([nvcc, *ARCH, "-shared", "-o", str(tmp_out), str(tmp / "obe_solver.o"), str(tmp / "obe_plan.o")])
+        run([nvcc, *ARCH, "-shared", "-o", str(tmp_out), *map(str, objs)])
         shutil.copy2(tmp_out, OUT)
     return OUT
 

@@ -150,6 +150,9 @@ struct obe_plan {
     void* d_scratch = nullptr;
     size_t scratch_bytes = 0;
     void* d_counter = nullptr;
+    // global stage buffers of large systems (grow-only)
+    void* d_gk = nullptr;
+    size_t gk_bytes = 0;
 };
 
 namespace obe {

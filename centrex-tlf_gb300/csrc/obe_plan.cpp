@@ -66,7 +66,7 @@ std::string fmt_f64(double v) {
 
 int threads_per_trajectory_for(int32_t n) {
     int64_t N = static_cast<int64_t>(n) * n;
-    int t = N <= 512 ? 32 : N <= 1024 ? 64 : N <= 2048 ? 128 : N <= 4096 ? 256 : 512;
+    int t = N <= 512 ? 32 : N <= 1024 ? 64 : N <= 2048 ? 128 : N <= 8192 ? 256 : 512;
     // OBE_TPT widens the group (64 or 128 threads per trajectory) for tuning runs
     if (const char* env = std::getenv("OBE_TPT")) {
         int v = std::atoi(env);

@@ -92,7 +92,7 @@ __device__ __forceinline__ double rabi_from_intensity(double intensity, double c
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kEdXtB = 0.315 * 1.602176634e-19 * 5.29177210544e-11;
 
-__device__ __noinline__ double2 helper_scalar(int fid, const double2* a, int argc) {
+static __device__ __noinline__ double2 helper_scalar(int fid, const double2* a, int argc) {
     auto S = [&](int i) { return i < argc ? a[i].x : 0.0; };
     switch (fid) {
     case 1: return make_double2(g2d(S(0), S(1), S(2), S(3), S(4), S(5), S(6)), 0.0);
@@ -147,7 +147,7 @@ __device__ __noinline__ double2 helper_scalar(int fid, const double2* a, int arg
 }
 
 // PCHIP derivative d[i] of the direct form (eval.rs:322-333), computed locally.
-__device__ double pchip_d(const double2* g, const double2* v, int n, int i) {
+static __device__ double pchip_d(const double2* g, const double2* v, int n, int i) {
     auto h = [&](int k) { return g[k + 1].x - g[k].x; };
     auto delta = [&](int k) { return (v[k + 1].x - v[k].x) / h(k); };
     if (i == 0) return delta(0);
@@ -163,7 +163,7 @@ __device__ __forceinline__ const double2* tuple_items(const DevPlan& P, int32_t 
     return reinterpret_cast<const double2*>(P.tuple_items) + P.tuple_ptr[id];
 }
 
-__device__ __noinline__ double2 helper_general(const DevPlan& P, int fid, const double2* a, const int32_t* tup, int argc) {
+static __device__ __noinline__ double2 helper_general(const DevPlan& P, int fid, const double2* a, const int32_t* tup, int argc) {
     if (fid == 8 || fid == 10) {
         int la, lx, ly;
         const double2* amp = tuple_items(P, tup[2], &la);
@@ -211,7 +211,7 @@ __device__ __noinline__ double2 helper_general(const DevPlan& P, int fid, const 
 }
 
 // PchipTable::evaluate (plan.rs:82-115) without the search hint.
-__device__ __noinline__ double pchip_table_eval(const DevPlan& P, int table, double x) {
+static __device__ __noinline__ double pchip_table_eval(const DevPlan& P, int table, double x) {
     int a = P.pchip_ptr[table], n = P.pchip_ptr[table + 1] - a;
     const double* g = P.pchip_grid + a;
     const double* coef = P.pchip_coef + P.pchip_cptr[table];
@@ -236,7 +236,7 @@ __device__ __noinline__ double pchip_table_eval(const DevPlan& P, int table, dou
 
 // Evaluate one program.  Programs were kind-checked on the host, so tuples only reach the
 // helpers that accept them and the result is a scalar.
-__device__ __noinline__ double2 vm_eval(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
+static __device__ __noinline__ double2 vm_eval(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
                                         const double* val, int32_t start, int32_t len, const double2* slots, double t,
                                         VStack S) {
     double2* st = S.v;
@@ -328,7 +328,7 @@ __device__ __noinline__ double2 vm_eval(const DevPlan& P, const int32_t* op, con
 // (a b) / (b b), tan(z) as sin(2z) / (cos(2z) + 1), integer powers by the same repeated
 // multiplication -- so the two paths agree bit for bit while the real one issues a fraction of
 // the double-precision instructions.  The stack is the caller's VM stack storage.
-__device__ __noinline__ double vm_eval_real(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
+static __device__ __noinline__ double vm_eval_real(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
                                             const double* val, int32_t start, int32_t len, const double2* slots, double t,
                                             double* st) {
     int sp = 0;

@@ -18,6 +18,8 @@ What it writes (all JSON through ``codec.py``):
 * ``rk45_<name>.json``: trajectories from the reference's SciPy RK45 solve
   (``solve_lindblad(..., backend="python")``, centrex_tlf/lindblad/solve.py:155-199):
   tolerance-level anchors for whole solves.
+* ``plan_rc_76.json`` / ``rhs_rc_76.json``: the 76-state rotational-cooling system (dense collapse
+  operators dropped: the expanded_sparse path does not read them).
 * ``kat_fixed_step.json``: the reference's recorded fixed-step solver runs
   (benchmarks/fixed_step_solver_results/fixed_step_solver_report.md and
   fixed_step_solver_validation.csv): step and RHS counts per case, and the photon-integral
@@ -193,6 +195,58 @@ def build_q1_16(centrex_tlf):
     return prepared, labels
 
 
+def build_rc_76(centrex_tlf):
+    """The 76-state rotational-cooling-sized system: X J=0-3 (64 hyperfine states) + B J'=1
+    F1'=1/2, 3/2 (P=-1, 12 states), driven by R(0) F1'=1/2 F'=1 and P(2) F1'=3/2 F'=1 with x and z
+    polarisation components; Γ = 2π·1.56 MHz.  Each laser's polarisation switches between x and
+    z as a 1 MHz square wave (the second a quarter period later), and a scanned end time t_end
+    can feed a `Time() - t_end` stop event.  (R(0) with Q(1) over 12 B states of one parity does
+    not build in the reference; R(0) with P(2) is the exact-size construction that does.)
+    """
+    from centrex_tlf import couplings, lindblad, states, transitions
+    from centrex_tlf.lindblad.parameters import LindbladParameters
+    from centrex_tlf.lindblad.plan_static import prepare_lindblad_problem
+
+    X = [states.QuantumSelector(J=j, electronic=states.ElectronicState.X) for j in (0, 1, 2, 3)]
+    B = [states.QuantumSelector(J=1, F1=f1, P=-1, electronic=states.ElectronicState.B) for f1 in (0.5, 1.5)]
+    trans = [transitions.R0_F1_1o2_F1, transitions.P2_F1_3o2_F1]
+    pol = [couplings.polarization_X, couplings.polarization_Z]
+    selectors = couplings.generate_transition_selectors(trans, [pol, pol])
+    obe = lindblad.generate_OBE_system(X, B, selectors, Γ=GAMMA)
+    quarter = 0.5 * np.pi
+    params = LindbladParameters.from_kwargs(
+        Ω0=GAMMA, Ω1=GAMMA, δ0=0.0, δ1=0.0, omega_pol=2.0 * np.pi * 1e6, t_end=50e-6,
+        PX0="square_wave(t, omega_pol, 0.0)", PZ0="1 - square_wave(t, omega_pol, 0.0)",
+        PX1=f"square_wave(t, omega_pol, {quarter!r})", PZ1=f"1 - square_wave(t, omega_pol, {quarter!r})",
+    )
+    prepared = prepare_lindblad_problem(obe, params, backend="python", hamiltonian_representation="decomposed")
+    labels = [str(s.largest) for s in obe.QN]
+    return prepared, labels
+
+
+def save_rc_76(centrex_tlf) -> None:
+    """plan_rc_76.json and rhs_rc_76.json: the 76-state system of build_rc_76."""
+    rc, labels = build_rc_76(centrex_tlf)
+    payload = rc.to_payload()
+    # the expanded_sparse path never reads the dense collapse operators (154 x 76 x 76 complex,
+    # 14 MB): keep their shape contract with zero operators
+    payload["dense_c_array"] = np.zeros((0, 76, 76), dtype=np.complex128)
+    n_x = sum(1 for lab in labels if "X" in lab)
+    rho = np.zeros((76, 76), dtype=np.complex128)
+    for i in range(n_x):
+        rho[i, i] = 1.0 / n_x
+    codec.save(
+        "plan_rc_76",
+        {
+            "payload": payload, "rho0_packed": rc.layout.pack(rho), "gamma": GAMMA, "state_labels": labels,
+            "n_ground": n_x, "excited_indices": [i for i, lab in enumerate(labels) if "B" in lab],
+            "scan_slots": ["Ω0", "Ω1", "δ0", "δ1", "t_end"],
+        },
+    )
+    cases = rhs_vectors(rc, [0.0, 3.1e-7, 7.7e-7], [{}, {0: 2.0 * GAMMA, 2: 0.3 * GAMMA}], seed=76, scale=0.02)
+    codec.save("rhs_rc_76", {"cases": cases})
+
+
 def _with_base_overrides(prepared, overrides: dict[int, complex]):
     """A shallow stand-in of ``prepared`` whose parameter graph has some base values replaced
     (what the batch drivers' scalar overrides do, rust/src/lindblad/rhs.rs:1176-1197)."""
@@ -364,6 +418,9 @@ def main() -> None:
     if "--kat-fixed-step" in sys.argv:
         codec.save("kat_fixed_step", fixed_step_kat())
         return
+    if "--rc-76" in sys.argv:
+        save_rc_76(_import_reference())
+        return
     centrex_tlf = _import_reference()
     started = time.perf_counter()
 
@@ -448,6 +505,9 @@ def main() -> None:
     codec.save("rk45_q1_16", rk)
 
     codec.save("kat_fixed_step", fixed_step_kat())
+
+    # --- 76-state rotational-cooling system (the large-system path, n > 45) ------------------
+    save_rc_76(centrex_tlf)
 
     # --- the native-boundary call contract of the reference's Python surface ----------------
     codec.save("ffi_calls", record_ffi_calls(centrex_tlf, q1, rho_q))
