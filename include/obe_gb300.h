@@ -250,6 +250,9 @@ obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options*
  * Limits: at most 65,536 trajectories per call, a plan device image of at most 1 MiB and at
  * most 64 KiB of per-call arguments (saveat, weights, selections, event program); larger
  * requests are rejected with OBE_ERR_INVALID and a message saying which limit was hit.
+ * Systems above 45 states are rejected with OBE_ERR_UNSUPPORTED: their per-trajectory stage
+ * buffers need device memory of the order of a megabyte per trajectory in flight, far beyond the
+ * fixed array; solve those with obe_solve_batch_device.
  * The first call on a device looks up the array's device address (once per device, with that
  * device current); make that first call before any stream capture begins.
  * Every call shares the one array and leaves its contents behind: calls whose GPU work overlaps

@@ -105,3 +105,26 @@ def test_noalloc_rejects_sizes_beyond_its_limit(golden):
             st_buf.data_ptr(), None)
     assert st == _abi.OBE_ERR_INVALID
     assert "at most 65536 trajectories" in _abi.last_error(lib)
+
+
+def test_noalloc_rejects_systems_above_45_states(golden):
+    """The 76-state system keeps its stage buffers in device memory the library allocates, so the
+    allocation-free entry point refuses it, naming the entry point that can solve it."""
+    torch = pytest.importorskip("torch")
+    d = golden("plan_rc_76")
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    native = plan.native
+    g = d["gamma"]
+    opts = native.options(t0=0.0, t1=1.0 / g, abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=np.array([1.0 / g]),
+                          save_start=False, maxiters=1000, solver="tsit5", output="populations", output_indices=None,
+                          output_when="final", integral_weights=None, stop_event=None)
+    lib = _abi.load_library()
+    fn = _noalloc(lib)
+    dev = torch.device("cuda:0")
+    rho = torch.from_numpy(d["rho0_packed"].reshape(1, -1).copy()).to(dev)
+    out = torch.zeros(76, dtype=torch.float64, device=dev)
+    st_buf = torch.zeros(6, dtype=torch.int64, device=dev)
+    st = fn(native.handle, ctypes.byref(opts.opts), 1, rho.data_ptr(), 0, None, None, 1, 76, out.data_ptr(),
+            st_buf.data_ptr(), None)
+    assert st == _abi.OBE_ERR_UNSUPPORTED
+    assert "obe_solve_batch_device" in _abi.last_error(lib)
