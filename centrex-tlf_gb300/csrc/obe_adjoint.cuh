@@ -1,0 +1,537 @@
+// obe_adjoint.cuh -- discrete adjoint of the double-precision adaptive solve (gradients of the
+// final populations or of a weighted time integral with respect to base parameters and to the
+// initial state).  No counterpart in the reference, whose Rust crate has no gradient path.
+//
+// The forward solve (integrate_kernel with a tape) records, for every accepted step n, its start
+// time t_n, size h_n, start state y_n and the stage derivatives K_1..K_6.  With the step sequence
+// frozen, one step of Dopri5/Tsit5 is the explicit six-stage map
+//     Y_s = y_n + h sum_{l<s} a_sl K_l,   K_s = L(t_n + c_s h; p) Y_s,   y_{n+1} = y_n + h sum_s b_s K_s
+// (the seventh, first-same-as-last stage only feeds the error estimate), and its reverse sweep is
+//     lambda_s = h b_s ybar' + h sum_{m>s} a_ms mu_m,    mu_s = L(t_s)^T lambda_s,
+//     ybar = ybar' + sum_s mu_s,                          pbar += sum_s lambda_s^T (dL/dp)(t_s) Y_s.
+// L(t) = sum_f formula_f(c(t)) E_f, with each formula a sum of factor x coefficient-class
+// products, so lambda^T (dL/dp) Y = sum_class Re(dc_class/dp * S_class) where S_class sums
+// factor * Y_in' * conj(lambda_out) over the records and products of that class.  The
+// coefficient derivatives dc/dp come from forward-mode (dual) evaluation of the parameter and
+// coefficient programs.  The trapezoid rule of the integral outputs (sum over accepted steps of
+// (t_{n+1} - t_n)(w.y_n + w.y_{n+1}) / 2) adds its weights to ybar at both ends of each segment.
+//
+// One warp per trajectory (systems up to 22 states); the transposed product L^T lambda runs on a
+// second, input-major record stream built by the packer.
+#pragma once
+
+#include "obe_kernels.cuh"
+
+namespace obe {
+
+constexpr int kMaxGrad = 8;
+
+// per-trajectory adjoint status codes
+enum AdjCode : int32_t { ADJ_OK = 0, ADJ_HELPER_DERIVATIVE = 1, ADJ_FORWARD_FAILED = 2 };
+
+struct AdjArgs {
+    int n_grad;
+    int grad_slot[kMaxGrad];    // base slots the gradient is taken with respect to
+    const double* tape;
+    long long tape_cap, tape_stride;
+    const obe_traj_stats* fwd_stats;  // the forward solve's statistics (accepted-step counts)
+    const double* out_grad;     // [traj][width]: d(loss)/d(output)
+    double* param_grad;         // [traj][n_grad]
+    double* rho0_grad;          // [traj][N] or null
+    int32_t* adj_status;        // [traj]
+    unsigned long long* counter;
+};
+
+// ------------------------------------------------------------------------------------------
+// forward-mode evaluation: value and derivatives with respect to the n_grad parameters
+
+// One program in dual numbers.  slots / dslots: values and derivatives ([slot * n_grad + g]) of
+// the parameter slots; the stack holds values in sv, derivatives in sd ([depth * kMaxGrad]) and
+// tuple ids in tp.  Returns the value and writes the derivatives to out_d[0..n_grad).  A helper
+// or table whose arguments carry a derivative sets *bad (its derivative is not implemented).
+static __device__ __noinline__ double2 vm_eval_dual(const DevPlan& P, int32_t start, int32_t len, const double2* slots,
+                                                    const double2* dslots, int ng, double t, double2* sv, double2* sd,
+                                                    int32_t* tp, double2* out_d, int* bad) {
+    const int32_t* op = P.ins_op;
+    const int32_t* arg = P.ins_arg;
+    const int32_t* fn = P.ins_fn;
+    const double* val = P.ins_val;
+    int sp = 0;
+    auto D = [&](int i, int g) -> double2& { return sd[i * kMaxGrad + g]; };
+    for (int32_t k = start; k < start + len; ++k) {
+        const int32_t o = op[k];
+        switch (o) {
+        case OP_CONST:
+            sv[sp] = make_double2(val[2 * k], val[2 * k + 1]);
+            for (int g = 0; g < ng; ++g) D(sp, g) = make_double2(0.0, 0.0);
+            tp[sp++] = -1;
+            break;
+        case OP_SLOT: {
+            const int32_t s = arg[k];
+            const int32_t tid = s < P.n_base ? P.base_tuple[s] : -1;
+            sv[sp] = tid >= 0 ? make_double2(0.0, 0.0) : slots[s];
+            for (int g = 0; g < ng; ++g) D(sp, g) = tid >= 0 ? make_double2(0.0, 0.0) : dslots[s * ng + g];
+            tp[sp++] = tid;
+            break;
+        }
+        case OP_TIME:
+            sv[sp] = make_double2(t, 0.0);
+            for (int g = 0; g < ng; ++g) D(sp, g) = make_double2(0.0, 0.0);
+            tp[sp++] = -1;
+            break;
+        case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW: {
+            const int ib = --sp, ia = sp - 1;
+            const double2 a = sv[ia], b = sv[ib];
+            double2 c;
+            if (o == OP_ADD || o == OP_SUB) {
+                const double sg = o == OP_ADD ? 1.0 : -1.0;
+                c = make_double2(a.x + sg * b.x, a.y + sg * b.y);
+                for (int g = 0; g < ng; ++g) D(ia, g) = make_double2(D(ia, g).x + sg * D(ib, g).x, D(ia, g).y + sg * D(ib, g).y);
+            } else if (o == OP_MUL) {
+                c = cmul(a, b);
+                for (int g = 0; g < ng; ++g) {
+                    const double2 x = cmul(D(ia, g), b), y = cmul(a, D(ib, g));
+                    D(ia, g) = make_double2(x.x + y.x, x.y + y.y);
+                }
+            } else if (o == OP_DIV) {
+                c = cdiv(a, b);
+                // (a'/b) - (a b'/b^2) = (a' - c b') / b
+                for (int g = 0; g < ng; ++g) {
+                    const double2 cb = cmul(c, D(ib, g));
+                    D(ia, g) = cdiv(make_double2(D(ia, g).x - cb.x, D(ia, g).y - cb.y), b);
+                }
+            } else {
+                c = cpow(a, b);
+                // integer exponent: k a^(k-1) a'; otherwise a^b (b' ln a + b a'/a)
+                const bool int_exp = b.y == 0.0 && b.x == rint(b.x) && fabs(b.x) <= 64.0;
+                double2 f1 = make_double2(0.0, 0.0), lna = make_double2(0.0, 0.0);
+                if (int_exp) {
+                    if (b.x != 0.0) f1 = cmul(make_double2(b.x, 0.0), cpow(a, make_double2(b.x - 1.0, 0.0)));
+                } else {
+                    lna = make_double2(log(hypot(a.x, a.y)), atan2(a.y, a.x));
+                    f1 = cmul(c, cdiv(b, a));
+                }
+                for (int g = 0; g < ng; ++g) {
+                    double2 dv = cmul(f1, D(ia, g));
+                    if (!int_exp) {
+                        const double2 t2 = cmul(c, cmul(D(ib, g), lna));
+                        dv = make_double2(dv.x + t2.x, dv.y + t2.y);
+                    } else if (D(ib, g).x != 0.0 || D(ib, g).y != 0.0) {
+                        *bad = 1;
+                    }
+                    D(ia, g) = dv;
+                }
+            }
+            sv[ia] = c;
+            tp[ia] = -1;
+            break;
+        }
+        case OP_NEG:
+            sv[sp - 1] = make_double2(-sv[sp - 1].x, -sv[sp - 1].y);
+            for (int g = 0; g < ng; ++g) D(sp - 1, g) = make_double2(-D(sp - 1, g).x, -D(sp - 1, g).y);
+            break;
+        case OP_CONJ:
+            sv[sp - 1].y = -sv[sp - 1].y;
+            for (int g = 0; g < ng; ++g) D(sp - 1, g).y = -D(sp - 1, g).y;  // the parameters are real
+            break;
+        case OP_BUILTIN: {
+            const int argc = arg[k];
+            const int iz = sp - argc;
+            const double2 z = sv[iz];
+            double2 r = make_double2(0.0, 0.0), dr = make_double2(0.0, 0.0);  // value and d(value)/dz
+            switch (fn[k]) {
+            case 1: {
+                double sn, cs;
+                sincos(z.x, &sn, &cs);
+                const double ch = z.y == 0.0 ? 1.0 : cosh(z.y), sh = z.y == 0.0 ? z.y : sinh(z.y);
+                r = make_double2(sn * ch, cs * sh);
+                dr = make_double2(cs * ch, -sn * sh);  // cos z
+                break;
+            }
+            case 2: {
+                double sn, cs;
+                sincos(z.x, &sn, &cs);
+                const double ch = z.y == 0.0 ? 1.0 : cosh(z.y), sh = z.y == 0.0 ? z.y : sinh(z.y);
+                r = make_double2(cs * ch, -sn * sh);
+                dr = make_double2(-sn * ch, -cs * sh);  // -sin z
+                break;
+            }
+            case 3: {
+                const double tr = z.x + z.x, ti = z.y + z.y, dd = cos(tr) + cosh(ti);
+                r = make_double2(sin(tr) / dd, sinh(ti) / dd);
+                const double2 r2 = cmul(r, r);
+                dr = make_double2(1.0 + r2.x, r2.y);  // 1 + tan^2 z
+                break;
+            }
+            case 4: r = cexp(z); dr = r; break;
+            case 5: r = make_double2(hypot(z.x, z.y), 0.0); break;
+            case 6: r = make_double2(z.x, 0.0); break;
+            default: r = make_double2(z.y, 0.0); break;
+            }
+            for (int g = 0; g < ng; ++g) {
+                const double2 dz = D(iz, g);
+                double2 dv;
+                if (fn[k] <= 4) {
+                    dv = cmul(dr, dz);
+                } else if (fn[k] == 5) {  // |z|' = Re(conj(z) z') / |z|
+                    const double m = hypot(z.x, z.y);
+                    dv = make_double2(m > 0.0 ? (z.x * dz.x + z.y * dz.y) / m : 0.0, 0.0);
+                } else if (fn[k] == 6) {
+                    dv = make_double2(dz.x, 0.0);
+                } else {
+                    dv = make_double2(dz.y, 0.0);
+                }
+                D(iz, g) = dv;
+            }
+            sp = iz;
+            sv[sp] = r;
+            tp[sp++] = -1;
+            break;
+        }
+        case OP_HELPER:
+        case OP_PCHIP_TABLE: {
+            const int argc = o == OP_PCHIP_TABLE ? 3 : arg[k];
+            sp -= argc;
+            for (int a = 0; a < argc; ++a)
+                for (int g = 0; g < ng; ++g)
+                    if (D(sp + a, g).x != 0.0 || D(sp + a, g).y != 0.0) *bad = 1;
+            double2 r;
+            if (o == OP_HELPER) r = helper_general(P, fn[k], sv + sp, tp + sp, argc);
+            else r = make_double2(pchip_table_eval(P, fn[k], sv[sp].x), 0.0);
+            sv[sp] = r;
+            for (int g = 0; g < ng; ++g) D(sp, g) = make_double2(0.0, 0.0);
+            tp[sp++] = -1;
+            break;
+        }
+        default: {  // comparisons: piecewise constant
+            const double r = sv[sp - 1].x, l = sv[sp - 2].x;
+            sp -= 2;
+            const bool res = o == OP_GT ? l > r : o == OP_GE ? l >= r : o == OP_LT ? l < r : o == OP_LE ? l <= r : o == OP_EQ ? l == r : l != r;
+            sv[sp] = make_double2(res ? 1.0 : 0.0, 0.0);
+            for (int g = 0; g < ng; ++g) D(sp, g) = make_double2(0.0, 0.0);
+            tp[sp++] = -1;
+            break;
+        }
+        }
+    }
+    for (int g = 0; g < ng; ++g) out_d[g] = D(0, g);
+    return sv[0];
+}
+
+// ------------------------------------------------------------------------------------------
+// shared-memory layout of one adjoint trajectory group (32 threads)
+
+struct AdjLayout {
+    size_t tab, G, LS, MU, YB, slots, dslots, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, traj, bytes;
+};
+
+__host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int n_coeff, int n_dyn, int n_slots, int vm_depth) {
+    const size_t U = static_cast<size_t>(n) * (n + 1) / 2;
+    const size_t nc = n_coeff > 0 ? n_coeff : 1, nd = n_dyn > 0 ? n_dyn : 1, ns = n_slots > 0 ? n_slots : 1;
+    AdjLayout L{};
+    size_t o = 0;
+    L.tab = o; o = align16(o + (1 + n_formula) * 16);
+    L.G = o; o = align16(o + U * 16);
+    L.LS = o; o = align16(o + U * 16);
+    L.MU = o; o = align16(o + 6 * static_cast<size_t>(N) * 8);
+    L.YB = o; o = align16(o + static_cast<size_t>(N) * 8);
+    L.slots = o; o = align16(o + 6 * ns * 16);
+    L.dslots = o; o = align16(o + 6 * ns * kMaxGrad * 16);
+    L.sv = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 16);
+    L.sd = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * kMaxGrad * 16);
+    L.tp = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 4);
+    L.cstat = o; o = align16(o + nc * 16);
+    L.dcstat = o; o = align16(o + nc * kMaxGrad * 16);
+    L.cdyn = o; o = align16(o + 6 * nd * 16);
+    L.ddyn = o; o = align16(o + 6 * nd * kMaxGrad * 16);
+    L.dcls = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 16);
+    L.S = o; o = align16(o + 2 * nc * 32 * 16);
+    L.traj = o; o = align16(o + 16);
+    L.bytes = o;
+    return L;
+}
+
+__host__ __device__ inline size_t adj_plan_smem_bytes(const DevPlan& P) {
+    return align16(static_cast<size_t>(P.n_iter + P.n_out + P.n_titer + P.n_tin) * 32 * 4);
+}
+
+// ------------------------------------------------------------------------------------------
+// the reverse sweep
+
+template <int EPT>
+__global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const CallArgs A, const AdjArgs J, int gpb,
+                                                         size_t group_bytes, int M) {
+    constexpr int TPT = 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int g = static_cast<int>(threadIdx.x) / TPT;
+    const int lt = static_cast<int>(threadIdx.x) % TPT;
+    const int n = P.n, N = P.N, U = P.U;
+    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* s_out = s_rec + static_cast<size_t>(P.n_iter) * TPT;
+    uint32_t* s_trec = s_out + static_cast<size_t>(P.n_out) * TPT;
+    uint32_t* s_lin = s_trec + static_cast<size_t>(P.n_titer) * TPT;
+    for (int i = threadIdx.x; i < P.n_iter * TPT; i += blockDim.x) s_rec[i] = P.rec[i];
+    for (int i = threadIdx.x; i < P.n_out * TPT; i += blockDim.x) s_out[i] = P.lane_out[i];
+    for (int i = threadIdx.x; i < P.n_titer * TPT; i += blockDim.x) s_trec[i] = P.trec[i];
+    for (int i = threadIdx.x; i < P.n_tin * TPT; i += blockDim.x) s_lin[i] = P.lane_in[i];
+    __syncthreads();
+    if (g >= gpb) return;
+
+    const AdjLayout Lay = adj_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth);
+    unsigned char* gb = smem + adj_plan_smem_bytes(P) + static_cast<size_t>(g) * group_bytes;
+    double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
+    double2* s_G = reinterpret_cast<double2*>(gb + Lay.G);
+    double* s_G64 = reinterpret_cast<double*>(gb + Lay.G);
+    double2* s_LS = reinterpret_cast<double2*>(gb + Lay.LS);
+    double* s_LS64 = reinterpret_cast<double*>(gb + Lay.LS);
+    double* s_MU = reinterpret_cast<double*>(gb + Lay.MU);
+    double* s_YB = reinterpret_cast<double*>(gb + Lay.YB);
+    double2* s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
+    double2* s_dcstat = reinterpret_cast<double2*>(gb + Lay.dcstat);
+    double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
+    double2* s_ddyn = reinterpret_cast<double2*>(gb + Lay.ddyn);
+    double2* s_dcls = reinterpret_cast<double2*>(gb + Lay.dcls);
+    double2* s_S = reinterpret_cast<double2*>(gb + Lay.S);
+    long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
+    const int ns = P.n_slots > 0 ? P.n_slots : 1;
+    const int nd = P.n_dyn > 0 ? P.n_dyn : 1;
+    const int nc2 = 2 * P.n_coeff;
+    const int ng = J.n_grad;
+    const int S = P.n_static_formula, F = P.n_formula;
+    const int vl = lt < 6 ? lt : 0;
+    double2* slots = reinterpret_cast<double2*>(gb + Lay.slots) + vl * ns;
+    double2* dslots = reinterpret_cast<double2*>(gb + Lay.dslots) + static_cast<size_t>(vl) * ns * kMaxGrad;
+    double2* sv = reinterpret_cast<double2*>(gb + Lay.sv) + vl * A.vm_depth;
+    double2* sd = reinterpret_cast<double2*>(gb + Lay.sd) + static_cast<size_t>(vl) * A.vm_depth * kMaxGrad;
+    int32_t* tp = reinterpret_cast<int32_t*>(gb + Lay.tp) + vl * A.vm_depth;
+    const bool integral = A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL;
+    // solution weights b (row 5 of the stage table) and stage times c_s
+    double bw[6], cs[6];
+#pragma unroll
+    for (int s = 0; s < 6; ++s) bw[s] = kTab.a[M][5][s];
+    cs[0] = 0.0;
+#pragma unroll
+    for (int s = 1; s < 5; ++s) cs[s] = kTab.c[M][s - 1];
+    cs[5] = 1.0;
+
+    while (true) {
+        if (lt == 0) *s_traj = static_cast<long long>(atomicAdd(J.counter, 1ull));
+        __syncwarp();
+        const long long traj = *s_traj;
+        __syncwarp();
+        if (traj >= A.n_traj) break;
+        int bad = 0;
+        const obe_traj_stats fst = J.fwd_stats[traj];
+        const long long n_acc = fst.accepted_steps;
+        if (fst.status != 0 || n_acc > J.tape_cap) {
+            if (lt == 0) J.adj_status[traj] = ADJ_FORWARD_FAILED;
+            for (int q = lt; q < ng; q += TPT) J.param_grad[traj * ng + q] = CUDART_NAN;
+            __syncwarp();
+            continue;
+        }
+
+        // ---- parameters, derivative seeds, time-independent coefficients ----
+        if (lt < 6) {
+            init_slots(P, A, traj, slots);
+            for (int s = 0; s < P.n_slots; ++s)
+                for (int q = 0; q < ng; ++q)
+                    dslots[s * ng + q] = make_double2(s == J.grad_slot[q] ? 1.0 : 0.0, 0.0);
+            double2 dtmp[kMaxGrad];
+            for (int c = 0; c < P.n_comp; ++c) {
+                const DevExpr e = P.comp_expr[c];
+                const int slot = P.comp_slot[c];
+                slots[slot] = vm_eval_dual(P, e.start, e.len, slots, dslots, ng, A.t0, sv, sd, tp, dtmp, &bad);
+                for (int q = 0; q < ng; ++q) dslots[slot * ng + q] = dtmp[q];
+            }
+        }
+        if (lt == 0) {
+            double2 dtmp[kMaxGrad];
+            for (int k = 0; k < P.n_coeff; ++k) {
+                if (P.coeff_dynamic[k]) {
+                    s_cstat[k] = make_double2(0.0, 0.0);
+                    for (int q = 0; q < ng; ++q) s_dcstat[k * kMaxGrad + q] = make_double2(0.0, 0.0);
+                } else {
+                    const DevExpr e = P.coeff_expr[k];
+                    s_cstat[k] = vm_eval_dual(P, e.start, e.len, slots, dslots, ng, A.t0, sv, sd, tp, dtmp, &bad);
+                    for (int q = 0; q < ng; ++q) s_dcstat[k * kMaxGrad + q] = dtmp[q];
+                }
+            }
+            s_tab[0] = make_double2(0.0, 0.0);
+        }
+        for (int i = lt; i < U; i += TPT) {
+            s_G[i] = make_double2(0.0, 0.0);
+            s_LS[i] = make_double2(0.0, 0.0);
+        }
+        for (int i = lt; i < N; i += TPT) s_YB[i] = 0.0;
+        __syncwarp();
+        fill_formulas<TPT>(P, 1, 1 + S, s_cstat, s_cdyn, s_tab, lt);  // static entries: once
+
+        // ---- the loss gradient at the final state ----
+        const double* og = J.out_grad + traj * (integral ? 1 : n);
+        const double gbar = integral ? og[0] : 0.0;
+        if (!integral)
+            for (int i = lt; i < n; i += TPT) s_YB[i] = og[i];
+        double pbar[kMaxGrad];
+#pragma unroll
+        for (int q = 0; q < kMaxGrad; ++q) pbar[q] = 0.0;
+        __syncwarp();
+        // the trapezoid weight of a segment of length dt on one of its end states
+        auto add_quadrature = [&](double dt) {
+            if (lt == 0)
+                for (int k = 0; k < A.n_weights; ++k) s_YB[A.w_idx[k]] += gbar * A.w_val[k] * (0.5 * dt);
+            __syncwarp();
+        };
+
+        // ---- the reverse sweep over the accepted steps ----
+        for (long long st = n_acc - 1; st >= 0; --st) {
+            const double* rec = J.tape + (static_cast<size_t>(traj) * J.tape_cap + st) * J.tape_stride;
+            const double tn = rec[0], h = rec[1];
+            const double* yn_t = rec + 2;
+            const double* Kt = rec + 2 + N;
+            const double dt = (tn + h) - tn;
+            const bool segment = integral && (st > 0 || A.save_start);
+            if (segment) add_quadrature(dt);  // the end state y_{n+1}
+            // coefficient values and derivatives at the six stage times, one VM lane each
+            if (lt < 6) {
+                const double ts = tn + h * cs[lt];
+                double2 dtmp[kMaxGrad];
+                for (int c = 0; c < P.n_comp; ++c) {
+                    if (!P.comp_dynamic[c]) continue;
+                    const DevExpr e = P.comp_expr[c];
+                    const int slot = P.comp_slot[c];
+                    slots[slot] = vm_eval_dual(P, e.start, e.len, slots, dslots, ng, ts, sv, sd, tp, dtmp, &bad);
+                    for (int q = 0; q < ng; ++q) dslots[slot * ng + q] = dtmp[q];
+                }
+                for (int j = 0; j < P.n_dyn; ++j) {
+                    const DevExpr e = P.coeff_expr[P.dyn_ids[j]];
+                    s_cdyn[lt * nd + j] = vm_eval_dual(P, e.start, e.len, slots, dslots, ng, ts, sv, sd, tp, dtmp, &bad);
+                    for (int q = 0; q < ng; ++q) s_ddyn[(lt * nd + j) * kMaxGrad + q] = dtmp[q];
+                }
+            }
+            __syncwarp();
+            // per stage row and coefficient class: d(class value)/dp
+            for (int q = lt; q < 6 * nc2 * ng; q += TPT) {
+                const int row = q / (nc2 * ng), rem = q - row * nc2 * ng, cls = rem / ng, gi = rem - cls * ng;
+                const int k = cls >> 1;
+                const int pos = P.coeff_dyn_pos[k];
+                double2 d = pos >= 0 ? s_ddyn[(row * nd + pos) * kMaxGrad + gi] : s_dcstat[k * kMaxGrad + gi];
+                if (cls & 1) d.y = -d.y;
+                s_dcls[(row * nc2 + cls) * kMaxGrad + gi] = d;
+            }
+            __syncwarp();
+            for (int s = 5; s >= 0; --s) {
+                // lambda_s (adjoint of K_s) into the lambda slot buffer; Y_s into the input buffer
+                for (int i = lt; i < N; i += TPT) {
+                    double lam = h * bw[s] * s_YB[i];
+                    for (int m = s + 1; m < 6; ++m) lam += h * kTab.a[M][m - 1][s] * s_MU[static_cast<size_t>(m) * N + i];
+                    s_LS64[gslot64(i, n)] = lam;
+                    double acc = 0.0;
+                    for (int l = 0; l < s; ++l) acc += kTab.a[M][s - 1][l] * Kt[static_cast<size_t>(l) * N + i];
+                    s_G64[gslot64(i, n)] = s > 0 ? yn_t[i] + h * acc : yn_t[i];
+                }
+                __syncwarp();
+                if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + s * nd, s_tab, lt);
+                __syncwarp();
+                // mu_s = L(t_s)^T lambda_s on the input-major stream
+                {
+                    double br = 0.0, bi = 0.0;
+                    int o = 0;
+                    for (int it = 0; it < P.n_titer; ++it) {
+                        const uint32_t w = s_trec[it * TPT + lt];
+                        const double2 c = s_tab[w >> kRecCoefShift];
+                        const double2 u = s_LS[w & kRecIndexMask];
+                        const double tr = c.x * u.x + c.y * u.y;
+                        double ti = c.x * u.y - c.y * u.x;
+                        if (w & kRecConj) ti = -ti;
+                        br += tr;
+                        bi += ti;
+                        if (w & kRecFlush) {
+                            const uint32_t d = s_lin[o * TPT + lt];
+                            s_MU[static_cast<size_t>(s) * N + (d & 0xFFFFu)] = br;
+                            if ((d >> 16) != kNoImag) s_MU[static_cast<size_t>(s) * N + (d >> 16)] = bi;
+                            br = 0.0;
+                            bi = 0.0;
+                            ++o;
+                        }
+                    }
+                }
+                // lambda_s^T (dL/dp) Y_s: per-class sums of factor * Y_in' * conj(lambda_out)
+                for (int c = 0; c < nc2; ++c) s_S[c * TPT + lt] = make_double2(0.0, 0.0);
+                {
+                    int o = 0;
+                    for (int it = 0; it < P.n_iter; ++it) {
+                        const uint32_t w = s_rec[it * TPT + lt];
+                        const int f = static_cast<int>(w >> kRecCoefShift);
+                        if (f > 0) {
+                            double2 a = s_G[w & kRecIndexMask];
+                            if (w & kRecConj) a.y = -a.y;
+                            const uint32_t d = s_out[o * TPT + lt];
+                            const int re = static_cast<int>(d & 0xFFFFu);
+                            const int oslot = re < n ? re : n + (re - n) / 2;
+                            const double2 lam = s_LS[oslot];
+                            const double2 z = cmul(a, make_double2(lam.x, -lam.y));
+                            for (int p = P.formula_ptr[f - 1]; p < P.formula_ptr[f]; ++p) {
+                                const int cls = P.prod_class[p];
+                                if (cls < 0) continue;
+                                const double2 v = cmul(make_double2(P.prod_factor[2 * p], P.prod_factor[2 * p + 1]), z);
+                                double2& acc = s_S[cls * TPT + lt];
+                                acc.x += v.x;
+                                acc.y += v.y;
+                            }
+                        }
+                        if (w & kRecFlush) ++o;
+                    }
+                }
+                for (int c = 0; c < nc2; ++c) {
+                    const double2 Sv = s_S[c * TPT + lt];
+                    for (int q = 0; q < ng; ++q) {
+                        const double2 d = s_dcls[(s * nc2 + c) * kMaxGrad + q];
+                        pbar[q] += d.x * Sv.x - d.y * Sv.y;
+                    }
+                }
+                __syncwarp();
+            }
+            // ybar_n = ybar_{n+1} + sum_s mu_s
+            for (int i = lt; i < N; i += TPT) {
+                double acc = s_YB[i];
+                for (int s = 0; s < 6; ++s) acc += s_MU[static_cast<size_t>(s) * N + i];
+                s_YB[i] = acc;
+            }
+            __syncwarp();
+            if (segment) add_quadrature(dt);  // the start state y_n
+        }
+
+        // ---- outputs ----
+#pragma unroll
+        for (int q = 0; q < kMaxGrad; ++q) {
+            double v = pbar[q];
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lt == 0 && q < ng) J.param_grad[traj * ng + q] = v;
+        }
+        if (J.rho0_grad)
+            for (int i = lt; i < N; i += TPT) J.rho0_grad[traj * N + i] = s_YB[i];
+        bad = static_cast<int>(__reduce_or_sync(0xffffffffu, static_cast<unsigned>(bad)));
+        if (lt == 0) J.adj_status[traj] = bad ? ADJ_HELPER_DERIVATIVE : ADJ_OK;
+        __syncwarp();
+    }
+}
+
+template <int EPT>
+cudaError_t launch_adjoint_shape(const DevPlan& P, const CallArgs& A, const AdjArgs& J, int blocks, int gpb, size_t smem,
+                                 size_t group_bytes, int method, cudaStream_t stream) {
+    auto k = adjoint_kernel<EPT>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    k<<<blocks, gpb * 32, smem, stream>>>(P, A, J, gpb, group_bytes, method);
+    return cudaGetLastError();
+}
+
+#ifndef OBE_INSTANCE_TU
+extern template cudaError_t launch_adjoint_shape<8>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, size_t, size_t, int,
+                                                    cudaStream_t);
+extern template cudaError_t launch_adjoint_shape<16>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, size_t, size_t, int,
+                                                     cudaStream_t);
+#endif
+
+}  // namespace obe

@@ -101,6 +101,13 @@ struct DevPlan {
     // | kFStreamFlush (last product of the formula) | formula << kFStreamFormulaShift
     int32_t n_fiter;
     const uint32_t* fstream;     // [n_fiter * tpt * 4]
+    // the transposed gather stream (adjoint: v_bar = L^T u_bar), thread-interleaved: each record
+    // reads an OUTPUT slot (the index field) and the formula of the forward record; each thread
+    // accumulates the adjoint of its own INPUT slots, written to lane_in (re | im << 16)
+    int32_t n_titer;
+    const uint32_t* trec;        // [n_titer * tpt]
+    int32_t n_tin;
+    const uint32_t* lane_in;     // [n_tin * tpt]
 };
 
 // Host-side result of packing (owned by obe_plan).
@@ -124,6 +131,8 @@ struct HostPacked {
     std::vector<float> prod_factor32;
     std::vector<uint32_t> rec, lane_out;
     std::vector<uint32_t> fstream;  // 4 words per entry
+    std::vector<uint32_t> trec, lane_in;
+    int32_t n_titer = 0, n_tin = 0;
     int32_t n_iter = 0, n_out = 0, tpt = 32, n_fiter = 0;
     int32_t n_formula = 0, n_static_formula = 0;
     int32_t max_stack = 0;

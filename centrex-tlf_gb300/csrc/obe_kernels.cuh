@@ -112,7 +112,8 @@ enum TrajCode : int32_t {
     ST_POINTS = 7,
     ST_BAD_MAXITERS = 8,
     ST_BACKWARD = 9,
-    ST_FIXED_DT = 10
+    ST_FIXED_DT = 10,
+    ST_TAPE = 11
 };
 
 struct TrajErr {
@@ -161,6 +162,10 @@ struct CallArgs {
     int k1_refresh;  // mixed form: recompute k_1 in double every this many accepted steps
     unsigned char* gscratch;  // large systems: per-group global slices of the stage buffers
     size_t gstride;           // bytes per slice
+    // gradient tape (double-precision adaptive solves): per trajectory up to tape_cap accepted
+    // steps of [t_n, h_n, y_n (N), K_1..K_6 (6 N)], tape_stride doubles apart; null when off
+    double* tape;
+    long long tape_cap, tape_stride;
     int vm_depth;    // VM stack depth of the plan's and the event's programs
     int fixed;       // 0: adaptive; else the fixed-step obe_solver value (double-precision form only)
 };
@@ -1352,6 +1357,18 @@ __global__ void __launch_bounds__(MIXED && TPT < 256 ? kThreadsMixed : kThreadsF
                 }
                 // accept: y <- yn; K_1 <- K_7
                 if constexpr (!MIXED) {
+                    if (A.tape) {
+                        // the step for the adjoint: start time, size, start state and stages 1-6
+                        if (accepted > A.tape_cap) { status = ST_TAPE; err_a = A.tape_cap; break; }
+                        double* rec = A.tape + (static_cast<size_t>(traj) * A.tape_cap + (accepted - 1)) * A.tape_stride;
+                        if (lt == 0) { rec[0] = xo; rec[1] = h; }
+#pragma unroll
+                        for (int e = 0; e < EPT; ++e) {
+                            int i = lt + e * TPT;
+                            if (i < N) rec[2 + i] = y[e];
+                        }
+                        for (int i = lt; i < 6 * N; i += TPT) rec[2 + N + i] = s_K[i];
+                    }
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;

@@ -628,6 +628,64 @@ obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
                 }
             }
         }
+        // ---- the transposed stream (adjoint): records regrouped by input slot -----------------
+        {
+            struct TRec { uint32_t out_slot, fid; bool conj; };
+            std::vector<std::vector<TRec>> in_recs(U);  // by input slot
+            std::vector<uint32_t> slot_re(U), slot_im(U);
+            for (int64_t u = 0; u < U; ++u) {
+                const uint32_t uslot = u_im[u] < 0 ? static_cast<uint32_t>(u_re[u]) : static_cast<uint32_t>(n + (u_re[u] - n) / 2);
+                slot_re[uslot] = static_cast<uint32_t>(u_re[u]);
+                slot_im[uslot] = u_im[u] < 0 ? kNoImag : static_cast<uint32_t>(u_im[u]);
+                for (const Rec& rc : out_recs[u]) {
+                    uint32_t fid = rc.dynamic ? static_cast<uint32_t>(1 + S + dyn_ids[rc.f]) : static_cast<uint32_t>(1 + static_ids[rc.f]);
+                    uint32_t slot = rc.cplx ? static_cast<uint32_t>(n + (rc.in_re - n) / 2) : static_cast<uint32_t>(rc.in_re);
+                    in_recs[slot].push_back(TRec{uslot, fid, rc.conj});
+                }
+            }
+            std::vector<int64_t> iorder(U);
+            std::iota(iorder.begin(), iorder.end(), 0);
+            auto icost = [&](int64_t v) { return std::max<int64_t>(1, static_cast<int64_t>(in_recs[v].size())); };
+            std::stable_sort(iorder.begin(), iorder.end(), [&](int64_t a, int64_t b) { return icost(a) > icost(b); });
+            std::vector<int64_t> iload(tpt, 0);
+            std::vector<std::vector<int64_t>> lane_inputs(tpt);
+            for (int64_t v : iorder) {
+                int lane = static_cast<int>(std::min_element(iload.begin(), iload.end()) - iload.begin());
+                lane_inputs[lane].push_back(v);
+                iload[lane] += icost(v);
+            }
+            const int64_t n_titer = *std::max_element(iload.begin(), iload.end());
+            size_t n_tin = 0;
+            for (auto& v : lane_inputs) {
+                std::sort(v.begin(), v.end());
+                n_tin = std::max(n_tin, v.size());
+            }
+            hp.n_titer = static_cast<int32_t>(n_titer);
+            hp.n_tin = static_cast<int32_t>(n_tin);
+            hp.trec.assign(static_cast<size_t>(n_titer) * tpt, 0u);  // padding: slot 0, formula 0 (zero)
+            hp.lane_in.assign(n_tin * tpt, 0u);
+            for (int lane = 0; lane < tpt; ++lane) {
+                int64_t it = 0;
+                for (size_t o = 0; o < lane_inputs[lane].size(); ++o) {
+                    const int64_t v = lane_inputs[lane][o];
+                    hp.lane_in[o * tpt + lane] = slot_re[v] | (slot_im[v] << 16);
+                    const auto& recs = in_recs[v];
+                    if (recs.empty()) {
+                        hp.trec[it * tpt + lane] = kRecFlush;
+                        ++it;
+                        continue;
+                    }
+                    for (size_t r = 0; r < recs.size(); ++r) {
+                        uint32_t w = recs[r].out_slot | (recs[r].fid << kRecCoefShift);
+                        if (recs[r].conj) w |= kRecConj;
+                        if (r + 1 == recs.size()) w |= kRecFlush;
+                        hp.trec[it * tpt + lane] = w;
+                        ++it;
+                    }
+                }
+            }
+        }
+
         // ---- time-dependent formulas as a thread-interleaved product stream -------------------
         // (mixed form: each thread sums its formulas' products and stores the finished entries;
         // formulas are dealt out longest first onto the least-loaded thread)

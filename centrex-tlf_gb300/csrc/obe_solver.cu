@@ -15,6 +15,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "obe_adjoint.cuh"
 #include "obe_kernels.cuh"
 
 namespace obe {
@@ -60,6 +61,7 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
     size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
     size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out), o_fs = put(blob, h.fstream);
+    size_t o_tr = put(blob, h.trec), o_li = put(blob, h.lane_in);
     P = DevPlan{};
     P.n = p->n;
     P.N = static_cast<int32_t>(p->N);
@@ -107,6 +109,10 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     P.lane_out = reinterpret_cast<const uint32_t*>(base + o_lo);
     P.n_fiter = h.n_fiter;
     P.fstream = reinterpret_cast<const uint32_t*>(base + o_fs);
+    P.n_titer = h.n_titer;
+    P.trec = reinterpret_cast<const uint32_t*>(base + o_tr);
+    P.n_tin = h.n_tin;
+    P.lane_in = reinterpret_cast<const uint32_t*>(base + o_li);
 }
 
 obe_status upload_plan(obe_plan* p) {
@@ -265,6 +271,7 @@ std::string traj_message(int code, const TrajErr& e) {
     case ST_BAD_MAXITERS: return "maxiters must be positive";
     case ST_BACKWARD: return "only forward integration";
     case ST_FIXED_DT: return "fixed-step solvers require positive finite dt";
+    case ST_TAPE: return "the gradient tape holds " + std::to_string(e.a) + " accepted steps per trajectory; pass a larger max_steps";
     default: return "trajectory failed with status " + std::to_string(code);
     }
 }
@@ -431,7 +438,7 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
                         const int64_t* axis_len, const double* d_axes, long long cap, long long out_stride, double* d_values,
                         double* d_times, obe_traj_stats* d_stats, TrajErr* d_errs, unsigned char* d_blob_area,
                         const CallBlob& cb, const std::vector<double>& save_times, unsigned long long* d_counter,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, double* d_tape = nullptr, long long tape_cap = 0, long long tape_stride = 0) {
     CallArgs A;
     fill_call_args(A, o, save_times, cb, d_blob_area);
     A.n_traj = n_traj;
@@ -456,6 +463,9 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
     A.counter = d_counter;
     A.k1_refresh = k1_refresh_interval();
     A.vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
+    A.tape = d_tape;
+    A.tape_cap = tape_cap;
+    A.tape_stride = tape_stride;
     LaunchShape s;
     obe_status st = plan_launch(p->dev, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s);
     if (st != OBE_OK) return st;
@@ -708,6 +718,156 @@ void obe_result_copy(const obe_result* res, double* times, double* values) {
 }
 
 void obe_result_destroy(obe_result* res) { delete res; }
+
+// ---- gradients: the forward solve with a tape, and the reverse sweep ----------------------
+
+// the outputs and options a gradient supports; *width_out: 1 (weighted integral) or n
+static obe_status grad_check(const obe_plan* p, const obe_solve_options* o, int64_t* width_out) {
+    if (!p->has_expanded) {
+        set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan");
+        return OBE_ERR_INVALID;
+    }
+    if (o->precision != OBE_PRECISION_FP64) {
+        set_error("gradients are implemented for the double-precision form (precision='fp64')");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    if (o->solver != OBE_SOLVER_DOPRI5 && o->solver != OBE_SOLVER_TSIT5) {
+        set_error("gradients are implemented for the adaptive solvers 'dopri5' and 'tsit5'");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    if (o->event_kind != OBE_EVENT_NONE) {
+        set_error("gradients through a stop_event are not supported");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    if (p->packed.tpt != 32) {
+        set_error("gradients are implemented for systems of up to 22 states");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    if (o->output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !o->store_trace && !o->has_saveat) {
+        *width_out = 1;
+        return OBE_OK;
+    }
+    if (o->output == OBE_OUTPUT_POPULATIONS && o->has_saveat && o->n_saveat == 1 && o->saveat[0] == o->t1 && !o->save_start) {
+        *width_out = p->n;
+        return OBE_OK;
+    }
+    set_error("gradients are implemented for final weighted integrals (output_when='final', saveat=None) and final "
+              "populations");
+    return OBE_ERR_UNSUPPORTED;
+}
+
+int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan) {
+    if (!plan) return 0;
+    return static_cast<int64_t>(align16((2 + 7 * static_cast<size_t>(plan->N)) * 8) / 8);
+}
+
+obe_status obe_grad_forward(const obe_plan* plan_c, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
+                            int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values, int64_t max_steps,
+                            double* d_tape, int64_t width, double* d_values, obe_traj_stats* d_stats, void* stream) {
+    g_launches = 0;
+    obe_plan* p = const_cast<obe_plan*>(plan_c);
+    if (!p || !opt || !d_tape || max_steps <= 0) { set_error("null argument or non-positive max_steps"); return OBE_ERR_INVALID; }
+    int64_t gw = 0;
+    obe_status st = grad_check(p, opt, &gw);
+    if (st != OBE_OK) return st;
+    if (gw != width) { set_error("output width mismatch"); return OBE_ERR_INVALID; }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    if ((st = ensure_ready(p)) != OBE_OK) return st;
+    if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
+    std::vector<double> save_times;
+    CallBlob cb;
+    int64_t w = 0;
+    int cplx = 0;
+    if ((st = validate_options(p, opt, save_times, cb, &w, &cplx)) != OBE_OK) return st;
+    size_t errs_off = align16(cb.bytes.size());
+    size_t need = errs_off + sizeof(TrajErr) * static_cast<size_t>(std::max<int64_t>(n_traj, 1));
+    unsigned char* d = nullptr;
+    if ((st = scratch(p, need, &d)) != OBE_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!cuda_ok(cudaMemcpyAsync(d, cb.bytes.data(), cb.bytes.size(), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(args)")) return OBE_ERR_CUDA;
+    return solve_device(p, opt, n_traj, d_rho0, p->N, n_param_slots, param_slots, d_param_values, 0, nullptr, nullptr, 1, width,
+                        d_values, nullptr, d_stats, reinterpret_cast<TrajErr*>(d + errs_off), d, cb, save_times,
+                        static_cast<unsigned long long*>(p->d_counter), s, d_tape, max_steps, obe_grad_tape_doubles_per_step(p));
+}
+
+obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
+                             int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values, int32_t n_grad,
+                             const int64_t* grad_slots, int64_t max_steps, const double* d_tape, const obe_traj_stats* d_stats,
+                             const double* d_out_grad, double* d_param_grad, double* d_rho0_grad, int32_t* d_adj_status,
+                             void* stream) {
+    g_launches = 0;
+    obe_plan* p = const_cast<obe_plan*>(plan_c);
+    if (!p || !opt || !d_tape || !d_stats || !d_out_grad || !d_adj_status || max_steps <= 0) {
+        set_error("null argument or non-positive max_steps");
+        return OBE_ERR_INVALID;
+    }
+    if (n_grad < 0 || n_grad > kMaxGrad || (n_grad > 0 && (!grad_slots || !d_param_grad))) {
+        set_error("gradients are taken with respect to at most " + std::to_string(kMaxGrad) + " parameter slots");
+        return OBE_ERR_INVALID;
+    }
+    int64_t gw = 0;
+    obe_status st = grad_check(p, opt, &gw);
+    if (st != OBE_OK) return st;
+    for (int q = 0; q < n_grad; ++q) {
+        if (grad_slots[q] < 0 || grad_slots[q] >= p->n_base || p->base_is_tuple[grad_slots[q]]) {
+            set_error("gradient slot " + std::to_string(grad_slots[q]) + " is not a scalar base parameter slot");
+            return OBE_ERR_INVALID;
+        }
+    }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    if ((st = ensure_ready(p)) != OBE_OK) return st;
+    if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
+    std::vector<double> save_times;
+    CallBlob cb;
+    int64_t w = 0;
+    int cplx = 0;
+    if ((st = validate_options(p, opt, save_times, cb, &w, &cplx)) != OBE_OK) return st;
+    unsigned char* d = nullptr;
+    if ((st = scratch(p, align16(cb.bytes.size()), &d)) != OBE_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!cuda_ok(cudaMemcpyAsync(d, cb.bytes.data(), cb.bytes.size(), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(args)")) return OBE_ERR_CUDA;
+    CallArgs A;
+    fill_call_args(A, opt, save_times, cb, d);
+    A.n_traj = n_traj;
+    A.rho0 = d_rho0;
+    A.rho0_stride = p->N;
+    A.n_param = d_param_values ? n_param_slots : 0;
+    for (int k = 0; k < A.n_param; ++k) A.param_slot[k] = static_cast<int>(param_slots[k]);
+    A.param_values = d_param_values;
+    A.vm_depth = std::max(p->dev.max_stack, 1);
+    AdjArgs J{};
+    J.n_grad = n_grad;
+    for (int q = 0; q < n_grad; ++q) J.grad_slot[q] = static_cast<int>(grad_slots[q]);
+    J.tape = d_tape;
+    J.tape_cap = max_steps;
+    J.tape_stride = obe_grad_tape_doubles_per_step(p);
+    J.fwd_stats = d_stats;
+    J.out_grad = d_out_grad;
+    J.param_grad = d_param_grad;
+    J.rho0_grad = d_rho0_grad;
+    J.adj_status = d_adj_status;
+    J.counter = static_cast<unsigned long long*>(p->d_counter);
+    const DevPlan& P = p->dev;
+    const size_t plan_bytes = adj_plan_smem_bytes(P);
+    const size_t group = adj_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth).bytes;
+    const size_t limit = 227 * 1024;
+    int gpb = 8;
+    while (gpb > 1 && plan_bytes + gpb * group > limit) --gpb;
+    if (plan_bytes + gpb * group > limit) { set_error("system too large for the adjoint's shared-memory layout"); return OBE_ERR_UNSUPPORTED; }
+    const long long per_sm = (n_traj + sm_count() - 1) / sm_count();
+    while (gpb > 1 && gpb > per_sm) --gpb;
+    const size_t smem = plan_bytes + gpb * group;
+    const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n_traj + gpb - 1) / gpb, sm_count())));
+    if (!cuda_ok(cudaMemsetAsync(J.counter, 0, sizeof(unsigned long long), s), "cudaMemsetAsync")) return OBE_ERR_CUDA;
+    const int method = opt->solver == OBE_SOLVER_TSIT5 ? 1 : 0;
+    const int ept = ept_for(P.N, 32);
+    cudaError_t e = ept == 8 ? launch_adjoint_shape<8>(P, A, J, blocks, gpb, smem, group, method, s)
+                             : launch_adjoint_shape<16>(P, A, J, blocks, gpb, smem, group, method, s);
+    if (!cuda_ok(e, "adjoint kernel launch")) return OBE_ERR_CUDA;
+    g_launches += 1;
+    set_error("");
+    return OBE_OK;
+}
 
 obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, const double* y, int32_t n_override_slots,
                         const int64_t* override_slots, const double* override_values, int32_t precision, double* dy) {

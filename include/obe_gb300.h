@@ -238,6 +238,38 @@ obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options*
                                   obe_traj_stats* d_stats, void* stream);
 
 /*
+ * Gradients (no counterpart in the reference, whose Rust crate has no gradient path): the
+ * discrete adjoint of the double-precision adaptive solve with its step sequence frozen, for
+ * final weighted integrals (output_when="final", saveat None) and final populations, with
+ * respect to base parameter slots and the initial state.  Device pointers, asynchronous on
+ * `stream`; systems of up to 22 states, dopri5/tsit5, no stop event.
+ *
+ * obe_grad_forward is obe_solve_batch_device that also records, per trajectory, every accepted
+ * step (start time, size, start state, stage derivatives 1-6) into d_tape:
+ * n_traj * max_steps * obe_grad_tape_doubles_per_step(plan) doubles, caller-owned.  A trajectory
+ * with more than max_steps accepted steps ends with a status whose message asks for a larger
+ * max_steps.
+ * obe_grad_backward runs the reverse sweep on that tape: given d(loss)/d(outputs) in d_out_grad
+ * ([n_traj][width]), it writes d(loss)/d(parameter) to d_param_grad ([n_traj][n_grad], for the
+ * base slots grad_slots, at most 8) and, if d_rho0_grad is not NULL, d(loss)/d(packed rho0) to
+ * d_rho0_grad ([n_traj][N]).  d_adj_status ([n_traj]): 0 = ok, 1 = a helper function or table
+ * received an argument that depends on a differentiated parameter (not differentiable here),
+ * 2 = the forward trajectory failed or overflowed the tape.  The parameter arguments must be
+ * those of the forward call.
+ */
+int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan);
+obe_status obe_grad_forward(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
+                            const double* d_rho0, int32_t n_param_slots, const int64_t* param_slots,
+                            const double* d_param_values, int64_t max_steps, double* d_tape,
+                            int64_t width, double* d_values, obe_traj_stats* d_stats, void* stream);
+obe_status obe_grad_backward(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
+                             const double* d_rho0, int32_t n_param_slots, const int64_t* param_slots,
+                             const double* d_param_values, int32_t n_grad, const int64_t* grad_slots,
+                             int64_t max_steps, const double* d_tape, const obe_traj_stats* d_stats,
+                             const double* d_out_grad, double* d_param_grad, double* d_rho0_grad,
+                             int32_t* d_adj_status, void* stream);
+
+/*
  * Allocation-free form of obe_solve_batch_device (no counterpart in the reference).  Some
  * callers cannot let a library allocate device memory while they solve: a caller that owns all
  * device memory up front through its own arena or a fixed memory budget, or one that records

@@ -2119,3 +2119,85 @@ int32_t orc_max_threads(void) {
     return 1;
 #endif
 }
+
+/* Replay of a frozen step sequence (test support for the GPU adjoint): for each trajectory, the
+ * given accepted steps (t_n, h_n) of Dopri5 (dopri5.rs:60-86) or Tsit5 (tsit5.rs:70-103), no step
+ * control, no error estimate; outputs the weighted trapezoid integral of the pushed points
+ * (output.rs:314-330; t0 pushed when save_start) or the final populations.  Central finite
+ * differences of this map check the adjoint of the same frozen sequence. */
+int orc_solve_replay(const orc_plan* plan, const obe_solve_options* opt, int64_t n_traj, const double* rho0, int64_t rho0_stride,
+                     int32_t n_param_slots, const int64_t* param_slots, const double* param_values, const int64_t* n_steps,
+                     const double* steps, int64_t max_steps, int64_t width, double* values, char* err, size_t err_len) {
+    errbuf e = {{0}, 0};
+    const int tsit = opt->solver == OBE_SOLVER_TSIT5;
+    if (opt->solver != OBE_SOLVER_DOPRI5 && !tsit) { fail(&e, "replay supports dopri5 and tsit5"); copy_err(&e, err, err_len); return 1; }
+    const int integral = opt->output == OBE_OUTPUT_WEIGHTED_INTEGRAL;
+    const int64_t n = plan->n, N = plan->N;
+    if (width != (integral ? 1 : n)) { fail(&e, "replay output width mismatch"); copy_err(&e, err, err_len); return 1; }
+    workspace w;
+    ws_init(&w, plan, 1);
+    rk_buf b;
+    rkb_init(&b, N);
+    int rc = 0;
+    for (int64_t t = 0; t < n_traj && !rc; ++t) {
+        if (n_param_slots > 0) ws_set_overrides(&w, n_param_slots, param_slots, param_values + 2 * t * n_param_slots);
+        else w.valid = 0;
+        double* y = b.y, *yt = b.yt, *yn = b.yn, *k = b.k;
+        memcpy(y, rho0 + t * rho0_stride, sizeof(double) * (size_t)N);
+        double integ = 0.0, last_t = 0.0, last_v = 0.0;
+        int have_last = 0;
+        if (integral && opt->save_start) {
+            last_t = opt->t0;
+            last_v = 0.0;
+            for (int32_t q = 0; q < opt->n_weights; ++q) last_v += opt->weight_value[q] * y[opt->weight_index[q]];
+            have_last = 1;
+        }
+        for (int64_t s = 0; s < n_steps[t] && !rc; ++s) {
+            const double x = steps[2 * (t * max_steps + s)], h = steps[2 * (t * max_steps + s) + 1];
+            if ((rc = ws_rhs(&w, x, y, k, &e))) break;
+            if (!tsit) {
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * D_A21 * k[i];
+                if ((rc = ws_rhs(&w, x + h * D_C2, yt, k + N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (D_A31 * k[i] + D_A32 * k[N + i]);
+                if ((rc = ws_rhs(&w, x + h * D_C3, yt, k + 2 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (D_A41 * k[i] + D_A42 * k[N + i] + D_A43 * k[2 * N + i]);
+                if ((rc = ws_rhs(&w, x + h * D_C4, yt, k + 3 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (D_A51 * k[i] + D_A52 * k[N + i] + D_A53 * k[2 * N + i] + D_A54 * k[3 * N + i]);
+                if ((rc = ws_rhs(&w, x + h * D_C5, yt, k + 4 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (D_A61 * k[i] + D_A62 * k[N + i] + D_A63 * k[2 * N + i] + D_A64 * k[3 * N + i] + D_A65 * k[4 * N + i]);
+                if ((rc = ws_rhs(&w, x + h, yt, k + 5 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yn[i] = y[i] + h * (D_A71 * k[i] + D_A72 * k[N + i] + D_A73 * k[2 * N + i] + D_A74 * k[3 * N + i] + D_A75 * k[4 * N + i] + D_A76 * k[5 * N + i]);
+            } else {
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * T_A21 * k[i];
+                if ((rc = ws_rhs(&w, x + h * T_C2, yt, k + N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (T_A31 * k[i] + T_A32 * k[N + i]);
+                if ((rc = ws_rhs(&w, x + h * T_C3, yt, k + 2 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (T_A41 * k[i] + T_A42 * k[N + i] + T_A43 * k[2 * N + i]);
+                if ((rc = ws_rhs(&w, x + h * T_C4, yt, k + 3 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (T_A51 * k[i] + T_A52 * k[N + i] + T_A53 * k[2 * N + i] + T_A54 * k[3 * N + i]);
+                if ((rc = ws_rhs(&w, x + h * T_C5, yt, k + 4 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yt[i] = y[i] + h * (T_A61 * k[i] + T_A62 * k[N + i] + T_A63 * k[2 * N + i] + T_A64 * k[3 * N + i] + T_A65 * k[4 * N + i]);
+                if ((rc = ws_rhs(&w, x + h, yt, k + 5 * N, &e))) break;
+                for (int64_t i = 0; i < N; ++i) yn[i] = y[i] + h * (T_A71 * k[i] + T_A72 * k[N + i] + T_A73 * k[2 * N + i] + T_A74 * k[3 * N + i] + T_A75 * k[4 * N + i] + T_A76 * k[5 * N + i]);
+            }
+            const double xn = x + h;
+            if (integral) {
+                double v = 0.0;
+                for (int32_t q = 0; q < opt->n_weights; ++q) v += opt->weight_value[q] * yn[opt->weight_index[q]];
+                if (have_last) integ += 0.5 * (last_v + v) * (xn - last_t);
+                last_t = xn;
+                last_v = v;
+                have_last = 1;
+            }
+            double* tmp = y; y = yn; yn = tmp;
+            b.y = y; b.yn = yn;
+        }
+        if (rc) break;
+        if (integral) values[t] = integ;
+        else memcpy(values + t * n, y, sizeof(double) * (size_t)n);
+    }
+    if (rc) copy_err(&e, err, err_len);
+    rkb_free(&b);
+    ws_free(&w);
+    return rc;
+}

@@ -70,6 +70,12 @@ int64_t orc_output_width(const orc_plan* plan, const obe_solve_options* opt, int
 /* Threads OpenMP will use for a batch with threads <= 0. */
 int32_t orc_max_threads(void);
 
+/* Frozen-step replay (test support for gradients): steps[traj][max_steps][2] = (t_n, h_n),
+ * n_steps[traj] of them; width 1 (weighted integral) or n (final populations). */
+int orc_solve_replay(const orc_plan* plan, const obe_solve_options* opt, int64_t n_traj, const double* rho0, int64_t rho0_stride,
+                     int32_t n_param_slots, const int64_t* param_slots, const double* param_values, const int64_t* n_steps,
+                     const double* steps, int64_t max_steps, int64_t width, double* values, char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

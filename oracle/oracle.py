@@ -63,6 +63,11 @@ def _lib():
     ]
     lib.orc_solve_single.restype = ctypes.c_int
     lib.orc_max_threads.restype = ctypes.c_int32
+    lib.orc_solve_replay.argtypes = [
+        vp, ctypes.POINTER(ObeSolveOptions), ctypes.c_int64, f64p, ctypes.c_int64, ctypes.c_int32, i64p, f64p, i64p, f64p,
+        ctypes.c_int64, ctypes.c_int64, f64p, ctypes.c_char_p, ctypes.c_size_t,
+    ]
+    lib.orc_solve_replay.restype = ctypes.c_int
     _LIB = lib
     return lib
 
@@ -158,6 +163,35 @@ class OraclePlan:
         if opts.is_complex:
             values = values.view(np.complex128)
         return values.reshape(b, time_count, width), times[:time_count], stats
+
+    def solve_replay(self, opts: SolveOptions, rho0, param_slots, param_values, steps):
+        """Replay frozen step sequences: steps[b] is an (n_b, 2) array of (t_n, h_n).  Returns the
+        weighted integral (B,) or the final populations (B, n) of opts' output."""
+        rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
+        pv = np.asarray(param_values, dtype=np.complex128)
+        b = pv.shape[0]
+        stride = self.N if rho0.ndim == 2 else 0
+        slots = np.ascontiguousarray(np.asarray(param_slots, dtype=np.int64))
+        pvals = np.ascontiguousarray(np.stack([pv.real, pv.imag], axis=-1).reshape(-1))
+        max_steps = max(1, max(len(s_) for s_ in steps))
+        flat = np.zeros((b, max_steps, 2))
+        counts = np.zeros(b, dtype=np.int64)
+        for i, s_ in enumerate(steps):
+            s_ = np.asarray(s_, dtype=np.float64).reshape(-1, 2)
+            flat[i, : len(s_)] = s_
+            counts[i] = len(s_)
+        width = opts.width
+        values = np.zeros(b * width)
+        err = ctypes.create_string_buffer(1024)
+        rc = _lib().orc_solve_replay(
+            self.handle, ctypes.byref(opts.opts), b, _abi.ptr(rho0, ctypes.c_double), stride, int(slots.size),
+            _abi.ptr(slots, ctypes.c_int64), _abi.ptr(pvals, ctypes.c_double), _abi.ptr(counts, ctypes.c_int64),
+            _abi.ptr(np.ascontiguousarray(flat.reshape(-1)), ctypes.c_double), max_steps, width,
+            _abi.ptr(values, ctypes.c_double), err, 1024,
+        )
+        if rc:
+            raise OracleError(err.value.decode())
+        return values.reshape(b, width) if width > 1 else values
 
     def solve_single(self, opts: SolveOptions, rho0, param_slots=None, param_values=None, capacity=1024,
                      use_split_input_rhs=True):
