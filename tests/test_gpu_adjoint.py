@@ -3,8 +3,12 @@ central finite differences of the CPU oracle replaying the same frozen step sequ
 
 The adjoint differentiates the discrete solve with its accepted steps frozen, so the check is
 the oracle's replay of exactly those steps at p +- eps (eps = 1e-6 |p|): agreement to 1e-5
-relative (the finite-difference truncation is ~1e-12, its rounding ~1e-10).  The forward values
-equal the plain FP64 solve's; the oracle's replay at p reproduces them to 1e-10.
+relative, plus a floor for the differences' rounding -- the loss carries ~1e-14 relative rounding
+from some thousand steps, i.e. ~1e-8 of its natural scale |J| / |p| once divided by eps (this
+matters for derivatives that are nearly zero, such as the final populations' dependence on the
+pulse centre when the pulse ends long before t1).  The loss is linear in the initial state, so
+its differences there use a unit step and are exact up to rounding.  The forward values equal
+the plain FP64 solve's; the oracle's replay at p reproduces them to 1e-10.
 """
 
 from __future__ import annotations
@@ -94,8 +98,9 @@ def test_parameter_gradients_match_frozen_step_finite_differences(q1, solver, ou
         pp[:, k] += eps
         pm[:, k] -= eps
         fd = (replay(pp) - replay(pm)) / (2 * eps)
-        scale = np.maximum(np.abs(fd), 1e-3 * np.max(np.abs(fd)) + 1e-300)
-        np.testing.assert_array_less(np.abs(grad[:, k] - fd) / scale, 1e-5, err_msg=f"parameter {k}")
+        natural = np.abs(base) / np.maximum(np.abs(p0[:, k]), 1e-300)
+        tol = 1e-5 * np.abs(fd) + 1e-8 * natural
+        assert np.all(np.abs(grad[:, k] - fd) <= tol), (k, grad[:, k], fd, tol)
 
 
 def test_initial_state_gradient_matches_finite_differences(q1):
@@ -113,13 +118,14 @@ def test_initial_state_gradient_matches_finite_differences(q1):
     steps = tape.steps()
     o = _oracle_opts(op, d, "tsit5", "excited_population")
     base = np.repeat(d["rho0_packed"].reshape(1, -1), 2, axis=0)
+    j0 = op.solve_replay(o, base, slots, p0.astype(complex), steps)
     for idx in (0, 5, 13, 40):  # populations and a coherence component
         ep, em = base.copy(), base.copy()
-        ep[:, idx] += 1e-6
-        em[:, idx] -= 1e-6
+        ep[:, idx] += 1.0
+        em[:, idx] -= 1.0
         fd = (op.solve_replay(o, ep, slots, p0.astype(complex), steps)
-              - op.solve_replay(o, em, slots, p0.astype(complex), steps)) / 2e-6
-        np.testing.assert_allclose(gr[:, idx], fd, rtol=1e-5, atol=1e-9 * np.max(np.abs(fd)) + 1e-18)
+              - op.solve_replay(o, em, slots, p0.astype(complex), steps)) / 2.0
+        np.testing.assert_allclose(gr[:, idx], fd, rtol=1e-6, atol=1e-12 * np.max(np.abs(j0)))
 
 
 def test_gradient_errors(golden, q1):
