@@ -185,6 +185,56 @@ def measure_gemm_peak(torch, dev, dtype) -> float:
     return best
 
 
+def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3) -> dict:
+    """The adjoint workload: n_traj points of the scan, d(excited-population integral)/d(rabi,
+    detuning, theta, t_center) through the discrete adjoint (FP64, Tsit5); the forward-with-tape
+    plus reverse-sweep time against the plain FP64 forward solve of the same points."""
+    from centrex_tlf_gb300.autograd import solve_batch_with_grad
+    from centrex_tlf_gb300.native import NativePlan
+
+    gamma, (t0, t1) = d["gamma"], d["t_span"]
+    names = d["payload"]["parameter_graph"]["slot_names"]
+    slots = [names.index(s) for s in ("rabi", "detuning", "theta", "t_center")]
+    p = np.concatenate([params_all[:n_traj].real, np.full((n_traj, 1), 100.0 / gamma)], axis=1)
+    plan = NativePlan(d["payload"])
+    opts = plan.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=None, save_start=True,
+                        maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
+                        output_when="final", integral_weights=W_EXCITED, stop_event=None)
+    d_rho = torch.from_numpy(np.repeat(d["rho0_packed"].reshape(1, -1), n_traj, axis=0)).to(dev)
+    d_par = torch.from_numpy(np.ascontiguousarray(p.astype(np.complex128)).view(np.float64).reshape(-1)).to(dev)
+    d_val = torch.zeros(n_traj, dtype=torch.float64, device=dev)
+    d_st = torch.zeros(n_traj * 6, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def fwd():
+        plan.solve_batch_device(opts, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, d_val.data_ptr(),
+                                d_st.data_ptr(), stream.cuda_stream)
+
+    def grad():
+        pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
+        j = solve_batch_with_grad(plan, d["rho0_packed"], (t0, t1), pt, slots, dt=1e-3 / gamma, integral_weights=W_EXCITED,
+                                  max_steps=2048)
+        j.sum().backward()
+        return pt.grad
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            start = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - start)
+        return best
+
+    t_fwd = timed(fwd)
+    t_grad = timed(grad)
+    return {"workload": f"{n_traj} scan points, d(excited-population integral)/d(rabi, detuning, theta, t_center), "
+                        "FP64 Tsit5 discrete adjoint", "fwd_ms": 1e3 * t_fwd, "fwd_plus_grad_ms": 1e3 * t_grad,
+            "grad_over_fwd": t_grad / t_fwd}
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -300,6 +350,7 @@ def run_gpu(args) -> None:
     max_pop_err = float(np.max(np.abs(pm - p64)))
     # and the observable against the CPU oracle on a sample (also the CPU baseline)
     cpu = cpu_oracle_rate(d, params, slots, args.cpu_sample)
+    gradient = measure_gradient(torch, d, params, dev) if not args.no_gradient else None
     gpu_obs = np.asarray(out[1])[: args.cpu_sample]
     obs_rel = float(np.max(np.abs(gpu_obs - cpu["values"]) / np.maximum(np.abs(cpu["values"]), 1e-300)))
 
@@ -337,6 +388,7 @@ def run_gpu(args) -> None:
                      if other else None),
         "accuracy": {"max_population_error_vs_fp64_gpu": max_pop_err, "observable_max_rel_err_vs_cpu_oracle": obs_rel},
         "clocks": clocks,
+        "gradient": gradient,
     }
     print(json.dumps(line))
     if world > 1:
@@ -351,6 +403,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 path beside mixed")
+    ap.add_argument("--no-gradient", action="store_true", help="skip timing the adjoint beside the forward solve")
     ap.add_argument("--points", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--ref-sample", type=int, default=256)
