@@ -132,6 +132,22 @@ def cpu_oracle_rate(d, params, slots, sample: int, threads: int = 0) -> dict:
             "seconds": dt, "values": vals.reshape(-1)}
 
 
+def cpu_oracle_populations(d, params, slots, sample: int) -> np.ndarray:
+    """Final populations of the first `sample` scan points from the FP64 oracle (accuracy check only)."""
+    import oracle
+
+    op = oracle.OraclePlan(d["payload"])
+    gamma, (t0, t1) = d["gamma"], d["t_span"]
+    # final populations: saveat=[t1], save_start=False, as the reference maps them (python_api.rs:589-617)
+    o = op.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=np.array([t1]), save_start=False,
+                   maxiters=100000, solver="tsit5", output="populations", output_indices=None,
+                   output_when="final", integral_weights=None, stop_event=None)
+    p = params[:sample]
+    rho0 = np.repeat(d["rho0_packed"].reshape(1, -1), p.shape[0], axis=0)
+    vals, _, _ = op.solve_batch(o, rho0, slots, p)
+    return vals.reshape(p.shape[0], -1)
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -348,11 +364,27 @@ def run_gpu(args) -> None:
     p64 = pops("fp64")
     pm = p64 if args.precision == "fp64" else pops(args.precision)
     max_pop_err = float(np.max(np.abs(pm - p64)))
+    # per-result diagnostics the solve reports beside its error: trace drift of the final state
+    # (|sum of populations - 1|; rho0 has unit trace) for both forms, and the error of both forms
+    # against the FP64 oracle on the CPU-baseline sample
+    p_orc = cpu_oracle_populations(d, params, slots, args.cpu_sample)
+    accuracy = {
+        "max_population_error_vs_fp64_gpu": max_pop_err,
+        "max_population_error_vs_fp64_oracle": float(np.max(np.abs(pm[: args.cpu_sample] - p_orc))),
+        "max_population_error_fp64_gpu_vs_fp64_oracle": float(np.max(np.abs(p64[: args.cpu_sample] - p_orc))),
+        "max_trace_drift": float(np.max(np.abs(pm.sum(axis=1) - 1.0))),
+        "max_trace_drift_fp64_gpu": float(np.max(np.abs(p64.sum(axis=1) - 1.0))),
+        "hermiticity_residual": 0.0,
+        "hermiticity_note": "the state is the packed upper triangle (real diagonal, re/im pairs above it), "
+                            "so the density matrix it stands for is Hermitian by construction",
+        "oracle_sample": args.cpu_sample,
+    }
     # and the observable against the CPU oracle on a sample (also the CPU baseline)
     cpu = cpu_oracle_rate(d, params, slots, args.cpu_sample)
     gradient = measure_gradient(torch, d, params, dev) if not args.no_gradient else None
     gpu_obs = np.asarray(out[1])[: args.cpu_sample]
     obs_rel = float(np.max(np.abs(gpu_obs - cpu["values"]) / np.maximum(np.abs(cpu["values"]), 1e-300)))
+    accuracy["observable_max_rel_err_vs_cpu_oracle"] = obs_rel
 
     f_rhs, per_step = flops_per_step_unit(d["payload"])
     flops_per_launch = attempted * per_step
@@ -386,7 +418,7 @@ def run_gpu(args) -> None:
                       "ms_per_step": sum(other[0]) / len(other[0]), "attempted_steps_per_launch": other[1],
                       "speedup_of_this_precision": (b * world * args.steps / total_s) / (b * world * args.steps / total64_s)}
                      if other else None),
-        "accuracy": {"max_population_error_vs_fp64_gpu": max_pop_err, "observable_max_rel_err_vs_cpu_oracle": obs_rel},
+        "accuracy": accuracy,
         "clocks": clocks,
         "gradient": gradient,
     }
