@@ -12,7 +12,9 @@ populations are compared with the plain FP64 path on every point, and the FP64 p
 the same batch beside it (`fp64_gpu`).  `value` times the device-resident entry
 point (obe_solve_batch_device) with CUDA events on its stream and the L2 flushed between steps;
 `e2e` times the reference-facing call solve_lindblad_batch_ode_py with host arrays (copies in
-the timed region).  `--impl reference` times the CPU path of the reference restated in C
+the timed region).  Beside the headline the line carries the adjoint's cost against the forward
+solve (`gradient`) and the heterogeneous batch of 16-, 39- and 76-state systems in one call
+(`heterogeneous`).  `--impl reference` times the CPU path of the reference restated in C
 (the oracle) on the host cores, on a bounded sample of the same scan.
 """
 
@@ -251,6 +253,118 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
             "grad_over_fwd": t_grad / t_fwd}
 
 
+HETERO_PLANS = (("plan_q1_16_tend", 6), ("plan_r0_39", 3), ("plan_rc_76", 1))
+
+
+def hetero_jobs(total: int, seed: int = 20241204, t_end_range=(50.0, 300.0)):
+    """The heterogeneous batch: `total` instances drawn 6:3:1 from the 16-state (Q(1)), 39-state
+    (R(0), X J=0-2) and 76-state (R(0) + P(2), square-wave polarisation) plans; parameters as in
+    the 16-state scan (peak Rabi Γ·10^U[-1,1], detuning U[-5Γ, 5Γ], angle U[0, π]) or, for the
+    76-state plan, per-laser Rabi U[0.5, 3]Γ and detuning N(0, 0.5Γ); end times U[50, 300]/Γ through
+    a `Time() - t_end` stop event; Tsit5, rtol 1e-8, atol 1e-11, excited-population integral."""
+    import codec
+
+    rng = np.random.default_rng(seed)
+    kinds = rng.choice(len(HETERO_PLANS), size=total, p=np.array([w for _, w in HETERO_PLANS]) / 10.0)
+    jobs = []
+    for k, (name, _) in enumerate(HETERO_PLANS):
+        count = int(np.sum(kinds == k))
+        d = codec.load(name)
+        g = d["gamma"]
+        names = d["payload"]["parameter_graph"]["slot_names"]
+        if name == "plan_rc_76":
+            slot_names = ["Ω0", "Ω1", "δ0", "δ1", "t_end"]
+            cols = [rng.uniform(0.5, 3.0, count) * g, rng.uniform(0.5, 3.0, count) * g,
+                    rng.normal(0.0, 0.5, count) * g, rng.normal(0.0, 0.5, count) * g]
+        else:
+            slot_names = ["rabi", "detuning", "theta", "t_end"]
+            cols = [g * 10 ** rng.uniform(-1.0, 1.0, count), rng.uniform(-5.0, 5.0, count) * g,
+                    rng.uniform(0.0, np.pi, count)]
+        t_end = rng.uniform(*t_end_range, count) / g
+        params = np.stack(cols + [t_end], axis=1).astype(np.complex128)
+        ev = {"kind": "runtime_expression",
+              "expression": {"instructions": [{"op": 4}, {"op": 2, "index": names.index("t_end")}, {"op": 6}],
+                             "scalar_only": True, "output_is_tuple": False}}
+        jobs.append({"name": name, "d": d, "count": count, "params": params,
+                     "slots": [names.index(s) for s in slot_names], "event": ev,
+                     "t1": 1.01 * t_end_range[1] / g, "weights": [(i, 1.0) for i in d["excited_indices"]]})
+    return jobs
+
+
+def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
+    """The heterogeneous batch, device-resident, through obe_solve_multi_device (one call, the
+    three plans' kernels concurrent): the mixed form timed after one untimed call, the same jobs
+    as three single-plan calls in a row on one stream (what a caller of the reference's
+    one-plan-per-call API does), and the FP64 form once, for the error of the mixed form."""
+    from centrex_tlf_gb300.native import NativePlan, multi_solve_device
+
+    spec = hetero_jobs(total)
+    stream = torch.cuda.current_stream(dev)
+    prepared = []
+    for j in spec:
+        d = j["d"]
+        plan = NativePlan(d["payload"])
+        g = d["gamma"]
+        opts = {prec: plan.options(t0=0.0, t1=j["t1"], abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=None,
+                                   save_start=True, maxiters=1000000, solver="tsit5", output="excited_population",
+                                   output_indices=None, output_when="final", integral_weights=j["weights"],
+                                   stop_event=j["event"], precision=prec)
+                for prec in ("mixed", "fp64")}
+        b = j["count"]
+        rho = torch.from_numpy(np.repeat(d["rho0_packed"].reshape(1, -1), b, axis=0)).to(dev)
+        par = torch.from_numpy(np.ascontiguousarray(j["params"]).view(np.float64).reshape(-1)).to(dev)
+        val = {prec: torch.zeros(b, dtype=torch.float64, device=dev) for prec in opts}
+        st = torch.zeros(b * 6, dtype=torch.int64, device=dev)
+        prepared.append((plan, opts, b, rho, j["slots"], par, val, st))
+
+    def multi(prec):
+        return multi_solve_device([(pl, o[prec], b, r.data_ptr(), sl, pa.data_ptr(), 1, v[prec].data_ptr(), s.data_ptr())
+                                   for pl, o, b, r, sl, pa, v, s in prepared], stream.cuda_stream)
+
+    def sequential(prec):
+        for pl, o, b, r, sl, pa, v, s in prepared:
+            pl.solve_batch_device(o[prec], b, r.data_ptr(), sl, pa.data_ptr(), 1, v[prec].data_ptr(), s.data_ptr(),
+                                  stream.cuda_stream)
+        return len(prepared)
+
+    def timed(fn, prec, warm=True):
+        if warm:
+            fn(prec)
+            torch.cuda.synchronize()
+        best, launches = float("inf"), 0
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launches = fn(prec)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+        return best, launches
+
+    t_multi, launches = timed(multi, "mixed")
+    failed = sum(int(np.count_nonzero(s.view(-1, 6)[:, 3].cpu().numpy() >> 32)) for *_, s in prepared)
+    steps = [int(s.view(-1, 6)[:, 0].sum().item()) for *_, s in prepared]
+    t_seq, _ = timed(sequential, "mixed", warm=False)
+    t_64, _ = timed(multi, "fp64", warm=False)
+    err = 0.0
+    for j, (*_, val, _) in zip(spec, prepared):
+        t_end = j["params"][:, -1].real
+        dv = (val["mixed"] - val["fp64"]).abs().cpu().numpy()
+        err = max(err, float(np.max(dv / t_end)))
+    return {
+        "workload": f"{total} instances, 16/39/76-state plans drawn 6:3:1, end times U[50, 300]/Γ by stop event, "
+                    "Tsit5 rtol 1e-8 atol 1e-11, excited-population integral; mixed precision; device-resident",
+        "value": total / t_multi, "unit": "trajectories/s", "ms": 1e3 * t_multi, "gpu_launches": launches,
+        "instances": {j["name"]: j["count"] for j in spec},
+        "accepted_steps": {j["name"]: n for j, n in zip(spec, steps)},
+        "failed_trajectories": failed,
+        "one_call_per_plan_ms": 1e3 * t_seq, "concurrency_gain": t_seq / t_multi,
+        "fp64_ms": 1e3 * t_64, "speedup_of_mixed": t_64 / t_multi,
+        "max_time_averaged_population_error_vs_fp64": err,
+        "note": "fp64 timed on its first call (plans already on the device); the error is |integral difference| / t_end",
+    }
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -382,6 +496,7 @@ def run_gpu(args) -> None:
     # and the observable against the CPU oracle on a sample (also the CPU baseline)
     cpu = cpu_oracle_rate(d, params, slots, args.cpu_sample)
     gradient = measure_gradient(torch, d, params, dev) if not args.no_gradient else None
+    hetero = measure_heterogeneous(torch, dev, total=args.hetero_instances) if args.hetero_instances > 0 else None
     gpu_obs = np.asarray(out[1])[: args.cpu_sample]
     obs_rel = float(np.max(np.abs(gpu_obs - cpu["values"]) / np.maximum(np.abs(cpu["values"]), 1e-300)))
     accuracy["observable_max_rel_err_vs_cpu_oracle"] = obs_rel
@@ -421,6 +536,7 @@ def run_gpu(args) -> None:
         "accuracy": accuracy,
         "clocks": clocks,
         "gradient": gradient,
+        "heterogeneous": hetero,
     }
     print(json.dumps(line))
     if world > 1:
@@ -436,6 +552,8 @@ def main() -> None:
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 path beside mixed")
     ap.add_argument("--no-gradient", action="store_true", help="skip timing the adjoint beside the forward solve")
+    ap.add_argument("--hetero-instances", type=int, default=8192,
+                    help="instances of the heterogeneous 16/39/76-state batch timed beside the scan (0 skips it)")
     ap.add_argument("--points", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--ref-sample", type=int, default=256)

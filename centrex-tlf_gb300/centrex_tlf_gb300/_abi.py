@@ -128,6 +128,27 @@ class ObeTrajStats(ctypes.Structure):
     ]
 
 
+class ObeBatchJob(ctypes.Structure):
+    """obe_batch_job: one device-resident batch of obe_solve_multi_device."""
+
+    _fields_ = [
+        ("plan", ctypes.c_void_p),
+        ("opt", ctypes.POINTER(ObeSolveOptions)),
+        ("n_traj", ctypes.c_int64),
+        ("d_rho0", ctypes.c_void_p),
+        ("n_param_slots", ctypes.c_int32),
+        ("param_slots", c_i64p),
+        ("d_param_values", ctypes.c_void_p),
+        ("time_count", ctypes.c_int64),
+        ("width", ctypes.c_int64),
+        ("d_values", ctypes.c_void_p),
+        ("d_stats", ctypes.c_void_p),
+    ]
+
+
+MAX_JOBS = 16  # OBE_MAX_JOBS
+
+
 # numpy view of obe_traj_stats (same layout: 8+8+8+4+4+8+8 = 48 bytes, naturally aligned)
 TRAJ_STATS_DTYPE = np.dtype(
     [
@@ -215,6 +236,8 @@ def load_library() -> ctypes.CDLL:
     ]
     lib.obe_solve_batch_device.restype = ctypes.c_int
     lib.obe_last_launch_count.restype = ctypes.c_int64
+    lib.obe_solve_multi_device.argtypes = [ctypes.c_int32, ctypes.POINTER(ObeBatchJob), ctypes.c_void_p]
+    lib.obe_solve_multi_device.restype = ctypes.c_int
     lib.obe_grad_tape_doubles_per_step.argtypes = [ctypes.c_void_p]
     lib.obe_grad_tape_doubles_per_step.restype = ctypes.c_int64
     lib.obe_grad_forward.argtypes = [

@@ -31,6 +31,7 @@ __all__ = [
     "prepare_lindblad_problem_py",
     "solve_lindblad_batch_ode_py",
     "solve_lindblad_grid_ode_py",
+    "solve_lindblad_multi_batch_ode_py",
     "solve_lindblad_ode_py",
 ]
 
@@ -293,6 +294,28 @@ def solve_lindblad_batch_ode_py(
     CPU thread pool and are accepted for compatibility.
 
     Returns ``(times, values, width, time_count, stats)``."""
+    prep = _prepare_batch(plan, packed_rho0_batch, t0, t1, abstol, reltol, dt, saveat, save_start, maxiters, mode,
+                          solver, output, output_indices, output_when, integral_weights, parameter_slot_indices,
+                          parameter_batch, stop_event, precision)
+    if prep.empty is not None:
+        return prep.empty
+    values, st = prep.native.solve_batch(prep.opts, prep.batch, prep.slots, prep.pv, prep.time_count)
+    return prep.result(values, st)
+
+
+class _PreparedBatch:
+    """A validated batch: the native plan, options, inputs and the result shaping of one call."""
+
+    __slots__ = ("native", "batch", "slots", "pv", "opts", "time_count", "ref_times", "t1", "solver", "stop_event", "empty")
+
+    def result(self, values, st):
+        return _batch_result(values, st, self.opts.width, self.time_count, self.ref_times, self.t1, self.solver,
+                             self.stop_event, self.opts.is_complex)
+
+
+def _prepare_batch(plan, packed_rho0_batch, t0, t1, abstol, reltol, dt, saveat, save_start, maxiters, mode, solver,
+                   output, output_indices, output_when, integral_weights, parameter_slot_indices, parameter_batch,
+                   stop_event, precision) -> _PreparedBatch:
     native = _native(plan)
     _check_mode(mode)
     _check_solver(solver)
@@ -309,20 +332,110 @@ def solve_lindblad_batch_ode_py(
             raise ValueError("parameter_batch shape mismatch")
     else:
         pv = None
+    prep = _PreparedBatch()
+    prep.native, prep.batch, prep.t1, prep.solver, prep.stop_event = native, batch, t1, solver, stop_event
+    prep.empty = None
     if batch.shape[0] == 0:
-        return np.zeros(0), np.zeros(0), 0, 0, {
+        prep.empty = (np.zeros(0), np.zeros(0), 0, 0, {
             "solver": solver, "accepted_steps": 0, "rejected_steps": 0, "rhs_calls": 0, "event_triggered": False,
-            "event_triggered_by_trajectory": [], "event_times": [], "event_count": 0}
+            "event_triggered_by_trajectory": [], "event_times": [], "event_count": 0})
+        return prep
     saveat_vec, eff_ss, time_count, ref_times = _batch_common(
         native, t0, t1, saveat, save_start, output, output_when, integral_weights, output_indices, stop_event
     )
-    opts = _opts(native, t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=saveat_vec, save_start=eff_ss,
-                 maxiters=maxiters, solver=solver, output=output, output_indices=output_indices,
-                 output_when=output_when, integral_weights=integral_weights, stop_event=stop_event,
-                 precision=precision)
+    prep.opts = _opts(native, t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=saveat_vec, save_start=eff_ss,
+                      maxiters=maxiters, solver=solver, output=output, output_indices=output_indices,
+                      output_when=output_when, integral_weights=integral_weights, stop_event=stop_event,
+                      precision=precision)
     use = pv is not None and len(slots) > 0
-    values, st = native.solve_batch(opts, batch, slots if use else None, pv if use else None, time_count)
-    return _batch_result(values, st, opts.width, time_count, ref_times, t1, solver, stop_event, opts.is_complex)
+    prep.slots, prep.pv = (slots, pv) if use else (None, None)
+    prep.time_count, prep.ref_times = time_count, ref_times
+    return prep
+
+
+_BATCH_DEFAULTS = dict(saveat=None, save_start=True, maxiters=100000, mode="expanded_sparse", solver="dopri5",
+                       output="populations", output_indices=None, output_when="final", integral_weights=None,
+                       parameter_slot_indices=None, parameter_batch=None, stop_event=None, precision="fp64")
+
+
+def solve_lindblad_multi_batch_ode_py(jobs, precision=None):
+    """Several batches on different plans (systems of different sizes) in one GPU call
+    (obe_solve_multi_device).  The reference has no counterpart: it solves one prepared plan per
+    call (rust/src/lindblad/ode_batch.rs:176-351), so a mixed workload there is one call per plan.
+
+    ``jobs`` is a sequence of dicts, each holding the arguments of ``solve_lindblad_batch_ode_py``
+    by name (``plan``, ``packed_rho0_batch``, ``t0``, ``t1``, ``abstol``, ``reltol``, ``dt`` and any
+    of its keywords).  ``precision``, when given, applies to every job.  The jobs' kernels run
+    concurrently on the GPU, the largest systems first.  Returns one
+    ``(times, values, width, time_count, stats)`` per job, as ``solve_lindblad_batch_ode_py``
+    would; a failing trajectory raises ``ValueError("job {k}: trajectory {i}: {msg}")``."""
+    import torch
+
+    from .native import multi_solve_device
+
+    preps = []
+    for k, job in enumerate(jobs):
+        kw = dict(_BATCH_DEFAULTS)
+        unknown = set(job) - set(kw) - {"plan", "packed_rho0_batch", "t0", "t1", "abstol", "reltol", "dt",
+                                         "parallel", "threads", "use_split_input_rhs"}
+        if unknown:
+            raise TypeError(f"job {k}: unexpected arguments {sorted(unknown)}")
+        kw.update({key: v for key, v in job.items() if key in kw})
+        if precision is not None:
+            kw["precision"] = precision
+        try:
+            preps.append(_prepare_batch(job["plan"], job["packed_rho0_batch"], job["t0"], job["t1"], job["abstol"],
+                                        job["reltol"], job["dt"], kw["saveat"], kw["save_start"], kw["maxiters"],
+                                        kw["mode"], kw["solver"], kw["output"], kw["output_indices"],
+                                        kw["output_when"], kw["integral_weights"], kw["parameter_slot_indices"],
+                                        kw["parameter_batch"], kw["stop_event"], kw["precision"]))
+        except (ValueError, NotImplementedError, TypeError) as exc:
+            raise type(exc)(f"job {k}: {exc}") from None
+    live = [k for k, p in enumerate(preps) if p.empty is None]
+    dev = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else None
+    if live and dev is None:
+        raise RuntimeError("no CUDA device is available: the GB300 solver has no CPU fallback")
+    bufs = {}
+    for k in live:
+        p = preps[k]
+        b = p.batch.shape[0]
+        vals = p.time_count * p.opts.width * (2 if p.opts.is_complex else 1)
+        bufs[k] = {
+            "rho0": torch.from_numpy(np.ascontiguousarray(p.batch)).to(dev),
+            "params": (torch.from_numpy(np.ascontiguousarray(p.pv).view(np.float64)).to(dev)
+                       if p.pv is not None else None),
+            "values": torch.empty(b * vals, dtype=torch.float64, device=dev),
+            "stats": torch.zeros(b * 6, dtype=torch.int64, device=dev),
+        }
+    if live:
+        stream = torch.cuda.current_stream(dev)
+        multi_solve_device(
+            [(preps[k].native, preps[k].opts, preps[k].batch.shape[0], bufs[k]["rho0"].data_ptr(), preps[k].slots,
+              bufs[k]["params"].data_ptr() if bufs[k]["params"] is not None else None, preps[k].time_count,
+              bufs[k]["values"].data_ptr(), bufs[k]["stats"].data_ptr()) for k in live],
+            stream.cuda_stream)
+        stream.synchronize()
+    out = []
+    for k, p in enumerate(preps):
+        if p.empty is not None:
+            out.append(p.empty)
+            continue
+        from . import _abi
+
+        st = bufs[k]["stats"].cpu().numpy().view(_abi.TRAJ_STATS_DTYPE)
+        if np.any(st["status"] != 0):
+            # the device form reports status codes only: re-run this job through the host-pointer
+            # call, which fails on the same trajectory with the reference's message
+            try:
+                p.native.solve_batch(p.opts, p.batch, p.slots, p.pv, p.time_count)
+            except ValueError as exc:
+                raise ValueError(f"job {k}: {exc}") from None
+            raise RuntimeError(f"job {k}: a trajectory failed on the device but not on the re-run")
+        values = bufs[k]["values"].cpu().numpy()
+        if p.opts.is_complex:
+            values = values.view(np.complex128)
+        out.append(p.result(values.reshape(p.batch.shape[0], p.time_count, p.opts.width), st))
+    return out
 
 
 def solve_lindblad_grid_ode_py(

@@ -211,6 +211,30 @@ class NativePlan:
         return int(self.lib.obe_last_launch_count())
 
 
+def multi_solve_device(jobs, stream: int = 0) -> int:
+    """obe_solve_multi_device over device-resident batches on different plans.
+
+    ``jobs``: sequence of ``(plan: NativePlan, opts: SolveOptions, n_traj, d_rho0, param_slots or
+    None, d_param_values or None, time_count, d_values, d_stats)``, data pointers as ints.  The
+    jobs' kernels run concurrently, asynchronous on ``stream``.  Returns the kernel launch count."""
+    if not jobs:
+        return 0
+    lib = load_library()
+    arr = (_abi.ObeBatchJob * len(jobs))()
+    keep = []
+    for k, (plan, opts, n_traj, d_rho0, slots, d_params, time_count, d_values, d_stats) in enumerate(jobs):
+        sl = np.ascontiguousarray(np.asarray(slots if slots else [0], dtype=np.int64))
+        keep.append(sl)
+        n_param = 0 if d_params is None or not slots else int(sl.size)
+        arr[k] = _abi.ObeBatchJob(plan.handle.value, ctypes.pointer(opts.opts), int(n_traj), d_rho0, n_param,
+                                  _abi.ptr(sl, ctypes.c_int64), d_params or 0, int(time_count), opts.width,
+                                  d_values, d_stats)
+    st = lib.obe_solve_multi_device(len(jobs), arr, ctypes.c_void_p(stream))
+    if st != _abi.OBE_OK:
+        _raise(lib, st)
+    return int(lib.obe_last_launch_count())
+
+
 def _stats_dict(st: ObeTrajStats) -> dict:
     return {
         "accepted_steps": int(st.accepted_steps),

@@ -166,6 +166,7 @@ struct obe_plan {
 
 namespace obe {
 void set_error(const std::string& msg);
+const char* last_error_cstr();  // the calling thread's last message
 std::string fmt_f64(double v);  // Rust Display of f64
 obe_status pack_plan(const obe_plan_desc* d, obe_plan* p);
 int threads_per_trajectory_for(int32_t n);

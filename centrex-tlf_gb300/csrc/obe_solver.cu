@@ -555,6 +555,136 @@ obe_status obe_solve_batch_device(const obe_plan* plan_c, const obe_solve_option
                         cb, save_times, static_cast<unsigned long long*>(p->d_counter), s);
 }
 
+// Streams of the heterogeneous batch: one non-blocking stream and completion event per job
+// slot, created on the first multi-job call on a device and kept for the process.
+namespace {
+struct JobStreams {
+    int device = -1;
+    cudaStream_t s[OBE_MAX_JOBS] = {};
+    cudaEvent_t done[OBE_MAX_JOBS] = {};
+    cudaEvent_t start = nullptr;
+};
+JobStreams g_job_streams;
+
+obe_status job_streams(int dev, JobStreams** out) {
+    JobStreams& J = g_job_streams;
+    if (J.device != dev) {
+        if (J.device >= 0) {
+            // another device is current: rebuild on this one (the old device's handles stay valid
+            // only there, so release them under it)
+            int cur = dev;
+            cudaSetDevice(J.device);
+            for (int k = 0; k < OBE_MAX_JOBS; ++k) {
+                if (J.s[k]) cudaStreamDestroy(J.s[k]);
+                if (J.done[k]) cudaEventDestroy(J.done[k]);
+                J.s[k] = nullptr;
+                J.done[k] = nullptr;
+            }
+            if (J.start) cudaEventDestroy(J.start);
+            J.start = nullptr;
+            cudaSetDevice(cur);
+        }
+        J.device = -1;
+        for (int k = 0; k < OBE_MAX_JOBS; ++k) {
+            if (!cuda_ok(cudaStreamCreateWithFlags(&J.s[k], cudaStreamNonBlocking), "cudaStreamCreateWithFlags")) return OBE_ERR_CUDA;
+            if (!cuda_ok(cudaEventCreateWithFlags(&J.done[k], cudaEventDisableTiming), "cudaEventCreateWithFlags")) return OBE_ERR_CUDA;
+        }
+        if (!cuda_ok(cudaEventCreateWithFlags(&J.start, cudaEventDisableTiming), "cudaEventCreateWithFlags")) return OBE_ERR_CUDA;
+        J.device = dev;
+    }
+    *out = &J;
+    return OBE_OK;
+}
+
+struct PreparedJob {
+    obe_plan* p;
+    const obe_batch_job* j;
+    std::vector<double> save_times;
+    CallBlob cb;
+    int cplx = 0;
+    unsigned char* d = nullptr;
+    size_t errs_off = 0;
+};
+}  // namespace
+
+obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, void* stream) {
+    g_launches = 0;
+    if (n_jobs < 0 || n_jobs > OBE_MAX_JOBS) {
+        set_error("n_jobs must be between 0 and " + std::to_string(OBE_MAX_JOBS));
+        return OBE_ERR_INVALID;
+    }
+    if (n_jobs == 0) return OBE_OK;
+    if (!jobs) { set_error("null argument"); return OBE_ERR_INVALID; }
+    auto fail = [](int k, obe_status st) {
+        set_error("job " + std::to_string(k) + ": " + last_error_cstr());
+        return st;
+    };
+    for (int k = 0; k < n_jobs; ++k) {
+        if (!jobs[k].plan || !jobs[k].opt) { set_error("null argument"); return fail(k, OBE_ERR_INVALID); }
+        if (jobs[k].n_traj < 0) { set_error("n_traj must be non-negative"); return fail(k, OBE_ERR_INVALID); }
+        for (int m = 0; m < k; ++m)
+            if (jobs[m].plan == jobs[k].plan) {
+                set_error("plan already used by job " + std::to_string(m) + " (one job per plan)");
+                return fail(k, OBE_ERR_INVALID);
+            }
+    }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::vector<PreparedJob> pj(n_jobs);
+    for (int k = 0; k < n_jobs; ++k) {
+        PreparedJob& q = pj[k];
+        q.j = &jobs[k];
+        q.p = const_cast<obe_plan*>(jobs[k].plan);
+        obe_status st = ensure_ready(q.p);
+        if (st != OBE_OK) return fail(k, st);
+        if ((st = check_params(q.p, q.j->n_param_slots, q.j->param_slots)) != OBE_OK) return fail(k, st);
+        int64_t w = 0;
+        if ((st = validate_options(q.p, q.j->opt, q.save_times, q.cb, &w, &q.cplx)) != OBE_OK) return fail(k, st);
+        if (w != q.j->width) { set_error("output width mismatch"); return fail(k, OBE_ERR_INVALID); }
+        LaunchShape s;
+        const int vm_depth = std::max(q.p->dev.max_stack, std::max(q.cb.ev_len, 1));
+        if ((st = plan_launch(q.p->dev, q.j->opt->precision == OBE_PRECISION_MIXED, std::max<int64_t>(q.j->n_traj, 1), vm_depth, &s)) != OBE_OK)
+            return fail(k, st);
+        q.errs_off = align16(q.cb.bytes.size());
+        size_t need = q.errs_off + sizeof(TrajErr) * static_cast<size_t>(std::max<int64_t>(q.j->n_traj, 1));
+        if ((st = scratch(q.p, need, &q.d)) != OBE_OK) return fail(k, st);
+    }
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
+    JobStreams* J = nullptr;
+    obe_status st = job_streams(dev, &J);
+    if (st != OBE_OK) return st;
+    // largest systems first: their trajectories are the longest single pieces of work, so they
+    // take the SMs first and the small systems fill in behind them (longest-processing-time order)
+    std::vector<int> order(n_jobs);
+    for (int k = 0; k < n_jobs; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pj[a].p->N > pj[b].p->N; });
+    cudaStream_t caller = static_cast<cudaStream_t>(stream);
+    if (!cuda_ok(cudaEventRecord(J->start, caller), "cudaEventRecord")) return OBE_ERR_CUDA;
+    long long launches = 0;
+    for (int r = 0; r < n_jobs; ++r) {
+        const int k = order[r];
+        PreparedJob& q = pj[k];
+        cudaStream_t js = J->s[r];
+        if (!cuda_ok(cudaStreamWaitEvent(js, J->start, 0), "cudaStreamWaitEvent")) return OBE_ERR_CUDA;
+        if (q.j->n_traj > 0) {
+            if (!cuda_ok(cudaMemcpyAsync(q.d, q.cb.bytes.data(), q.cb.bytes.size(), cudaMemcpyHostToDevice, js), "cudaMemcpyAsync(args)"))
+                return OBE_ERR_CUDA;
+            st = solve_device(q.p, q.j->opt, q.j->n_traj, q.j->d_rho0, q.p->N, q.j->n_param_slots, q.j->param_slots,
+                              q.j->d_param_values, 0, nullptr, nullptr, q.j->time_count,
+                              q.j->time_count * q.j->width * (q.cplx ? 2 : 1), q.j->d_values, nullptr, q.j->d_stats,
+                              reinterpret_cast<TrajErr*>(q.d + q.errs_off), q.d, q.cb, q.save_times,
+                              static_cast<unsigned long long*>(q.p->d_counter), js);
+            if (st != OBE_OK) return fail(k, st);
+            launches += g_launches;
+            g_launches = 0;
+        }
+        if (!cuda_ok(cudaEventRecord(J->done[r], js), "cudaEventRecord")) return OBE_ERR_CUDA;
+        if (!cuda_ok(cudaStreamWaitEvent(caller, J->done[r], 0), "cudaStreamWaitEvent")) return OBE_ERR_CUDA;
+    }
+    g_launches = launches;
+    return OBE_OK;
+}
+
 // Host-pointer batch/grid/single driver.
 static obe_status solve_host(obe_plan* p, const obe_solve_options* o, long long n_traj, const double* rho0, long long rho0_stride,
                              int32_t n_param, const int64_t* param_slots, const double* param_values, int n_axes,

@@ -238,6 +238,35 @@ obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options*
                                   obe_traj_stats* d_stats, void* stream);
 
 /*
+ * Heterogeneous batch (no counterpart in the reference, which solves one prepared plan per
+ * call, ode_batch.rs:176-351): several device-resident batches, each on its own plan (systems
+ * of different sizes, different options, parameter slots and outputs), solved by one call.
+ * Every job is what obe_solve_batch_device takes; all pointers inside are device memory except
+ * `plan`, `opt` and `param_slots`.  The jobs' persistent kernels run concurrently, the largest
+ * systems first, so the GPU is shared between the jobs and the smaller systems fill the SMs
+ * that the larger ones leave while they drain.  Asynchronous on `stream`: the jobs start after
+ * the work already queued on `stream` and later work on `stream` waits for all of them.  Each
+ * plan may appear in at most one job (a plan's scratch serves one solve at a time); at most
+ * OBE_MAX_JOBS jobs.  A validation failure names its job: "job {k}: {msg}", and nothing is
+ * launched.
+ */
+#define OBE_MAX_JOBS 16
+typedef struct {
+    const obe_plan* plan;
+    const obe_solve_options* opt;
+    int64_t n_traj;
+    const double* d_rho0;          /* [n_traj][N] */
+    int32_t n_param_slots;
+    const int64_t* param_slots;    /* host, [n_param_slots] */
+    const double* d_param_values;  /* [n_traj][n_param_slots] complex, or NULL */
+    int64_t time_count;
+    int64_t width;
+    double* d_values;              /* [n_traj][time_count][width] (x2 for selected) */
+    obe_traj_stats* d_stats;       /* [n_traj] */
+} obe_batch_job;
+obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, void* stream);
+
+/*
  * Gradients (no counterpart in the reference, whose Rust crate has no gradient path): the
  * discrete adjoint of the double-precision adaptive solve with its step sequence frozen, for
  * final weighted integrals (output_when="final", saveat None) and final populations, with

@@ -162,13 +162,15 @@ def build_chain(centrex_tlf, n_states: int):
     return prepare_lindblad_problem(system, params, backend="python", hamiltonian_representation="decomposed")
 
 
-def build_q1_16(centrex_tlf):
+def build_q1_16(centrex_tlf, with_t_end: bool = False):
     """The 16-state TlF system of the single-solve and scan benchmarks.
 
     X J=1 (12 hyperfine states) + B J'=1 F1'=1/2 F'=1 (3 mF states) + the X J=3 level the
     B state also decays to, lumped into one state by the builder's own ``qn_compact=True``
     (centrex_tlf/lindblad/utils_setup.py:515-629).  Q(1) F'=1 drive with z- and x-linear
-    polarisation components; a Gaussian-in-time Rabi pulse; Γ = 2π·1.56 MHz.
+    polarisation components; a Gaussian-in-time Rabi pulse; Γ = 2π·1.56 MHz.  With
+    ``with_t_end`` the parameter graph also holds a scalar ``t_end`` that a `Time() - t_end` stop
+    event can read (ragged end times in a batch); the Hamiltonian does not depend on it.
     """
     from centrex_tlf import couplings, lindblad, transitions
     from centrex_tlf.lindblad.parameters import LindbladParameters
@@ -179,20 +181,76 @@ def build_q1_16(centrex_tlf):
         trans, [[couplings.polarization_Z, couplings.polarization_X]]
     )
     obe = lindblad.generate_OBE_system_transitions(trans, selectors, qn_compact=True, Γ=GAMMA)
-    params = LindbladParameters.from_kwargs(
+    params = LindbladParameters.from_kwargs(**_gaussian_pulse_parameters(with_t_end))
+    prepared = prepare_lindblad_problem(obe, params, backend="python", hamiltonian_representation="decomposed")
+    labels = [str(s.largest) for s in obe.QN]
+    return prepared, labels
+
+
+def _gaussian_pulse_parameters(with_t_end: bool) -> dict:
+    kw = dict(
         rabi=GAMMA,
         detuning=0.0,
         theta=0.0,
         t_center=100.0 / GAMMA,
         sigma=20.0 / GAMMA,
+    )
+    if with_t_end:
+        kw["t_end"] = 200.0 / GAMMA
+    kw.update(
         Ω0="rabi*exp(-(t-t_center)**2/(2*sigma**2))",
         δ0="detuning",
         PZ0="cos(theta)",
         PX0="sin(theta)",
     )
+    return kw
+
+
+def build_r0_39(centrex_tlf):
+    """The 39-state system of the heterogeneous batch: X J=0-2 (36 hyperfine states) + B J'=1
+    F1'=1/2 F'=1 (P=-1, 3 mF states), driven on R(0) F1'=1/2 F'=1 with z- and x-linear
+    polarisation components by the same Gaussian pulse and parameters as the 16-state system,
+    plus a scalar ``t_end`` for a `Time() - t_end` stop event; Γ = 2π·1.56 MHz.
+    """
+    from centrex_tlf import couplings, lindblad, states, transitions
+    from centrex_tlf.lindblad.parameters import LindbladParameters
+    from centrex_tlf.lindblad.plan_static import prepare_lindblad_problem
+
+    X = [states.QuantumSelector(J=j, electronic=states.ElectronicState.X) for j in (0, 1, 2)]
+    B = [states.QuantumSelector(J=1, F1=0.5, F=1, P=-1, electronic=states.ElectronicState.B)]
+    trans = [transitions.R0_F1_1o2_F1]
+    selectors = couplings.generate_transition_selectors(trans, [[couplings.polarization_Z, couplings.polarization_X]])
+    obe = lindblad.generate_OBE_system(X, B, selectors, Γ=GAMMA)
+    params = LindbladParameters.from_kwargs(**_gaussian_pulse_parameters(True))
     prepared = prepare_lindblad_problem(obe, params, backend="python", hamiltonian_representation="decomposed")
     labels = [str(s.largest) for s in obe.QN]
     return prepared, labels
+
+
+def save_multi(centrex_tlf) -> None:
+    """plan_r0_39.json and plan_q1_16_tend.json: the two smaller systems of the heterogeneous
+    batch (the 76-state one is plan_rc_76), each with a scannable t_end slot; rhs_r0_39.json:
+    the reference's Python RHS on the 39-state payload."""
+    # rho0: equal populations over the driven ground level (X J=0 for R(0), X J=1 for Q(1))
+    for name, (prep, labels), driven in (("plan_r0_39", build_r0_39(centrex_tlf), "J = 0,"),
+                                         ("plan_q1_16_tend", build_q1_16(centrex_tlf, with_t_end=True), "J = 1,")):
+        n = len(labels)
+        ground = [i for i, lab in enumerate(labels) if lab.startswith("|X") and driven in lab]
+        rho = np.zeros((n, n), dtype=np.complex128)
+        for i in ground:
+            rho[i, i] = 1.0 / len(ground)
+        payload = prep.to_payload()
+        payload["dense_c_array"] = np.zeros((0, n, n), dtype=np.complex128)
+        codec.save(name, {
+            "payload": payload, "rho0_packed": prep.layout.pack(rho), "gamma": GAMMA, "state_labels": labels,
+            "excited_indices": [i for i, lab in enumerate(labels) if "B" in lab],
+            "scan_slots": ["rabi", "detuning", "theta", "t_end"],
+        })
+        if name == "plan_r0_39":
+            slots = prep.parameter_graph["slot_names"]
+            ov = [{}, {slots.index("rabi"): 2.5 * GAMMA, slots.index("detuning"): -1.5 * GAMMA, slots.index("theta"): 0.9}]
+            cases = rhs_vectors(prep, [0.0, 80.0 / GAMMA, 100.0 / GAMMA], ov, seed=39, scale=0.05)
+            codec.save("rhs_r0_39", {"cases": cases})
 
 
 def build_rc_76(centrex_tlf):
@@ -421,6 +479,9 @@ def main() -> None:
     if "--rc-76" in sys.argv:
         save_rc_76(_import_reference())
         return
+    if "--multi" in sys.argv:
+        save_multi(_import_reference())
+        return
     centrex_tlf = _import_reference()
     started = time.perf_counter()
 
@@ -508,6 +569,7 @@ def main() -> None:
 
     # --- 76-state rotational-cooling system (the large-system path, n > 45) ------------------
     save_rc_76(centrex_tlf)
+    save_multi(centrex_tlf)
 
     # --- the native-boundary call contract of the reference's Python surface ----------------
     codec.save("ffi_calls", record_ffi_calls(centrex_tlf, q1, rho_q))

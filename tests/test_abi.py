@@ -112,6 +112,33 @@ def test_argument_validation_before_any_device_work(golden):
                                         saveat=np.array([0.5, 2.0]), output_when="saveat")
 
 
+def test_multi_batch_validation_before_device_work(golden):
+    """The heterogeneous batch checks every job before it touches the device, and names the job."""
+    d = golden("plan_two_level")
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    job = dict(plan=plan, packed_rho0_batch=np.zeros((2, 4)), t0=0.0, t1=1.0, abstol=1e-8, reltol=1e-6, dt=1e-3)
+    with pytest.raises(ValueError, match=r"^job 1: rho0 dim mismatch: 3 vs 4$"):
+        api.solve_lindblad_multi_batch_ode_py([job, dict(job, packed_rho0_batch=np.zeros((2, 3)))])
+    with pytest.raises(TypeError, match=r"^job 0: unexpected arguments \['bogus'\]$"):
+        api.solve_lindblad_multi_batch_ode_py([dict(job, bogus=1)])
+    with pytest.raises(ValueError, match=r"^job 0: solver must be"):
+        api.solve_lindblad_multi_batch_ode_py([dict(job, solver="rk45")])
+    # the C entry point: one job per plan, at most OBE_MAX_JOBS jobs, nothing to do for none
+    lib = _abi.load_library()
+    native = plan.native
+    opts = native.options(t0=0.0, t1=1.0, abstol=1e-8, reltol=1e-6, dt=1e-3, saveat=np.array([1.0]), save_start=False,
+                          maxiters=1000, solver="dopri5", output="populations", output_indices=None,
+                          output_when="final", integral_weights=None, stop_event=None)
+    arr = (_abi.ObeBatchJob * 2)()
+    for k in range(2):
+        arr[k] = _abi.ObeBatchJob(native.handle.value, ctypes.pointer(opts.opts), 1, None, 0, None, None, 1,
+                                  opts.width, None, None)
+    assert lib.obe_solve_multi_device(2, arr, None) == _abi.OBE_ERR_INVALID
+    assert _abi.last_error(lib) == "job 1: plan already used by job 0 (one job per plan)"
+    assert lib.obe_solve_multi_device(_abi.MAX_JOBS + 1, arr, None) == _abi.OBE_ERR_INVALID
+    assert lib.obe_solve_multi_device(0, None, None) == _abi.OBE_OK
+
+
 def test_no_cpu_fallback_without_gpu(golden):
     """Without a CUDA device the solver refuses instead of computing on the CPU."""
     if _abi.load_library().obe_device_count() > 0:

@@ -69,7 +69,7 @@ def test_two_level_grid_known_answer(golden):
     np.testing.assert_allclose(line, line[::-1], rtol=1e-6)
 
 
-@pytest.mark.parametrize("name", PLANS + ["rc_76"])
+@pytest.mark.parametrize("name", PLANS + ["rc_76", "r0_39"])
 def test_rhs_matches_python_reference(golden, name):
     p = _plan(golden, name)
     for case in golden(f"rhs_{name}")["cases"]:
