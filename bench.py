@@ -248,9 +248,19 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
 
     t_fwd = timed(fwd)
     t_grad = timed(grad)
+    # the same at the launch shape the autotuner picks for this batch (forward, taped forward and
+    # reverse sweep all at the tuned width)
+    cands = plan.autotune(opts, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, probe_steps=64,
+                          stream=stream.cuda_stream)
+    t_fwd_t = timed(fwd)
+    t_grad_t = timed(grad)
+    plan.set_shape(0, 0)
     return {"workload": f"{n_traj} scan points, d(excited-population integral)/d(rabi, detuning, theta, t_center), "
                         "FP64 Tsit5 discrete adjoint", "fwd_ms": 1e3 * t_fwd, "fwd_plus_grad_ms": 1e3 * t_grad,
-            "grad_over_fwd": t_grad / t_fwd}
+            "grad_over_fwd": t_grad / t_fwd,
+            "autotuned": {"threads_per_trajectory": cands[0]["threads_per_trajectory"],
+                          "trajectories_per_cta": cands[0]["trajectories_per_cta"], "fwd_ms": 1e3 * t_fwd_t,
+                          "fwd_plus_grad_ms": 1e3 * t_grad_t, "grad_over_fwd": t_grad_t / t_fwd_t}}
 
 
 HETERO_PLANS = (("plan_q1_16_tend", 6), ("plan_r0_39", 3), ("plan_rc_76", 1))

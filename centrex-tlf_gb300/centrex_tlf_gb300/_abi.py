@@ -238,6 +238,17 @@ def load_library() -> ctypes.CDLL:
     lib.obe_last_launch_count.restype = ctypes.c_int64
     lib.obe_solve_multi_device.argtypes = [ctypes.c_int32, ctypes.POINTER(ObeBatchJob), ctypes.c_void_p]
     lib.obe_solve_multi_device.restype = ctypes.c_int
+    lib.obe_plan_set_shape.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]
+    lib.obe_plan_set_shape.restype = ctypes.c_int
+    lib.obe_plan_get_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]
+    lib.obe_plan_get_shape.restype = None
+    lib.obe_plan_autotune.argtypes = [
+        ctypes.c_void_p, ctypes.POINTER(ObeSolveOptions), ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32, c_i64p,
+        ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+        ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float),
+        ctypes.POINTER(ctypes.c_int32), ctypes.c_void_p,
+    ]
+    lib.obe_plan_autotune.restype = ctypes.c_int
     lib.obe_grad_tape_doubles_per_step.argtypes = [ctypes.c_void_p]
     lib.obe_grad_tape_doubles_per_step.restype = ctypes.c_int64
     lib.obe_grad_forward.argtypes = [

@@ -27,6 +27,7 @@ from .native import NativePlan
 
 __all__ = [
     "PreparedLindbladPlan",
+    "autotune_lindblad_batch_py",
     "install",
     "prepare_lindblad_problem_py",
     "solve_lindblad_batch_ode_py",
@@ -436,6 +437,36 @@ def solve_lindblad_multi_batch_ode_py(jobs, precision=None):
             values = values.view(np.complex128)
         out.append(p.result(values.reshape(p.batch.shape[0], p.time_count, p.opts.width), st))
     return out
+
+
+def autotune_lindblad_batch_py(plan, packed_rho0_batch, t0, t1, abstol, reltol, dt, probe_steps=64, **kwargs):
+    """Choose the GPU launch shape of ``plan`` for batches like this one (obe_plan_autotune): the
+    arguments are those of ``solve_lindblad_batch_ode_py``; every candidate shape solves the batch
+    with at most ``probe_steps`` steps per trajectory and the fastest is kept for the plan's later
+    solves.  No counterpart in the reference (its CPU path has no launch shape).  Returns the
+    candidates with their probe times, the chosen one first."""
+    import torch
+
+    kw = dict(_BATCH_DEFAULTS)
+    unknown = set(kwargs) - set(kw) - {"parallel", "threads", "use_split_input_rhs"}
+    if unknown:
+        raise TypeError(f"unexpected arguments {sorted(unknown)}")
+    kw.update({key: v for key, v in kwargs.items() if key in kw})
+    prep = _prepare_batch(plan, packed_rho0_batch, t0, t1, abstol, reltol, dt, kw["saveat"], kw["save_start"],
+                          kw["maxiters"], kw["mode"], kw["solver"], kw["output"], kw["output_indices"], kw["output_when"],
+                          kw["integral_weights"], kw["parameter_slot_indices"], kw["parameter_batch"], kw["stop_event"],
+                          kw["precision"])
+    if prep.empty is not None:
+        raise ValueError("autotuning needs a non-empty batch")
+    if not torch.cuda.is_available():
+        raise RuntimeError("no CUDA device is available: the GB300 solver has no CPU fallback")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rho0 = torch.from_numpy(np.ascontiguousarray(prep.batch)).to(dev)
+    params = (torch.from_numpy(np.ascontiguousarray(prep.pv).view(np.float64)).to(dev) if prep.pv is not None else None)
+    stream = torch.cuda.current_stream(dev)
+    return prep.native.autotune(prep.opts, prep.batch.shape[0], rho0.data_ptr(), prep.slots,
+                                params.data_ptr() if params is not None else None, prep.time_count,
+                                probe_steps=probe_steps, stream=stream.cuda_stream)
 
 
 def solve_lindblad_grid_ode_py(

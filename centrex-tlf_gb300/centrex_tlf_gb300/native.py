@@ -173,6 +173,42 @@ class NativePlan:
         if st != _abi.OBE_OK:
             _raise(self.lib, st)
 
+    # ---- launch shape (obe_plan_set_shape / obe_plan_get_shape / obe_plan_autotune) -------
+    def set_shape(self, threads_per_trajectory: int = 0, trajectories_per_cta: int = 0) -> None:
+        """Fix the launch shape of later solves (0, 0: the automatic choice)."""
+        st = self.lib.obe_plan_set_shape(self.handle, int(threads_per_trajectory), int(trajectories_per_cta))
+        if st != _abi.OBE_OK:
+            _raise(self.lib, st)
+
+    def shape(self) -> tuple[int, int]:
+        """(threads per trajectory in use, fixed trajectories per CTA or 0 for automatic)."""
+        t, g = ctypes.c_int32(), ctypes.c_int32()
+        self.lib.obe_plan_get_shape(self.handle, ctypes.byref(t), ctypes.byref(g))
+        return int(t.value), int(g.value)
+
+    def autotune(self, opts: SolveOptions, n_traj: int, d_rho0: int, param_slots, d_param_values: int | None,
+                 time_count: int, probe_steps: int = 64, stream: int = 0) -> list[dict]:
+        """Time the candidate launch shapes on a probe of this device-resident batch and fix the
+        fastest; returns every candidate with its probe time, the chosen one first."""
+        slots = np.ascontiguousarray(np.asarray(param_slots if param_slots else [0], dtype=np.int64))
+        n_param = 0 if d_param_values is None or not param_slots else int(slots.size)
+        cap = 32
+        ct, cg = (ctypes.c_int32 * cap)(), (ctypes.c_int32 * cap)()
+        cm = (ctypes.c_float * cap)()
+        nc = ctypes.c_int32()
+        st = self.lib.obe_plan_autotune(
+            self.handle, ctypes.byref(opts.opts), int(n_traj), ctypes.c_void_p(d_rho0), n_param,
+            _abi.ptr(slots, ctypes.c_int64), ctypes.c_void_p(d_param_values or 0), int(time_count), opts.width,
+            int(probe_steps), cap, ct, cg, cm, ctypes.byref(nc), ctypes.c_void_p(stream),
+        )
+        if st != _abi.OBE_OK:
+            _raise(self.lib, st)
+        cands = [{"threads_per_trajectory": int(ct[k]), "trajectories_per_cta": int(cg[k]), "probe_ms": float(cm[k])}
+                 for k in range(min(nc.value, cap))]
+        chosen = self.shape()
+        cands.sort(key=lambda c: (c["threads_per_trajectory"], c["trajectories_per_cta"]) != chosen)
+        return cands
+
     # ---- gradients (obe_grad_forward / obe_grad_backward) -------------------------------
     def grad_tape_doubles_per_step(self) -> int:
         return int(self.lib.obe_grad_tape_doubles_per_step(self.handle))

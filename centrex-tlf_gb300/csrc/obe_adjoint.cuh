@@ -16,8 +16,9 @@
 // coefficient programs.  The trapezoid rule of the integral outputs (sum over accepted steps of
 // (t_{n+1} - t_n)(w.y_n + w.y_{n+1}) / 2) adds its weights to ybar at both ends of each segment.
 //
-// One warp per trajectory (systems up to 22 states); the transposed product L^T lambda runs on a
-// second, input-major record stream built by the packer.
+// One group of 32, 64 or 128 threads per trajectory (the plan's width; systems up to 45 states);
+// the transposed product L^T lambda runs on a second, input-major record stream built by the
+// packer.
 #pragma once
 
 #include "obe_kernels.cuh"
@@ -219,13 +220,14 @@ static __device__ __noinline__ double2 vm_eval_dual(const DevPlan& P, int32_t st
 }
 
 // ------------------------------------------------------------------------------------------
-// shared-memory layout of one adjoint trajectory group (32 threads)
+// shared-memory layout of one adjoint trajectory group (tpt threads)
 
 struct AdjLayout {
-    size_t tab, G, LS, MU, YB, slots, dslots, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, traj, bytes;
+    size_t tab, G, LS, MU, YB, slots, dslots, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, red, traj, bytes;
 };
 
-__host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int n_coeff, int n_dyn, int n_slots, int vm_depth) {
+__host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int n_coeff, int n_dyn, int n_slots, int vm_depth,
+                                                int tpt) {
     const size_t U = static_cast<size_t>(n) * (n + 1) / 2;
     const size_t nc = n_coeff > 0 ? n_coeff : 1, nd = n_dyn > 0 ? n_dyn : 1, ns = n_slots > 0 ? n_slots : 1;
     AdjLayout L{};
@@ -245,23 +247,24 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     L.cdyn = o; o = align16(o + 6 * nd * 16);
     L.ddyn = o; o = align16(o + 6 * nd * kMaxGrad * 16);
     L.dcls = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 16);
-    L.S = o; o = align16(o + 2 * nc * 32 * 16);
+    L.S = o; o = align16(o + 2 * nc * static_cast<size_t>(tpt) * 16);
+    L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
     L.traj = o; o = align16(o + 16);
     L.bytes = o;
     return L;
 }
 
-__host__ __device__ inline size_t adj_plan_smem_bytes(const DevPlan& P) {
-    return align16(static_cast<size_t>(P.n_iter + P.n_out + P.n_titer + P.n_tin) * 32 * 4);
+__host__ __device__ inline size_t adj_plan_smem_bytes(const DevPlan& P, int tpt) {
+    return align16(static_cast<size_t>(P.n_iter + P.n_out + P.n_titer + P.n_tin) * tpt * 4);
 }
 
 // ------------------------------------------------------------------------------------------
 // the reverse sweep
 
-template <int EPT>
+template <int TPT, int EPT>
 __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const CallArgs A, const AdjArgs J, int gpb,
                                                          size_t group_bytes, int M) {
-    constexpr int TPT = 32;
+    static_assert(TPT >= 32 && TPT <= 128, "the adjoint runs 32, 64 or 128 threads per trajectory");
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
@@ -277,8 +280,8 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     __syncthreads();
     if (g >= gpb) return;
 
-    const AdjLayout Lay = adj_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth);
-    unsigned char* gb = smem + adj_plan_smem_bytes(P) + static_cast<size_t>(g) * group_bytes;
+    const AdjLayout Lay = adj_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, TPT);
+    unsigned char* gb = smem + adj_plan_smem_bytes(P, TPT) + static_cast<size_t>(g) * group_bytes;
     double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
     double2* s_G = reinterpret_cast<double2*>(gb + Lay.G);
     double* s_G64 = reinterpret_cast<double*>(gb + Lay.G);
@@ -292,6 +295,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     double2* s_ddyn = reinterpret_cast<double2*>(gb + Lay.ddyn);
     double2* s_dcls = reinterpret_cast<double2*>(gb + Lay.dcls);
     double2* s_S = reinterpret_cast<double2*>(gb + Lay.S);
+    double* s_red = reinterpret_cast<double*>(gb + Lay.red);
     long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
     const int ns = P.n_slots > 0 ? P.n_slots : 1;
     const int nd = P.n_dyn > 0 ? P.n_dyn : 1;
@@ -316,9 +320,9 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
 
     while (true) {
         if (lt == 0) *s_traj = static_cast<long long>(atomicAdd(J.counter, 1ull));
-        __syncwarp();
+        gsync<TPT>(g);
         const long long traj = *s_traj;
-        __syncwarp();
+        gsync<TPT>(g);
         if (traj >= A.n_traj) break;
         int bad = 0;
         const obe_traj_stats fst = J.fwd_stats[traj];
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         if (fst.status != 0 || n_acc > J.tape_cap) {
             if (lt == 0) J.adj_status[traj] = ADJ_FORWARD_FAILED;
             for (int q = lt; q < ng; q += TPT) J.param_grad[traj * ng + q] = CUDART_NAN;
-            __syncwarp();
+            gsync<TPT>(g);
             continue;
         }
 
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
             s_LS[i] = make_double2(0.0, 0.0);
         }
         for (int i = lt; i < N; i += TPT) s_YB[i] = 0.0;
-        __syncwarp();
+        gsync<TPT>(g);
         fill_formulas<TPT>(P, 1, 1 + S, s_cstat, s_cdyn, s_tab, lt);  // static entries: once
 
         // ---- the loss gradient at the final state ----
@@ -374,12 +378,12 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         double pbar[kMaxGrad];
 #pragma unroll
         for (int q = 0; q < kMaxGrad; ++q) pbar[q] = 0.0;
-        __syncwarp();
+        gsync<TPT>(g);
         // the trapezoid weight of a segment of length dt on one of its end states
         auto add_quadrature = [&](double dt) {
             if (lt == 0)
                 for (int k = 0; k < A.n_weights; ++k) s_YB[A.w_idx[k]] += gbar * A.w_val[k] * (0.5 * dt);
-            __syncwarp();
+            gsync<TPT>(g);
         };
 
         // ---- the reverse sweep over the accepted steps ----
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     for (int q = 0; q < ng; ++q) s_ddyn[(lt * nd + j) * kMaxGrad + q] = dtmp[q];
                 }
             }
-            __syncwarp();
+            gsync<TPT>(g);
             // per stage row and coefficient class: d(class value)/dp
             for (int q = lt; q < 6 * nc2 * ng; q += TPT) {
                 const int row = q / (nc2 * ng), rem = q - row * nc2 * ng, cls = rem / ng, gi = rem - cls * ng;
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 if (cls & 1) d.y = -d.y;
                 s_dcls[(row * nc2 + cls) * kMaxGrad + gi] = d;
             }
-            __syncwarp();
+            gsync<TPT>(g);
             for (int s = 5; s >= 0; --s) {
                 // lambda_s (adjoint of K_s) into the lambda slot buffer; Y_s into the input buffer
                 for (int i = lt; i < N; i += TPT) {
@@ -429,9 +433,9 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     for (int l = 0; l < s; ++l) acc += kTab.a[M][s - 1][l] * Kt[static_cast<size_t>(l) * N + i];
                     s_G64[gslot64(i, n)] = s > 0 ? yn_t[i] + h * acc : yn_t[i];
                 }
-                __syncwarp();
+                gsync<TPT>(g);
                 if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + s * nd, s_tab, lt);
-                __syncwarp();
+                gsync<TPT>(g);
                 // mu_s = L(t_s)^T lambda_s on the input-major stream
                 {
                     double br = 0.0, bi = 0.0;
@@ -489,7 +493,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                         pbar[q] += d.x * Sv.x - d.y * Sv.y;
                     }
                 }
-                __syncwarp();
+                gsync<TPT>(g);
             }
             // ybar_n = ybar_{n+1} + sum_s mu_s
             for (int i = lt; i < N; i += TPT) {
@@ -497,41 +501,41 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 for (int s = 0; s < 6; ++s) acc += s_MU[static_cast<size_t>(s) * N + i];
                 s_YB[i] = acc;
             }
-            __syncwarp();
+            gsync<TPT>(g);
             if (segment) add_quadrature(dt);  // the start state y_n
         }
 
         // ---- outputs ----
-#pragma unroll
-        for (int q = 0; q < kMaxGrad; ++q) {
-            double v = pbar[q];
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-            if (lt == 0 && q < ng) J.param_grad[traj * ng + q] = v;
+        for (int q = 0; q < ng; ++q) {
+            const double v = group_sum<TPT>(pbar[q], s_red, lt, g);
+            if (lt == 0) J.param_grad[traj * ng + q] = v;
         }
         if (J.rho0_grad)
             for (int i = lt; i < N; i += TPT) J.rho0_grad[traj * N + i] = s_YB[i];
-        bad = static_cast<int>(__reduce_or_sync(0xffffffffu, static_cast<unsigned>(bad)));
-        if (lt == 0) J.adj_status[traj] = bad ? ADJ_HELPER_DERIVATIVE : ADJ_OK;
-        __syncwarp();
+        const double any_bad = group_sum<TPT>(bad ? 1.0 : 0.0, s_red, lt, g);
+        if (lt == 0) J.adj_status[traj] = any_bad > 0.0 ? ADJ_HELPER_DERIVATIVE : ADJ_OK;
+        gsync<TPT>(g);
     }
 }
 
-template <int EPT>
+template <int TPT, int EPT>
 cudaError_t launch_adjoint_shape(const DevPlan& P, const CallArgs& A, const AdjArgs& J, int blocks, int gpb, size_t smem,
                                  size_t group_bytes, int method, cudaStream_t stream) {
-    auto k = adjoint_kernel<EPT>;
+    auto k = adjoint_kernel<TPT, EPT>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    k<<<blocks, gpb * 32, smem, stream>>>(P, A, J, gpb, group_bytes, method);
+    k<<<blocks, gpb * TPT, smem, stream>>>(P, A, J, gpb, group_bytes, method);
     return cudaGetLastError();
 }
 
+// the adjoint widths (the integrator shapes below 256 threads per trajectory)
+#define OBE_FOR_EACH_ADJOINT(X) X(32, 8) X(32, 16) X(64, 16) X(128, 16)
 #ifndef OBE_INSTANCE_TU
-extern template cudaError_t launch_adjoint_shape<8>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, size_t, size_t, int,
-                                                    cudaStream_t);
-extern template cudaError_t launch_adjoint_shape<16>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, size_t, size_t, int,
-                                                     cudaStream_t);
+#define OBE_EXTERN_ADJOINT(T, E)                                                                                      \
+    extern template cudaError_t launch_adjoint_shape<T, E>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, \
+                                                           size_t, size_t, int, cudaStream_t);
+OBE_FOR_EACH_ADJOINT(OBE_EXTERN_ADJOINT)
+#undef OBE_EXTERN_ADJOINT
 #endif
 
 }  // namespace obe

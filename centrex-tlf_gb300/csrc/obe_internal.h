@@ -129,6 +129,12 @@ struct HostPacked {
     std::vector<int32_t> formula_ptr, prod_class;
     std::vector<double> prod_factor;
     std::vector<float> prod_factor32;
+    // width-independent record lists, laid out for a number of threads per trajectory by
+    // lay_out_lanes: per output (upper index) its gather words without the flush bit, per input
+    // slot its transposed words; *_lane_word is the lane_out / lane_in word of each
+    std::vector<int64_t> g_ptr, t_ptr;  // [U + 1]
+    std::vector<uint32_t> g_word, t_word, g_lane_word, t_lane_word;
+    // the lane layout of the current width
     std::vector<uint32_t> rec, lane_out;
     std::vector<uint32_t> fstream;  // 4 words per entry
     std::vector<uint32_t> trec, lane_in;
@@ -162,6 +168,8 @@ struct obe_plan {
     // global stage buffers of large systems (grow-only)
     void* d_gk = nullptr;
     size_t gk_bytes = 0;
+    // launch shape fixed by obe_plan_set_shape / obe_plan_autotune (0: the automatic choice)
+    int32_t shape_tpt = 0, shape_gpb = 0;
 };
 
 namespace obe {
@@ -170,4 +178,6 @@ const char* last_error_cstr();  // the calling thread's last message
 std::string fmt_f64(double v);  // Rust Display of f64
 obe_status pack_plan(const obe_plan_desc* d, obe_plan* p);
 int threads_per_trajectory_for(int32_t n);
+int64_t shape_capacity(int tpt);  // packed elements one trajectory of that compiled width holds (0: none)
+void lay_out_lanes(HostPacked& hp, int tpt);
 }  // namespace obe

@@ -181,7 +181,7 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 //               share their storage
 //   both: ybuf double[N] (outputs, events), VM slot and stack storage for the six VM lanes,
 //   coefficient rows, reduction scratch.
-//   large systems (256 threads per trajectory, n > 45): the stage buffers K (k1, k1f) and ybuf --
+//   large systems (256 or 512 threads per trajectory, n > 45): the stage buffers K (k1, k1f) and ybuf --
 //   and in the mixed form also the refresh buffers tab and G -- live in a per-group slice of
 //   global memory (L2-resident: one trajectory per SM); `gbytes` is the slice's size.
 struct GroupLayout {
@@ -550,7 +550,7 @@ constexpr int kThreadsFp64 = 256;
 constexpr int kThreadsMixed = 352;
 
 template <int TPT, int EPT, bool MIXED>
-__global__ void __launch_bounds__(MIXED && TPT < 256 ? kThreadsMixed : kThreadsFp64, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
+__global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThreadsMixed : kThreadsFp64, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
@@ -1448,7 +1448,7 @@ __global__ void __launch_bounds__(MIXED && TPT < 256 ? kThreadsMixed : kThreadsF
 // One RHS evaluation per state (lindblad_rhs_py), batched; overrides per state.  The mixed
 // form evaluates the products in single precision.
 template <int TPT, bool MIXED>
-__global__ void __launch_bounds__(256) rhs_kernel(const DevPlan P, long long count, const double* ts, const double* ys,
+__global__ void __launch_bounds__(TPT > 256 ? TPT : 256) rhs_kernel(const DevPlan P, long long count, const double* ts, const double* ys,
                                                   int n_ov, const int* ov_slots, const double* ov_vals, double* dys,
                                                   int gpb, size_t group_bytes, int vm_depth, unsigned char* gscratch,
                                                   size_t gstride) {
@@ -1543,8 +1543,8 @@ cudaError_t launch_rhs_shape(const DevPlan& P, long long count, const double* ts
 
 // the integrator shapes (threads per trajectory, elements per thread) and the RHS widths; the
 // build compiles obe_instance.cu once per shape (centrex_tlf_gb300/build.py: SHAPES, RHS_SHAPES)
-#define OBE_FOR_EACH_SHAPE(X) X(32, 8) X(32, 16) X(64, 16) X(128, 16) X(256, 32)
-#define OBE_FOR_EACH_RHS(X) X(32) X(64) X(128) X(256)
+#define OBE_FOR_EACH_SHAPE(X) X(32, 8) X(32, 16) X(64, 16) X(128, 16) X(256, 32) X(512, 16)
+#define OBE_FOR_EACH_RHS(X) X(32) X(64) X(128) X(256) X(512)
 #ifndef OBE_INSTANCE_TU
 #define OBE_EXTERN_SHAPE(T, E)                                                                                          \
     extern template cudaError_t launch_integrate_shape<T, E, false>(const DevPlan&, const CallArgs&, int, int, size_t,   \

@@ -64,13 +64,115 @@ std::string fmt_f64(double v) {
     return out;
 }
 
+int64_t shape_capacity(int tpt) {
+    switch (tpt) {
+        case 32: case 64: case 128: case 512: return static_cast<int64_t>(tpt) * 16;
+        case 256: return 256 * 32;
+        default: return 0;
+    }
+}
+
+// Deals a plan's record lists out onto `tpt` threads of one trajectory: gather outputs (and, for
+// the adjoint, input slots) longest first onto the least-loaded thread, each thread's records in
+// iteration-major order (record it of thread l at it * tpt + l) ending its output with the flush
+// bit; and the time-dependent formulas' products as the mixed form's product stream.
+void lay_out_lanes(HostPacked& hp, int tpt) {
+    const int64_t U = static_cast<int64_t>(hp.g_lane_word.size());
+    auto emit = [&](const std::vector<int64_t>& ptr, const std::vector<uint32_t>& words, const std::vector<uint32_t>& lane_word,
+                    std::vector<uint32_t>& recs, std::vector<uint32_t>& lane_tab, int32_t& n_iter, int32_t& n_lane) {
+        std::vector<int64_t> order(U);
+        std::iota(order.begin(), order.end(), 0);
+        auto cost = [&](int64_t u) { return std::max<int64_t>(1, ptr[u + 1] - ptr[u]); };
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cost(a) > cost(b); });
+        std::vector<int64_t> load(tpt, 0);
+        std::vector<std::vector<int64_t>> lanes(tpt);
+        for (int64_t u : order) {
+            const int lane = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+            lanes[lane].push_back(u);
+            load[lane] += cost(u);
+        }
+        const int64_t iters = U > 0 ? *std::max_element(load.begin(), load.end()) : 0;
+        size_t n_o = 0;
+        for (auto& v : lanes) {
+            std::sort(v.begin(), v.end());
+            n_o = std::max(n_o, v.size());
+        }
+        n_iter = static_cast<int32_t>(iters);
+        n_lane = static_cast<int32_t>(n_o);
+        recs.assign(static_cast<size_t>(iters) * tpt, 0u);  // padding: slot 0, formula 0 (zero)
+        lane_tab.assign(n_o * tpt, 0u);
+        for (int lane = 0; lane < tpt; ++lane) {
+            int64_t it = 0;
+            for (size_t o = 0; o < lanes[lane].size(); ++o) {
+                const int64_t u = lanes[lane][o];
+                lane_tab[o * tpt + lane] = lane_word[u];
+                if (ptr[u + 1] == ptr[u]) {
+                    recs[it * tpt + lane] = kRecFlush;  // an output with no terms stays 0
+                    ++it;
+                    continue;
+                }
+                for (int64_t r = ptr[u]; r < ptr[u + 1]; ++r) {
+                    recs[it * tpt + lane] = words[r] | (r + 1 == ptr[u + 1] ? kRecFlush : 0u);
+                    ++it;
+                }
+            }
+        }
+    };
+    emit(hp.g_ptr, hp.g_word, hp.g_lane_word, hp.rec, hp.lane_out, hp.n_iter, hp.n_out);
+    emit(hp.t_ptr, hp.t_word, hp.t_lane_word, hp.trec, hp.lane_in, hp.n_titer, hp.n_tin);
+
+    // time-dependent formulas as a thread-interleaved product stream (mixed form: each thread
+    // sums its formulas' products and stores the finished entries; formulas are dealt out
+    // longest first onto the least-loaded thread)
+    const int32_t S = hp.n_static_formula, D = hp.n_formula - hp.n_static_formula;
+    auto fsize = [&](int32_t f) { return static_cast<int64_t>(hp.formula_ptr[S + f + 1] - hp.formula_ptr[S + f]); };
+    std::vector<int32_t> forder(D);
+    std::iota(forder.begin(), forder.end(), 0);
+    std::stable_sort(forder.begin(), forder.end(), [&](int32_t a, int32_t b) { return fsize(a) > fsize(b); });
+    std::vector<int64_t> fload(tpt, 0);
+    std::vector<std::vector<int32_t>> lane_f(tpt);
+    for (int32_t f : forder) {
+        const int lane = static_cast<int>(std::min_element(fload.begin(), fload.end()) - fload.begin());
+        lane_f[lane].push_back(f);
+        fload[lane] += std::max<int64_t>(1, fsize(f));
+    }
+    const int64_t n_fiter = D > 0 ? *std::max_element(fload.begin(), fload.end()) : 0;
+    hp.n_fiter = static_cast<int32_t>(n_fiter);
+    hp.fstream.assign(static_cast<size_t>(n_fiter) * tpt * 4, 0u);  // padding: constant 0, no store
+    for (int lane = 0; lane < tpt; ++lane) {
+        int64_t it = 0;
+        for (int32_t f : lane_f[lane]) {
+            const uint32_t fid = static_cast<uint32_t>(1 + S + f);
+            const int64_t p0 = hp.formula_ptr[S + f], len = fsize(f);
+            for (int64_t q = 0; q < std::max<int64_t>(1, len); ++q) {
+                uint32_t* e = &hp.fstream[(static_cast<size_t>(it) * tpt + lane) * 4];
+                float fr = 0.f, fi = 0.f;
+                uint32_t meta = 0u;
+                if (q < len) {
+                    fr = hp.prod_factor32[2 * (p0 + q)];
+                    fi = hp.prod_factor32[2 * (p0 + q) + 1];
+                    meta = static_cast<uint32_t>(hp.prod_class[p0 + q] + 1);
+                }
+                if (q + 1 >= len) meta |= kFStreamFlush | (fid << kFStreamFormulaShift);
+                std::memcpy(&e[0], &fr, 4);
+                std::memcpy(&e[1], &fi, 4);
+                e[2] = meta;
+                ++it;
+            }
+        }
+    }
+    hp.tpt = tpt;
+}
+
 int threads_per_trajectory_for(int32_t n) {
     int64_t N = static_cast<int64_t>(n) * n;
-    int t = N <= 512 ? 32 : N <= 1024 ? 64 : N <= 2048 ? 128 : N <= 8192 ? 256 : 512;
-    // OBE_TPT widens the group (64 or 128 threads per trajectory) for tuning runs
+    int t = N <= 512 ? 32 : N <= 1024 ? 64 : N <= 2048 ? 128 : N <= 8192 ? 256 : 1024;
+    // OBE_TPT picks another compiled width for tuning runs, if its shape holds the state
+    // (elements per trajectory: 16 per thread, 32 at 256 threads)
     if (const char* env = std::getenv("OBE_TPT")) {
         int v = std::atoi(env);
-        if ((v == 64 || v == 128) && v > t) t = v;
+        const int64_t cap = v == 256 ? 256 * 32 : static_cast<int64_t>(v) * 16;
+        if ((v == 32 || v == 64 || v == 128 || v == 256 || v == 512) && cap >= N) t = v;
     }
     return t;
 }
@@ -577,157 +679,54 @@ obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
                 hp.formula_ptr.push_back(static_cast<int32_t>(hp.prod_class.size()));
             }
 
-        // ---- bin-pack outputs onto the threads of one trajectory (longest first) -----------
-        const int tpt = threads_per_trajectory_for(n);
-        hp.tpt = tpt;
-        std::vector<int64_t> order(U);
-        std::iota(order.begin(), order.end(), 0);
-        auto cost = [&](int64_t u) { return std::max<int64_t>(1, static_cast<int64_t>(out_recs[u].size())); };
-        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cost(a) > cost(b); });
-        std::vector<int64_t> load(tpt, 0);
-        std::vector<std::vector<int64_t>> lane_outputs(tpt);
-        for (int64_t u : order) {
-            int lane = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
-            lane_outputs[lane].push_back(u);
-            load[lane] += cost(u);
-        }
-        int64_t n_iter = *std::max_element(load.begin(), load.end());
-        size_t n_out = 0;
-        for (auto& v : lane_outputs) {
-            std::sort(v.begin(), v.end());
-            n_out = std::max(n_out, v.size());
-        }
-        hp.n_iter = static_cast<int32_t>(n_iter);
-        hp.n_out = static_cast<int32_t>(n_out);
-        hp.rec.assign(static_cast<size_t>(n_iter) * tpt, 0u);  // padding: input 0, formula 0 (zero)
-        hp.lane_out.assign(n_out * tpt, 0u);
-        for (int lane = 0; lane < tpt; ++lane) {
-            int64_t it = 0;
-            for (size_t o = 0; o < lane_outputs[lane].size(); ++o) {
-                int64_t u = lane_outputs[lane][o];
-                uint32_t im = u_im[u] < 0 ? kNoImag : static_cast<uint32_t>(u_im[u]);
-                hp.lane_out[o * tpt + lane] = static_cast<uint32_t>(u_re[u]) | (im << 16);
-                const auto& recs = out_recs[u];
-                if (recs.empty()) {
-                    hp.rec[it * tpt + lane] = kRecFlush;  // an output with no terms stays 0
-                    ++it;
-                    continue;
-                }
-                for (size_t r = 0; r < recs.size(); ++r) {
-                    const Rec& rc = recs[r];
-                    uint32_t fid = rc.dynamic ? static_cast<uint32_t>(1 + S + dyn_ids[rc.f]) : static_cast<uint32_t>(1 + static_ids[rc.f]);
-                    // the gather reads 16-byte input slots: diagonal i -> slot i, the (re, im)
-                    // pair at packed index r >= n -> slot n + (r - n) / 2
-                    uint32_t slot = rc.cplx ? static_cast<uint32_t>(n + (rc.in_re - n) / 2) : static_cast<uint32_t>(rc.in_re);
-                    uint32_t w = slot | (fid << kRecCoefShift);
-                    if (rc.cplx) w |= kRecComplex;
-                    if (rc.conj) w |= kRecConj;
-                    if (r + 1 == recs.size()) w |= kRecFlush;
-                    hp.rec[it * tpt + lane] = w;
-                    ++it;
-                }
+        // ---- width-independent record lists ----------------------------------------------
+        // gather: per output u its records (a 16-byte input slot, the formula, complex and
+        // conjugate bits); the gather reads 16-byte input slots: diagonal i -> slot i, the
+        // (re, im) pair at packed index r >= n -> slot n + (r - n) / 2
+        auto fid_of = [&](const Rec& rc) {
+            return rc.dynamic ? static_cast<uint32_t>(1 + S + dyn_ids[rc.f]) : static_cast<uint32_t>(1 + static_ids[rc.f]);
+        };
+        auto slot_of = [&](const Rec& rc) {
+            return rc.cplx ? static_cast<uint32_t>(n + (rc.in_re - n) / 2) : static_cast<uint32_t>(rc.in_re);
+        };
+        hp.g_ptr.assign(U + 1, 0);
+        hp.g_lane_word.assign(U, 0u);
+        hp.g_word.clear();
+        for (int64_t u = 0; u < U; ++u) {
+            const uint32_t im = u_im[u] < 0 ? kNoImag : static_cast<uint32_t>(u_im[u]);
+            hp.g_lane_word[u] = static_cast<uint32_t>(u_re[u]) | (im << 16);
+            for (const Rec& rc : out_recs[u]) {
+                uint32_t w = slot_of(rc) | (fid_of(rc) << kRecCoefShift);
+                if (rc.cplx) w |= kRecComplex;
+                if (rc.conj) w |= kRecConj;
+                hp.g_word.push_back(w);
             }
+            hp.g_ptr[u + 1] = static_cast<int64_t>(hp.g_word.size());
         }
-        // ---- the transposed stream (adjoint): records regrouped by input slot -----------------
+        // transposed (adjoint): the same records regrouped by input slot, each reading the
+        // output slot of its forward record
         {
-            struct TRec { uint32_t out_slot, fid; bool conj; };
-            std::vector<std::vector<TRec>> in_recs(U);  // by input slot
-            std::vector<uint32_t> slot_re(U), slot_im(U);
+            std::vector<std::vector<uint32_t>> in_words(U);
+            hp.t_lane_word.assign(U, 0u);
             for (int64_t u = 0; u < U; ++u) {
                 const uint32_t uslot = u_im[u] < 0 ? static_cast<uint32_t>(u_re[u]) : static_cast<uint32_t>(n + (u_re[u] - n) / 2);
-                slot_re[uslot] = static_cast<uint32_t>(u_re[u]);
-                slot_im[uslot] = u_im[u] < 0 ? kNoImag : static_cast<uint32_t>(u_im[u]);
+                hp.t_lane_word[uslot] = static_cast<uint32_t>(u_re[u]) | ((u_im[u] < 0 ? kNoImag : static_cast<uint32_t>(u_im[u])) << 16);
                 for (const Rec& rc : out_recs[u]) {
-                    uint32_t fid = rc.dynamic ? static_cast<uint32_t>(1 + S + dyn_ids[rc.f]) : static_cast<uint32_t>(1 + static_ids[rc.f]);
-                    uint32_t slot = rc.cplx ? static_cast<uint32_t>(n + (rc.in_re - n) / 2) : static_cast<uint32_t>(rc.in_re);
-                    in_recs[slot].push_back(TRec{uslot, fid, rc.conj});
+                    uint32_t w = uslot | (fid_of(rc) << kRecCoefShift);
+                    if (rc.conj) w |= kRecConj;
+                    in_words[slot_of(rc)].push_back(w);
                 }
             }
-            std::vector<int64_t> iorder(U);
-            std::iota(iorder.begin(), iorder.end(), 0);
-            auto icost = [&](int64_t v) { return std::max<int64_t>(1, static_cast<int64_t>(in_recs[v].size())); };
-            std::stable_sort(iorder.begin(), iorder.end(), [&](int64_t a, int64_t b) { return icost(a) > icost(b); });
-            std::vector<int64_t> iload(tpt, 0);
-            std::vector<std::vector<int64_t>> lane_inputs(tpt);
-            for (int64_t v : iorder) {
-                int lane = static_cast<int>(std::min_element(iload.begin(), iload.end()) - iload.begin());
-                lane_inputs[lane].push_back(v);
-                iload[lane] += icost(v);
-            }
-            const int64_t n_titer = *std::max_element(iload.begin(), iload.end());
-            size_t n_tin = 0;
-            for (auto& v : lane_inputs) {
-                std::sort(v.begin(), v.end());
-                n_tin = std::max(n_tin, v.size());
-            }
-            hp.n_titer = static_cast<int32_t>(n_titer);
-            hp.n_tin = static_cast<int32_t>(n_tin);
-            hp.trec.assign(static_cast<size_t>(n_titer) * tpt, 0u);  // padding: slot 0, formula 0 (zero)
-            hp.lane_in.assign(n_tin * tpt, 0u);
-            for (int lane = 0; lane < tpt; ++lane) {
-                int64_t it = 0;
-                for (size_t o = 0; o < lane_inputs[lane].size(); ++o) {
-                    const int64_t v = lane_inputs[lane][o];
-                    hp.lane_in[o * tpt + lane] = slot_re[v] | (slot_im[v] << 16);
-                    const auto& recs = in_recs[v];
-                    if (recs.empty()) {
-                        hp.trec[it * tpt + lane] = kRecFlush;
-                        ++it;
-                        continue;
-                    }
-                    for (size_t r = 0; r < recs.size(); ++r) {
-                        uint32_t w = recs[r].out_slot | (recs[r].fid << kRecCoefShift);
-                        if (recs[r].conj) w |= kRecConj;
-                        if (r + 1 == recs.size()) w |= kRecFlush;
-                        hp.trec[it * tpt + lane] = w;
-                        ++it;
-                    }
-                }
+            hp.t_ptr.assign(U + 1, 0);
+            hp.t_word.clear();
+            for (int64_t v = 0; v < U; ++v) {
+                hp.t_word.insert(hp.t_word.end(), in_words[v].begin(), in_words[v].end());
+                hp.t_ptr[v + 1] = static_cast<int64_t>(hp.t_word.size());
             }
         }
-
-        // ---- time-dependent formulas as a thread-interleaved product stream -------------------
-        // (mixed form: each thread sums its formulas' products and stores the finished entries;
-        // formulas are dealt out longest first onto the least-loaded thread)
         if (2 * static_cast<int64_t>(p->n_coeff) + 1 > static_cast<int64_t>(kFStreamClassMask))
             fail(OBE_ERR_UNSUPPORTED, "too many Hamiltonian coefficients for the GPU solver");
-        {
-            std::vector<int32_t> forder(D);
-            std::iota(forder.begin(), forder.end(), 0);
-            std::stable_sort(forder.begin(), forder.end(), [&](int32_t a, int32_t b) { return dyn_list[a].size() > dyn_list[b].size(); });
-            std::vector<int64_t> fload(tpt, 0);
-            std::vector<std::vector<int32_t>> lane_f(tpt);
-            for (int32_t f : forder) {
-                int lane = static_cast<int>(std::min_element(fload.begin(), fload.end()) - fload.begin());
-                lane_f[lane].push_back(f);
-                fload[lane] += std::max<int64_t>(1, static_cast<int64_t>(dyn_list[f].size()));
-            }
-            const int64_t n_fiter = D > 0 ? *std::max_element(fload.begin(), fload.end()) : 0;
-            hp.n_fiter = static_cast<int32_t>(n_fiter);
-            hp.fstream.assign(static_cast<size_t>(n_fiter) * tpt * 4, 0u);  // padding: constant 0, no store
-            for (int lane = 0; lane < tpt; ++lane) {
-                int64_t it = 0;
-                for (int32_t f : lane_f[lane]) {
-                    const uint32_t fid = static_cast<uint32_t>(1 + S + f);
-                    const Formula& fl = dyn_list[f];
-                    for (size_t q = 0; q < std::max<size_t>(1, fl.size()); ++q) {
-                        uint32_t* e = &hp.fstream[(static_cast<size_t>(it) * tpt + lane) * 4];
-                        float fr = 0.f, fi = 0.f;
-                        uint32_t meta = 0u;
-                        if (q < fl.size()) {
-                            fr = static_cast<float>(std::get<1>(fl[q]));
-                            fi = static_cast<float>(std::get<2>(fl[q]));
-                            meta = static_cast<uint32_t>(std::get<0>(fl[q]) + 1);
-                        }
-                        if (q + 1 >= fl.size()) meta |= kFStreamFlush | (fid << kFStreamFormulaShift);
-                        std::memcpy(&e[0], &fr, 4);
-                        std::memcpy(&e[1], &fi, 4);
-                        e[2] = meta;
-                        ++it;
-                    }
-                }
-            }
-        }
+        lay_out_lanes(hp, threads_per_trajectory_for(n));
         return OBE_OK;
     } catch (const Fail& f) {
         set_error(f.msg);

@@ -154,10 +154,12 @@ obe_status scratch(obe_plan* p, size_t bytes, unsigned char** out) {
     return OBE_OK;
 }
 
+// elements per thread of the compiled shape of a width (OBE_FOR_EACH_SHAPE): 8 or 16 at 32
+// threads, 32 at 256, 16 otherwise
 int ept_for(int N, int tpt) {
-    if (tpt >= 256) return 32;
-    int need = (N + tpt - 1) / tpt;
-    return need <= 8 ? 8 : 16;
+    if (tpt == 32) return N <= 32 * 8 ? 8 : 16;
+    if (tpt == 256) return 32;
+    return 16;
 }
 
 struct LaunchShape {
@@ -199,9 +201,10 @@ int sm_count() {
     return count;
 }
 
-obe_status plan_launch(const DevPlan& P, bool mixed, long long n_traj, int vm_depth, LaunchShape* s) {
+// gpb_fixed > 0: that many trajectories per CTA (at most what fits), else the automatic choice
+obe_status plan_launch(const DevPlan& P, bool mixed, long long n_traj, int vm_depth, LaunchShape* s, int gpb_fixed = 0) {
     s->tpt = P.tpt;
-    if (s->tpt > 256) {
+    if (s->tpt > 512) {
         set_error("systems with more than 90 states are not supported by this build of the GPU solver");
         return OBE_ERR_UNSUPPORTED;
     }
@@ -219,9 +222,13 @@ obe_status plan_launch(const DevPlan& P, bool mixed, long long n_traj, int vm_de
         set_error("system too large for the GPU solver's shared-memory layout");
         return OBE_ERR_UNSUPPORTED;
     }
-    // fewer groups per CTA when the batch is small, so that every SM gets work
-    long long per_sm = (n_traj + sm_count() - 1) / sm_count();
-    while (gpb > 1 && gpb > per_sm) --gpb;
+    if (gpb_fixed > 0) {
+        gpb = std::min(gpb, gpb_fixed);
+    } else {
+        // fewer groups per CTA when the batch is small, so that every SM gets work
+        long long per_sm = (n_traj + sm_count() - 1) / sm_count();
+        while (gpb > 1 && gpb > per_sm) --gpb;
+    }
     s->gpb = gpb;
     s->smem = plan_bytes + gpb * L.bytes;
     int blocks_per_sm = std::max<int>(1, static_cast<int>(limit / s->smem));
@@ -467,7 +474,7 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
     A.tape_cap = tape_cap;
     A.tape_stride = tape_stride;
     LaunchShape s;
-    obe_status st = plan_launch(p->dev, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s);
+    obe_status st = plan_launch(p->dev, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s, p->shape_gpb);
     if (st != OBE_OK) return st;
     if (s.gstride > 0) {
         unsigned char* gk = nullptr;
@@ -528,6 +535,11 @@ static obe_status ensure_ready(obe_plan* p) {
     return OBE_OK;
 }
 
+static obe_status solve_batch_device_locked(obe_plan* p, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
+                                            int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values,
+                                            int64_t time_count, int64_t width, double* d_values, obe_traj_stats* d_stats,
+                                            void* stream);
+
 obe_status obe_solve_batch_device(const obe_plan* plan_c, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
                                   int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values,
                                   int64_t time_count, int64_t width, double* d_values, obe_traj_stats* d_stats, void* stream) {
@@ -535,6 +547,14 @@ obe_status obe_solve_batch_device(const obe_plan* plan_c, const obe_solve_option
     obe_plan* p = const_cast<obe_plan*>(plan_c);
     if (!p || !opt) { set_error("null argument"); return OBE_ERR_INVALID; }
     std::lock_guard<std::mutex> lock(g_plan_mutex);
+    return solve_batch_device_locked(p, opt, n_traj, d_rho0, n_param_slots, param_slots, d_param_values, time_count, width,
+                                     d_values, d_stats, stream);
+}
+
+static obe_status solve_batch_device_locked(obe_plan* p, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
+                                            int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values,
+                                            int64_t time_count, int64_t width, double* d_values, obe_traj_stats* d_stats,
+                                            void* stream) {
     obe_status st = ensure_ready(p);
     if (st != OBE_OK) return st;
     if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
@@ -553,6 +573,145 @@ obe_status obe_solve_batch_device(const obe_plan* plan_c, const obe_solve_option
     return solve_device(p, opt, n_traj, d_rho0, p->N, n_param_slots, param_slots, d_param_values, 0, nullptr, nullptr, time_count,
                         time_count * width * (cplx ? 2 : 1), d_values, nullptr, d_stats, reinterpret_cast<TrajErr*>(d + errs_off), d,
                         cb, save_times, static_cast<unsigned long long*>(p->d_counter), s);
+}
+
+// ---- launch-shape tuning ---------------------------------------------------------------------
+namespace {
+constexpr int kWidths[] = {32, 64, 128, 256, 512};  // the compiled threads-per-trajectory widths
+
+// Lays the plan's record streams out for `tpt` threads per trajectory; the device image follows
+// on the next solve.
+void relayout(obe_plan* p, int tpt) {
+    if (p->packed.tpt == tpt) return;
+    lay_out_lanes(p->packed, tpt);
+    if (p->d_blob) cudaFree(p->d_blob);
+    p->d_blob = nullptr;
+    p->d_device = -1;
+}
+}  // namespace
+
+obe_status obe_plan_set_shape(obe_plan* p, int32_t tpt, int32_t gpb) {
+    if (!p) { set_error("null argument"); return OBE_ERR_INVALID; }
+    if (tpt != 0 && shape_capacity(tpt) <= 0) {
+        set_error("threads per trajectory must be 0 (automatic) or one of 32, 64, 128, 256, 512");
+        return OBE_ERR_INVALID;
+    }
+    if (tpt != 0 && shape_capacity(tpt) < p->N) {
+        set_error("a trajectory of " + std::to_string(tpt) + " threads holds at most " + std::to_string(shape_capacity(tpt)) +
+                  " packed elements; this system has " + std::to_string(p->N));
+        return OBE_ERR_INVALID;
+    }
+    if (gpb < 0) { set_error("trajectories per CTA must be non-negative"); return OBE_ERR_INVALID; }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    relayout(p, tpt > 0 ? tpt : threads_per_trajectory_for(p->n));
+    p->shape_tpt = tpt;
+    p->shape_gpb = gpb;
+    return OBE_OK;
+}
+
+void obe_plan_get_shape(const obe_plan* p, int32_t* tpt, int32_t* gpb) {
+    if (tpt) *tpt = p ? p->packed.tpt : 0;
+    if (gpb) *gpb = p ? p->shape_gpb : 0;
+}
+
+obe_status obe_plan_autotune(obe_plan* p, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
+                             int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values,
+                             int64_t time_count, int64_t width, int32_t probe_steps, int32_t cand_cap, int32_t* cand_tpt,
+                             int32_t* cand_gpb, float* cand_ms, int32_t* n_cand, void* stream) {
+    g_launches = 0;
+    if (!p || !opt) { set_error("null argument"); return OBE_ERR_INVALID; }
+    if (n_traj <= 0) { set_error("autotuning needs a non-empty batch"); return OBE_ERR_INVALID; }
+    if (probe_steps < 1) { set_error("probe_steps must be positive"); return OBE_ERR_INVALID; }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    const int gpb_before = p->shape_gpb;
+    obe_status st = ensure_ready(p);
+    if (st != OBE_OK) return st;
+    if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
+    std::vector<double> save_times;
+    CallBlob cb;
+    int64_t w = 0;
+    int cplx = 0;
+    if ((st = validate_options(p, opt, save_times, cb, &w, &cplx)) != OBE_OK) return st;
+    if (w != width) { set_error("output width mismatch"); return OBE_ERR_INVALID; }
+    const bool mixed = opt->precision == OBE_PRECISION_MIXED;
+    const int vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
+    // candidates: the automatic width and the wider compiled ones up to 4x it, in the same
+    // memory layout; each with as many trajectories per CTA as fit, half of that, and one
+    const int w0 = threads_per_trajectory_for(p->n);
+    std::vector<std::pair<int, int>> cands;
+    for (int tw : kWidths) {
+        if (tw < w0 || tw > 4 * w0 || shape_capacity(tw) < p->N || (tw >= 256) != (w0 >= 256)) continue;
+        relayout(p, tw);
+        if ((st = ensure_ready(p)) != OBE_OK) return st;
+        LaunchShape s;
+        if (plan_launch(p->dev, mixed, n_traj, vm_depth, &s, 1 << 20) != OBE_OK) continue;
+        std::vector<int> gs = {s.gpb, (s.gpb + 1) / 2, 1};
+        std::sort(gs.begin(), gs.end());
+        gs.erase(std::unique(gs.begin(), gs.end()), gs.end());
+        for (int g : gs) cands.emplace_back(tw, g);
+    }
+    if (cands.empty()) {
+        relayout(p, p->shape_tpt > 0 ? p->shape_tpt : w0);
+        set_error("no compiled launch shape holds this system");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    const size_t vals = static_cast<size_t>(n_traj) * static_cast<size_t>(std::max<int64_t>(time_count, 1)) *
+                        static_cast<size_t>(std::max<int64_t>(width, 1)) * (cplx ? 2 : 1);
+    double* d_vals = nullptr;
+    obe_traj_stats* d_st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        if (d_vals) cudaFree(d_vals);
+        if (d_st) cudaFree(d_st);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    if (!cuda_ok(cudaMalloc(&d_vals, vals * sizeof(double)), "cudaMalloc(probe values)") ||
+        !cuda_ok(cudaMalloc(&d_st, static_cast<size_t>(n_traj) * sizeof(obe_traj_stats)), "cudaMalloc(probe stats)") ||
+        !cuda_ok(cudaEventCreate(&e0), "cudaEventCreate") || !cuda_ok(cudaEventCreate(&e1), "cudaEventCreate")) {
+        cleanup();
+        relayout(p, p->shape_tpt > 0 ? p->shape_tpt : w0);
+        return OBE_ERR_CUDA;
+    }
+    obe_solve_options probe = *opt;
+    probe.maxiters = probe_steps;
+    cudaStream_t sm = static_cast<cudaStream_t>(stream);
+    std::vector<float> ms(cands.size(), 0.f);
+    long long launches = 0;
+    size_t best = 0;
+    for (size_t c = 0; c < cands.size(); ++c) {
+        relayout(p, cands[c].first);
+        p->shape_gpb = cands[c].second;
+        for (int rep = 0; rep < 2 && st == OBE_OK; ++rep) {  // one untimed run, one timed
+            if (rep == 1 && !cuda_ok(cudaEventRecord(e0, sm), "cudaEventRecord")) st = OBE_ERR_CUDA;
+            if (st == OBE_OK)
+                st = solve_batch_device_locked(p, &probe, n_traj, d_rho0, n_param_slots, param_slots, d_param_values, time_count,
+                                               width, d_vals, d_st, stream);
+            launches += g_launches;
+            if (st == OBE_OK && rep == 1 && !cuda_ok(cudaEventRecord(e1, sm), "cudaEventRecord")) st = OBE_ERR_CUDA;
+        }
+        if (st == OBE_OK && !cuda_ok(cudaEventSynchronize(e1), "probe solve")) st = OBE_ERR_CUDA;
+        if (st == OBE_OK && !cuda_ok(cudaEventElapsedTime(&ms[c], e0, e1), "cudaEventElapsedTime")) st = OBE_ERR_CUDA;
+        if (st != OBE_OK) break;
+        if (ms[c] < ms[best]) best = c;
+    }
+    cleanup();
+    if (st != OBE_OK) {
+        relayout(p, p->shape_tpt > 0 ? p->shape_tpt : w0);
+        p->shape_gpb = gpb_before;
+        return st;
+    }
+    relayout(p, cands[best].first);
+    p->shape_tpt = cands[best].first;
+    p->shape_gpb = cands[best].second;
+    if (n_cand) *n_cand = static_cast<int32_t>(cands.size());
+    for (size_t c = 0; c < cands.size() && static_cast<int32_t>(c) < cand_cap; ++c) {
+        if (cand_tpt) cand_tpt[c] = cands[c].first;
+        if (cand_gpb) cand_gpb[c] = cands[c].second;
+        if (cand_ms) cand_ms[c] = ms[c];
+    }
+    g_launches = launches;
+    return OBE_OK;
 }
 
 // Streams of the heterogeneous batch: one non-blocking stream and completion event per job
@@ -642,7 +801,8 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
         if (w != q.j->width) { set_error("output width mismatch"); return fail(k, OBE_ERR_INVALID); }
         LaunchShape s;
         const int vm_depth = std::max(q.p->dev.max_stack, std::max(q.cb.ev_len, 1));
-        if ((st = plan_launch(q.p->dev, q.j->opt->precision == OBE_PRECISION_MIXED, std::max<int64_t>(q.j->n_traj, 1), vm_depth, &s)) != OBE_OK)
+        if ((st = plan_launch(q.p->dev, q.j->opt->precision == OBE_PRECISION_MIXED, std::max<int64_t>(q.j->n_traj, 1), vm_depth, &s,
+                              q.p->shape_gpb)) != OBE_OK)
             return fail(k, st);
         q.errs_off = align16(q.cb.bytes.size());
         size_t need = q.errs_off + sizeof(TrajErr) * static_cast<size_t>(std::max<int64_t>(q.j->n_traj, 1));
@@ -869,8 +1029,10 @@ static obe_status grad_check(const obe_plan* p, const obe_solve_options* o, int6
         set_error("gradients through a stop_event are not supported");
         return OBE_ERR_UNSUPPORTED;
     }
-    if (p->packed.tpt != 32) {
-        set_error("gradients are implemented for systems of up to 22 states");
+    if (p->packed.tpt > 128) {
+        set_error(threads_per_trajectory_for(p->n) <= 128
+                      ? "gradients need the plan at 128 threads per trajectory or fewer: call obe_plan_set_shape"
+                      : "gradients are implemented for systems of up to 45 states");
         return OBE_ERR_UNSUPPORTED;
     }
     if (o->output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !o->store_trace && !o->has_saveat) {
@@ -978,10 +1140,11 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     J.adj_status = d_adj_status;
     J.counter = static_cast<unsigned long long*>(p->d_counter);
     const DevPlan& P = p->dev;
-    const size_t plan_bytes = adj_plan_smem_bytes(P);
-    const size_t group = adj_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth).bytes;
+    const int tpt = P.tpt;
+    const size_t plan_bytes = adj_plan_smem_bytes(P, tpt);
+    const size_t group = adj_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, tpt).bytes;
     const size_t limit = 227 * 1024;
-    int gpb = 8;
+    int gpb = 256 / tpt;
     while (gpb > 1 && plan_bytes + gpb * group > limit) --gpb;
     if (plan_bytes + gpb * group > limit) { set_error("system too large for the adjoint's shared-memory layout"); return OBE_ERR_UNSUPPORTED; }
     const long long per_sm = (n_traj + sm_count() - 1) / sm_count();
@@ -990,9 +1153,12 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n_traj + gpb - 1) / gpb, sm_count())));
     if (!cuda_ok(cudaMemsetAsync(J.counter, 0, sizeof(unsigned long long), s), "cudaMemsetAsync")) return OBE_ERR_CUDA;
     const int method = opt->solver == OBE_SOLVER_TSIT5 ? 1 : 0;
-    const int ept = ept_for(P.N, 32);
-    cudaError_t e = ept == 8 ? launch_adjoint_shape<8>(P, A, J, blocks, gpb, smem, group, method, s)
-                             : launch_adjoint_shape<16>(P, A, J, blocks, gpb, smem, group, method, s);
+    const int ept = ept_for(P.N, tpt);
+    cudaError_t e = cudaErrorInvalidConfiguration;
+#define OBE_ADJ_DISPATCH(T, E) \
+    if (tpt == T && ept == E) e = launch_adjoint_shape<T, E>(P, A, J, blocks, gpb, smem, group, method, s);
+    OBE_FOR_EACH_ADJOINT(OBE_ADJ_DISPATCH)
+#undef OBE_ADJ_DISPATCH
     if (!cuda_ok(e, "adjoint kernel launch")) return OBE_ERR_CUDA;
     g_launches += 1;
     set_error("");
@@ -1156,7 +1322,7 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
 
     const bool mixed = opt->precision == OBE_PRECISION_MIXED;
     LaunchShape shape;
-    if ((st = plan_launch(P, mixed, n_traj, A.vm_depth, &shape)) != OBE_OK) return st;
+    if ((st = plan_launch(P, mixed, n_traj, A.vm_depth, &shape, p->shape_gpb)) != OBE_OK) return st;
     if (shape.gstride > 0) {
         set_error("systems with more than 45 states keep per-trajectory stage buffers in device memory the library "
                   "allocates; solve them with obe_solve_batch_device");

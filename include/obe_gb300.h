@@ -238,6 +238,38 @@ obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options*
                                   obe_traj_stats* d_stats, void* stream);
 
 /*
+ * Launch-shape tuning (no counterpart in the reference, whose CPU path has no launch shape).
+ * A solve runs each trajectory on a group of threads (32, 64, 128, 256 or 512: the compiled
+ * widths; 16 packed elements per thread, 32 at 256 threads) and puts one or more groups in a
+ * CTA.  By default the width is the smallest that holds the state (256 above 2,048 elements)
+ * and a CTA takes as many groups as its shared memory fits, fewer for small batches.
+ *
+ * obe_plan_set_shape fixes both for every later solve of the plan: threads_per_trajectory 0 is
+ * the default rule; trajectories_per_cta 0 is the automatic count, otherwise at most what fits.
+ * A width that cannot hold the state is rejected.  Results of different widths differ by
+ * rounding (another summation order), statistics by the steps that rounding moves.
+ * obe_plan_get_shape reads the width in use and the fixed trajectories per CTA (0: automatic).
+ *
+ * obe_plan_autotune measures candidate shapes on a probe of the caller's own batch (arguments as
+ * obe_solve_batch_device) and fixes the fastest, as obe_plan_set_shape would.  Each candidate
+ * solves the batch with maxiters capped at probe_steps, once untimed and once timed with CUDA
+ * events on `stream`.  Candidates: the default width and the wider compiled widths up to 4x it
+ * in the same memory layout (stage buffers on chip below 256 threads, in device memory from
+ * 256), each with as many trajectories per CTA as fit, half that, and one.  The candidates and
+ * their probe times (ms) go to cand_tpt / cand_gpb / cand_ms (up to cand_cap entries; n_cand
+ * receives the count).  Synchronises `stream`; allocates and frees its probe outputs.
+ * Gradients need a plan width of 128 threads or fewer.  None of these may run while a solve of
+ * the same plan is in flight on another thread.
+ */
+obe_status obe_plan_set_shape(obe_plan* plan, int32_t threads_per_trajectory, int32_t trajectories_per_cta);
+void obe_plan_get_shape(const obe_plan* plan, int32_t* threads_per_trajectory, int32_t* trajectories_per_cta);
+obe_status obe_plan_autotune(obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
+                             const double* d_rho0, int32_t n_param_slots, const int64_t* param_slots,
+                             const double* d_param_values, int64_t time_count, int64_t width,
+                             int32_t probe_steps, int32_t cand_cap, int32_t* cand_tpt,
+                             int32_t* cand_gpb, float* cand_ms, int32_t* n_cand, void* stream);
+
+/*
  * Heterogeneous batch (no counterpart in the reference, which solves one prepared plan per
  * call, ode_batch.rs:176-351): several device-resident batches, each on its own plan (systems
  * of different sizes, different options, parameter slots and outputs), solved by one call.
@@ -271,7 +303,8 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
  * discrete adjoint of the double-precision adaptive solve with its step sequence frozen, for
  * final weighted integrals (output_when="final", saveat None) and final populations, with
  * respect to base parameter slots and the initial state.  Device pointers, asynchronous on
- * `stream`; systems of up to 22 states, dopri5/tsit5, no stop event.
+ * `stream`; systems of up to 45 states (a plan width of 128 threads or fewer), dopri5/tsit5, no
+ * stop event.
  *
  * obe_grad_forward is obe_solve_batch_device that also records, per trajectory, every accepted
  * step (start time, size, start state, stage derivatives 1-6) into d_tape:

@@ -139,6 +139,26 @@ def test_multi_batch_validation_before_device_work(golden):
     assert lib.obe_solve_multi_device(0, None, None) == _abi.OBE_OK
 
 
+def test_launch_shape_validation_on_host(golden):
+    """obe_plan_set_shape accepts the compiled widths that hold the state and re-lays the plan's
+    record streams out for them (host work only)."""
+    q = NativePlan(golden("plan_q1_16")["payload"])
+    assert q.shape() == (32, 0)
+    for t, g in ((64, 0), (128, 2), (512, 1), (0, 0)):
+        q.set_shape(t, g)
+        assert q.shape() == ((t or 32), g)
+    with pytest.raises(ValueError, match="threads per trajectory must be 0"):
+        q.set_shape(48, 0)
+    with pytest.raises(ValueError, match="trajectories per CTA must be non-negative"):
+        q.set_shape(64, -1)
+    big = NativePlan(golden("plan_chain45")["payload"])
+    assert big.shape() == (128, 0)
+    with pytest.raises(ValueError, match="a trajectory of 64 threads holds at most 1024 packed elements; this system has 2025"):
+        big.set_shape(64, 0)
+    big.set_shape(256, 0)
+    assert big.shape() == (256, 0)
+
+
 def test_no_cpu_fallback_without_gpu(golden):
     """Without a CUDA device the solver refuses instead of computing on the CPU."""
     if _abi.load_library().obe_device_count() > 0:

@@ -103,6 +103,63 @@ def test_parameter_gradients_match_frozen_step_finite_differences(q1, solver, ou
         assert np.all(np.abs(grad[:, k] - fd) <= tol), (k, grad[:, k], fd, tol)
 
 
+def _fd_check(d, plan, op, p0, slots, solver="tsit5", t_span=None, weights=None):
+    """Gradients of the excited-population integral against central differences of the oracle's
+    replay of the frozen steps (the bar of the test above)."""
+    g = d["gamma"]
+    t_span = d["t_span"] if t_span is None else t_span
+    w = weights if weights is not None else [(i, 1.0) for i in d["excited_indices"]]
+    b = p0.shape[0]
+    params = torch.tensor(p0, dtype=torch.float64, device="cuda", requires_grad=True)
+    out, tape = solve_batch_with_grad(plan, d["rho0_packed"], t_span, params, slots, solver=solver, dt=1e-3 / g,
+                                      integral_weights=w, return_tape=True)
+    out.sum().backward()
+    grad = params.grad.cpu().numpy()
+    steps = tape.steps()
+    o = op.options(t0=t_span[0], t1=t_span[1], abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=None, save_start=True,
+                   maxiters=100000, solver=solver, output="excited_population", output_indices=None,
+                   output_when="final", integral_weights=w, stop_event=None)
+
+    def replay(p):
+        return np.asarray(op.solve_replay(o, d["rho0_packed"], slots, p.astype(complex), steps)).reshape(b)
+
+    base = replay(p0)
+    np.testing.assert_allclose(base, out.detach().cpu().numpy().reshape(-1), rtol=1e-10, atol=1e-22)
+    for k in range(p0.shape[1]):
+        eps = 1e-6 * np.abs(p0[:, k])
+        eps[eps == 0] = 1e-6 * g
+        pp, pm = p0.copy(), p0.copy()
+        pp[:, k] += eps
+        pm[:, k] -= eps
+        fd = (replay(pp) - replay(pm)) / (2 * eps)
+        tol = 1e-5 * np.abs(fd) + 1e-8 * np.abs(base) / np.maximum(np.abs(p0[:, k]), 1e-300)
+        assert np.all(np.abs(grad[:, k] - fd) <= tol), (k, grad[:, k], fd, tol)
+
+
+@pytest.mark.parametrize("tpt", [64, 128])
+def test_gradients_at_wider_launch_shapes(q1, tpt):
+    """The 16-state plan laid out for 64 or 128 threads per trajectory (what the autotuner picks
+    for small batches): the adjoint runs at that width too and matches the finite differences."""
+    d, plan, op = q1
+    plan.set_shape(tpt, 0)
+    try:
+        _fd_check(d, plan, op, _params(d)[:3], _slots(d))
+    finally:
+        plan.set_shape(0, 0)
+
+
+def test_gradients_of_the_39_state_system(golden):
+    """X J=0-2 + B (39 states, 128 threads per trajectory): gradients with respect to the peak
+    Rabi rate, detuning, polarisation angle and pulse centre over [0, 150/Γ]."""
+    d = golden("plan_r0_39")
+    g = d["gamma"]
+    plan = NativePlan(d["payload"])
+    assert plan.shape()[0] == 128
+    op = oracle.OraclePlan(d["payload"])
+    p0 = np.array([[1.5 * g, 0.5 * g, 0.4, 70.0 / g], [4.0 * g, -1.0 * g, 1.2, 75.0 / g]])
+    _fd_check(d, plan, op, p0, _slots(d), t_span=(0.0, 150.0 / g))
+
+
 def test_initial_state_gradient_matches_finite_differences(q1):
     d, plan, op = q1
     g = d["gamma"]
