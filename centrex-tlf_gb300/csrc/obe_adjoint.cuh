@@ -255,7 +255,7 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
 }
 
 __host__ __device__ inline size_t adj_plan_smem_bytes(const DevPlan& P, int tpt) {
-    return align16(static_cast<size_t>(P.n_iter + P.n_out + P.n_titer + P.n_tin) * tpt * 4);
+    return align16(static_cast<size_t>(P.n_biter + P.n_titer + P.n_tin) * tpt * 4);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -269,12 +269,10 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
     const int n = P.n, N = P.N, U = P.U;
-    uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem);
-    uint32_t* s_out = s_rec + static_cast<size_t>(P.n_iter) * TPT;
-    uint32_t* s_trec = s_out + static_cast<size_t>(P.n_out) * TPT;
+    uint32_t* s_bil = reinterpret_cast<uint32_t*>(smem);
+    uint32_t* s_trec = s_bil + static_cast<size_t>(P.n_biter) * TPT;
     uint32_t* s_lin = s_trec + static_cast<size_t>(P.n_titer) * TPT;
-    for (int i = threadIdx.x; i < P.n_iter * TPT; i += blockDim.x) s_rec[i] = P.rec[i];
-    for (int i = threadIdx.x; i < P.n_out * TPT; i += blockDim.x) s_out[i] = P.lane_out[i];
+    for (int i = threadIdx.x; i < P.n_biter * TPT; i += blockDim.x) s_bil[i] = P.bil[i];
     for (int i = threadIdx.x; i < P.n_titer * TPT; i += blockDim.x) s_trec[i] = P.trec[i];
     for (int i = threadIdx.x; i < P.n_tin * TPT; i += blockDim.x) s_lin[i] = P.lane_in[i];
     __syncthreads();
@@ -459,31 +457,33 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                         }
                     }
                 }
-                // lambda_s^T (dL/dp) Y_s: per-class sums of factor * Y_in' * conj(lambda_out)
+                // lambda_s^T (dL/dp) Y_s: per-class sums of factor * Y_in' * conj(lambda_out), formula
+                // by formula: z = sum over the formula's records of Y_in' conj(lambda_out), then
+                // each of its class products adds factor * z
                 for (int c = 0; c < nc2; ++c) s_S[c * TPT + lt] = make_double2(0.0, 0.0);
                 {
-                    int o = 0;
-                    for (int it = 0; it < P.n_iter; ++it) {
-                        const uint32_t w = s_rec[it * TPT + lt];
-                        const int f = static_cast<int>(w >> kRecCoefShift);
-                        if (f > 0) {
-                            double2 a = s_G[w & kRecIndexMask];
-                            if (w & kRecConj) a.y = -a.y;
-                            const uint32_t d = s_out[o * TPT + lt];
-                            const int re = static_cast<int>(d & 0xFFFFu);
-                            const int oslot = re < n ? re : n + (re - n) / 2;
-                            const double2 lam = s_LS[oslot];
-                            const double2 z = cmul(a, make_double2(lam.x, -lam.y));
+                    double zr = 0.0, zi = 0.0;
+                    for (int it = 0; it < P.n_biter; ++it) {
+                        const uint32_t w = s_bil[it * TPT + lt];
+                        if (w & kBilEnd) {
+                            const int f = static_cast<int>(w & ~kBilEnd);
                             for (int p = P.formula_ptr[f - 1]; p < P.formula_ptr[f]; ++p) {
                                 const int cls = P.prod_class[p];
                                 if (cls < 0) continue;
-                                const double2 v = cmul(make_double2(P.prod_factor[2 * p], P.prod_factor[2 * p + 1]), z);
+                                const double fr = P.prod_factor[2 * p], fi = P.prod_factor[2 * p + 1];
                                 double2& acc = s_S[cls * TPT + lt];
-                                acc.x += v.x;
-                                acc.y += v.y;
+                                acc.x += fr * zr - fi * zi;
+                                acc.y += fr * zi + fi * zr;
                             }
+                            zr = 0.0;
+                            zi = 0.0;
+                        } else {
+                            double2 a = s_G[w & kBilSlotMask];
+                            if (w & kBilConj) a.y = -a.y;
+                            const double2 lam = s_LS[(w >> kBilOutShift) & kBilSlotMask];
+                            zr += a.x * lam.x + a.y * lam.y;
+                            zi += a.y * lam.x - a.x * lam.y;
                         }
-                        if (w & kRecFlush) ++o;
                     }
                 }
                 for (int c = 0; c < nc2; ++c) {

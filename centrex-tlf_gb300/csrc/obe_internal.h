@@ -48,6 +48,13 @@ constexpr uint32_t kFStreamFlush = 1u << 12;
 constexpr int kFStreamFormulaShift = 13;
 constexpr uint32_t kMaxFormulas = (1u << 15) - 1;
 constexpr uint32_t kNoImag = 0xFFFFu;
+// formula-major stream of the adjoint's parameter pass: record entries (input slot [0, 14),
+// output slot [14, 28), conjugate input bit 28) follow each other per formula, then a formula
+// entry (bit 31, formula index in the low bits) closes the formula
+constexpr uint32_t kBilSlotMask = 0x3FFFu;
+constexpr int kBilOutShift = 14;
+constexpr uint32_t kBilConj = 1u << 28;
+constexpr uint32_t kBilEnd = 1u << 31;
 
 // Device view of a packed plan.  All pointers point into one device allocation.
 struct DevPlan {
@@ -108,6 +115,10 @@ struct DevPlan {
     const uint32_t* trec;        // [n_titer * tpt]
     int32_t n_tin;
     const uint32_t* lane_in;     // [n_tin * tpt]
+    // the adjoint's parameter pass: the records of every formula with a parameter-dependent
+    // product, formula-major and thread-interleaved (kBil* entries)
+    int32_t n_biter;
+    const uint32_t* bil;         // [n_biter * tpt]
 };
 
 // Host-side result of packing (owned by obe_plan).
@@ -139,6 +150,8 @@ struct HostPacked {
     std::vector<uint32_t> fstream;  // 4 words per entry
     std::vector<uint32_t> trec, lane_in;
     int32_t n_titer = 0, n_tin = 0;
+    std::vector<uint32_t> bil;
+    int32_t n_biter = 0;
     int32_t n_iter = 0, n_out = 0, tpt = 32, n_fiter = 0;
     int32_t n_formula = 0, n_static_formula = 0;
     int32_t max_stack = 0;

@@ -121,6 +121,57 @@ void lay_out_lanes(HostPacked& hp, int tpt) {
     emit(hp.g_ptr, hp.g_word, hp.g_lane_word, hp.rec, hp.lane_out, hp.n_iter, hp.n_out);
     emit(hp.t_ptr, hp.t_word, hp.t_lane_word, hp.trec, hp.lane_in, hp.n_titer, hp.n_tin);
 
+    // the adjoint's parameter pass, formula-major: every formula with a product of a coefficient
+    // class, followed by the records that use it (input slot, output slot, conjugate bit); the
+    // formulas are dealt out longest first onto the least-loaded thread and each ends with its
+    // formula entry
+    {
+        int64_t n = 0;
+        while (n * (n + 1) / 2 < U) ++n;  // U = n (n + 1) / 2
+        const int32_t F = hp.n_formula;
+        std::vector<uint8_t> parametric(static_cast<size_t>(F) + 1, 0);
+        for (int32_t f = 1; f <= F; ++f)
+            for (int32_t q = hp.formula_ptr[f - 1]; q < hp.formula_ptr[f]; ++q)
+                if (hp.prod_class[q] >= 0) parametric[f] = 1;
+        std::vector<std::vector<uint32_t>> frecs(static_cast<size_t>(F) + 1);
+        for (int64_t u = 0; u < U; ++u) {
+            const int64_t re = static_cast<int64_t>(hp.g_lane_word[u] & 0xFFFFu);
+            const uint32_t oslot = static_cast<uint32_t>(re < n ? re : n + (re - n) / 2);
+            for (int64_t r = hp.g_ptr[u]; r < hp.g_ptr[u + 1]; ++r) {
+                const uint32_t w = hp.g_word[r];
+                const uint32_t f = w >> kRecCoefShift;
+                if (f == 0 || f > static_cast<uint32_t>(F) || !parametric[f]) continue;
+                uint32_t e = (w & kRecIndexMask) | (oslot << kBilOutShift);
+                if (w & kRecConj) e |= kBilConj;
+                frecs[f].push_back(e);
+            }
+        }
+        std::vector<int32_t> forder;
+        for (int32_t f = 1; f <= F; ++f)
+            if (!frecs[f].empty()) forder.push_back(f);
+        auto fcost = [&](int32_t f) {
+            return static_cast<int64_t>(frecs[f].size()) + 1 + (hp.formula_ptr[f] - hp.formula_ptr[f - 1]);
+        };
+        std::stable_sort(forder.begin(), forder.end(), [&](int32_t a, int32_t b) { return fcost(a) > fcost(b); });
+        std::vector<int64_t> bload(tpt, 0);
+        std::vector<std::vector<int32_t>> lane_fs(tpt);
+        for (int32_t f : forder) {
+            const int lane = static_cast<int>(std::min_element(bload.begin(), bload.end()) - bload.begin());
+            lane_fs[lane].push_back(f);
+            bload[lane] += static_cast<int64_t>(frecs[f].size()) + 1;
+        }
+        const int64_t n_biter = forder.empty() ? 0 : *std::max_element(bload.begin(), bload.end());
+        hp.n_biter = static_cast<int32_t>(n_biter);
+        hp.bil.assign(static_cast<size_t>(n_biter) * tpt, 0u);  // padding: a record after the last formula, never closed
+        for (int lane = 0; lane < tpt; ++lane) {
+            int64_t it = 0;
+            for (int32_t f : lane_fs[lane]) {
+                for (uint32_t e : frecs[f]) hp.bil[static_cast<size_t>(it++) * tpt + lane] = e;
+                hp.bil[static_cast<size_t>(it++) * tpt + lane] = kBilEnd | static_cast<uint32_t>(f);
+            }
+        }
+    }
+
     // time-dependent formulas as a thread-interleaved product stream (mixed form: each thread
     // sums its formulas' products and stores the finished entries; formulas are dealt out
     // longest first onto the least-loaded thread)

@@ -61,7 +61,7 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     size_t o_pp = put(blob, h.pchip_ptr), o_pg = put(blob, h.pchip_grid), o_pc = put(blob, h.pchip_coef), o_pcp = put(blob, h.pchip_cptr);
     size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
     size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out), o_fs = put(blob, h.fstream);
-    size_t o_tr = put(blob, h.trec), o_li = put(blob, h.lane_in);
+    size_t o_tr = put(blob, h.trec), o_li = put(blob, h.lane_in), o_bil = put(blob, h.bil);
     P = DevPlan{};
     P.n = p->n;
     P.N = static_cast<int32_t>(p->N);
@@ -113,6 +113,8 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     P.trec = reinterpret_cast<const uint32_t*>(base + o_tr);
     P.n_tin = h.n_tin;
     P.lane_in = reinterpret_cast<const uint32_t*>(base + o_li);
+    P.n_biter = h.n_biter;
+    P.bil = reinterpret_cast<const uint32_t*>(base + o_bil);
 }
 
 obe_status upload_plan(obe_plan* p) {
