@@ -553,6 +553,73 @@ def run_gpu(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+def run_case(args) -> None:
+    """One workload on its own, for profiling: `gradient` (the adjoint workload at a fixed launch
+    width), `heterogeneous` (the 16/39/76-state batch) or `large` (one wave of 76-state
+    trajectories, end times U[15, 20]/Γ).  Runs it `--steps` times and prints the times."""
+    import torch
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    times = []
+    if args.case == "heterogeneous":
+        r = measure_heterogeneous(torch, dev, total=args.points, reps=max(1, args.steps))
+        print(json.dumps({"case": args.case, **r}))
+        return
+    if args.case == "gradient":
+        from centrex_tlf_gb300.autograd import solve_batch_with_grad
+        from centrex_tlf_gb300.native import NativePlan
+
+        d, params_all, _ = workload(max(args.points, 1))
+        gamma, (t0, t1) = d["gamma"], d["t_span"]
+        names = d["payload"]["parameter_graph"]["slot_names"]
+        slots = [names.index(s) for s in ("rabi", "detuning", "theta", "t_center")]
+        p = np.concatenate([params_all.real, np.full((params_all.shape[0], 1), 100.0 / gamma)], axis=1)
+        plan = NativePlan(d["payload"])
+        plan.set_shape(args.threads_per_trajectory, 0)
+        for _ in range(args.steps):
+            pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
+            start = time.perf_counter()
+            j = solve_batch_with_grad(plan, d["rho0_packed"], (t0, t1), pt, slots, dt=1e-3 / gamma,
+                                      integral_weights=W_EXCITED, max_steps=2048)
+            j.sum().backward()
+            torch.cuda.synchronize()
+            times.append(1e3 * (time.perf_counter() - start))
+            assert bool(torch.isfinite(pt.grad).all())
+        print(json.dumps({"case": args.case, "points": p.shape[0], "threads_per_trajectory": plan.shape()[0],
+                          "fwd_plus_grad_ms": times}))
+        return
+    # large: one wave of the 76-state system through the device entry point
+    from centrex_tlf_gb300.native import NativePlan
+
+    spec = [j for j in hetero_jobs(args.points * 10, t_end_range=(15.0, 20.0)) if j["name"] == "plan_rc_76"][0]
+    d, g, b = spec["d"], spec["d"]["gamma"], spec["count"]
+    plan = NativePlan(d["payload"])
+    plan.set_shape(args.threads_per_trajectory, 0)
+    o = plan.options(t0=0.0, t1=spec["t1"], abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=None, save_start=True,
+                     maxiters=1000000, solver="tsit5", output="excited_population", output_indices=None,
+                     output_when="final", integral_weights=spec["weights"], stop_event=spec["event"],
+                     precision=args.precision)
+    rho = torch.from_numpy(np.repeat(d["rho0_packed"].reshape(1, -1), b, axis=0)).to(dev)
+    par = torch.from_numpy(np.ascontiguousarray(spec["params"]).view(np.float64).reshape(-1)).to(dev)
+    val = torch.zeros(b, dtype=torch.float64, device=dev)
+    st = torch.zeros(b * 6, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.solve_batch_device(o, b, rho.data_ptr(), spec["slots"], par.data_ptr(), 1, val.data_ptr(), st.data_ptr(),
+                                stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    stv = st.view(-1, 6).cpu().numpy()
+    assert not np.any(stv[:, 3] >> 32), "a 76-state trajectory failed"
+    print(json.dumps({"case": args.case, "trajectories": b, "precision": args.precision,
+                      "threads_per_trajectory": plan.shape()[0], "ms": times,
+                      "accepted_steps": int(stv[:, 0].sum()), "rejected_steps": int(stv[:, 1].sum())}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -567,9 +634,15 @@ def main() -> None:
     ap.add_argument("--points", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--ref-sample", type=int, default=256)
+    ap.add_argument("--case", choices=["scan", "gradient", "heterogeneous", "large"], default="scan",
+                    help="scan: the benchmark line; the others run one workload alone (profiling)")
+    ap.add_argument("--threads-per-trajectory", type=int, default=0,
+                    help="launch width of the gradient and large cases (0: automatic)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.case != "scan":
+        run_case(args)
     else:
         run_gpu(args)
 
