@@ -101,19 +101,66 @@ void lay_out_lanes(HostPacked& hp, int tpt) {
         n_lane = static_cast<int32_t>(n_o);
         recs.assign(static_cast<size_t>(iters) * tpt, 0u);  // padding: slot 0, formula 0 (zero)
         lane_tab.assign(n_o * tpt, 0u);
-        for (int lane = 0; lane < tpt; ++lane) {
-            int64_t it = 0;
-            for (size_t o = 0; o < lanes[lane].size(); ++o) {
-                const int64_t u = lanes[lane][o];
-                lane_tab[o * tpt + lane] = lane_word[u];
-                if (ptr[u + 1] == ptr[u]) {
-                    recs[it * tpt + lane] = kRecFlush;  // an output with no terms stays 0
-                    ++it;
-                    continue;
-                }
-                for (int64_t r = ptr[u]; r < ptr[u + 1]; ++r) {
-                    recs[it * tpt + lane] = words[r] | (r + 1 == ptr[u + 1] ? kRecFlush : 0u);
-                    ++it;
+        // The order of the records inside an output is free (its products are summed), so each
+        // iteration picks, lane by lane, the record whose two 16-byte operands (input slot, formula
+        // entry) least crowd those already chosen in the lane's quarter-warp: a 16-byte shared load
+        // is served 8 lanes at a time, one wavefront per distinct address in the busiest of the 8
+        // bank groups (address mod 8).  Greedy and deterministic; the iteration count does not
+        // change.
+        std::vector<size_t> next(tpt, 0);
+        std::vector<std::vector<uint32_t>> pool(tpt);
+        std::vector<uint8_t> open(tpt, 0);
+        std::vector<uint32_t> seen_slot, seen_fid;
+        // wavefronts of a phase after adding address a: the most distinct addresses in one bank group
+        auto wavefronts = [](const std::vector<uint32_t>& seen, uint32_t a) {
+            int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            bool have = false;
+            for (size_t k = 0; k < seen.size(); ++k) {
+                bool dup = false;
+                for (size_t m = 0; m < k; ++m) dup = dup || seen[m] == seen[k];
+                if (!dup) ++cnt[seen[k] & 7u];
+                have = have || seen[k] == a;
+            }
+            if (!have) ++cnt[a & 7u];
+            int mx = 0;
+            for (int b = 0; b < 8; ++b) mx = cnt[b] > mx ? cnt[b] : mx;
+            return mx * 16 + cnt[a & 7u];  // the phase's wavefronts, then the crowding of a's group
+        };
+        for (int64_t it = 0; it < iters; ++it) {
+            for (int q0 = 0; q0 < tpt; q0 += 8) {
+                seen_slot.clear();
+                seen_fid.clear();
+                for (int lane = q0; lane < q0 + 8 && lane < tpt; ++lane) {
+                    uint32_t w = 0u;  // padding record: slot 0, formula 0
+                    if (!open[lane] && next[lane] < lanes[lane].size()) {
+                        const size_t o = next[lane]++;
+                        const int64_t u = lanes[lane][o];
+                        lane_tab[o * tpt + lane] = lane_word[u];
+                        if (ptr[u + 1] == ptr[u]) {
+                            w = kRecFlush;  // an output with no terms stays 0
+                        } else {
+                            pool[lane].assign(words.begin() + ptr[u], words.begin() + ptr[u + 1]);
+                            open[lane] = 1;
+                        }
+                    }
+                    if (open[lane]) {
+                        auto& pl = pool[lane];
+                        size_t best = 0;
+                        int best_cost = 1 << 30;
+                        for (size_t k = 0; k < pl.size(); ++k) {
+                            const int c = wavefronts(seen_slot, pl[k] & kRecIndexMask) + wavefronts(seen_fid, pl[k] >> kRecCoefShift);
+                            if (c < best_cost) { best_cost = c; best = k; }
+                        }
+                        w = pl[best];
+                        pl.erase(pl.begin() + static_cast<std::ptrdiff_t>(best));
+                        if (pl.empty()) {
+                            w |= kRecFlush;
+                            open[lane] = 0;
+                        }
+                    }
+                    recs[static_cast<size_t>(it) * tpt + lane] = w;
+                    seen_slot.push_back(w & kRecIndexMask);
+                    seen_fid.push_back(w >> kRecCoefShift);
                 }
             }
         }

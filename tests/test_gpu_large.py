@@ -6,8 +6,11 @@ Tolerances: the FP64 RHS within 1e-10 relative of the reference's Python RHS (pu
 The square-wave drive makes the RHS discontinuous in time: at each switch the controller rejects
 and retries, and rounding-level differences in h decide where the step past the jump lands, so
 whole solves agree to the solver's tolerance (rtol 1e-8) rather than to rounding -- 1e-7
-absolute on populations for both forms (the mixed form's headline bar is 1e-6), and 1e-6
-relative on time integrals, which are trapezoids over the accepted steps.
+absolute on populations for both forms (the mixed form's headline bar is 1e-6), and 5e-6
+relative on time integrals, which are trapezoids over the accepted steps and collect the
+landing error of every jump (any change of the gather's summation order moves one of these
+integrals by 1.4e-6 relative; with the switching frequency at zero the same system agrees with
+the oracle to 1e-9, test_rc76_smooth_drive_matches_oracle_to_rounding).
 """
 
 from __future__ import annotations
@@ -98,7 +101,7 @@ def test_rc76_ragged_end_times_by_stop_event(rc):
                    maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
                    output_when="final", integral_weights=w, stop_event=ev)
     ref, _, _ = op.solve_batch(o, rho0, slots, params)
-    np.testing.assert_allclose(np.asarray(v).reshape(-1), ref.reshape(-1), rtol=1e-6, atol=0.0)
+    np.testing.assert_allclose(np.asarray(v).reshape(-1), ref.reshape(-1), rtol=5e-6, atol=0.0)
 
 
 @pytest.mark.parametrize("solver", ["tsit5", "dopri5"])
