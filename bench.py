@@ -228,10 +228,10 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
         plan.solve_batch_device(opts, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, d_val.data_ptr(),
                                 d_st.data_ptr(), stream.cuda_stream)
 
-    def grad():
+    def grad(checkpoint_every=0):
         pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
         j = solve_batch_with_grad(plan, d["rho0_packed"], (t0, t1), pt, slots, dt=1e-3 / gamma, integral_weights=W_EXCITED,
-                                  max_steps=2048)
+                                  max_steps=2048, checkpoint_every=checkpoint_every)
         j.sum().backward()
         return pt.grad
 
@@ -254,13 +254,17 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
                           stream=stream.cuda_stream)
     t_fwd_t = timed(fwd)
     t_grad_t = timed(grad)
+    t_grad_ck = timed(lambda: grad(512))
     plan.set_shape(0, 0)
     return {"workload": f"{n_traj} scan points, d(excited-population integral)/d(rabi, detuning, theta, t_center), "
                         "FP64 Tsit5 discrete adjoint", "fwd_ms": 1e3 * t_fwd, "fwd_plus_grad_ms": 1e3 * t_grad,
             "grad_over_fwd": t_grad / t_fwd,
             "autotuned": {"threads_per_trajectory": cands[0]["threads_per_trajectory"],
                           "trajectories_per_cta": cands[0]["trajectories_per_cta"], "fwd_ms": 1e3 * t_fwd_t,
-                          "fwd_plus_grad_ms": 1e3 * t_grad_t, "grad_over_fwd": t_grad_t / t_fwd_t}}
+                          "fwd_plus_grad_ms": 1e3 * t_grad_t, "grad_over_fwd": t_grad_t / t_fwd_t,
+                          "checkpointed_512": {"fwd_plus_grad_ms": 1e3 * t_grad_ck, "grad_over_fwd": t_grad_ck / t_fwd_t,
+                                               "tape_bytes_per_trajectory": 8 * plan.grad_tape_doubles(2048, 512),
+                                               "full_tape_bytes_per_trajectory": 8 * plan.grad_tape_doubles(2048, 0)}}}
 
 
 HETERO_PLANS = (("plan_q1_16_tend", 6), ("plan_r0_39", 3), ("plan_rc_76", 1))

@@ -251,15 +251,18 @@ def load_library() -> ctypes.CDLL:
     lib.obe_plan_autotune.restype = ctypes.c_int
     lib.obe_grad_tape_doubles_per_step.argtypes = [ctypes.c_void_p]
     lib.obe_grad_tape_doubles_per_step.restype = ctypes.c_int64
+    lib.obe_grad_tape_doubles.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32]
+    lib.obe_grad_tape_doubles.restype = ctypes.c_int64
     lib.obe_grad_forward.argtypes = [
         ctypes.c_void_p, ctypes.POINTER(ObeSolveOptions), ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32, c_i64p,
-        ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p,
     ]
     lib.obe_grad_forward.restype = ctypes.c_int
     lib.obe_grad_backward.argtypes = [
         ctypes.c_void_p, ctypes.POINTER(ObeSolveOptions), ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32, c_i64p,
-        ctypes.c_void_p, ctypes.c_int32, c_i64p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_int32, c_i64p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
     ]
     lib.obe_grad_backward.restype = ctypes.c_int
     _LIB = lib

@@ -41,32 +41,46 @@ class ForwardTape:
     """What the backward pass needs of a forward solve: its options, inputs, tape and statistics."""
 
     def __init__(self, plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals: torch.Tensor,
-                 max_steps: int, tape: torch.Tensor, stats: torch.Tensor):
+                 max_steps: int, tape: torch.Tensor, stats: torch.Tensor, checkpoint_every: int = 0):
         self.plan, self.opts, self.rho0, self.slots, self.pvals = plan, opts, rho0, slots, pvals
         self.max_steps, self.tape, self.stats = max_steps, tape, stats
+        self.checkpoint_every = checkpoint_every
 
     def steps(self) -> list[np.ndarray]:
         """The accepted steps (t_n, h_n) of every trajectory, as recorded."""
         st = self.stats.view(-1, 6).cpu().numpy()
-        per = self.plan.grad_tape_doubles_per_step()
-        tape = self.tape.view(-1, self.max_steps, per)[:, :, :2].cpu().numpy()
-        return [tape[b, : int(st[b, 0])] for b in range(st.shape[0])]
+        b = st.shape[0]
+        if self.checkpoint_every > 0:
+            per = self.plan.grad_tape_doubles(self.max_steps, self.checkpoint_every)
+            tape = self.tape.view(b, per)[:, : 2 * self.max_steps].reshape(b, self.max_steps, 2).cpu().numpy()
+        else:
+            per = self.plan.grad_tape_doubles_per_step()
+            tape = self.tape.view(b, self.max_steps, per)[:, :, :2].cpu().numpy()
+        return [tape[k, : int(st[k, 0])] for k in range(b)]
 
 
-def _forward(plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals: torch.Tensor, max_steps: int):
+def _checkpoint_every(plan: NativePlan, b: int, max_steps: int, requested: int | None) -> int:
+    """The full tape while it stays under 4 GiB, else a start state every 512 steps."""
+    if requested is not None:
+        return int(requested)
+    return 0 if b * plan.grad_tape_doubles(max_steps, 0) * 8 <= (4 << 30) else 512
+
+
+def _forward(plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals: torch.Tensor, max_steps: int,
+             checkpoint_every: int | None = None):
     b = rho0.shape[0]
-    per = plan.grad_tape_doubles_per_step()
     stream = torch.cuda.current_stream(rho0.device).cuda_stream
     while True:
-        tape = torch.empty(b * max_steps * per, dtype=torch.float64, device=rho0.device)
+        ck = _checkpoint_every(plan, b, max_steps, checkpoint_every)
+        tape = torch.empty(b * plan.grad_tape_doubles(max_steps, ck), dtype=torch.float64, device=rho0.device)
         values = torch.empty(b * opts.width, dtype=torch.float64, device=rho0.device)
         stats = torch.zeros(b * 6, dtype=torch.int64, device=rho0.device)
         plan.grad_forward(opts, b, rho0.data_ptr(), slots, pvals.data_ptr() if slots else None, max_steps,
-                          tape.data_ptr(), values.data_ptr(), stats.data_ptr(), stream)
+                          tape.data_ptr(), values.data_ptr(), stats.data_ptr(), stream, checkpoint_every=ck)
         st = stats.view(b, 6).cpu().numpy()
         status = st[:, 3] >> 32
         if np.all(status == 0):
-            return values.view(b, opts.width), ForwardTape(plan, opts, rho0, slots, pvals, max_steps, tape, stats)
+            return values.view(b, opts.width), ForwardTape(plan, opts, rho0, slots, pvals, max_steps, tape, stats, ck)
         if int(st[:, 0].max()) < max_steps:
             bad = int(np.flatnonzero(status != 0)[0])
             raise ValueError(f"trajectory {bad}: the forward solve failed (status {int(status[bad])})")
@@ -75,13 +89,14 @@ def _forward(plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals
 
 class _SolveWithGrad(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, params: torch.Tensor, rho0: torch.Tensor, plan: NativePlan, opts, slots: list[int], max_steps: int):
+    def forward(ctx, params: torch.Tensor, rho0: torch.Tensor, plan: NativePlan, opts, slots: list[int], max_steps: int,
+                checkpoint_every):
         b = rho0.shape[0]
         pvals = torch.zeros(b, len(slots), 2, dtype=torch.float64, device=rho0.device)
         if slots:
             pvals[:, :, 0] = params.detach()
         pvals = pvals.contiguous()
-        values, tape = _forward(plan, opts, rho0.detach().contiguous(), slots, pvals, max_steps)
+        values, tape = _forward(plan, opts, rho0.detach().contiguous(), slots, pvals, max_steps, checkpoint_every)
         ctx.tape = tape
         return values.squeeze(1) if opts.width == 1 else values
 
@@ -99,24 +114,28 @@ class _SolveWithGrad(torch.autograd.Function):
         t.plan.grad_backward(t.opts, b, t.rho0.data_ptr(), t.slots, t.pvals.data_ptr() if t.slots else None, t.slots,
                              t.max_steps, t.tape.data_ptr(), t.stats.data_ptr(), g.data_ptr(),
                              pgrad.data_ptr() if n_grad else None, rgrad.data_ptr() if rgrad is not None else None,
-                             status.data_ptr(), stream)
+                             status.data_ptr(), stream, checkpoint_every=t.checkpoint_every)
         st = status.cpu().numpy()
         if np.any(st != 0):
             bad = int(np.flatnonzero(st != 0)[0])
             raise ValueError(f"trajectory {bad}: gradient not available: {_ADJ_MESSAGES.get(int(st[bad]), int(st[bad]))}")
-        return (pgrad[:, :n_grad] if n_grad else None), rgrad, None, None, None, None
+        return (pgrad[:, :n_grad] if n_grad else None), rgrad, None, None, None, None, None
 
 
 def solve_batch_with_grad(plan: NativePlan, rho0, t_span: Sequence[float], params: torch.Tensor,
                           parameter_slot_indices: Sequence[int], *, solver: str = "tsit5", abstol: float = 1e-11,
                           reltol: float = 1e-8, dt: float = 0.0, maxiters: int = 100000,
                           output: str = "excited_population", integral_weights=None, max_steps: int = 4096,
-                          return_tape: bool = False):
+                          checkpoint_every: int | None = None, return_tape: bool = False):
     """Batched double-precision solve whose outputs are differentiable in ``params`` ((B, S) real,
     the values of the base slots ``parameter_slot_indices``) and in ``rho0`` ((B, N) packed).
 
     ``output``: a weighted integral (final value, shape (B,)) or ``"populations"`` (final
     populations, shape (B, n)).  ``max_steps`` sizes the tape (doubled and retried on overflow).
+    ``checkpoint_every``: 0 records every step's stage derivatives; C > 0 records the start state
+    of every C-th step and the reverse sweep recomputes each segment from it (one more forward's
+    work, a tape of 2 + N / C doubles per step); None takes the full tape while it stays under
+    4 GiB.
     With ``return_tape`` the forward tape comes back too (its ``steps()`` are the frozen steps).
     """
     t0, t1 = float(t_span[0]), float(t_span[1])
@@ -138,7 +157,7 @@ def solve_batch_with_grad(plan: NativePlan, rho0, t_span: Sequence[float], param
     if rho0.dim() == 1:
         rho0 = rho0.unsqueeze(0).expand(params.shape[0], -1)
     slots = [int(s) for s in parameter_slot_indices]
-    out = _SolveWithGrad.apply(params, rho0.contiguous(), plan, opts, slots, int(max_steps))
+    out = _SolveWithGrad.apply(params, rho0.contiguous(), plan, opts, slots, int(max_steps), checkpoint_every)
     if return_tape:
         return out, out.grad_fn.tape if out.grad_fn is not None else None
     return out

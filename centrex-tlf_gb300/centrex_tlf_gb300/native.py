@@ -213,22 +213,27 @@ class NativePlan:
     def grad_tape_doubles_per_step(self) -> int:
         return int(self.lib.obe_grad_tape_doubles_per_step(self.handle))
 
+    def grad_tape_doubles(self, max_steps: int, checkpoint_every: int = 0) -> int:
+        """Doubles of one trajectory's tape (full records, or checkpoints every C steps)."""
+        return int(self.lib.obe_grad_tape_doubles(self.handle, int(max_steps), int(checkpoint_every)))
+
     def grad_forward(self, opts: SolveOptions, n_traj: int, d_rho0: int, param_slots, d_param_values: int | None,
-                     max_steps: int, d_tape: int, d_values: int, d_stats: int, stream: int = 0) -> None:
+                     max_steps: int, d_tape: int, d_values: int, d_stats: int, stream: int = 0,
+                     checkpoint_every: int = 0) -> None:
         """The double-precision batch solve that records the gradient tape (device pointers)."""
         slots = np.ascontiguousarray(np.asarray(param_slots if param_slots else [0], dtype=np.int64))
         n_param = 0 if d_param_values is None else int(slots.size)
         st = self.lib.obe_grad_forward(
             self.handle, ctypes.byref(opts.opts), int(n_traj), ctypes.c_void_p(d_rho0), n_param,
-            _abi.ptr(slots, ctypes.c_int64), ctypes.c_void_p(d_param_values or 0), int(max_steps), ctypes.c_void_p(d_tape),
-            opts.width, ctypes.c_void_p(d_values), ctypes.c_void_p(d_stats), ctypes.c_void_p(stream),
+            _abi.ptr(slots, ctypes.c_int64), ctypes.c_void_p(d_param_values or 0), int(max_steps), int(checkpoint_every),
+            ctypes.c_void_p(d_tape), opts.width, ctypes.c_void_p(d_values), ctypes.c_void_p(d_stats), ctypes.c_void_p(stream),
         )
         if st != _abi.OBE_OK:
             _raise(self.lib, st)
 
     def grad_backward(self, opts: SolveOptions, n_traj: int, d_rho0: int, param_slots, d_param_values: int | None,
                       grad_slots, max_steps: int, d_tape: int, d_stats: int, d_out_grad: int, d_param_grad: int | None,
-                      d_rho0_grad: int | None, d_adj_status: int, stream: int = 0) -> None:
+                      d_rho0_grad: int | None, d_adj_status: int, stream: int = 0, checkpoint_every: int = 0) -> None:
         """The reverse sweep over a tape of grad_forward (device pointers)."""
         slots = np.ascontiguousarray(np.asarray(param_slots if param_slots else [0], dtype=np.int64))
         n_param = 0 if d_param_values is None else int(slots.size)
@@ -236,7 +241,8 @@ class NativePlan:
         st = self.lib.obe_grad_backward(
             self.handle, ctypes.byref(opts.opts), int(n_traj), ctypes.c_void_p(d_rho0), n_param,
             _abi.ptr(slots, ctypes.c_int64), ctypes.c_void_p(d_param_values or 0), len(grad_slots),
-            _abi.ptr(gslots, ctypes.c_int64), int(max_steps), ctypes.c_void_p(d_tape), ctypes.c_void_p(d_stats),
+            _abi.ptr(gslots, ctypes.c_int64), int(max_steps), int(checkpoint_every), ctypes.c_void_p(d_tape),
+            ctypes.c_void_p(d_stats),
             ctypes.c_void_p(d_out_grad), ctypes.c_void_p(d_param_grad or 0), ctypes.c_void_p(d_rho0_grad or 0),
             ctypes.c_void_p(d_adj_status), ctypes.c_void_p(stream),
         )

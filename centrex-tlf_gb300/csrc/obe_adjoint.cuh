@@ -35,6 +35,12 @@ struct AdjArgs {
     int grad_slot[kMaxGrad];    // base slots the gradient is taken with respect to
     const double* tape;
     long long tape_cap, tape_stride;
+    // checkpointed tape (ckpt = C > 0, the integrator's tape_ckpt layout): each segment of C steps
+    // is replayed from its start state into the group's segment buffer (seg + group * seg_stride:
+    // C records of [t_n, h_n, y_n, K_1..K_6], rec_stride doubles apart) before its reverse sweep
+    int ckpt;
+    double* seg;
+    long long seg_stride, rec_stride;
     const obe_traj_stats* fwd_stats;  // the forward solve's statistics (accepted-step counts)
     const double* out_grad;     // [traj][width]: d(loss)/d(output)
     double* param_grad;         // [traj][n_grad]
@@ -384,9 +390,64 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
             gsync<TPT>(g);
         };
 
-        // ---- the reverse sweep over the accepted steps ----
-        for (long long st = n_acc - 1; st >= 0; --st) {
-            const double* rec = J.tape + (static_cast<size_t>(traj) * J.tape_cap + st) * J.tape_stride;
+        // ---- the reverse sweep over the accepted steps, segment by segment ----
+        const long long seg_len = J.ckpt > 0 ? J.ckpt : (n_acc > 0 ? n_acc : 1);
+        const long long n_seg = J.ckpt > 0 ? (n_acc + seg_len - 1) / seg_len : 1;
+        double* segbuf = J.ckpt > 0 ? J.seg + (static_cast<size_t>(blockIdx.x) * gpb + g) * J.seg_stride : nullptr;
+        const double* tbase = J.tape + static_cast<size_t>(traj) * (J.ckpt > 0 ? J.tape_stride : J.tape_cap * J.tape_stride);
+        for (long long sg = n_seg - 1; sg >= 0; --sg) {
+        const long long s0 = sg * seg_len, s1 = s0 + seg_len < n_acc ? s0 + seg_len : n_acc;
+        if (J.ckpt > 0) {
+            // replay the segment's steps from its checkpointed start state with the recorded
+            // (t_n, h_n): the stage derivatives of the frozen steps, as the forward solve took them
+            const double* ck = tbase + 2 * J.tape_cap + static_cast<size_t>(sg) * N;
+            for (int i = lt; i < N; i += TPT) segbuf[2 + i] = ck[i];
+            for (long long st = s0; st < s1; ++st) {
+                double* rec = segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
+                const double tn = tbase[2 * st], h = tbase[2 * st + 1];
+                if (lt == 0) { rec[0] = tn; rec[1] = h; }
+                if (lt < 6) {
+                    const double ts = tn + h * cs[lt];
+                    double2 dtmp[kMaxGrad];
+                    for (int c = 0; c < P.n_comp; ++c) {
+                        if (!P.comp_dynamic[c]) continue;
+                        const DevExpr e = P.comp_expr[c];
+                        slots[P.comp_slot[c]] = vm_eval_dual(P, e.start, e.len, slots, dslots, 0, ts, sv, sd, tp, dtmp, &bad);
+                    }
+                    for (int j = 0; j < P.n_dyn; ++j) {
+                        const DevExpr e = P.coeff_expr[P.dyn_ids[j]];
+                        s_cdyn[lt * nd + j] = vm_eval_dual(P, e.start, e.len, slots, dslots, 0, ts, sv, sd, tp, dtmp, &bad);
+                    }
+                }
+                gsync<TPT>(g);
+                const double* yn_r = rec + 2;
+                double* K_r = rec + 2 + N;
+                for (int s = 0; s < 6; ++s) {
+                    for (int i = lt; i < N; i += TPT) {
+                        double acc = 0.0;
+                        for (int l = 0; l < s; ++l) acc += kTab.a[M][s - 1][l] * K_r[static_cast<size_t>(l) * N + i];
+                        s_G64[gslot64(i, n)] = s > 0 ? yn_r[i] + h * acc : yn_r[i];
+                    }
+                    gsync<TPT>(g);
+                    if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + s * nd, s_tab, lt);
+                    gsync<TPT>(g);
+                    gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, K_r + static_cast<size_t>(s) * N, lt);
+                    gsync<TPT>(g);
+                }
+                if (st + 1 < s1) {
+                    double* yn_next = rec + J.rec_stride + 2;
+                    for (int i = lt; i < N; i += TPT) {
+                        double acc = 0.0;
+                        for (int s = 0; s < 6; ++s) acc += bw[s] * K_r[static_cast<size_t>(s) * N + i];
+                        yn_next[i] = yn_r[i] + h * acc;
+                    }
+                }
+                gsync<TPT>(g);
+            }
+        }
+        for (long long st = s1 - 1; st >= s0; --st) {
+            const double* rec = J.ckpt > 0 ? segbuf + static_cast<size_t>(st - s0) * J.rec_stride
+                                           : tbase + static_cast<size_t>(st) * J.tape_stride;
             const double tn = rec[0], h = rec[1];
             const double* yn_t = rec + 2;
             const double* Kt = rec + 2 + N;
@@ -504,6 +565,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
             gsync<TPT>(g);
             if (segment) add_quadrature(dt);  // the start state y_n
         }
+        }  // segments
 
         // ---- outputs ----
         for (int q = 0; q < ng; ++q) {

@@ -162,10 +162,13 @@ struct CallArgs {
     int k1_refresh;  // mixed form: recompute k_1 in double every this many accepted steps
     unsigned char* gscratch;  // large systems: per-group global slices of the stage buffers
     size_t gstride;           // bytes per slice
-    // gradient tape (double-precision adaptive solves): per trajectory up to tape_cap accepted
-    // steps of [t_n, h_n, y_n (N), K_1..K_6 (6 N)], tape_stride doubles apart; null when off
+    // gradient tape (double-precision adaptive solves), null when off.  tape_ckpt == 0: per
+    // trajectory up to tape_cap accepted steps of [t_n, h_n, y_n (N), K_1..K_6 (6 N)], tape_stride
+    // doubles apart.  tape_ckpt = C > 0: per trajectory (tape_stride doubles apart) the step log
+    // [tape_cap][t_n, h_n], then y_n of every C-th step (steps 0, C, 2C, ...), N doubles each
     double* tape;
     long long tape_cap, tape_stride;
+    int tape_ckpt;
     int vm_depth;    // VM stack depth of the plan's and the event's programs
     int fixed;       // 0: adaptive; else the fixed-step obe_solver value (double-precision form only)
 };
@@ -1359,15 +1362,29 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 if constexpr (!MIXED) {
                     if (A.tape) {
                         // the step for the adjoint: start time, size, start state and stages 1-6
+                        // (or, checkpointed, the step and every tape_ckpt-th start state)
                         if (accepted > A.tape_cap) { status = ST_TAPE; err_a = A.tape_cap; break; }
-                        double* rec = A.tape + (static_cast<size_t>(traj) * A.tape_cap + (accepted - 1)) * A.tape_stride;
-                        if (lt == 0) { rec[0] = xo; rec[1] = h; }
-#pragma unroll
-                        for (int e = 0; e < EPT; ++e) {
-                            int i = lt + e * TPT;
-                            if (i < N) rec[2 + i] = y[e];
+                        const long long j = accepted - 1;
+                        double* rec;
+                        bool keep_y = true;
+                        if (A.tape_ckpt == 0) {
+                            rec = A.tape + (static_cast<size_t>(traj) * A.tape_cap + j) * A.tape_stride;
+                            if (lt == 0) { rec[0] = xo; rec[1] = h; }
+                            rec += 2;
+                            for (int i = lt; i < 6 * N; i += TPT) rec[N + i] = s_K[i];
+                        } else {
+                            double* base = A.tape + static_cast<size_t>(traj) * A.tape_stride;
+                            if (lt == 0) { base[2 * j] = xo; base[2 * j + 1] = h; }
+                            keep_y = j % A.tape_ckpt == 0;
+                            rec = base + 2 * A.tape_cap + static_cast<size_t>(j / A.tape_ckpt) * N;
                         }
-                        for (int i = lt; i < 6 * N; i += TPT) rec[2 + N + i] = s_K[i];
+                        if (keep_y) {
+#pragma unroll
+                            for (int e = 0; e < EPT; ++e) {
+                                int i = lt + e * TPT;
+                                if (i < N) rec[i] = y[e];
+                            }
+                        }
                     }
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {

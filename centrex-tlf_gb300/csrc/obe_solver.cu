@@ -447,7 +447,8 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
                         const int64_t* axis_len, const double* d_axes, long long cap, long long out_stride, double* d_values,
                         double* d_times, obe_traj_stats* d_stats, TrajErr* d_errs, unsigned char* d_blob_area,
                         const CallBlob& cb, const std::vector<double>& save_times, unsigned long long* d_counter,
-                        cudaStream_t stream, double* d_tape = nullptr, long long tape_cap = 0, long long tape_stride = 0) {
+                        cudaStream_t stream, double* d_tape = nullptr, long long tape_cap = 0, long long tape_stride = 0,
+                        int tape_ckpt = 0) {
     CallArgs A;
     fill_call_args(A, o, save_times, cb, d_blob_area);
     A.n_traj = n_traj;
@@ -475,6 +476,7 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
     A.tape = d_tape;
     A.tape_cap = tape_cap;
     A.tape_stride = tape_stride;
+    A.tape_ckpt = tape_ckpt;
     LaunchShape s;
     obe_status st = plan_launch(p->dev, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s, p->shape_gpb);
     if (st != OBE_OK) return st;
@@ -1055,12 +1057,21 @@ int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan) {
     return static_cast<int64_t>(align16((2 + 7 * static_cast<size_t>(plan->N)) * 8) / 8);
 }
 
+int64_t obe_grad_tape_doubles(const obe_plan* plan, int64_t max_steps, int32_t checkpoint_every) {
+    if (!plan || max_steps <= 0 || checkpoint_every < 0) return 0;
+    if (checkpoint_every == 0) return max_steps * obe_grad_tape_doubles_per_step(plan);
+    const int64_t n_ck = (max_steps + checkpoint_every - 1) / checkpoint_every;
+    return static_cast<int64_t>(align16((2 * static_cast<size_t>(max_steps) + static_cast<size_t>(n_ck) * plan->N) * 8) / 8);
+}
+
 obe_status obe_grad_forward(const obe_plan* plan_c, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
                             int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values, int64_t max_steps,
-                            double* d_tape, int64_t width, double* d_values, obe_traj_stats* d_stats, void* stream) {
+                            int32_t checkpoint_every, double* d_tape, int64_t width, double* d_values, obe_traj_stats* d_stats,
+                            void* stream) {
     g_launches = 0;
     obe_plan* p = const_cast<obe_plan*>(plan_c);
     if (!p || !opt || !d_tape || max_steps <= 0) { set_error("null argument or non-positive max_steps"); return OBE_ERR_INVALID; }
+    if (checkpoint_every < 0) { set_error("checkpoint_every must be non-negative"); return OBE_ERR_INVALID; }
     int64_t gw = 0;
     obe_status st = grad_check(p, opt, &gw);
     if (st != OBE_OK) return st;
@@ -1081,12 +1092,16 @@ obe_status obe_grad_forward(const obe_plan* plan_c, const obe_solve_options* opt
     if (!cuda_ok(cudaMemcpyAsync(d, cb.bytes.data(), cb.bytes.size(), cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(args)")) return OBE_ERR_CUDA;
     return solve_device(p, opt, n_traj, d_rho0, p->N, n_param_slots, param_slots, d_param_values, 0, nullptr, nullptr, 1, width,
                         d_values, nullptr, d_stats, reinterpret_cast<TrajErr*>(d + errs_off), d, cb, save_times,
-                        static_cast<unsigned long long*>(p->d_counter), s, d_tape, max_steps, obe_grad_tape_doubles_per_step(p));
+                        static_cast<unsigned long long*>(p->d_counter), s, d_tape, max_steps,
+                        checkpoint_every > 0 ? obe_grad_tape_doubles(p, max_steps, checkpoint_every)
+                                             : obe_grad_tape_doubles_per_step(p),
+                        checkpoint_every);
 }
 
 obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
                              int32_t n_param_slots, const int64_t* param_slots, const double* d_param_values, int32_t n_grad,
-                             const int64_t* grad_slots, int64_t max_steps, const double* d_tape, const obe_traj_stats* d_stats,
+                             const int64_t* grad_slots, int64_t max_steps, int32_t checkpoint_every, const double* d_tape,
+                             const obe_traj_stats* d_stats,
                              const double* d_out_grad, double* d_param_grad, double* d_rho0_grad, int32_t* d_adj_status,
                              void* stream) {
     g_launches = 0;
@@ -1095,6 +1110,7 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
         set_error("null argument or non-positive max_steps");
         return OBE_ERR_INVALID;
     }
+    if (checkpoint_every < 0) { set_error("checkpoint_every must be non-negative"); return OBE_ERR_INVALID; }
     if (n_grad < 0 || n_grad > kMaxGrad || (n_grad > 0 && (!grad_slots || !d_param_grad))) {
         set_error("gradients are taken with respect to at most " + std::to_string(kMaxGrad) + " parameter slots");
         return OBE_ERR_INVALID;
@@ -1134,7 +1150,9 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     for (int q = 0; q < n_grad; ++q) J.grad_slot[q] = static_cast<int>(grad_slots[q]);
     J.tape = d_tape;
     J.tape_cap = max_steps;
-    J.tape_stride = obe_grad_tape_doubles_per_step(p);
+    J.ckpt = checkpoint_every;
+    J.rec_stride = obe_grad_tape_doubles_per_step(p);
+    J.tape_stride = checkpoint_every > 0 ? obe_grad_tape_doubles(p, max_steps, checkpoint_every) : J.rec_stride;
     J.fwd_stats = d_stats;
     J.out_grad = d_out_grad;
     J.param_grad = d_param_grad;
@@ -1153,6 +1171,13 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     while (gpb > 1 && gpb > per_sm) --gpb;
     const size_t smem = plan_bytes + gpb * group;
     const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n_traj + gpb - 1) / gpb, sm_count())));
+    if (checkpoint_every > 0) {
+        // one segment of full records per resident trajectory group
+        J.seg_stride = static_cast<long long>(checkpoint_every) * J.rec_stride;
+        unsigned char* gk = nullptr;
+        if ((st = kscratch(p, static_cast<size_t>(J.seg_stride) * 8 * static_cast<size_t>(blocks) * gpb, &gk)) != OBE_OK) return st;
+        J.seg = reinterpret_cast<double*>(gk);
+    }
     if (!cuda_ok(cudaMemsetAsync(J.counter, 0, sizeof(unsigned long long), s), "cudaMemsetAsync")) return OBE_ERR_CUDA;
     const int method = opt->solver == OBE_SOLVER_TSIT5 ? 1 : 0;
     const int ept = ept_for(P.N, tpt);

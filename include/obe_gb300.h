@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define OBE_ABI_VERSION 1
+#define OBE_ABI_VERSION 2
 
 typedef enum {
     OBE_OK = 0,
@@ -306,30 +306,37 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
  * `stream`; systems of up to 45 states (a plan width of 128 threads or fewer), dopri5/tsit5, no
  * stop event.
  *
- * obe_grad_forward is obe_solve_batch_device that also records, per trajectory, every accepted
- * step (start time, size, start state, stage derivatives 1-6) into d_tape:
- * n_traj * max_steps * obe_grad_tape_doubles_per_step(plan) doubles, caller-owned.  A trajectory
- * with more than max_steps accepted steps ends with a status whose message asks for a larger
- * max_steps.
- * obe_grad_backward runs the reverse sweep on that tape: given d(loss)/d(outputs) in d_out_grad
- * ([n_traj][width]), it writes d(loss)/d(parameter) to d_param_grad ([n_traj][n_grad], for the
- * base slots grad_slots, at most 8) and, if d_rho0_grad is not NULL, d(loss)/d(packed rho0) to
- * d_rho0_grad ([n_traj][N]).  d_adj_status ([n_traj]): 0 = ok, 1 = a helper function or table
- * received an argument that depends on a differentiated parameter (not differentiable here),
- * 2 = the forward trajectory failed or overflowed the tape.  The parameter arguments must be
- * those of the forward call.
+ * obe_grad_forward is obe_solve_batch_device that also records a tape per trajectory into d_tape
+ * (caller-owned, n_traj * obe_grad_tape_doubles(plan, max_steps, checkpoint_every) doubles).
+ * checkpoint_every = 0: every accepted step with its start time, size, start state and stage
+ * derivatives 1-6 (obe_grad_tape_doubles_per_step doubles each).  checkpoint_every = C > 0: the
+ * start time and size of every step and the start state of every C-th step; the reverse sweep
+ * then replays each segment of C steps from its start state (frozen steps, double precision)
+ * into a library-owned buffer of C full records per resident trajectory before sweeping it --
+ * one more forward's arithmetic for a tape of 2 + N / C doubles per step.  A trajectory with more
+ * than max_steps accepted steps ends with a status whose message asks for a larger max_steps.
+ * obe_grad_backward runs the reverse sweep on that tape (same max_steps and checkpoint_every):
+ * given d(loss)/d(outputs) in d_out_grad ([n_traj][width]), it writes d(loss)/d(parameter) to
+ * d_param_grad ([n_traj][n_grad], for the base slots grad_slots, at most 8) and, if d_rho0_grad
+ * is not NULL, d(loss)/d(packed rho0) to d_rho0_grad ([n_traj][N]).  d_adj_status ([n_traj]):
+ * 0 = ok, 1 = a helper function or table received an argument that depends on a differentiated
+ * parameter (not differentiable here), 2 = the forward trajectory failed or overflowed the tape.
+ * The parameter arguments must be those of the forward call.
  */
 int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan);
+int64_t obe_grad_tape_doubles(const obe_plan* plan, int64_t max_steps, int32_t checkpoint_every);
 obe_status obe_grad_forward(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
                             const double* d_rho0, int32_t n_param_slots, const int64_t* param_slots,
-                            const double* d_param_values, int64_t max_steps, double* d_tape,
-                            int64_t width, double* d_values, obe_traj_stats* d_stats, void* stream);
+                            const double* d_param_values, int64_t max_steps, int32_t checkpoint_every,
+                            double* d_tape, int64_t width, double* d_values, obe_traj_stats* d_stats,
+                            void* stream);
 obe_status obe_grad_backward(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
                              const double* d_rho0, int32_t n_param_slots, const int64_t* param_slots,
                              const double* d_param_values, int32_t n_grad, const int64_t* grad_slots,
-                             int64_t max_steps, const double* d_tape, const obe_traj_stats* d_stats,
-                             const double* d_out_grad, double* d_param_grad, double* d_rho0_grad,
-                             int32_t* d_adj_status, void* stream);
+                             int64_t max_steps, int32_t checkpoint_every, const double* d_tape,
+                             const obe_traj_stats* d_stats, const double* d_out_grad,
+                             double* d_param_grad, double* d_rho0_grad, int32_t* d_adj_status,
+                             void* stream);
 
 /*
  * Allocation-free form of obe_solve_batch_device (no counterpart in the reference).  Some

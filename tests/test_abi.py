@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol():
     assert "obe_solve_batch" in names and "obe_plan_create" in names
     for name in names:
         assert hasattr(lib, name), f"{name} is declared in include/obe_gb300.h but not exported"
-    assert lib.obe_abi_version() == 1
+    assert lib.obe_abi_version() == 2
 
 
 def test_struct_layouts_match_header_sizes():

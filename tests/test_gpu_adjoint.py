@@ -103,7 +103,7 @@ def test_parameter_gradients_match_frozen_step_finite_differences(q1, solver, ou
         assert np.all(np.abs(grad[:, k] - fd) <= tol), (k, grad[:, k], fd, tol)
 
 
-def _fd_check(d, plan, op, p0, slots, solver="tsit5", t_span=None, weights=None):
+def _fd_check(d, plan, op, p0, slots, solver="tsit5", t_span=None, weights=None, checkpoint_every=0):
     """Gradients of the excited-population integral against central differences of the oracle's
     replay of the frozen steps (the bar of the test above)."""
     g = d["gamma"]
@@ -112,7 +112,8 @@ def _fd_check(d, plan, op, p0, slots, solver="tsit5", t_span=None, weights=None)
     b = p0.shape[0]
     params = torch.tensor(p0, dtype=torch.float64, device="cuda", requires_grad=True)
     out, tape = solve_batch_with_grad(plan, d["rho0_packed"], t_span, params, slots, solver=solver, dt=1e-3 / g,
-                                      integral_weights=w, return_tape=True)
+                                      integral_weights=w, return_tape=True, checkpoint_every=checkpoint_every)
+    assert tape.checkpoint_every == checkpoint_every
     out.sum().backward()
     grad = params.grad.cpu().numpy()
     steps = tape.steps()
@@ -158,6 +159,31 @@ def test_gradients_of_the_39_state_system(golden):
     op = oracle.OraclePlan(d["payload"])
     p0 = np.array([[1.5 * g, 0.5 * g, 0.4, 70.0 / g], [4.0 * g, -1.0 * g, 1.2, 75.0 / g]])
     _fd_check(d, plan, op, p0, _slots(d), t_span=(0.0, 150.0 / g))
+
+
+@pytest.mark.parametrize("ck", [7, 512])
+def test_checkpointed_tape_matches_the_full_tape(q1, ck):
+    """Checkpoints every C accepted steps, segments replayed in the reverse sweep: the same
+    gradients as the full tape up to the replay's rounding, for parameters and the initial state,
+    and the finite differences of the frozen steps."""
+    d, plan, op = q1
+    g = d["gamma"]
+    slots = _slots(d)
+    p0 = _params(d)[:3]
+    res = {}
+    for c in (0, ck):
+        params = torch.tensor(p0, dtype=torch.float64, device="cuda", requires_grad=True)
+        rho0 = torch.tensor(np.repeat(d["rho0_packed"].reshape(1, -1), 3, axis=0), dtype=torch.float64, device="cuda",
+                            requires_grad=True)
+        out, tape = solve_batch_with_grad(plan, rho0, d["t_span"], params, slots, dt=1e-3 / g, integral_weights=W,
+                                          return_tape=True, checkpoint_every=c)
+        out.sum().backward()
+        res[c] = (out.detach().cpu().numpy(), params.grad.cpu().numpy(), rho0.grad.cpu().numpy(), tape.tape.numel())
+    np.testing.assert_array_equal(res[ck][0], res[0][0])  # the same forward solve
+    np.testing.assert_allclose(res[ck][1], res[0][1], rtol=1e-9, atol=0.0)
+    np.testing.assert_allclose(res[ck][2], res[0][2], rtol=1e-9, atol=1e-12 * np.max(np.abs(res[0][2])))
+    assert res[ck][3] < res[0][3] / 5  # 2 + N / C doubles per step instead of 2 + 7 N
+    _fd_check(d, plan, op, p0, slots, checkpoint_every=ck)
 
 
 def test_initial_state_gradient_matches_finite_differences(q1):
