@@ -16,9 +16,10 @@
 // coefficient programs.  The trapezoid rule of the integral outputs (sum over accepted steps of
 // (t_{n+1} - t_n)(w.y_n + w.y_{n+1}) / 2) adds its weights to ybar at both ends of each segment.
 //
-// One group of 32, 64 or 128 threads per trajectory (the plan's width; systems up to 45 states);
-// the transposed product L^T lambda runs on a second, input-major record stream built by the
-// packer.
+// One group of 32, 64, 128 or 256 threads per trajectory (the plan's width; above 45 states the
+// stage-derivative adjoints, ybar and the class sums move to a per-group slice of device memory
+// and the record streams are read from the plan's device image); the transposed product
+// L^T lambda runs on a second, input-major record stream built by the packer.
 #pragma once
 
 #include "obe_kernels.cuh"
@@ -41,6 +42,10 @@ struct AdjArgs {
     int ckpt;
     double* seg;
     long long seg_stride, rec_stride;
+    // large systems (256 threads per trajectory): each group's mu, ybar and class sums live in a
+    // slice of device memory, gscratch + group * gstride bytes
+    unsigned char* gscratch;
+    size_t gstride;
     const obe_traj_stats* fwd_stats;  // the forward solve's statistics (accepted-step counts)
     const double* out_grad;     // [traj][width]: d(loss)/d(output)
     double* param_grad;         // [traj][n_grad]
@@ -230,6 +235,8 @@ static __device__ __noinline__ double2 vm_eval_dual(const DevPlan& P, int32_t st
 
 struct AdjLayout {
     size_t tab, G, LS, MU, YB, slots, dslots, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, red, traj, bytes;
+    size_t gbytes;  // large systems: bytes of the group's device-memory slice (MU, YB, S)
+    bool glob;
 };
 
 __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int n_coeff, int n_dyn, int n_slots, int vm_depth,
@@ -237,12 +244,14 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     const size_t U = static_cast<size_t>(n) * (n + 1) / 2;
     const size_t nc = n_coeff > 0 ? n_coeff : 1, nd = n_dyn > 0 ? n_dyn : 1, ns = n_slots > 0 ? n_slots : 1;
     AdjLayout L{};
-    size_t o = 0;
+    L.glob = tpt >= 256;
+    size_t o = 0, og = 0;
+    size_t& om = L.glob ? og : o;  // cursor of the buffers that move to device memory
     L.tab = o; o = align16(o + (1 + n_formula) * 16);
     L.G = o; o = align16(o + U * 16);
     L.LS = o; o = align16(o + U * 16);
-    L.MU = o; o = align16(o + 6 * static_cast<size_t>(N) * 8);
-    L.YB = o; o = align16(o + static_cast<size_t>(N) * 8);
+    L.MU = om; om = align16(om + 6 * static_cast<size_t>(N) * 8);
+    L.YB = om; om = align16(om + static_cast<size_t>(N) * 8);
     L.slots = o; o = align16(o + 6 * ns * 16);
     L.dslots = o; o = align16(o + 6 * ns * kMaxGrad * 16);
     L.sv = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 16);
@@ -253,15 +262,17 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     L.cdyn = o; o = align16(o + 6 * nd * 16);
     L.ddyn = o; o = align16(o + 6 * nd * kMaxGrad * 16);
     L.dcls = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 16);
-    L.S = o; o = align16(o + 2 * nc * static_cast<size_t>(tpt) * 16);
+    L.S = om; om = align16(om + 2 * nc * static_cast<size_t>(tpt) * 16);
     L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
     L.traj = o; o = align16(o + 16);
     L.bytes = o;
+    L.gbytes = og;
     return L;
 }
 
+// the record streams staged per CTA (large systems read them from the plan's device image)
 __host__ __device__ inline size_t adj_plan_smem_bytes(const DevPlan& P, int tpt) {
-    return align16(static_cast<size_t>(P.n_biter + P.n_titer + P.n_tin) * tpt * 4);
+    return tpt >= 256 ? 0 : align16(static_cast<size_t>(P.n_biter + P.n_titer + P.n_tin) * tpt * 4);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -270,35 +281,44 @@ __host__ __device__ inline size_t adj_plan_smem_bytes(const DevPlan& P, int tpt)
 template <int TPT, int EPT>
 __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const CallArgs A, const AdjArgs J, int gpb,
                                                          size_t group_bytes, int M) {
-    static_assert(TPT >= 32 && TPT <= 128, "the adjoint runs 32, 64 or 128 threads per trajectory");
+    static_assert(TPT >= 32 && TPT <= 256, "the adjoint runs 32, 64, 128 or 256 threads per trajectory");
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
     const int n = P.n, N = P.N, U = P.U;
-    uint32_t* s_bil = reinterpret_cast<uint32_t*>(smem);
-    uint32_t* s_trec = s_bil + static_cast<size_t>(P.n_biter) * TPT;
-    uint32_t* s_lin = s_trec + static_cast<size_t>(P.n_titer) * TPT;
-    for (int i = threadIdx.x; i < P.n_biter * TPT; i += blockDim.x) s_bil[i] = P.bil[i];
-    for (int i = threadIdx.x; i < P.n_titer * TPT; i += blockDim.x) s_trec[i] = P.trec[i];
-    for (int i = threadIdx.x; i < P.n_tin * TPT; i += blockDim.x) s_lin[i] = P.lane_in[i];
+    const uint32_t* s_bil = P.bil;
+    const uint32_t* s_trec = P.trec;
+    const uint32_t* s_lin = P.lane_in;
+    if constexpr (TPT < 256) {
+        uint32_t* b = reinterpret_cast<uint32_t*>(smem);
+        uint32_t* tr = b + static_cast<size_t>(P.n_biter) * TPT;
+        uint32_t* li = tr + static_cast<size_t>(P.n_titer) * TPT;
+        for (int i = threadIdx.x; i < P.n_biter * TPT; i += blockDim.x) b[i] = P.bil[i];
+        for (int i = threadIdx.x; i < P.n_titer * TPT; i += blockDim.x) tr[i] = P.trec[i];
+        for (int i = threadIdx.x; i < P.n_tin * TPT; i += blockDim.x) li[i] = P.lane_in[i];
+        s_bil = b;
+        s_trec = tr;
+        s_lin = li;
+    }
     __syncthreads();
     if (g >= gpb) return;
 
     const AdjLayout Lay = adj_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, TPT);
     unsigned char* gb = smem + adj_plan_smem_bytes(P, TPT) + static_cast<size_t>(g) * group_bytes;
+    unsigned char* gm = Lay.glob ? J.gscratch + (static_cast<size_t>(blockIdx.x) * gpb + g) * J.gstride : gb;
     double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
     double2* s_G = reinterpret_cast<double2*>(gb + Lay.G);
     double* s_G64 = reinterpret_cast<double*>(gb + Lay.G);
     double2* s_LS = reinterpret_cast<double2*>(gb + Lay.LS);
     double* s_LS64 = reinterpret_cast<double*>(gb + Lay.LS);
-    double* s_MU = reinterpret_cast<double*>(gb + Lay.MU);
-    double* s_YB = reinterpret_cast<double*>(gb + Lay.YB);
+    double* s_MU = reinterpret_cast<double*>(gm + Lay.MU);
+    double* s_YB = reinterpret_cast<double*>(gm + Lay.YB);
     double2* s_cstat = reinterpret_cast<double2*>(gb + Lay.cstat);
     double2* s_dcstat = reinterpret_cast<double2*>(gb + Lay.dcstat);
     double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
     double2* s_ddyn = reinterpret_cast<double2*>(gb + Lay.ddyn);
     double2* s_dcls = reinterpret_cast<double2*>(gb + Lay.dcls);
-    double2* s_S = reinterpret_cast<double2*>(gb + Lay.S);
+    double2* s_S = reinterpret_cast<double2*>(gm + Lay.S);
     double* s_red = reinterpret_cast<double*>(gb + Lay.red);
     long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
     const int ns = P.n_slots > 0 ? P.n_slots : 1;
@@ -590,8 +610,8 @@ cudaError_t launch_adjoint_shape(const DevPlan& P, const CallArgs& A, const AdjA
     return cudaGetLastError();
 }
 
-// the adjoint widths (the integrator shapes below 256 threads per trajectory)
-#define OBE_FOR_EACH_ADJOINT(X) X(32, 8) X(32, 16) X(64, 16) X(128, 16)
+// the adjoint widths (the integrator shapes up to 256 threads per trajectory)
+#define OBE_FOR_EACH_ADJOINT(X) X(32, 8) X(32, 16) X(64, 16) X(128, 16) X(256, 32)
 #ifndef OBE_INSTANCE_TU
 #define OBE_EXTERN_ADJOINT(T, E)                                                                                      \
     extern template cudaError_t launch_adjoint_shape<T, E>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, \

@@ -1,7 +1,7 @@
 // obe_instance.cu -- one kernel shape per compilation: the build compiles this file once per
 // (threads per trajectory, elements per thread) pair, -DOBE_TPT=.. -DOBE_EPT=.., which
 // instantiates the integrator in both forms (and, with -DOBE_RHS, the RHS kernel of that width;
-// up to 128 threads per trajectory also the adjoint kernel).
+// up to 256 threads per trajectory also the adjoint kernel).
 #define OBE_INSTANCE_TU
 #include "obe_kernels.cuh"
 #include "obe_adjoint.cuh"
@@ -23,7 +23,7 @@ template cudaError_t launch_rhs_shape<OBE_TPT, true>(const DevPlan&, long long, 
                                                      const double*, double*, int, int, size_t, size_t, int, unsigned char*,
                                                      size_t);
 #endif
-#if OBE_TPT <= 128
+#if OBE_TPT <= 256
 template cudaError_t launch_adjoint_shape<OBE_TPT, OBE_EPT>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, size_t,
                                                             size_t, int, cudaStream_t);
 #endif

@@ -1033,10 +1033,8 @@ static obe_status grad_check(const obe_plan* p, const obe_solve_options* o, int6
         set_error("gradients through a stop_event are not supported");
         return OBE_ERR_UNSUPPORTED;
     }
-    if (p->packed.tpt > 128) {
-        set_error(threads_per_trajectory_for(p->n) <= 128
-                      ? "gradients need the plan at 128 threads per trajectory or fewer: call obe_plan_set_shape"
-                      : "gradients are implemented for systems of up to 45 states");
+    if (p->packed.tpt > 256) {
+        set_error("gradients need the plan at 256 threads per trajectory or fewer: call obe_plan_set_shape");
         return OBE_ERR_UNSUPPORTED;
     }
     if (o->output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !o->store_trace && !o->has_saveat) {
@@ -1162,7 +1160,8 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     const DevPlan& P = p->dev;
     const int tpt = P.tpt;
     const size_t plan_bytes = adj_plan_smem_bytes(P, tpt);
-    const size_t group = adj_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, tpt).bytes;
+    const AdjLayout AL = adj_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, tpt);
+    const size_t group = AL.bytes;
     const size_t limit = 227 * 1024;
     int gpb = 256 / tpt;
     while (gpb > 1 && plan_bytes + gpb * group > limit) --gpb;
@@ -1171,12 +1170,17 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     while (gpb > 1 && gpb > per_sm) --gpb;
     const size_t smem = plan_bytes + gpb * group;
     const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n_traj + gpb - 1) / gpb, sm_count())));
-    if (checkpoint_every > 0) {
-        // one segment of full records per resident trajectory group
-        J.seg_stride = static_cast<long long>(checkpoint_every) * J.rec_stride;
+    // per resident trajectory group, in the plan's device scratch: one segment of full records
+    // (checkpointed tape) and the large systems' slice
+    const size_t groups = static_cast<size_t>(blocks) * gpb;
+    const size_t seg_bytes = checkpoint_every > 0 ? align16(static_cast<size_t>(checkpoint_every) * J.rec_stride * 8) : 0;
+    if (seg_bytes + AL.gbytes > 0) {
         unsigned char* gk = nullptr;
-        if ((st = kscratch(p, static_cast<size_t>(J.seg_stride) * 8 * static_cast<size_t>(blocks) * gpb, &gk)) != OBE_OK) return st;
+        if ((st = kscratch(p, groups * (seg_bytes + AL.gbytes), &gk)) != OBE_OK) return st;
         J.seg = reinterpret_cast<double*>(gk);
+        J.seg_stride = static_cast<long long>(seg_bytes / 8);
+        J.gscratch = gk + groups * seg_bytes;
+        J.gstride = AL.gbytes;
     }
     if (!cuda_ok(cudaMemsetAsync(J.counter, 0, sizeof(unsigned long long), s), "cudaMemsetAsync")) return OBE_ERR_CUDA;
     const int method = opt->solver == OBE_SOLVER_TSIT5 ? 1 : 0;

@@ -1,5 +1,6 @@
 """GPU gradients (centrex_tlf_gb300.autograd over obe_grad_forward / obe_grad_backward) against
-central finite differences of the CPU oracle replaying the same frozen step sequence.
+central finite differences of the CPU oracle replaying the same frozen step sequence, for the
+16-, 39- and 76-state systems, full and checkpointed tapes.
 
 The adjoint differentiates the discrete solve with its accepted steps frozen, so the check is
 the oracle's replay of exactly those steps at p +- eps (eps = 1e-6 |p|): agreement to 1e-5
@@ -184,6 +185,20 @@ def test_checkpointed_tape_matches_the_full_tape(q1, ck):
     np.testing.assert_allclose(res[ck][2], res[0][2], rtol=1e-9, atol=1e-12 * np.max(np.abs(res[0][2])))
     assert res[ck][3] < res[0][3] / 5  # 2 + N / C doubles per step instead of 2 + 7 N
     _fd_check(d, plan, op, p0, slots, checkpoint_every=ck)
+
+
+@pytest.mark.parametrize("ck", [0, 16])
+def test_gradients_of_the_76_state_system(golden, ck):
+    """The 76-state system (256 threads per trajectory; the adjoint's mu, ybar and class sums in
+    device memory), square-wave polarisations: gradients of the excited-population integral over
+    [0, 6/Γ] with respect to both lasers' Rabi rates and detunings, full and checkpointed tape."""
+    d = golden("plan_rc_76")
+    g = d["gamma"]
+    plan = NativePlan(d["payload"])
+    assert plan.shape()[0] == 256
+    op = oracle.OraclePlan(d["payload"])
+    p0 = np.array([[1.2 * g, 2.0 * g, 0.3 * g, -0.2 * g], [2.5 * g, 0.8 * g, -0.4 * g, 0.6 * g]])
+    _fd_check(d, plan, op, p0, _slots(d, ("Ω0", "Ω1", "δ0", "δ1")), t_span=(0.0, 6.0 / g), checkpoint_every=ck)
 
 
 def test_initial_state_gradient_matches_finite_differences(q1):

@@ -121,8 +121,8 @@ def test_gradients_need_a_narrow_layout(golden):
     plan = NativePlan(d["payload"])
     names = d["payload"]["parameter_graph"]["slot_names"]
     p = torch.tensor([[d["gamma"], 0.0]], dtype=torch.float64, device="cuda", requires_grad=True)
-    plan.set_shape(256, 0)
-    with pytest.raises(NotImplementedError, match="gradients need the plan at 128 threads per trajectory or fewer"):
+    plan.set_shape(512, 0)
+    with pytest.raises(NotImplementedError, match="gradients need the plan at 256 threads per trajectory or fewer"):
         solve_batch_with_grad(plan, d["rho0_packed"], d["t_span"], p, [names.index("rabi"), names.index("detuning")],
                               dt=1e-3 / d["gamma"], integral_weights=[(13, 1.0)])
     plan.set_shape(0, 0)
