@@ -258,7 +258,7 @@ obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options*
  * 256), each with as many trajectories per CTA as fit, half that, and one.  The candidates and
  * their probe times (ms) go to cand_tpt / cand_gpb / cand_ms (up to cand_cap entries; n_cand
  * receives the count).  Synchronises `stream`; allocates and frees its probe outputs.
- * Gradients need a plan width of 128 threads or fewer.  None of these may run while a solve of
+ * Gradients need a plan width of 256 threads or fewer.  None of these may run while a solve of
  * the same plan is in flight on another thread.
  */
 obe_status obe_plan_set_shape(obe_plan* plan, int32_t threads_per_trajectory, int32_t trajectories_per_cta);
@@ -303,8 +303,8 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
  * discrete adjoint of the double-precision adaptive solve with its step sequence frozen, for
  * final weighted integrals (output_when="final", saveat None) and final populations, with
  * respect to base parameter slots and the initial state.  Device pointers, asynchronous on
- * `stream`; systems of up to 45 states (a plan width of 128 threads or fewer), dopri5/tsit5, no
- * stop event.
+ * `stream`; every system the solver takes (up to 90 states, a plan width of 256 threads or
+ * fewer), dopri5/tsit5, no stop event.
  *
  * obe_grad_forward is obe_solve_batch_device that also records a tape per trajectory into d_tape
  * (caller-owned, n_traj * obe_grad_tape_doubles(plan, max_steps, checkpoint_every) doubles).
