@@ -253,6 +253,87 @@ def save_multi(centrex_tlf) -> None:
             codec.save("rhs_r0_39", {"cases": cases})
 
 
+def build_r2_38(centrex_tlf):
+    """The 38-state R(2) system of the reference's expanded_sparse solve benchmark
+    (benchmarks/bench_expanded_sparse_packed_rhs_kernels.py:36-47 constants, :162-300 construction):
+    R(2) F1'=7/2 F'=3 with x polarisation, ground and excited mains X J=2 F1=5/2 F=2 mF=0 and
+    B F'=3 mF=1, opposite-parity levels retained, E = 200 V/cm and B = 1e-5 G along z, the Rabi
+    rate of 60 mW in a 2 cm x 2 cm rectangular beam, zero detuning; rho0 = the lowest-energy
+    X J=2 F1=5/2 F=2 mF=0 state; photon integral with weight Γ on every B state over 0.02 m /
+    184 m/s.  The reference records its Rust solve of this system
+    (benchmarks/expanded_sparse_static_dynamic_results/validation.csv, solve_timings.csv,
+    grid_timings.csv).  Those records predate the reference's 0.2.4 constants (CHANGELOG.md:118-123:
+    Γ = 1/τ_B instead of the hard-coded 2π·1.56 MHz, a new X rotational model), so the system is
+    built with Γ = 2π·1.56 MHz, the value of `hamiltonian.Γ` then; with it the recorded step and
+    RHS counts are reproduced exactly and the photon integral to 1e-4 (the X-model change).
+    """
+    from centrex_tlf import couplings, lindblad, states, transitions
+    from centrex_tlf.lindblad.parameters import LindbladParameters
+    from centrex_tlf.lindblad.plan_static import prepare_lindblad_problem
+    from centrex_tlf.utils.rabi import power_to_rabi_rectangular_beam
+
+    tr = transitions.R2_F1_7o2_F3
+    gamma_ref = GAMMA  # 2π·1.56 MHz (see above)
+    x_main = 1 * next(iter(states.generate_coupled_states_X(states.QuantumSelector(
+        electronic=states.ElectronicState.X, J=tr.J_ground, F1=5 / 2, F=2, mF=0, P=tr.P_ground))))
+    b_main = 1 * next(iter(states.generate_coupled_states_B(states.QuantumSelector(
+        electronic=states.ElectronicState.B, J=tr.J_excited, F1=tr.F1_excited, F=tr.F_excited, mF=1,
+        P=tr.P_excited))))
+    selectors = couplings.generate_transition_selectors(
+        transitions=[tr], polarizations=[[couplings.polarization_X]], ground_mains=[x_main], excited_mains=[b_main])
+    import warnings
+    with warnings.catch_warnings():
+        warnings.filterwarnings("ignore", message="Low overlap detected.*")
+        system = lindblad.generate_OBE_system_transitions(
+            [tr], selectors, qn_compact=True, E=np.array([0.0, 0.0, 200.0]), B=np.array([0.0, 0.0, 1e-5]),
+            retain_opposite_parity_levels=True, Γ=gamma_ref)
+    rabi_rad_s = power_to_rabi_rectangular_beam(60e-3, abs(system.couplings[0].main_coupling), 0.02, 0.02)
+    params = LindbladParameters()
+    rabi = params.real("rabi", rabi_rad_s)
+    detuning = params.real("detuning", 0.0)
+    det_symbol = getattr(selectors[0], "\u03b4")
+    for sym in system.H_symbolic.free_symbols:
+        if sym in system.coupling_symbols:
+            params.bind(sym, rabi, finalize=False)
+        elif sym == det_symbol:
+            params.bind(sym, detuning, finalize=False)
+        else:
+            params.real(str(sym), 0.0)
+    for group in system.polarization_symbols:
+        for sym in (group if isinstance(group, (list, tuple)) else [group]):
+            params.bind(sym, 1.0, finalize=False)
+    params._finalize()
+    prepared = prepare_lindblad_problem(system, params, backend="python", hamiltonian_representation="decomposed")
+    cands = [i for i, st in enumerate(system.QN)
+             if st.largest.electronic_state == states.ElectronicState.X and st.largest.J == tr.J_ground
+             and st.largest.F1 == 5 / 2 and st.largest.F == 2 and st.largest.mF == 0]
+    start = min(cands, key=lambda i: float(np.real(system.H_int[i, i])))
+    excited = [i for i, st in enumerate(system.QN) if st.largest.electronic_state == states.ElectronicState.B]
+    return prepared, start, excited, gamma_ref
+
+
+def save_r2_38(centrex_tlf) -> None:
+    """plan_r2_38.json: the 38-state R(2) benchmark system with the reference's recorded Rust
+    results for it (single photon integral, step and RHS counts; 9-point detuning grid counts)."""
+    prep, start, excited, gamma_ref = build_r2_38(centrex_tlf)
+    payload = prep.to_payload()
+    n = payload["n_states"]
+    payload["dense_c_array"] = np.zeros((0, n, n), dtype=np.complex128)  # never read on this path
+    rho = np.zeros((n, n), dtype=np.complex128)
+    rho[start, start] = 1.0
+    codec.save("plan_r2_38", {
+        "payload": payload, "rho0_packed": prep.layout.pack(rho), "gamma": gamma_ref,
+        "t_span": [0.0, 0.02 / 184.0],
+        # benchmarks/expanded_sparse_static_dynamic_results: validation.csv (static_dynamic =
+        # expanded_sparse), solve_timings.csv:7, grid_timings.csv:7
+        "kat": {"photon_integral": 1.2128563927511686, "accepted_steps": 28651, "rejected_steps": 0,
+                "rhs_calls": 171907, "abstol": 1e-9, "reltol": 1e-7, "dt": 1e-9, "solver": "dopri5",
+                "weights": [[int(i), gamma_ref] for i in excited]},
+        "kat_grid": {"detuning": 2 * np.pi * 1e6 * np.linspace(-80.0, 80.0, 9), "accepted_steps": 329395,
+                     "rejected_steps": 0, "rhs_calls": 1976397},
+    })
+
+
 def build_rc_76(centrex_tlf):
     """The 76-state rotational-cooling-sized system: X J=0-3 (64 hyperfine states) + B J'=1
     F1'=1/2, 3/2 (P=-1, 12 states), driven by R(0) F1'=1/2 F'=1 and P(2) F1'=3/2 F'=1 with x and z
@@ -482,6 +563,9 @@ def main() -> None:
     if "--multi" in sys.argv:
         save_multi(_import_reference())
         return
+    if "--r2-38" in sys.argv:
+        save_r2_38(_import_reference())
+        return
     centrex_tlf = _import_reference()
     started = time.perf_counter()
 
@@ -570,6 +654,7 @@ def main() -> None:
     # --- 76-state rotational-cooling system (the large-system path, n > 45) ------------------
     save_rc_76(centrex_tlf)
     save_multi(centrex_tlf)
+    save_r2_38(centrex_tlf)
 
     # --- the native-boundary call contract of the reference's Python surface ----------------
     codec.save("ffi_calls", record_ffi_calls(centrex_tlf, q1, rho_q))

@@ -260,3 +260,26 @@ def test_fixed_step_saveat_and_errors(golden):
         p.solve_single(_opts(p, dt=0.0, solver="fixed_rk2"), d["rho0_packed"])
     with pytest.raises(oracle.OracleError, match=r"^Stopped at x=0\.2\. Need more than 2 steps\.$"):
         p.solve_single(_opts(p, dt=0.1, maxiters=2, solver="fixed_dopri5"), d["rho0_packed"])
+
+
+def test_r2_38_state_known_answer(golden):
+    """The reference's heavy known answer: its Rust solve of the 38-state R(2) benchmark system
+    (benchmarks/expanded_sparse_static_dynamic_results/solve_timings.csv:7: 28651 accepted, 0
+    rejected, 171907 RHS calls; validation.csv: photon integral 1.2128563927511686; grid_timings.csv:7:
+    the 9-point detuning grid, 329395 accepted steps, 1976397 RHS calls).  The records predate the
+    reference's 0.2.4 X rotational model, which moves the integral by 8.6e-5 relative and the grid
+    by one step; the single solve's step and RHS counts are exact."""
+    d = golden("plan_r2_38")
+    k, kg = d["kat"], d["kat_grid"]
+    p = oracle.OraclePlan(d["payload"])
+    o = p.options(t0=0.0, t1=d["t_span"][1], abstol=k["abstol"], reltol=k["reltol"], dt=k["dt"], saveat=None,
+                  save_start=True, maxiters=100000, solver=k["solver"], output="photon_integral", output_indices=None,
+                  output_when="final", integral_weights=[tuple(w) for w in k["weights"]], stop_event=None)
+    _, v, st = p.solve_single(o, d["rho0_packed"])
+    assert (st["accepted_steps"], st["rejected_steps"], st["rhs_calls"]) == (k["accepted_steps"], 0, k["rhs_calls"])
+    assert abs(float(np.asarray(v).reshape(-1)[0]) / k["photon_integral"] - 1.0) < 1e-4
+    _, _, gst = p.solve_batch(o, d["rho0_packed"], [p.slot_names.index("detuning")],
+                              kg["detuning"].reshape(-1, 1).astype(complex))
+    assert abs(int(gst["accepted_steps"].sum()) - kg["accepted_steps"]) <= 2
+    assert int(gst["rejected_steps"].sum()) == 0
+    assert abs(int(gst["rhs_calls"].sum()) - kg["rhs_calls"]) <= 12
