@@ -128,6 +128,28 @@ class ObeTrajStats(ctypes.Structure):
     ]
 
 
+class ObeInterpOperator(ctypes.Structure):
+    """obe_interp_operator: a CSR matrix whose entries are cubics in the field coordinate."""
+
+    _fields_ = [("row_ptrs", c_i64p), ("col_indices", c_i64p), ("coeffs", c_f64p), ("nnz", ctypes.c_int64)]
+
+
+class ObeEffectiveDesc(ctypes.Structure):
+    """obe_effective_desc: the operators and slots of an interpolated effective-Hamiltonian plan."""
+
+    _fields_ = [
+        ("real_dim", ctypes.c_int64),
+        ("n_grid", ctypes.c_int32),
+        ("field_grid", c_f64p),
+        ("combined", ObeInterpOperator),
+        ("optical", ObeInterpOperator),
+        ("detuning", ObeInterpOperator),
+        ("field_slot", ctypes.c_int32),
+        ("rabi_slot", ctypes.c_int32),
+        ("detuning_slot", ctypes.c_int32),
+    ]
+
+
 class ObeBatchJob(ctypes.Structure):
     """obe_batch_job: one device-resident batch of obe_solve_multi_device."""
 
@@ -238,6 +260,9 @@ def load_library() -> ctypes.CDLL:
     lib.obe_last_launch_count.restype = ctypes.c_int64
     lib.obe_solve_multi_device.argtypes = [ctypes.c_int32, ctypes.POINTER(ObeBatchJob), ctypes.c_void_p]
     lib.obe_solve_multi_device.restype = ctypes.c_int
+    lib.obe_effective_plan_create.argtypes = [ctypes.POINTER(ObePlanDesc), ctypes.POINTER(ObeEffectiveDesc),
+                                              ctypes.POINTER(ctypes.c_void_p)]
+    lib.obe_effective_plan_create.restype = ctypes.c_int
     lib.obe_plan_set_shape.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]
     lib.obe_plan_set_shape.restype = ctypes.c_int
     lib.obe_plan_get_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]

@@ -52,7 +52,10 @@ class SolveOptions:
         integral_weights: Sequence[tuple[int, float]] | None,
         stop_event: dict[str, Any] | None,
         precision: str = "fp64",
+        state_len: int | None = None,
     ) -> None:
+        # the state vector's length: n^2 packed Hermitian, or 2 n^2 split-real (effective plans)
+        state_len = n_states * n_states if state_len is None else int(state_len)
         if solver not in _abi.SOLVERS:
             raise ValueError(
                 "solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4', "
@@ -108,7 +111,7 @@ class SolveOptions:
                 raise ValueError(f"output='{output}' requires integral_weights")
             w = [(int(i), float(v)) for i, v in integral_weights]
             for i, _ in w:
-                if not (0 <= i < n_states * n_states):
+                if not (0 <= i < state_len):
                     raise ValueError(f"integral weight index {i} out of bounds")
             self.weight_index = np.asarray([x[0] for x in w] or [0], dtype=np.int64)
             self.weight_value = np.asarray([x[1] for x in w] or [0.0], dtype=np.float64)
@@ -121,7 +124,7 @@ class SolveOptions:
             self.width = 1
         elif output == "full":
             o.output = _abi.OUTPUT_FULL
-            self.width = n_states * n_states
+            self.width = state_len
         else:
             raise ValueError(f"unknown output mode: {output!r}")
         o.weight_index = _abi.ptr(self.weight_index, ctypes.c_int64)

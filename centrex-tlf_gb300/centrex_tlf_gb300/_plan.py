@@ -226,3 +226,80 @@ class PlanArrays:
     @property
     def packed_len(self) -> int:
         return self.n_states * self.n_states
+
+
+def _required_key(d: dict, key: str):
+    if key not in d:
+        raise ValueError(f"missing key: {key}")
+    return d[key]
+
+
+class EffectiveArrays:
+    """Owns every array of an interpolated effective-Hamiltonian plan and its two descriptors:
+    the parameter graph as an ``obe_plan_desc`` (no Hamiltonian coefficients, no expanded plan)
+    and the operators as an ``obe_effective_desc``.  ``plan_dict`` is what the reference's
+    prepare_effective_lindblad_rust_plan hands to its native prepare_effective_lindblad_plan_py
+    (centrex_tlf/effective_hamiltonian/rust_plan.py:185-200; parsed in
+    rust/src/effective_lindblad/plan.rs:116-203, whose error texts these checks keep)."""
+
+    def __init__(self, plan_dict: dict) -> None:
+        if "parameter_graph" not in plan_dict:
+            raise ValueError("missing 'parameter_graph'")
+        self.n_states = int(_required_key(plan_dict, "n_states"))
+        self.real_dim = int(_required_key(plan_dict, "real_dim"))
+        self.n_grid = int(_required_key(plan_dict, "n_grid"))
+        self.field_grid = np.ascontiguousarray(np.asarray(_required_key(plan_dict, "field_grid"), dtype=np.float64).reshape(-1))
+        for key in ("excited_indices", "ground_indices", "sink_indices"):
+            _required_key(plan_dict, key)
+        self.field_slot = int(_required_key(plan_dict, "field_coordinate_slot"))
+        self.rabi_slot = int(_required_key(plan_dict, "rabi_rate_slot"))
+        self.detuning_slot = int(_required_key(plan_dict, "detuning_slot"))
+        bool(_required_key(plan_dict, "is_time_dependent"))
+        if self.field_grid.size != self.n_grid:
+            raise ValueError("field_grid length mismatch")
+        n = self.n_states
+        graph_payload = {
+            "n_states": n, "parameter_graph": plan_dict["parameter_graph"],
+            "hamiltonian_plan": {"kind": "decomposed", "n": n, "coefficients": []},
+            "source_decay_rates": np.zeros(n), "incoming_transfers_by_target": [],
+            "dense_c_array": np.zeros((0, n, n), dtype=np.complex128), "expanded_rhs_plan": None,
+        }
+        self.graph = PlanArrays(graph_payload)
+        n_slots = len(self.graph.slot_names)
+        for name, slot in (("field_coordinate", self.field_slot), ("rabi_rate", self.rabi_slot),
+                           ("detuning", self.detuning_slot)):
+            if not 0 <= slot < n_slots:
+                raise ValueError(f"{name} slot {slot} out of range")
+        self.ops = {}
+        desc = _abi.ObeEffectiveDesc()
+        desc.real_dim = self.real_dim
+        desc.n_grid = self.n_grid
+        desc.field_grid = _abi.ptr(self.field_grid, ctypes.c_double)
+        for key, field in (("sparse_combined", "combined"), ("sparse_opt", "optical"), ("sparse_det", "detuning")):
+            if key not in plan_dict:
+                raise ValueError(f"missing sparse operator: {key}")
+            op = plan_dict[key]
+            rows = np.ascontiguousarray(np.asarray(_required_key(op, "row_ptrs"), dtype=np.int64).reshape(-1))
+            cols = np.ascontiguousarray(np.asarray(_required_key(op, "col_indices"), dtype=np.int64).reshape(-1))
+            coef = np.ascontiguousarray(np.asarray(_required_key(op, "pchip_coeffs"), dtype=np.float64).reshape(-1))
+            _required_key(op, "grid")
+            nnz = int(_required_key(op, "nnz"))
+            if rows.size != self.real_dim + 1 or rows[0] != 0 or rows[-1] != nnz or np.any(np.diff(rows) < 0):
+                raise ValueError(f"{key}: row_ptrs must be {self.real_dim + 1} monotonic offsets from 0 to nnz")
+            if cols.size != nnz or (nnz and (cols.min() < 0 or cols.max() >= self.real_dim)):
+                raise ValueError(f"{key}: col_indices must hold nnz indices below real_dim")
+            if coef.size != max(self.n_grid - 1, 0) * nnz * 4:
+                raise ValueError(f"{key}: pchip_coeffs must hold (n_grid - 1) * nnz * 4 values")
+            keep = (rows, cols if cols.size else np.zeros(1, np.int64), coef if coef.size else np.zeros(1))
+            self.ops[key] = keep
+            target = getattr(desc, field)
+            target.row_ptrs = _abi.ptr(keep[0], ctypes.c_int64)
+            target.col_indices = _abi.ptr(keep[1], ctypes.c_int64)
+            target.coeffs = _abi.ptr(keep[2], ctypes.c_double)
+            target.nnz = nnz
+        desc.field_slot = self.field_slot
+        desc.rabi_slot = self.rabi_slot
+        desc.detuning_slot = self.detuning_slot
+        self.desc = desc
+        self.slot_names = self.graph.slot_names
+        self.n_base = self.graph.n_base

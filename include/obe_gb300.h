@@ -238,6 +238,46 @@ obe_status obe_solve_batch_device(const obe_plan* plan, const obe_solve_options*
                                   obe_traj_stats* d_stats, void* stream);
 
 /*
+ * Interpolated effective-Hamiltonian Lindblad plans (rust/src/effective_lindblad: the native side
+ * of centrex_tlf/effective_hamiltonian/rust_plan.py).  The state is the split-real density
+ * matrix [Re rho (row-major n x n), Im rho] of real_dim = 2 n^2 doubles, and
+ *     dy = L_c(x) y + (Omega / 2) L_o(x) y + delta L_d(x) y          (effective_lindblad/rhs.rs:88-137)
+ * with x, Omega and delta the parameter-graph slots field_slot, rabi_slot and detuning_slot at
+ * time t, and each operator a real CSR matrix whose entries are cubics in x on the field grid:
+ * on interval k (grid[k] <= x <= grid[k + 1], found with the reference's cached search and its
+ * 1e-10 range tolerance), entry p is c0 + dx (c1 + dx (c2 + dx c3)) with dx = x - grid[k] and
+ * (c0..c3) = coeffs[(k * nnz + p) * 4 ..].  As in the reference, a Rabi or detuning slot that is a
+ * base scalar, or a compound that does not depend on time, is fixed at plan creation to its value
+ * from the base parameters (effective_lindblad/plan.rs: detect_constant_slot), so batch overrides
+ * do not reach it.
+ *
+ * obe_effective_plan_create takes the parameter graph in `graph` (n_states and the parameter
+ * fields; no Hamiltonian coefficients, no expanded plan) and the operators in `eff`.  The plan
+ * then solves through obe_solve_single / obe_solve_batch / obe_solve_batch_device with the
+ * effective API's output conventions: populations are the diagonal y[i (n + 1)], a selected
+ * (i, j) is (y[i n + j], y[n^2 + i n + j]), full outputs and integral weights index the
+ * real_dim-vector.  Double precision only; no stop events.  obe_rhs_eval evaluates its RHS
+ * (debug_effective_lindblad_rhs_py), y and dy holding real_dim doubles per state.
+ */
+typedef struct {
+    const int64_t* row_ptrs;     /* [real_dim + 1]                                            */
+    const int64_t* col_indices;  /* [nnz]                                                     */
+    const double* coeffs;        /* [(n_grid - 1) * nnz * 4], interval-major                  */
+    int64_t nnz;
+} obe_interp_operator;
+
+typedef struct {
+    int64_t real_dim;            /* 2 n_states^2                                              */
+    int32_t n_grid;
+    const double* field_grid;    /* [n_grid], increasing                                     */
+    obe_interp_operator combined, optical, detuning;
+    int32_t field_slot, rabi_slot, detuning_slot;
+} obe_effective_desc;
+
+obe_status obe_effective_plan_create(const obe_plan_desc* graph, const obe_effective_desc* eff,
+                                     obe_plan** out_plan);
+
+/*
  * Launch-shape tuning (no counterpart in the reference, whose CPU path has no launch shape).
  * A solve runs each trajectory on a group of threads (32, 64, 128, 256 or 512: the compiled
  * widths; 16 packed elements per thread, 32 at 256 threads) and puts one or more groups in a

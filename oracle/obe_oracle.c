@@ -784,6 +784,19 @@ struct orc_plan {
     /* grouped split-input layout (n > 40) */
     int64_t *gr_ptr, *gc_ptr;
     dyn_term *gr, *gc;
+    /* populations are y[i * pop_stride]: 1 in the packed layout, n + 1 in the split-real one */
+    int64_t pop_stride;
+    /* interpolated effective-Hamiltonian plans (effective_lindblad/plan.rs, rhs.rs) */
+    int32_t eff;
+    int32_t eff_ngrid;
+    double* eff_grid;
+    int64_t* eff_rows[3];
+    int64_t* eff_cols[3];
+    double* eff_coef[3];
+    int64_t eff_nnz[3];
+    int32_t eff_field, eff_rabi, eff_det;
+    int32_t eff_rabi_const, eff_det_const;
+    double eff_rabi_val, eff_det_val;
 };
 
 #define PARTITIONED_MAX_STATES 40
@@ -869,7 +882,93 @@ static void plan_free(orc_plan* p) {
     free(p);
 }
 
-void orc_plan_destroy(orc_plan* plan) { plan_free(plan); }
+void orc_plan_destroy(orc_plan* plan) {
+    if (plan && plan->eff) {
+        free(plan->eff_grid);
+        for (int k = 0; k < 3; ++k) { free(plan->eff_rows[k]); free(plan->eff_cols[k]); free(plan->eff_coef[k]); }
+    }
+    plan_free(plan);
+}
+
+/* detect_constant_slot (effective_lindblad/plan.rs:205-277): a base scalar, or a compound whose
+   program neither reads the time nor a slot whose (first) compound reads it, evaluated at t = 0
+   from the base values with the compounds before it (no interpolation tables) */
+static int eff_constant_slot(const orc_plan* p, int32_t slot, double* out) {
+    if (slot < p->n_base && !p->base[slot].is_tuple) { *out = p->base[slot].s.re; return 1; }
+    for (int32_t i = 0; i < p->n_comp; ++i) {
+        if (p->comp_slot[i] != slot) continue;
+        const expr_t* x = &p->comp_expr[i];
+        if (x->uses_time) return 0;
+        for (int64_t k = 0; k < x->n; ++k) {
+            if (x->op[k] != OP_SLOT) continue;
+            for (int32_t j = 0; j < p->n_comp; ++j)
+                if (p->comp_slot[j] == x->index[k]) {
+                    if (p->comp_expr[j].uses_time) return 0;
+                    break;
+                }
+        }
+        int32_t ns = p->n_slots > 0 ? p->n_slots : 1;
+        rv* slots = (rv*)calloc((size_t)ns, sizeof(rv));
+        for (int32_t b = 0; b < p->n_base; ++b) slots[b] = p->base[b];
+        int64_t ms = p->max_stack + 4;
+        rv* stack = (rv*)malloc(sizeof(rv) * (size_t)ms);
+        arena ar;
+        memset(&ar, 0, sizeof ar);
+        errbuf e = {{0}, 0};
+        pchip_ctx none = {NULL, 0, NULL};
+        for (int32_t j = 0; j < p->n_comp; ++j) {
+            if (p->comp_slot[j] == slot) break;
+            rv r;
+            e.set = 0;
+            if (!eval_general(&p->comp_expr[j], slots, 0.0, stack, &ar, &none, &r, &e)) slots[p->comp_slot[j]] = r;
+        }
+        rv r;
+        e.set = 0;
+        int ok = !eval_general(x, slots, 0.0, stack, &ar, &none, &r, &e) && !r.is_tuple;
+        if (ok) *out = r.s.re;
+        free(slots);
+        free(stack);
+        arena_free(&ar);
+        return ok;
+    }
+    return 0;
+}
+
+orc_plan* orc_effective_plan_create(const obe_plan_desc* graph, const obe_effective_desc* d, char* err, size_t err_len) {
+    errbuf e = {{0}, 0};
+    if (!graph || !d) { snprintf(err, err_len, "null argument"); return NULL; }
+    orc_plan* p = orc_plan_create(graph, err, err_len);
+    if (!p) return NULL;
+    if (d->n_grid < 1 || d->real_dim != 2 * (int64_t)p->n * p->n) {
+        fail(&e, d->n_grid < 1 ? "field_grid length mismatch" : "real_dim must be 2 n_states^2");
+        copy_err(&e, err, err_len);
+        plan_free(p);
+        return NULL;
+    }
+    p->eff = 1;
+    p->N = d->real_dim;
+    p->pop_stride = p->n + 1;
+    p->eff_ngrid = d->n_grid;
+    p->eff_grid = (double*)malloc(sizeof(double) * (size_t)d->n_grid);
+    memcpy(p->eff_grid, d->field_grid, sizeof(double) * (size_t)d->n_grid);
+    const obe_interp_operator* ops[3] = {&d->combined, &d->optical, &d->detuning};
+    for (int k = 0; k < 3; ++k) {
+        const int64_t nnz = ops[k]->nnz, nc = (int64_t)(d->n_grid > 1 ? d->n_grid - 1 : 0) * nnz * 4;
+        p->eff_nnz[k] = nnz;
+        p->eff_rows[k] = (int64_t*)malloc(sizeof(int64_t) * (size_t)(p->N + 1));
+        memcpy(p->eff_rows[k], ops[k]->row_ptrs, sizeof(int64_t) * (size_t)(p->N + 1));
+        p->eff_cols[k] = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nnz > 0 ? nnz : 1));
+        if (nnz > 0) memcpy(p->eff_cols[k], ops[k]->col_indices, sizeof(int64_t) * (size_t)nnz);
+        p->eff_coef[k] = (double*)malloc(sizeof(double) * (size_t)(nc > 0 ? nc : 1));
+        if (nc > 0) memcpy(p->eff_coef[k], ops[k]->coeffs, sizeof(double) * (size_t)nc);
+    }
+    p->eff_field = d->field_slot;
+    p->eff_rabi = d->rabi_slot;
+    p->eff_det = d->detuning_slot;
+    p->eff_rabi_const = eff_constant_slot(p, d->rabi_slot, &p->eff_rabi_val);
+    p->eff_det_const = eff_constant_slot(p, d->detuning_slot, &p->eff_det_val);
+    return p;
+}
 
 static int64_t upper_index(int32_t n, int32_t i, int32_t j) {
     /* row-major upper triangle including the diagonal (ir.py:463-475) */
@@ -885,6 +984,7 @@ orc_plan* orc_plan_create(const obe_plan_desc* d, char* err, size_t err_len) {
     p->n = d->n_states;
     p->N = (int64_t)p->n * p->n;
     p->U = (int64_t)p->n * (p->n + 1) / 2;
+    p->pop_stride = 1;
     p->n_slots = d->n_slots;
     p->n_base = d->n_base;
     if (p->n_base > p->n_slots) { fail(&e, "more base values than slots"); goto bad; }
@@ -1092,6 +1192,7 @@ typedef struct {
     cx* over_val;
     int valid;              /* cached coefficients valid (time-independent plans) */
     int use_split_input;
+    int64_t eff_hint;       /* the effective RHS's last field interval (rhs.rs: last_interval) */
     /* stop event */
     int ev_kind;
     expr_t ev_expr;
@@ -1206,10 +1307,88 @@ static inline void write_out(const orc_plan* p, double* out, int64_t u, double r
     if (q.im != NO_IM) out[q.im] = im;
 }
 
+/* Rust's `{:.6e}`: six decimals, exponent without sign padding ("1.000000e2", "-3.500000e-1") */
+static void fmt_rust_exp6(double v, char* out, size_t len) {
+    char buf[64];
+    snprintf(buf, sizeof buf, "%.6e", v);
+    char* e = strchr(buf, 'e');
+    if (!e) { snprintf(out, len, "%s", buf); return; }
+    int ex = atoi(e + 1);
+    *e = 0;
+    snprintf(out, len, "%.24se%d", buf, ex);
+}
+
+/* find_interval_cached (effective_lindblad/rhs.rs:48-86) */
+static int eff_find_interval(double x, const double* grid, int64_t n, int64_t* hint, int64_t* idx, errbuf* e) {
+    if (n < 2) { *idx = 0; return 0; }
+    const double tol = 1e-10 * fmax(fabs(grid[n - 1] - grid[0]), 1.0);
+    char a[64], b[64];
+    if (x < grid[0] - tol) {
+        fmt_rust_exp6(x, a, sizeof a);
+        fmt_rust_exp6(grid[0], b, sizeof b);
+        return fail(e, "field coordinate %s is below the operator grid minimum %s", a, b);
+    }
+    if (x > grid[n - 1] + tol) {
+        fmt_rust_exp6(x, a, sizeof a);
+        fmt_rust_exp6(grid[n - 1], b, sizeof b);
+        return fail(e, "field coordinate %s is above the operator grid maximum %s", a, b);
+    }
+    const double xc = x < grid[0] ? grid[0] : (x > grid[n - 1] ? grid[n - 1] : x);  /* NaN stays NaN */
+    if (xc <= grid[0]) { *hint = 0; *idx = 0; return 0; }
+    if (xc >= grid[n - 1]) { *hint = n - 2; *idx = n - 2; return 0; }
+    const int64_t h = *hint;
+    if (h < n - 1 && grid[h] <= xc && xc <= grid[h + 1]) { *idx = h; return 0; }
+    int64_t cnt = 0;
+    while (cnt < n && grid[cnt] <= xc) ++cnt;  /* partition_point(g <= x) */
+    int64_t k = cnt > 0 ? cnt - 1 : 0;
+    if (k > n - 2) k = n - 2;
+    *hint = k;
+    *idx = k;
+    return 0;
+}
+
+/* SparseOperator::sparse_matvec_interpolated (effective_lindblad/plan.rs:19-42) */
+static void eff_matvec(const orc_plan* p, int op, int64_t idx, double dx, double scale, const double* y, double* dy) {
+    const int64_t nnz = p->eff_nnz[op];
+    const int64_t interval = idx < p->eff_ngrid - 2 ? idx : (p->eff_ngrid >= 2 ? p->eff_ngrid - 2 : 0);
+    const double* cb = p->eff_coef[op] + interval * nnz * 4;
+    for (int64_t i = 0; i < p->N; ++i) {
+        double sum = 0.0;
+        for (int64_t q = p->eff_rows[op][i]; q < p->eff_rows[op][i + 1]; ++q) {
+            const double* c = cb + q * 4;
+            const double val = c[0] + dx * (c[1] + dx * (c[2] + dx * c[3]));
+            sum += val * y[p->eff_cols[op][q]];
+        }
+        dy[i] += scale * sum;
+    }
+}
+
+/* rhs_effective_lindblad (effective_lindblad/rhs.rs:88-137) */
+static int ws_rhs_effective(workspace* w, double t, const double* y, double* out, errbuf* e) {
+    const orc_plan* p = w->p;
+    if (ws_eval_params(w, t, e)) return 1;
+    const rv* fv = &w->slots[p->eff_field];
+    if (fv->is_tuple) return fail(e, "field_coordinate must be scalar");
+    const double x = fv->s.re;
+    const rv* rvv = &w->slots[p->eff_rabi];
+    const rv* dvv = &w->slots[p->eff_det];
+    const double rabi = p->eff_rabi_const ? p->eff_rabi_val : (rvv->is_tuple ? 0.0 : rvv->s.re);
+    const double det = p->eff_det_const ? p->eff_det_val : (dvv->is_tuple ? 0.0 : dvv->s.re);
+    int64_t idx = 0;
+    if (eff_find_interval(x, p->eff_grid, p->eff_ngrid, &w->eff_hint, &idx, e)) return 1;
+    const double dx = x - p->eff_grid[idx];
+    for (int64_t i = 0; i < p->N; ++i) out[i] = 0.0;
+    eff_matvec(p, 0, idx, dx, 1.0, y, out);
+    eff_matvec(p, 1, idx, dx, 0.5 * rabi, y, out);
+    eff_matvec(p, 2, idx, dx, det, y, out);
+    return 0;
+}
+
 /* rhs_packed_expanded_sparse_into_with_profile (rhs.rs:1789-1867) + the partitioned kernel
    (rhs.rs:815-876), or for n > 40 the split-input path (rhs.rs:1869-1968, 633-695) */
 static int ws_rhs(workspace* w, double t, const double* y, double* out, errbuf* e) {
     const orc_plan* p = w->p;
+    if (p->eff) return ws_rhs_effective(w, t, y, out, e);
     if (!p->has_expanded) return fail(e, "execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan");
     if (p->n <= PARTITIONED_MAX_STATES) {
         int init = !w->valid;
@@ -1392,6 +1571,14 @@ static void sink_init(sink* s, const orc_plan* p, const obe_solve_options* opt, 
         s->sel_kind = (int8_t*)malloc((size_t)(m > 0 ? m : 1));
         for (int32_t k = 0; k < m; ++k) {
             int64_t i = opt->selected_i[k], j = opt->selected_j[k];
+            if (p->eff) {
+                /* split_real_selected_extractions (effective_lindblad/solver.rs:58-76) */
+                const int64_t n = p->n;
+                s->sel_kind[k] = i == j ? 0 : 1;
+                s->sel_re[k] = i * n + j;
+                s->sel_im[k] = i == j ? i * n + j : n * n + i * n + j;
+                continue;
+            }
             if (i == j) { s->sel_kind[k] = 0; s->sel_re[k] = i; s->sel_im[k] = i; }
             else if (i < j) { int64_t r = packed_upper_real_index(p->n, i, j); s->sel_kind[k] = 1; s->sel_re[k] = r; s->sel_im[k] = r + 1; }
             else { int64_t r = packed_upper_real_index(p->n, j, i); s->sel_kind[k] = 2; s->sel_re[k] = r; s->sel_im[k] = r + 1; }
@@ -1441,7 +1628,7 @@ static void sink_push(sink* s, double t, const double* y) {
     case OBE_OUTPUT_POPULATIONS:
         if (s->count < s->capacity) {
             s->times[s->count] = t;
-            for (int64_t i = 0; i < w; ++i) s->vals[s->count * w + i] = y[i];
+            for (int64_t i = 0; i < w; ++i) s->vals[s->count * w + i] = y[i * s->p->pop_stride];
         }
         s->count++;
         return;
@@ -1976,6 +2163,7 @@ done:
 }
 
 static int solve_any(workspace* w, const double* y0, const obe_solve_options* o, sink* out, obe_traj_stats* st, errbuf* e) {
+    w->eff_hint = 0;  /* a fresh RHS workspace per trajectory (effective_lindblad/rhs.rs:14-24) */
     if (o->solver == OBE_SOLVER_DOPRI5 || o->solver == OBE_SOLVER_TSIT5)
         return solve_rk(w, o->solver == OBE_SOLVER_TSIT5, y0, o, out, st, e);
     return solve_fixed(w, o->solver, y0, o, out, st, e);

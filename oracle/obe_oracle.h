@@ -67,6 +67,11 @@ int orc_solve_single(const orc_plan* plan, const obe_solve_options* opt, const d
 /* Width of an output spec (ode_batch.rs:150-157) and whether it is complex. */
 int64_t orc_output_width(const orc_plan* plan, const obe_solve_options* opt, int32_t* is_complex);
 
+/* An interpolated effective-Hamiltonian plan (effective_lindblad/plan.rs): the parameter graph in
+ * `graph`, the operators in `eff` (include/obe_gb300.h).  It solves and evaluates its RHS through
+ * the functions above with the effective API's output conventions (split-real state). */
+orc_plan* orc_effective_plan_create(const obe_plan_desc* graph, const obe_effective_desc* eff, char* err, size_t err_len);
+
 /* Threads OpenMP will use for a batch with threads <= 0. */
 int32_t orc_max_threads(void);
 

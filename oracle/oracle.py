@@ -63,6 +63,9 @@ def _lib():
     ]
     lib.orc_solve_single.restype = ctypes.c_int
     lib.orc_max_threads.restype = ctypes.c_int32
+    lib.orc_effective_plan_create.argtypes = [ctypes.POINTER(ObePlanDesc), ctypes.POINTER(_abi.ObeEffectiveDesc),
+                                              ctypes.c_char_p, ctypes.c_size_t]
+    lib.orc_effective_plan_create.restype = vp
     lib.orc_solve_replay.argtypes = [
         vp, ctypes.POINTER(ObeSolveOptions), ctypes.c_int64, f64p, ctypes.c_int64, ctypes.c_int32, i64p, f64p, i64p, f64p,
         ctypes.c_int64, ctypes.c_int64, f64p, ctypes.c_char_p, ctypes.c_size_t,
@@ -225,3 +228,28 @@ class OraclePlan:
             "event_time": float(st.event_time),
         }
         return times[:n].copy(), values[: n * width].reshape(n, width).copy(), stats
+
+
+class EffectiveOraclePlan(OraclePlan):
+    """The oracle on an interpolated effective-Hamiltonian plan (the reference's plan_dict of
+    prepare_effective_lindblad_plan_py): split-real state of 2 n^2 doubles, the effective API's
+    output conventions."""
+
+    def __init__(self, plan_dict: dict) -> None:
+        from centrex_tlf_gb300._plan import EffectiveArrays
+
+        self.eff = EffectiveArrays(plan_dict)
+        self.arrays = self.eff.graph
+        err = ctypes.create_string_buffer(512)
+        handle = _lib().orc_effective_plan_create(ctypes.byref(self.eff.graph.desc), ctypes.byref(self.eff.desc), err, 512)
+        if not handle:
+            raise OracleError(err.value.decode())
+        self.handle = handle
+        self.n = self.eff.n_states
+        self.N = self.eff.real_dim
+        self.slot_names = self.eff.slot_names
+
+    def options(self, **kw) -> SolveOptions:
+        kw.setdefault("output_when", "saveat")
+        kw.setdefault("stop_event", None)
+        return SolveOptions(n_states=self.n, state_len=self.N, **kw)

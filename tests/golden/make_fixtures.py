@@ -334,6 +334,97 @@ def save_r2_38(centrex_tlf) -> None:
     })
 
 
+def build_effective_r0(centrex_tlf, detuning_expr: str):
+    """An interpolated effective-Hamiltonian model (centrex_tlf/effective_hamiltonian): R(0)
+    F1'=1/2 F'=1 with z polarisation, compact Lindblad-safe model on the field grid 100, 150,
+    200 V/cm (B = 1e-3 G along z, master field 150 V/cm; as tests/effective_hamiltonian/
+    test_interpolated_preparation.py builds one), and the payload that the reference's
+    prepare_effective_lindblad_rust_plan (effective_hamiltonian/rust_plan.py:42-200) hands to its
+    native prepare_effective_lindblad_plan_py, captured by a stand-in for that native function.
+    Parameters: the field oscillates inside the grid, Ez = 150 + 40 sin(2π·1e5 t) V/cm; a Gaussian
+    Rabi pulse Ω0 = rabi exp(-(t - 2.5e-6)² / (2 (1e-6)²)); δ0 = `detuning_expr`.  Also returns the
+    split-real superoperators at the grid nodes (the reference's own _hamiltonian_superoperator and
+    dissipator), from which the golden RHS values are made."""
+    import types
+
+    import centrex_tlf as ct
+    from centrex_tlf import couplings, transitions
+    from centrex_tlf.effective_hamiltonian._superoperators import _hamiltonian_superoperator
+    from centrex_tlf.effective_hamiltonian.preparation import prepare_lindblad_safe_compact_interpolated_model
+    from centrex_tlf.effective_hamiltonian.rust_plan import (
+        _complex_superop_to_split_real,
+        prepare_effective_lindblad_rust_plan,
+    )
+    from centrex_tlf.lindblad.parameters import LindbladParameters
+
+    pol = couplings.Polarization(np.array([0.0, 0.0, 1.0], dtype=np.complex128), name="Z")
+    model = prepare_lindblad_safe_compact_interpolated_model(
+        field_points=(100.0, 150.0, 200.0), transition=transitions.R0_F1_1o2_F1, optical_polarization=pol,
+        magnetic_field=(0.0, 0.0, 1e-3), master_field=150.0)
+    params = LindbladParameters.from_kwargs(
+        rabi=1.0e7, detuning=0.0, chirp=2.0e11, Ez="150.0 + 40.0*sin(2*pi*1e5*t)",
+        Ω0="rabi*exp(-(t - 2.5e-6)**2/(2*(1e-6)**2))", δ0=detuning_expr)
+    saved = sys.modules.get("centrex_tlf.centrex_tlf_rust")
+    stub = types.ModuleType("centrex_tlf.centrex_tlf_rust")
+    stub.prepare_effective_lindblad_plan_py = lambda d: d  # capture the payload
+    sys.modules["centrex_tlf.centrex_tlf_rust"] = stub
+    ct.centrex_tlf_rust = stub
+    try:
+        plan = prepare_effective_lindblad_rust_plan(model, params, operator_interpolation="linear")
+    finally:
+        if saved is not None:
+            sys.modules["centrex_tlf.centrex_tlf_rust"] = saved
+    nodes = []
+    for field_z in model.field_points.tolist():
+        b = model.effective_bundle(float(field_z))
+        nodes.append({
+            "combined": _complex_superop_to_split_real(_hamiltonian_superoperator(b.h_internal) + b.dissipator_superoperator()),
+            "optical": _complex_superop_to_split_real(_hamiltonian_superoperator(b.h_opt)),
+            "detuning": _complex_superop_to_split_real(_hamiltonian_superoperator(b.h_det)),
+        })
+    return model, plan, nodes
+
+
+def save_effective(centrex_tlf) -> None:
+    """plan_eff_r0.json: the effective model's payload, a split-real initial state (the ground
+    main state), and golden RHS values dy = (L_c(x) + Ω/2 L_o(x) + δ L_d(x)) y from the
+    reference's node superoperators -- at the nodes and, between them, their linear interpolation
+    (the payload's `linear` coefficients); plan_eff_r0_static.json: the same model with a
+    time-independent detuning program δ0 = detuning, which the reference's plan freezes at its
+    base value (effective_lindblad/plan.rs: detect_constant_slot)."""
+    model, plan, nodes = build_effective_r0(centrex_tlf, "detuning + chirp*(t - 2.5e-6)")
+    n = plan["n_states"]
+    rho = np.zeros((n, n), dtype=np.complex128)
+    g = int(model.ground_main_index)
+    rho[g, g] = 1.0
+    y0 = np.concatenate([rho.real.reshape(-1), rho.imag.reshape(-1)])
+    grid = np.asarray(plan["field_grid"], dtype=np.float64)
+    rng = np.random.default_rng(210)
+    cases = []
+    # the field program Ez(t) = 150 + 40 sin(2π·1e5 t) spans [110, 190]: cases at the middle node
+    # and between the nodes, each at the time t where Ez(t) = x, with the base values (rabi,
+    # detuning) that give the wanted Ω0(t) and δ0(t)
+    for x, om, de in ((150.0, 1.3e7, 2.0e6), (123.4, 8.0e6, 1.0e6), (187.9, 2.5e6, -3.0e6), (110.0, 0.0, -5.0e6),
+                      (176.5, 4.0e6, 0.0)):
+        t = float(np.arcsin((x - 150.0) / 40.0) / (2 * np.pi * 1e5)) % 1e-5
+        x = 150.0 + 40.0 * np.sin(2 * np.pi * 1e5 * t)
+        pulse = np.exp(-(t - 2.5e-6) ** 2 / (2 * (1e-6) ** 2))
+        rabi, det = om / pulse, de - 2.0e11 * (t - 2.5e-6)
+        om = rabi * pulse
+        de = det + 2.0e11 * (t - 2.5e-6)
+        k = min(int(np.searchsorted(grid, x, side="right")) - 1, grid.size - 2)
+        w = (x - grid[k]) / (grid[k + 1] - grid[k])
+        mats = {key: (1.0 - w) * nodes[k][key] + w * nodes[k + 1][key] for key in ("combined", "optical", "detuning")}
+        y = rng.normal(size=2 * n * n) * 0.1
+        dy = mats["combined"] @ y + 0.5 * om * (mats["optical"] @ y) + de * (mats["detuning"] @ y)
+        cases.append({"t": t, "field": x, "rabi": om, "detuning": de, "base_rabi": rabi, "base_detuning": det,
+                      "y": y, "dy": dy})
+    codec.save("plan_eff_r0", {"plan": plan, "y0": y0, "ground_main": g, "rhs_cases": cases,
+                               "t_span": [0.0, 5.0e-6]})
+    _, plan_s, _ = build_effective_r0(centrex_tlf, "detuning")
+    codec.save("plan_eff_r0_static", {"plan": plan_s, "y0": y0})
+
+
 def build_rc_76(centrex_tlf):
     """The 76-state rotational-cooling-sized system: X J=0-3 (64 hyperfine states) + B J'=1
     F1'=1/2, 3/2 (P=-1, 12 states), driven by R(0) F1'=1/2 F'=1 and P(2) F1'=3/2 F'=1 with x and z
@@ -566,6 +657,9 @@ def main() -> None:
     if "--r2-38" in sys.argv:
         save_r2_38(_import_reference())
         return
+    if "--effective" in sys.argv:
+        save_effective(_import_reference())
+        return
     centrex_tlf = _import_reference()
     started = time.perf_counter()
 
@@ -655,6 +749,7 @@ def main() -> None:
     save_rc_76(centrex_tlf)
     save_multi(centrex_tlf)
     save_r2_38(centrex_tlf)
+    save_effective(centrex_tlf)
 
     # --- the native-boundary call contract of the reference's Python surface ----------------
     codec.save("ffi_calls", record_ffi_calls(centrex_tlf, q1, rho_q))
