@@ -263,6 +263,8 @@ def load_library() -> ctypes.CDLL:
     lib.obe_effective_plan_create.argtypes = [ctypes.POINTER(ObePlanDesc), ctypes.POINTER(ObeEffectiveDesc),
                                               ctypes.POINTER(ctypes.c_void_p)]
     lib.obe_effective_plan_create.restype = ctypes.c_int
+    lib.obe_effective_rhs_debug.argtypes = [ctypes.c_void_p, ctypes.c_double, c_f64p, c_f64p, c_f64p]
+    lib.obe_effective_rhs_debug.restype = ctypes.c_int
     lib.obe_plan_set_shape.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]
     lib.obe_plan_set_shape.restype = ctypes.c_int
     lib.obe_plan_get_shape.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]

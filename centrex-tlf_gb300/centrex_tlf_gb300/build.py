@@ -8,6 +8,7 @@ linked with nvcc into one shared library with the C ABI of include/obe_gb300.h.
 from __future__ import annotations
 
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -38,11 +39,25 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp")) + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [INCLUDE / "obe_gb300.h"]
 
 
+HASH = OUT.with_name("libobe_gb300.sources.sha256")
+
+
+def sources_hash() -> str:
+    import hashlib
+
+    h = hashlib.sha256()
+    for src in sources():
+        h.update(src.name.encode())
+        h.update(src.read_bytes())
+    h.update(" ".join(ARCH).encode())
+    h.update(platform.machine().encode())  # a hash written on another architecture never matches
+    return h.hexdigest()
+
+
 def up_to_date() -> bool:
-    if not OUT.exists():
-        return False
-    mtime = OUT.stat().st_mtime
-    return all(src.stat().st_mtime <= mtime for src in sources())
+    # by content, not by time stamps: a library built from other sources (or on a machine whose
+    # clock disagrees with the sources' time stamps) is rebuilt
+    return OUT.exists() and HASH.exists() and HASH.read_text().strip() == sources_hash()
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
@@ -77,6 +92,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         tmp_out = tmp / "libobe_gb300.so"
         run([nvcc, *ARCH, "-shared", "-o", str(tmp_out), *map(str, objs)])
         shutil.copy2(tmp_out, OUT)
+    HASH.write_text(sources_hash() + "\n")
     return OUT
 
 

@@ -28,6 +28,10 @@ from .native import NativePlan
 __all__ = [
     "PreparedLindbladPlan",
     "autotune_lindblad_batch_py",
+    "debug_effective_lindblad_rhs_py",
+    "prepare_effective_lindblad_plan_py",
+    "solve_effective_lindblad_batch_py",
+    "solve_effective_lindblad_py",
     "install",
     "prepare_lindblad_problem_py",
     "solve_lindblad_batch_ode_py",
@@ -522,6 +526,134 @@ def solve_lindblad_grid_ode_py(
                  precision=precision)
     values, st = native.solve_grid(opts, rho0, list(parameter_slot_indices), axes, time_count)
     return _batch_result(values, st, opts.width, time_count, ref_times, t1, solver, stop_event, opts.is_complex)
+
+
+# ---- interpolated effective-Hamiltonian Lindblad path (rust/src/effective_lindblad) --------------
+
+
+class PreparedEffectiveLindbladPlan:
+    """The GB300 counterpart of the reference's EffectiveLindbladPlan pyclass
+    (effective_lindblad/plan.rs:43-86): read-only n_states, real_dim, n_grid, slot_names."""
+
+    def __init__(self, plan_dict: dict) -> None:
+        self.native = NativePlan.from_effective(plan_dict)
+        self.n_states = self.native.n_states
+        self.real_dim = self.native.packed_len
+        self.n_grid = self.native.arrays.n_grid
+
+    @property
+    def slot_names(self) -> list[str]:
+        return list(self.native.slot_names)
+
+    def __repr__(self) -> str:
+        return f"EffectiveLindbladPlan(n_states={self.n_states}, real_dim={self.real_dim}, n_grid={self.n_grid})"
+
+
+def prepare_effective_lindblad_plan_py(plan_dict: dict) -> PreparedEffectiveLindbladPlan:
+    """effective_lindblad/python_api.rs:16-29."""
+    return PreparedEffectiveLindbladPlan(plan_dict)
+
+
+def _effective_native(plan) -> NativePlan:
+    if isinstance(plan, PreparedEffectiveLindbladPlan):
+        return plan.native
+    raise TypeError("plan must be an EffectiveLindbladPlan from prepare_effective_lindblad_plan_py")
+
+
+def _effective_output(output: str) -> str:
+    # effective_lindblad/solver.rs:102-132: anything but these three kinds is the full state
+    if output in ("populations", "selected") or output in INTEGRAL_OUTPUTS:
+        return output
+    return "full"
+
+
+def _effective_opts(native, t0, t1, abstol, reltol, dt, saveat, save_start, maxiters, solver, output, output_indices,
+                    integral_weights):
+    _check_solver(solver)
+    out = _effective_output(output)
+    if out == "selected" and output_indices is None:
+        raise ValueError("output='selected' requires output_indices")
+    if out in INTEGRAL_OUTPUTS and integral_weights is None:
+        raise ValueError(f"output='{output}' requires integral_weights")
+    sv = None if saveat is None else np.asarray(saveat, dtype=np.float64).reshape(-1)
+    # the integral outputs report their final value (WeightedIntegralOutput::finish)
+    opts = native.options(t0=float(t0), t1=float(t1), abstol=abstol, reltol=reltol, dt=dt, saveat=sv,
+                          save_start=bool(save_start), maxiters=int(maxiters), solver=solver, output=out,
+                          output_indices=output_indices, output_when="final", integral_weights=integral_weights,
+                          stop_event=None)
+    return opts, out, sv
+
+
+def solve_effective_lindblad_py(plan, y0, t0, t1, abstol, reltol, dt, saveat=None, save_start=True, maxiters=100000,
+                                solver="dopri5", output="full", output_indices=None, integral_weights=None):
+    """effective_lindblad/python_api.rs:44-92 -> solver.rs:78-132: one trajectory of the split-real
+    state; returns ``(times, values, width)`` (values complex for ``selected``)."""
+    native = _effective_native(plan)
+    y = np.ascontiguousarray(np.asarray(y0, dtype=np.float64).reshape(-1))
+    if y.size != native.packed_len:
+        raise ValueError(f"expected state length {native.packed_len}, got {y.size}")
+    opts, out, _ = _effective_opts(native, t0, t1, abstol, reltol, dt, saveat, save_start, maxiters, solver, output,
+                                   output_indices, integral_weights)
+    times, values, width, _ = native.solve_single(opts, y)
+    return np.asarray(times, dtype=np.float64), np.ascontiguousarray(values).reshape(-1), int(width)
+
+
+def solve_effective_lindblad_batch_py(plan, packed_rho0, t0, t1, abstol, reltol, dt, saveat=None, save_start=True,
+                                      maxiters=100000, solver="dopri5", output="populations", output_indices=None,
+                                      integral_weights=None, parameter_slot_indices=None, parameter_batch=None,
+                                      trajectory_count=1, parallel=True, threads=None):
+    """effective_lindblad/python_api.rs:154-250 -> solver.rs:134-281: `trajectory_count` solves
+    from one initial state with real per-trajectory base-slot values, one GPU launch.  Returns
+    ``(times, values, width, time_count, stats)``; selected values interleave (re, im) as the
+    reference flattens them.  ``parallel``/``threads`` choose the reference's CPU pool."""
+    native = _effective_native(plan)
+    y = np.ascontiguousarray(np.asarray(packed_rho0, dtype=np.float64).reshape(-1))
+    dim = native.packed_len
+    slots = list(parameter_slot_indices or [])
+    b = int(trajectory_count)
+    if parameter_batch is not None:
+        pb = np.asarray(parameter_batch, dtype=np.float64)
+        if pb.ndim != 2 or pb.shape[0] != b or pb.shape[1] != len(slots):
+            shape = pb.shape if pb.ndim == 2 else (pb.size, 1)
+            raise ValueError(f"parameter_batch shape ({shape[0]},{shape[1]}) doesn't match ({b},{len(slots)})")
+    else:
+        pb = np.zeros((b, len(slots)))
+    if y.size != dim:
+        raise ValueError(f"expected state length {dim}, got {y.size}")
+    opts, out, sv = _effective_opts(native, t0, t1, abstol, reltol, dt, saveat, save_start, maxiters, solver, output,
+                                    output_indices, integral_weights)
+    plan_times = _save_plan(sv, float(t0), float(t1), bool(save_start))
+    if out in INTEGRAL_OUTPUTS:
+        time_count, ref_times = 1, [plan_times[-1] if plan_times else float(t1)]
+    elif plan_times is not None:
+        time_count, ref_times = len(plan_times), list(plan_times)
+    else:
+        raise NotImplementedError("batch outputs at every accepted step (saveat=None) are not supported by the GB300 "
+                                  "solver; pass explicit saveat values")
+    stats = {"solver": solver, "accepted_steps": 0, "rejected_steps": 0, "rhs_calls": 0, "trajectory_count": b}
+    if b == 0:
+        return np.zeros(0), np.zeros(0), 0, 0, stats
+    batch = np.ascontiguousarray(np.broadcast_to(y, (b, dim)))
+    use = len(slots) > 0
+    values, st = native.solve_batch(opts, batch, slots if use else None, pb.astype(np.complex128) if use else None, time_count)
+    stats.update(accepted_steps=int(st["accepted_steps"].sum()), rejected_steps=int(st["rejected_steps"].sum()),
+                 rhs_calls=int(st["rhs_calls"].sum()))
+    flat = np.ascontiguousarray(values).reshape(-1)
+    if opts.is_complex:
+        flat = flat.view(np.float64)
+    return np.asarray(ref_times, dtype=np.float64), flat, int(opts.width), int(time_count), stats
+
+
+def debug_effective_lindblad_rhs_py(plan, y0, t):
+    """effective_lindblad/python_api.rs:94-152: one RHS and what it read."""
+    native = _effective_native(plan)
+    dy, info = native.effective_rhs_debug(np.asarray(y0, dtype=np.float64).reshape(-1), float(t))
+    return {
+        "field_val": float(info[0]), "rabi_val": float(info[1]), "detuning_val": float(info[2]),
+        "dy_norm": float(np.sqrt(np.sum(dy * dy))), "dy_max": float(np.max(np.abs(dy))) if dy.size else 0.0,
+        "has_nan": bool(np.isnan(dy).any()), "has_inf": bool(np.isinf(dy).any()),
+        "last_interval": int(info[3]), "dy": dy,
+    }
 
 
 def install() -> None:

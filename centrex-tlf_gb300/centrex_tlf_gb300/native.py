@@ -59,8 +59,44 @@ class NativePlan:
             self.lib.obe_plan_destroy(h)
             self.handle = None
 
+    @classmethod
+    def from_effective(cls, plan_dict: dict) -> "NativePlan":
+        """An interpolated effective-Hamiltonian plan (obe_effective_plan_create) from the plan
+        dict the reference's prepare_effective_lindblad_rust_plan builds; its state is split-real
+        (2 n^2 doubles)."""
+        from ._plan import EffectiveArrays
+
+        self = cls.__new__(cls)
+        self.lib = load_library()
+        self.arrays = EffectiveArrays(plan_dict)
+        handle = ctypes.c_void_p()
+        st = self.lib.obe_effective_plan_create(ctypes.byref(self.arrays.graph.desc), ctypes.byref(self.arrays.desc),
+                                                ctypes.byref(handle))
+        if st != _abi.OBE_OK:
+            msg = _abi.last_error(self.lib)
+            if st == _abi.OBE_ERR_UNSUPPORTED:
+                raise NotImplementedError(msg)
+            raise ValueError(msg)
+        self.handle = handle
+        self.n_states = self.arrays.n_states
+        self.packed_len = self.arrays.real_dim
+        self.slot_names = list(self.arrays.slot_names)
+        self.n_base = self.arrays.n_base
+        return self
+
     def options(self, **kw) -> SolveOptions:
-        return SolveOptions(n_states=self.n_states, **kw)
+        return SolveOptions(n_states=self.n_states, state_len=self.packed_len, **kw)
+
+    def effective_rhs_debug(self, y, t: float) -> tuple[np.ndarray, np.ndarray]:
+        """One effective RHS at t: (dy, [field, rabi, detuning, interval])."""
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        dy = np.zeros(self.packed_len)
+        info = np.zeros(4)
+        st = self.lib.obe_effective_rhs_debug(self.handle, float(t), _abi.ptr(y, ctypes.c_double),
+                                              _abi.ptr(dy, ctypes.c_double), _abi.ptr(info, ctypes.c_double))
+        if st != _abi.OBE_OK:
+            _raise(self.lib, st)
+        return dy, info
 
     # -- RHS ------------------------------------------------------------------------------
     def rhs(self, y, t, override_slots=None, override_values=None, precision: str = "fp64") -> np.ndarray:

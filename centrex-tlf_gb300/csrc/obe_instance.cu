@@ -18,10 +18,10 @@ template cudaError_t launch_integrate_shape<OBE_TPT, OBE_EPT, true>(const DevPla
 #ifdef OBE_RHS
 template cudaError_t launch_rhs_shape<OBE_TPT, false>(const DevPlan&, long long, const double*, const double*, int, const int*,
                                                       const double*, double*, int, int, size_t, size_t, int, unsigned char*,
-                                                      size_t);
+                                                      size_t, double*);
 template cudaError_t launch_rhs_shape<OBE_TPT, true>(const DevPlan&, long long, const double*, const double*, int, const int*,
                                                      const double*, double*, int, int, size_t, size_t, int, unsigned char*,
-                                                     size_t);
+                                                     size_t, double*);
 #endif
 #if OBE_TPT <= 256
 template cudaError_t launch_adjoint_shape<OBE_TPT, OBE_EPT>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, size_t,

@@ -119,6 +119,19 @@ struct DevPlan {
     // product, formula-major and thread-interleaved (kBil* entries)
     int32_t n_biter;
     const uint32_t* bil;         // [n_biter * tpt]
+    // populations are y[i * pop_stride] (1 packed; n + 1 for the split-real effective state)
+    int32_t pop_stride;
+    // interpolated effective-Hamiltonian plans (eff != 0; N = real_dim): the RHS is
+    // L_c(x) y + (Omega / 2) L_o(x) y + delta L_d(x) y with x, Omega, delta = coefficients 0, 1, 2
+    int32_t eff;
+    int32_t eff_ngrid;
+    const double* eff_grid;      // [eff_ngrid]
+    const int32_t* eff_rows;     // [3][N + 1], offsets within each operator
+    const int32_t* eff_cols;     // operator k at eff_col_off[k]
+    const double* eff_coef;      // operator k at eff_coef_off[k]: [(eff_ngrid - 1)][nnz_k][4]
+    int32_t eff_nnz[3];
+    int32_t eff_col_off[3];
+    int64_t eff_coef_off[3];
 };
 
 // Host-side result of packing (owned by obe_plan).
@@ -152,6 +165,14 @@ struct HostPacked {
     int32_t n_titer = 0, n_tin = 0;
     std::vector<uint32_t> bil;
     int32_t n_biter = 0;
+    // effective-Hamiltonian plans
+    int32_t pop_stride = 1;
+    int32_t eff = 0;
+    std::vector<double> eff_grid, eff_coef;
+    std::vector<int32_t> eff_rows, eff_cols;
+    int32_t eff_nnz[3] = {0, 0, 0};
+    int32_t eff_col_off[3] = {0, 0, 0};
+    int64_t eff_coef_off[3] = {0, 0, 0};
     int32_t n_iter = 0, n_out = 0, tpt = 32, n_fiter = 0;
     int32_t n_formula = 0, n_static_formula = 0;
     int32_t max_stack = 0;
@@ -191,6 +212,7 @@ const char* last_error_cstr();  // the calling thread's last message
 std::string fmt_f64(double v);  // Rust Display of f64
 obe_status pack_plan(const obe_plan_desc* d, obe_plan* p);
 int threads_per_trajectory_for(int32_t n);
+int threads_per_trajectory_len(int64_t len);  // the same rule for a state of len doubles
 int64_t shape_capacity(int tpt);  // packed elements one trajectory of that compiled width holds (0: none)
 void lay_out_lanes(HostPacked& hp, int tpt);
 }  // namespace obe

@@ -113,7 +113,9 @@ enum TrajCode : int32_t {
     ST_BAD_MAXITERS = 8,
     ST_BACKWARD = 9,
     ST_FIXED_DT = 10,
-    ST_TAPE = 11
+    ST_TAPE = 11,
+    ST_FIELD_LOW = 12,   // effective plans: field coordinate below the operator grid (a = x, b = grid min)
+    ST_FIELD_HIGH = 13   // ... above it (b = grid max)
 };
 
 struct TrajErr {
@@ -196,7 +198,9 @@ struct GroupLayout {
 
 __host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula, int n_coeff, int n_dyn, int n_slots,
                                                     int vm_depth, int tpt, bool mixed) {
-    const size_t U = static_cast<size_t>(n) * (n + 1) / 2;
+    // slot-buffer entries: the packed layout's n (n + 1) / 2, or N / 2 for a split-real state
+    const size_t U_packed = static_cast<size_t>(n) * (n + 1) / 2, U_split = (static_cast<size_t>(N) + 1) / 2;
+    const size_t U = U_packed > U_split ? U_packed : U_split;
     const bool big = tpt >= 256;
     GroupLayout L{};
     L.kglob = big;
@@ -463,6 +467,70 @@ __device__ __forceinline__ void stage_classes(const DevPlan& P, const double2* c
     }
 }
 
+// The interpolated effective-Hamiltonian RHS (effective_lindblad/rhs.rs:88-137): the field
+// interval by the reference's cached search (rhs.rs:48-86; `hint` is the trajectory's
+// last_interval), then dy_i = 1 * (L_c y)_i + Omega/2 (L_o y)_i + delta (L_d y)_i, each row a sum of
+// cubic-in-dx entries times y[col].  Every lane sees the same x, so the interval, the hint and
+// the first range error (kept in err, err_x, err_g) are the same on all lanes.
+template <int TPT>
+__device__ __forceinline__ void eff_rhs(const DevPlan& P, double x, double rabi, double det, const double* __restrict__ yv,
+                                        double* __restrict__ out, int& hint, int& err, double& err_x, double& err_g, int lt) {
+    const int ng = P.eff_ngrid;
+    const double* grid = P.eff_grid;
+    int idx = 0;
+    if (ng >= 2) {
+        const double tol = 1e-10 * fmax(fabs(grid[ng - 1] - grid[0]), 1.0);
+        if (x < grid[0] - tol) {
+            if (!err) { err = ST_FIELD_LOW; err_x = x; err_g = grid[0]; }
+        } else if (x > grid[ng - 1] + tol) {
+            if (!err) { err = ST_FIELD_HIGH; err_x = x; err_g = grid[ng - 1]; }
+        } else {
+            const double xc = x < grid[0] ? grid[0] : (x > grid[ng - 1] ? grid[ng - 1] : x);
+            if (xc <= grid[0]) {
+                hint = 0;
+            } else if (xc >= grid[ng - 1]) {
+                hint = ng - 2;
+                idx = ng - 2;
+            } else if (hint < ng - 1 && grid[hint] <= xc && xc <= grid[hint + 1]) {
+                idx = hint;
+            } else {
+                int c = 0;
+                while (c < ng && grid[c] <= xc) ++c;
+                idx = c > 0 ? c - 1 : 0;
+                if (idx > ng - 2) idx = ng - 2;
+                hint = idx;
+            }
+        }
+    }
+    const double dx = x - grid[idx];
+    const int interval = ng >= 2 && idx > ng - 2 ? ng - 2 : idx;
+    const double scale[3] = {1.0, 0.5 * rabi, det};
+    for (int i = lt; i < P.N; i += TPT) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int32_t* rows = P.eff_rows + static_cast<size_t>(k) * (P.N + 1);
+            const int32_t* cols = P.eff_cols + P.eff_col_off[k];
+            const double2* cb = reinterpret_cast<const double2*>(P.eff_coef + P.eff_coef_off[k] +
+                                                                 static_cast<size_t>(interval) * P.eff_nnz[k] * 4);
+            double sum = 0.0;
+            for (int q = rows[i]; q < rows[i + 1]; ++q) {
+                const double2 c01 = cb[2 * q], c23 = cb[2 * q + 1];
+                const double val = c01.x + dx * (c01.y + dx * (c23.x + dx * c23.y));
+                sum += val * yv[cols[q]];
+            }
+            acc += scale[k] * sum;
+        }
+        out[i] = acc;
+    }
+}
+
+// coefficient k of stage row `row` (the effective RHS's field, Rabi rate, detuning)
+__device__ __forceinline__ double coef_re(const DevPlan& P, const double2* cstat, const double2* cdyn_row, int k) {
+    const int pos = P.coeff_dyn_pos[k];
+    return pos >= 0 ? cdyn_row[pos].x : cstat[k].x;
+}
+
 // The packed expanded_sparse RHS: one record = one 16-byte coefficient and one 16-byte input.
 // The formula table, the slot buffer and the output are disjoint (restrict), so the operand
 // loads of later records can be issued ahead of the output stores of earlier ones.
@@ -561,6 +629,11 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 
     // stage the plan's gather stream and time-dependent formula products once per CTA
     const PlanSmem PS = plan_smem(P, TPT, MIXED);
+    // packed index -> double index in the slot buffer (identity for the split-real effective state)
+    auto gsl = [&](int i) -> int {
+        if constexpr (MIXED) return gslot64(i, P.n);
+        else return P.eff ? i : gslot64(i, P.n);
+    };
     uint32_t* s_rec = reinterpret_cast<uint32_t*>(smem + PS.rec);
     uint32_t* s_out = reinterpret_cast<uint32_t*>(smem + PS.out);
     int32_t* s_fptr = reinterpret_cast<int32_t*>(smem + PS.fptr);
@@ -667,13 +740,23 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             int i = lt + e * TPT;
             y[e] = i < N ? r0[i] : 0.0;
             yn[e] = 0.0;
-            if (i < N) s_G64[gslot64(i, n)] = y[e];
+            if (i < N) s_G64[gsl(i)] = y[e];
         }
 
         long long accepted = 0, rejected = 0, rhs_calls = 0, count = 0;
         int status = ST_OK;
         double err_x = 0.0;
         long long err_a = 0, err_b = 0;
+        // effective plans: the field interval hint and the first field-range error of this trajectory
+        int eff_hint = 0, eff_err = 0;
+        double eff_x = 0.0, eff_g = 0.0;
+        auto eff_failed = [&]() {
+            if (!eff_err) return false;
+            status = eff_err;
+            err_x = eff_x;
+            err_a = __double_as_longlong(eff_g);
+            return true;
+        };
         int ev_triggered = 0;
         double ev_time = CUDART_NAN;
         double integral = 0.0, last_t = CUDART_NAN, last_value = 0.0, last_time = 0.0;
@@ -690,7 +773,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             switch (A.output) {
             case OBE_OUTPUT_POPULATIONS:
                 if (store)
-                    for (int i = lt; i < n; i += TPT) out_vals[pt * n + i] = s_ybuf[i];
+                    for (int i = lt; i < n; i += TPT) out_vals[pt * n + i] = s_ybuf[static_cast<size_t>(i) * P.pop_stride];
                 break;
             case OBE_OUTPUT_FULL:
                 if (store)
@@ -787,6 +870,13 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 fill_formulas<TPT>(P, 1, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
             } else {
                 gsync<TPT>(g);  // G written, coefficient row ready
+                if (P.eff) {
+                    const double2* cr = s_cdyn + row * nd;
+                    eff_rhs<TPT>(P, coef_re(P, s_cstat, cr, 0), coef_re(P, s_cstat, cr, 1), coef_re(P, s_cstat, cr, 2), s_G64,
+                                 out, eff_hint, eff_err, eff_x, eff_g, lt);
+                    gsync<TPT>(g);  // out complete, G free
+                    return;
+                }
                 if (F > S) fill_formulas_dyn<TPT>(P, s_fptr, s_fcls, s_ffac64, s_cstat, s_cdyn + row * nd, s_tab, lt);
             }
             gsync<TPT>(g);
@@ -843,6 +933,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 double x = t0;
                 long long steps = 0;
                 while (status == ST_OK && x < t1 - time_tol(t1)) {
+                    if (eff_failed()) break;
                     if (steps >= A.maxiters) { status = ST_MAXITERS; err_x = x; err_a = steps; break; }
                     // next_step_limit (fixed.rs:16-26): dt, clipped to t1 and the next saveat time
                     double target = fmin(x + A.dt, t1);
@@ -864,7 +955,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
-                        if (i < N) s_G64[gslot64(i, n)] = y[e];
+                        if (i < N) s_G64[gsl(i)] = y[e];
                     }
                     rhs64(5, s_K);
                     if (A.fixed == OBE_SOLVER_FIXED_RK2) {
@@ -872,7 +963,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 #pragma unroll
                         for (int e = 0; e < EPT; ++e) {
                             int i = lt + e * TPT;
-                            if (i < N) s_G64[gslot64(i, n)] = y[e] + 0.5 * h * s_K[i];
+                            if (i < N) s_G64[gsl(i)] = y[e] + 0.5 * h * s_K[i];
                         }
                         rhs64(0, s_K + N);
 #pragma unroll
@@ -889,7 +980,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 #pragma unroll
                             for (int e = 0; e < EPT; ++e) {
                                 int i = lt + e * TPT;
-                                if (i < N) s_G64[gslot64(i, n)] = y[e] + c * s_K[static_cast<size_t>(s) * N + i];
+                                if (i < N) s_G64[gsl(i)] = y[e] + c * s_K[static_cast<size_t>(s) * N + i];
                             }
                             rhs64(s < 2 ? 0 : 4, s_K + static_cast<size_t>(s + 1) * N);
                         }
@@ -914,7 +1005,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                                         if (j <= s) acc += kTab.a[0][s][j] * s_K[static_cast<size_t>(j) * N + i];
                                     double v = y[e] + h * acc;
                                     if (s == 5) yn[e] = v;
-                                    else s_G64[gslot64(i, n)] = v;
+                                    else s_G64[gsl(i)] = v;
                                 }
                             }
                             if (s < 5) rhs64(s, s_K + static_cast<size_t>(s + 1) * N);
@@ -998,7 +1089,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
-                    if (i < N) s_G64[gslot64(i, n)] = y[e] + k1_out[i] * h0;
+                    if (i < N) s_G64[gsl(i)] = y[e] + k1_out[i] * h0;
                 }
                 dyn_coeffs_at(x + h0, 4);
                 rhs64(4, s_ybuf);
@@ -1019,7 +1110,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
-                    if (i < N) s_G64[gslot64(i, n)] = y[e];
+                    if (i < N) s_G64[gsl(i)] = y[e];
                 }
             }
         }
@@ -1078,6 +1169,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
         int since_refresh = 0;
         bool last = false;
         while (!done && !last) {
+            if (eff_failed()) break;
             if (ns > A.maxiters) { status = ST_MAXITERS; err_x = x; err_a = ns; break; }
             if (0.1 * fabs(h) <= 2.220446049250313e-16 * fabs(x)) { status = ST_UNDERFLOW; err_x = x; break; }
             if ((x + 1.01 * h - t1) * posneg > 0.0) {
@@ -1112,7 +1204,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                                 if (j <= s) acc += kTab.a[M][s][j] * Kat(j, i);
                             double v = y[e] + h * acc;
                             if (s == 5) yn[e] = v;
-                            s_G64[gslot64(i, n)] = v;
+                            s_G64[gsl(i)] = v;
                         }
                     }
                     rhs64(s < 4 ? s : 4, s_K + static_cast<size_t>(s + 1) * N);
@@ -1403,7 +1495,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                         y[e] = yn[e];
                         if (i < N) {
                             if (refresh) {
-                                s_G64[gslot64(i, n)] = y[e];
+                                s_G64[gsl(i)] = y[e];
                             } else {
                                 // first-same-as-last: k_1 of the next step is k_7 = k_1 + d_7
                                 double k = s_k1[i] + f2d(s_K32[static_cast<size_t>(5) * N + i]);
@@ -1438,6 +1530,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
         }
 
         // ---------------- finalise ----------------
+        if (status == ST_OK) eff_failed();  // a range error in the last step
         if (lt == 0) {
             if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace && has_last_time && A.cap > 0) {
                 out_vals[0] = integral;
@@ -1468,7 +1561,7 @@ template <int TPT, bool MIXED>
 __global__ void __launch_bounds__(TPT > 256 ? TPT : 256) rhs_kernel(const DevPlan P, long long count, const double* ts, const double* ys,
                                                   int n_ov, const int* ov_slots, const double* ov_vals, double* dys,
                                                   int gpb, size_t group_bytes, int vm_depth, unsigned char* gscratch,
-                                                  size_t gstride) {
+                                                  size_t gstride, double* errs) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
     const int lt = static_cast<int>(threadIdx.x) % TPT;
@@ -1513,7 +1606,30 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : 256) rhs_kernel(const DevPla
         }
         for (int i = lt; i < U; i += TPT) s_G[i] = make_double2(0.0, 0.0);
         gsync<TPT>(g);
-        for (int i = lt; i < N; i += TPT) reinterpret_cast<double*>(s_G)[gslot64(i, n)] = ys[st * N + i];
+        for (int i = lt; i < N; i += TPT) reinterpret_cast<double*>(s_G)[P.eff ? i : gslot64(i, n)] = ys[st * N + i];
+        if (P.eff) {
+            // the effective RHS at t (a fresh interval hint, as the reference's debug call builds a
+            // new workspace); errs[st] = (status, x, grid bound) of a field-range error, then the
+            // field, Rabi rate and detuning used and the interval
+            gsync<TPT>(g);
+            int hint = 0, err = 0;
+            double ex = 0.0, eg = 0.0;
+            eff_rhs<TPT>(P, s_cstat[0].x, s_cstat[1].x, s_cstat[2].x, reinterpret_cast<const double*>(s_G), dys + st * N, hint,
+                         err, ex, eg, lt);
+            if (lt == 0 && errs) {
+                double* r = errs + 8 * st;
+                r[0] = err;
+                r[1] = ex;
+                r[2] = eg;
+                r[3] = s_cstat[0].x;
+                r[4] = s_cstat[1].x;
+                r[5] = s_cstat[2].x;
+                r[6] = hint;
+                r[7] = 0.0;
+            }
+            gsync<TPT>(g);
+            continue;
+        }
         fill_formulas<TPT>(P, 1, 1 + P.n_formula, s_cstat, s_cdyn, s_tab, lt);
         gsync<TPT>(g);
         if constexpr (MIXED) {
@@ -1550,11 +1666,12 @@ cudaError_t launch_integrate_shape(const DevPlan& P, const CallArgs& A, int bloc
 template <int TPT, bool MIXED>
 cudaError_t launch_rhs_shape(const DevPlan& P, long long count, const double* ts, const double* ys, int n_ov, const int* ov_slots,
                              const double* ov_vals, double* dys, int blocks, int gpb, size_t smem, size_t group_bytes,
-                             int vm_depth, unsigned char* gscratch, size_t gstride) {
+                             int vm_depth, unsigned char* gscratch, size_t gstride, double* errs) {
     auto k = rhs_kernel<TPT, MIXED>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    k<<<blocks, gpb * TPT, smem>>>(P, count, ts, ys, n_ov, ov_slots, ov_vals, dys, gpb, group_bytes, vm_depth, gscratch, gstride);
+    k<<<blocks, gpb * TPT, smem>>>(P, count, ts, ys, n_ov, ov_slots, ov_vals, dys, gpb, group_bytes, vm_depth, gscratch, gstride,
+                                   errs);
     return cudaGetLastError();
 }
 
@@ -1571,10 +1688,10 @@ cudaError_t launch_rhs_shape(const DevPlan& P, long long count, const double* ts
 #define OBE_EXTERN_RHS(T)                                                                                               \
     extern template cudaError_t launch_rhs_shape<T, false>(const DevPlan&, long long, const double*, const double*, int, \
                                                            const int*, const double*, double*, int, int, size_t, size_t, \
-                                                           int, unsigned char*, size_t);                                 \
+                                                           int, unsigned char*, size_t, double*);                        \
     extern template cudaError_t launch_rhs_shape<T, true>(const DevPlan&, long long, const double*, const double*, int,  \
                                                           const int*, const double*, double*, int, int, size_t, size_t,  \
-                                                          int, unsigned char*, size_t);
+                                                          int, unsigned char*, size_t, double*);
 OBE_FOR_EACH_SHAPE(OBE_EXTERN_SHAPE)
 OBE_FOR_EACH_RHS(OBE_EXTERN_RHS)
 #undef OBE_EXTERN_SHAPE

@@ -10,6 +10,7 @@
 // word per thread.
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
@@ -260,6 +261,10 @@ void lay_out_lanes(HostPacked& hp, int tpt) {
         }
     }
     hp.tpt = tpt;
+}
+
+int threads_per_trajectory_len(int64_t N) {
+    return N <= 512 ? 32 : N <= 1024 ? 64 : N <= 2048 ? 128 : N <= 8192 ? 256 : 1024;
 }
 
 int threads_per_trajectory_for(int32_t n) {
@@ -870,3 +875,222 @@ const char* last_error_cstr() { return g_last_error.c_str(); }
 }
 
 extern "C" const char* obe_last_error(void) { return obe::last_error_cstr(); }
+
+// ------------------------------------------------------------------------------------------
+// interpolated effective-Hamiltonian plans (rust/src/effective_lindblad/plan.rs)
+
+namespace obe {
+namespace {
+
+using cxd = std::complex<double>;
+
+// A parameter program evaluated on the host at t = 0 (the plan-time constant rule below): the
+// scalar operations of the VM; a tuple value, a helper function or an unknown operation makes
+// the program not evaluable here.
+bool host_eval(const obe_expr& e, const std::vector<cxd>& slots, const std::vector<uint8_t>& is_tuple, cxd* out) {
+    std::vector<cxd> st;
+    for (int64_t k = 0; k < e.n_instr; ++k) {
+        const int32_t op = e.op[k];
+        auto pop2 = [&](cxd& l, cxd& r) {
+            if (st.size() < 2) return false;
+            r = st.back(); st.pop_back();
+            l = st.back(); st.pop_back();
+            return true;
+        };
+        cxd l, r;
+        switch (op) {
+        case 1: st.emplace_back(e.value[2 * k], e.value[2 * k + 1]); break;           // CONST
+        case 2: {                                                                       // SLOT
+            const int64_t s = e.index[k];
+            if (s < 0 || s >= static_cast<int64_t>(slots.size()) || is_tuple[s]) return false;
+            st.push_back(slots[s]);
+            break;
+        }
+        case 4: st.emplace_back(0.0, 0.0); break;                                       // TIME
+        case 5: if (!pop2(l, r)) return false; st.push_back(l + r); break;
+        case 6: if (!pop2(l, r)) return false; st.push_back(l - r); break;
+        case 7: if (!pop2(l, r)) return false; st.push_back(l * r); break;
+        case 8: if (!pop2(l, r)) return false; st.push_back(l / r); break;
+        case 9: if (!pop2(l, r)) return false; st.push_back(r == cxd(0.0, 0.0) ? cxd(1.0, 0.0) : std::exp(r * std::log(l))); break;
+        case 10: if (st.empty()) return false; st.back() = -st.back(); break;           // NEG
+        case 11: if (st.empty()) return false; st.back() = std::conj(st.back()); break; // CONJ
+        case 12: {                                                                      // BUILTIN
+            const int64_t argc = e.argc[k];
+            if (argc < 1 || static_cast<int64_t>(st.size()) < argc) return false;
+            const cxd v = st[st.size() - argc];
+            st.resize(st.size() - argc);
+            switch (e.function[k]) {
+            case 1: st.push_back(std::sin(v)); break;
+            case 2: st.push_back(std::cos(v)); break;
+            case 3: st.push_back(std::tan(v)); break;
+            case 4: st.push_back(std::exp(v)); break;
+            case 5: st.emplace_back(std::abs(v), 0.0); break;
+            case 6: st.emplace_back(v.real(), 0.0); break;
+            case 7: st.emplace_back(v.imag(), 0.0); break;
+            default: return false;
+            }
+            break;
+        }
+        case 14: case 15: case 16: case 17: case 18: case 19: {                        // comparisons
+            if (!pop2(l, r)) return false;
+            const double a = l.real(), b = r.real();
+            const bool v = op == 14 ? a > b : op == 15 ? a >= b : op == 16 ? a < b : op == 17 ? a <= b : op == 18 ? a == b : a != b;
+            st.emplace_back(v ? 1.0 : 0.0, 0.0);
+            break;
+        }
+        default: return false;  // TEMP, HELPER, ...
+        }
+    }
+    if (st.size() != 1) return false;
+    *out = st[0];
+    return true;
+}
+
+bool expr_uses_time(const obe_expr& e) {
+    for (int64_t k = 0; k < e.n_instr; ++k)
+        if (e.op[k] == 4) return true;
+    return false;
+}
+
+// detect_constant_slot (effective_lindblad/plan.rs:205-277): a scalar base slot is its base
+// value; a compound whose program reads neither the time nor a slot whose first compound reads
+// the time is its value at t = 0 from the base values and the compounds before it.
+bool constant_slot(const obe_plan_desc* g, int32_t slot, double* out) {
+    if (slot < g->n_base && !(g->base_is_tuple && g->base_is_tuple[slot])) {
+        *out = g->base_scalar[2 * slot];
+        return true;
+    }
+    for (int32_t i = 0; i < g->n_compounds; ++i) {
+        if (g->compound_slot[i] != slot) continue;
+        const obe_expr& e = g->compound_expr[i];
+        if (expr_uses_time(e)) return false;
+        for (int64_t k = 0; k < e.n_instr; ++k) {
+            if (e.op[k] != 2) continue;
+            for (int32_t j = 0; j < g->n_compounds; ++j)
+                if (g->compound_slot[j] == e.index[k]) {
+                    if (expr_uses_time(g->compound_expr[j])) return false;
+                    break;
+                }
+        }
+        std::vector<cxd> slots(std::max(g->n_slots, 1), cxd(0.0, 0.0));
+        std::vector<uint8_t> tup(slots.size(), 0);
+        for (int32_t b = 0; b < g->n_base; ++b) {
+            if (g->base_is_tuple && g->base_is_tuple[b]) tup[b] = 1;
+            else slots[b] = cxd(g->base_scalar[2 * b], g->base_scalar[2 * b + 1]);
+        }
+        for (int32_t j = 0; j < g->n_compounds; ++j) {
+            if (g->compound_slot[j] == slot) break;
+            cxd v;
+            if (host_eval(g->compound_expr[j], slots, tup, &v)) {
+                slots[g->compound_slot[j]] = v;
+                tup[g->compound_slot[j]] = 0;
+            }
+        }
+        cxd v;
+        if (!host_eval(e, slots, tup, &v)) return false;
+        *out = v.real();
+        return true;
+    }
+    return false;
+}
+
+}  // namespace
+
+obe_status pack_effective(const obe_plan_desc* graph, const obe_effective_desc* eff, obe_plan* p) {
+    try {
+        if (!graph || !eff) fail(OBE_ERR_INVALID, "null plan descriptor");
+        const int32_t n = graph->n_states;
+        if (n <= 0) fail(OBE_ERR_INVALID, "layout dimension must be positive");
+        if (eff->real_dim != 2 * static_cast<int64_t>(n) * n) fail(OBE_ERR_INVALID, "real_dim must be 2 n_states^2");
+        if (eff->n_grid < 1 || !eff->field_grid) fail(OBE_ERR_INVALID, "field_grid length mismatch");
+        for (int32_t s : {eff->field_slot, eff->rabi_slot, eff->detuning_slot})
+            if (s < 0 || s >= graph->n_slots) fail(OBE_ERR_INVALID, strf("parameter slot %lld out of bounds", s));
+        // the RHS reads three plan coefficients: the field slot, the Rabi rate and the detuning,
+        // the latter two fixed at plan creation when the reference's constant rule applies
+        double crabi = 0.0, cdet = 0.0;
+        const bool rabi_const = constant_slot(graph, eff->rabi_slot, &crabi);
+        const bool det_const = constant_slot(graph, eff->detuning_slot, &cdet);
+        int32_t ops[3] = {2, rabi_const ? 1 : 2, det_const ? 1 : 2};
+        int64_t idx[3] = {eff->field_slot, eff->rabi_slot, eff->detuning_slot};
+        double vals[6] = {0.0, 0.0, crabi, 0.0, cdet, 0.0};
+        int32_t zero[3] = {0, 0, 0};
+        obe_expr prog[3];
+        for (int k = 0; k < 3; ++k) {
+            prog[k].n_instr = 1;
+            prog[k].op = &ops[k];
+            prog[k].index = &idx[k];
+            prog[k].argc = &zero[k];
+            prog[k].function = &zero[k];
+            prog[k].value = &vals[2 * k];
+            prog[k].scalar_only = 1;
+            prog[k].output_is_tuple = 0;
+        }
+        obe_plan_desc d = *graph;
+        d.hamiltonian_decomposed = 1;
+        d.n_coefficients = 3;
+        d.coefficient_expr = prog;
+        d.has_expanded = 0;
+        d.n_terms = 0;
+        obe_status st = pack_plan(&d, p);
+        if (st != OBE_OK) return st;
+        HostPacked& hp = p->packed;
+        const int64_t N = eff->real_dim;
+        if (N > 8192) fail(OBE_ERR_UNSUPPORTED, "effective-Hamiltonian states above 8192 doubles are not supported by the GPU solver");
+        p->N = N;
+        p->U = N / 2;
+        hp.eff = 1;
+        hp.pop_stride = n + 1;
+        hp.eff_grid.assign(eff->field_grid, eff->field_grid + eff->n_grid);
+        for (int32_t k = 1; k < eff->n_grid; ++k)
+            if (!(hp.eff_grid[k] > hp.eff_grid[k - 1])) fail(OBE_ERR_INVALID, "field_grid must be increasing");
+        const obe_interp_operator* opsd[3] = {&eff->combined, &eff->optical, &eff->detuning};
+        const char* names[3] = {"sparse_combined", "sparse_opt", "sparse_det"};
+        hp.eff_rows.clear();
+        hp.eff_cols.clear();
+        hp.eff_coef.clear();
+        const int64_t n_int = eff->n_grid > 1 ? eff->n_grid - 1 : 0;
+        for (int k = 0; k < 3; ++k) {
+            const obe_interp_operator& o = *opsd[k];
+            if (!o.row_ptrs || (o.nnz > 0 && (!o.col_indices || !o.coeffs)) || o.nnz < 0 || o.nnz > (1LL << 30))
+                fail(OBE_ERR_INVALID, std::string(names[k]) + ": missing or oversized arrays");
+            if (o.row_ptrs[0] != 0 || o.row_ptrs[N] != o.nnz) fail(OBE_ERR_INVALID, std::string(names[k]) + ": row_ptrs must run from 0 to nnz");
+            for (int64_t i = 0; i < N; ++i) {
+                if (o.row_ptrs[i + 1] < o.row_ptrs[i]) fail(OBE_ERR_INVALID, std::string(names[k]) + ": row_ptrs must be monotonic");
+                hp.eff_rows.push_back(static_cast<int32_t>(o.row_ptrs[i]));
+            }
+            hp.eff_rows.push_back(static_cast<int32_t>(o.row_ptrs[N]));
+            hp.eff_nnz[k] = static_cast<int32_t>(o.nnz);
+            hp.eff_col_off[k] = static_cast<int32_t>(hp.eff_cols.size());
+            for (int64_t q = 0; q < o.nnz; ++q) {
+                if (o.col_indices[q] < 0 || o.col_indices[q] >= N) fail(OBE_ERR_INVALID, std::string(names[k]) + ": column index out of bounds");
+                hp.eff_cols.push_back(static_cast<int32_t>(o.col_indices[q]));
+            }
+            hp.eff_coef_off[k] = static_cast<int64_t>(hp.eff_coef.size());
+            hp.eff_coef.insert(hp.eff_coef.end(), o.coeffs, o.coeffs + n_int * o.nnz * 4);
+        }
+        lay_out_lanes(hp, threads_per_trajectory_len(N));
+        return OBE_OK;
+    } catch (const Fail& f) {
+        set_error(f.msg);
+        return f.code;
+    }
+}
+
+}  // namespace obe
+
+extern "C" obe_status obe_effective_plan_create(const obe_plan_desc* graph, const obe_effective_desc* eff, obe_plan** out_plan) {
+    if (!out_plan) {
+        obe::set_error("null output pointer");
+        return OBE_ERR_INVALID;
+    }
+    *out_plan = nullptr;
+    obe_plan* p = new obe_plan();
+    obe_status st = obe::pack_effective(graph, eff, p);
+    if (st != OBE_OK) {
+        delete p;
+        return st;
+    }
+    *out_plan = p;
+    obe::set_error("");
+    return OBE_OK;
+}

@@ -62,6 +62,7 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     size_t o_fp = put(blob, h.formula_ptr), o_pf = put(blob, h.prod_factor), o_pcl = put(blob, h.prod_class), o_pf32 = put(blob, h.prod_factor32);
     size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out), o_fs = put(blob, h.fstream);
     size_t o_tr = put(blob, h.trec), o_li = put(blob, h.lane_in), o_bil = put(blob, h.bil);
+    size_t o_eg = put(blob, h.eff_grid), o_er = put(blob, h.eff_rows), o_ec = put(blob, h.eff_cols), o_ef = put(blob, h.eff_coef);
     P = DevPlan{};
     P.n = p->n;
     P.N = static_cast<int32_t>(p->N);
@@ -115,6 +116,18 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     P.lane_in = reinterpret_cast<const uint32_t*>(base + o_li);
     P.n_biter = h.n_biter;
     P.bil = reinterpret_cast<const uint32_t*>(base + o_bil);
+    P.pop_stride = h.pop_stride;
+    P.eff = h.eff;
+    P.eff_ngrid = static_cast<int32_t>(h.eff_grid.size());
+    P.eff_grid = reinterpret_cast<const double*>(base + o_eg);
+    P.eff_rows = reinterpret_cast<const int32_t*>(base + o_er);
+    P.eff_cols = reinterpret_cast<const int32_t*>(base + o_ec);
+    P.eff_coef = reinterpret_cast<const double*>(base + o_ef);
+    for (int k = 0; k < 3; ++k) {
+        P.eff_nnz[k] = h.eff_nnz[k];
+        P.eff_col_off[k] = h.eff_col_off[k];
+        P.eff_coef_off[k] = h.eff_coef_off[k];
+    }
 }
 
 obe_status upload_plan(obe_plan* p) {
@@ -268,6 +281,23 @@ int64_t packed_upper_real_index(int32_t n, int64_t i, int64_t j) {
     return n + 2 * (off + (j - i - 1));
 }
 
+// Rust's `{:.6e}` (six decimals, exponent without sign padding: 1.000000e2, -3.500000e-1)
+std::string fmt_rust_exp6(double v) {
+    char buf[64];
+    std::snprintf(buf, sizeof buf, "%.6e", v);
+    char* ep = std::strchr(buf, 'e');
+    if (!ep) return buf;
+    const int ex = std::atoi(ep + 1);
+    *ep = 0;
+    return std::string(buf) + "e" + std::to_string(ex);
+}
+
+// effective_lindblad/rhs.rs:56-67
+std::string field_range_message(bool above, double x, double bound) {
+    return "field coordinate " + fmt_rust_exp6(x) + (above ? " is above the operator grid maximum " : " is below the operator grid minimum ") +
+           fmt_rust_exp6(bound);
+}
+
 std::string traj_message(int code, const TrajErr& e) {
     switch (code) {
     case ST_MAXITERS: return "Stopped at x=" + fmt_f64(e.x) + ". Need more than " + std::to_string(e.a) + " steps.";
@@ -281,6 +311,11 @@ std::string traj_message(int code, const TrajErr& e) {
     case ST_BACKWARD: return "only forward integration";
     case ST_FIXED_DT: return "fixed-step solvers require positive finite dt";
     case ST_TAPE: return "the gradient tape holds " + std::to_string(e.a) + " accepted steps per trajectory; pass a larger max_steps";
+    case ST_FIELD_LOW: case ST_FIELD_HIGH: {
+        double g;
+        std::memcpy(&g, &e.a, sizeof g);
+        return field_range_message(code == ST_FIELD_HIGH, e.x, g);
+    }
     default: return "trajectory failed with status " + std::to_string(code);
     }
 }
@@ -294,7 +329,16 @@ struct CallBlob {
 
 obe_status validate_options(const obe_plan* p, const obe_solve_options* o, std::vector<double>& save_times, CallBlob& cb,
                             int64_t* width_out, int* is_complex) {
-    if (!p->has_expanded) {
+    const bool eff = p->packed.eff != 0;
+    if (eff && o->precision == OBE_PRECISION_MIXED) {
+        set_error("effective-Hamiltonian plans solve in double precision");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    if (eff && o->event_kind != OBE_EVENT_NONE) {
+        set_error("effective-Hamiltonian solves take no stop event");
+        return OBE_ERR_UNSUPPORTED;
+    }
+    if (!p->has_expanded && !eff) {
         set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan");
         return OBE_ERR_INVALID;
     }
@@ -322,6 +366,14 @@ obe_status validate_options(const obe_plan* p, const obe_solve_options* o, std::
         for (int k = 0; k < o->n_selected; ++k) {
             int64_t i = o->selected_i[k], j = o->selected_j[k];
             if (i < 0 || j < 0 || i >= p->n || j >= p->n) { set_error("selected output index out of bounds"); return OBE_ERR_INVALID; }
+            if (eff) {
+                // split_real_selected_extractions (effective_lindblad/solver.rs:58-76)
+                const int64_t nn = p->n;
+                sre.push_back(static_cast<int32_t>(i * nn + j));
+                sim.push_back(static_cast<int32_t>(i == j ? i * nn + j : nn * nn + i * nn + j));
+                skind.push_back(i == j ? 0 : 1);
+                continue;
+            }
             if (i == j) { sre.push_back(static_cast<int32_t>(i)); sim.push_back(static_cast<int32_t>(i)); skind.push_back(0); }
             else if (i < j) { int64_t r = packed_upper_real_index(p->n, i, j); sre.push_back(static_cast<int32_t>(r)); sim.push_back(static_cast<int32_t>(r + 1)); skind.push_back(1); }
             else { int64_t r = packed_upper_real_index(p->n, j, i); sre.push_back(static_cast<int32_t>(r)); sim.push_back(static_cast<int32_t>(r + 1)); skind.push_back(2); }
@@ -583,6 +635,11 @@ static obe_status solve_batch_device_locked(obe_plan* p, const obe_solve_options
 namespace {
 constexpr int kWidths[] = {32, 64, 128, 256, 512};  // the compiled threads-per-trajectory widths
 
+// the automatic width: by the number of states, or by the state length for effective plans
+int default_width(const obe_plan* p) {
+    return p->packed.eff ? threads_per_trajectory_len(p->N) : threads_per_trajectory_for(p->n);
+}
+
 // Lays the plan's record streams out for `tpt` threads per trajectory; the device image follows
 // on the next solve.
 void relayout(obe_plan* p, int tpt) {
@@ -607,7 +664,7 @@ obe_status obe_plan_set_shape(obe_plan* p, int32_t tpt, int32_t gpb) {
     }
     if (gpb < 0) { set_error("trajectories per CTA must be non-negative"); return OBE_ERR_INVALID; }
     std::lock_guard<std::mutex> lock(g_plan_mutex);
-    relayout(p, tpt > 0 ? tpt : threads_per_trajectory_for(p->n));
+    relayout(p, tpt > 0 ? tpt : default_width(p));
     p->shape_tpt = tpt;
     p->shape_gpb = gpb;
     return OBE_OK;
@@ -641,7 +698,7 @@ obe_status obe_plan_autotune(obe_plan* p, const obe_solve_options* opt, int64_t 
     const int vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
     // candidates: the automatic width and the wider compiled ones up to 4x it, in the same
     // memory layout; each with as many trajectories per CTA as fit, half of that, and one
-    const int w0 = threads_per_trajectory_for(p->n);
+    const int w0 = default_width(p);
     std::vector<std::pair<int, int>> cands;
     for (int tw : kWidths) {
         if (tw < w0 || tw > 4 * w0 || shape_capacity(tw) < p->N || (tw >= 256) != (w0 >= 256)) continue;
@@ -1017,6 +1074,10 @@ void obe_result_destroy(obe_result* res) { delete res; }
 
 // the outputs and options a gradient supports; *width_out: 1 (weighted integral) or n
 static obe_status grad_check(const obe_plan* p, const obe_solve_options* o, int64_t* width_out) {
+    if (p->packed.eff) {
+        set_error("gradients are implemented for expanded_sparse plans");
+        return OBE_ERR_UNSUPPORTED;
+    }
     if (!p->has_expanded) {
         set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan");
         return OBE_ERR_INVALID;
@@ -1196,12 +1257,29 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     return OBE_OK;
 }
 
+static obe_status rhs_eval(const obe_plan* plan, int64_t count, const double* t, const double* y, int32_t n_override_slots,
+                           const int64_t* override_slots, const double* override_values, int32_t precision, double* dy,
+                           double* eff_info);
+
 obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, const double* y, int32_t n_override_slots,
                         const int64_t* override_slots, const double* override_values, int32_t precision, double* dy) {
+    return rhs_eval(plan, count, t, y, n_override_slots, override_slots, override_values, precision, dy, nullptr);
+}
+
+obe_status obe_effective_rhs_debug(const obe_plan* plan, double t, const double* y, double* dy, double* info) {
+    if (!plan || !plan->packed.eff) { set_error("not an effective-Hamiltonian plan"); return OBE_ERR_INVALID; }
+    if (!info) { set_error("null argument"); return OBE_ERR_INVALID; }
+    return rhs_eval(plan, 1, &t, y, 0, nullptr, nullptr, OBE_PRECISION_FP64, dy, info);
+}
+
+static obe_status rhs_eval(const obe_plan* plan, int64_t count, const double* t, const double* y, int32_t n_override_slots,
+                           const int64_t* override_slots, const double* override_values, int32_t precision, double* dy,
+                           double* eff_info) {
     g_launches = 0;
     obe_plan* p = const_cast<obe_plan*>(plan);
     if (!p || !t || !y || !dy || count <= 0) { set_error("invalid RHS arguments"); return OBE_ERR_INVALID; }
-    if (!p->has_expanded) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
+    if (!p->has_expanded && !p->packed.eff) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
+    if (p->packed.eff && precision == OBE_PRECISION_MIXED) { set_error("effective-Hamiltonian plans solve in double precision"); return OBE_ERR_UNSUPPORTED; }
     std::lock_guard<std::mutex> lock(g_plan_mutex);
     obe_status st = ensure_ready(p);
     if (st != OBE_OK) return st;
@@ -1220,6 +1298,7 @@ obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, co
     size_t o_dy = off; off = align16(off + 8 * count * p->N);
     size_t o_sl = off; off = align16(off + 4 * std::max<size_t>(slots.size(), 1));
     size_t o_ov = off; off = align16(off + 16 * count * std::max<int32_t>(n_override_slots, 1));
+    size_t o_er = off; off = align16(off + 64 * count);
     unsigned char* d = nullptr;
     if ((st = scratch(p, off, &d)) != OBE_OK) return st;
     cudaMemcpy(d + o_t, t, 8 * count, cudaMemcpyHostToDevice);
@@ -1234,12 +1313,24 @@ obe_status obe_rhs_eval(const obe_plan* plan, int64_t count, const double* t, co
         le = (mixed ? launch_rhs_shape<T, true> : launch_rhs_shape<T, false>)(                                            \
             p->dev, count, reinterpret_cast<double*>(d + o_t), reinterpret_cast<double*>(d + o_y), n_override_slots,      \
             reinterpret_cast<int*>(d + o_sl), reinterpret_cast<double*>(d + o_ov), reinterpret_cast<double*>(d + o_dy),   \
-            s.blocks, s.gpb, s.smem, s.group_bytes, vm_depth, gk, s.gstride);
+            s.blocks, s.gpb, s.smem, s.group_bytes, vm_depth, gk, s.gstride, reinterpret_cast<double*>(d + o_er));
     OBE_FOR_EACH_RHS(OBE_RHS_DISPATCH)
 #undef OBE_RHS_DISPATCH
     g_launches += 1;
     if (!cuda_ok(le, "rhs kernel launch")) return OBE_ERR_CUDA;
     if (!cuda_ok(cudaMemcpy(dy, d + o_dy, 8 * count * p->N, cudaMemcpyDeviceToHost), "rhs kernel")) return OBE_ERR_CUDA;
+    if (p->packed.eff) {
+        // effective plans: the first state whose field left the operator grid fails the call
+        std::vector<double> errs(8 * static_cast<size_t>(count));
+        if (!cuda_ok(cudaMemcpy(errs.data(), d + o_er, errs.size() * 8, cudaMemcpyDeviceToHost), "rhs kernel")) return OBE_ERR_CUDA;
+        for (int64_t k = 0; k < count; ++k)
+            if (errs[8 * k] != 0.0) {
+                set_error(field_range_message(errs[8 * k] == ST_FIELD_HIGH, errs[8 * k + 1], errs[8 * k + 2]));
+                return OBE_ERR_INVALID;
+            }
+        if (eff_info)
+            for (int q = 0; q < 4; ++q) eff_info[q] = errs[3 + q];
+    }
     set_error("");
     return OBE_OK;
 }
@@ -1291,7 +1382,7 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
                   " trajectories per call, got " + std::to_string(n_traj));
         return OBE_ERR_INVALID;
     }
-    if (!p->has_expanded) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
+    if (!p->has_expanded && !p->packed.eff) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
     if (obe_device_count() <= 0) { set_error("no CUDA device is available: the GB300 solver has no CPU fallback"); return OBE_ERR_CUDA; }
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     int dev = 0;

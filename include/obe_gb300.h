@@ -276,6 +276,10 @@ typedef struct {
 
 obe_status obe_effective_plan_create(const obe_plan_desc* graph, const obe_effective_desc* eff,
                                      obe_plan** out_plan);
+/* debug_effective_lindblad_rhs_py (effective_lindblad/python_api.rs:94-152): one RHS at t (host
+ * pointers, y and dy of real_dim doubles) with info[4] = the field coordinate, Rabi rate and
+ * detuning it used and the field interval. */
+obe_status obe_effective_rhs_debug(const obe_plan* plan, double t, const double* y, double* dy, double* info);
 
 /*
  * Launch-shape tuning (no counterpart in the reference, whose CPU path has no launch shape).
