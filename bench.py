@@ -13,8 +13,8 @@ the same batch beside it (`fp64_gpu`).  `value` times the device-resident entry
 point (obe_solve_batch_device) with CUDA events on its stream and the L2 flushed between steps;
 `e2e` times the reference-facing call solve_lindblad_batch_ode_py with host arrays (copies in
 the timed region).  Beside the headline the line carries the adjoint's cost against the forward
-solve (`gradient`) and the heterogeneous batch of 16-, 39- and 76-state systems in one call
-(`heterogeneous`).  `--impl reference` times the CPU path of the reference restated in C
+solve (`gradient`), the heterogeneous batch of 16-, 39- and 76-state systems in one call
+(`heterogeneous`) and the interpolated effective-Hamiltonian path (`effective`).  `--impl reference` times the CPU path of the reference restated in C
 (the oracle) on the host cores, on a bounded sample of the same scan.
 """
 
@@ -379,6 +379,54 @@ def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
     }
 
 
+def measure_effective(torch, dev, total: int = 4096, cpu_sample: int = 256, reps: int = 2) -> dict:
+    """The interpolated effective-Hamiltonian path (solve_effective_lindblad_batch_py): the R(0)
+    compact model of tests/golden/plan_eff_r0.json (10 states, split-real state of 200 doubles,
+    field oscillating across the 100-200 V/cm operator grid), `total` trajectories with seeded
+    Rabi rates U[0.3, 2]·1e7 and detunings U[-5, 5]·1e6, Tsit5 rtol 1e-7 atol 1e-9 over 5 µs, the
+    excited-population integral; host arrays in and out (the reference-facing call), against the
+    FP64 oracle on a sample on all host threads."""
+    import codec
+    import oracle
+    from centrex_tlf_gb300 import centrex_tlf_rust as api
+
+    d = codec.load("plan_eff_r0")
+    plan = api.prepare_effective_lindblad_plan_py(d["plan"])
+    rng = np.random.default_rng(20241205)
+    pb = np.stack([rng.uniform(0.3e7, 2.0e7, total), rng.uniform(-5e6, 5e6, total)], axis=1)
+    w = [(i * 11, 1.0) for i in (7, 8, 9)]
+    t0, t1 = d["t_span"]
+
+    def run():
+        return api.solve_effective_lindblad_batch_py(plan, d["y0"], t0, t1, 1e-9, 1e-7, 1e-10, None, True, 100000, "tsit5",
+                                                     "excited_population", None, w, [0, 1], pb, total)
+
+    run()
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        start = time.perf_counter()
+        out = run()
+        torch.cuda.synchronize()
+        best = min(best, time.perf_counter() - start)
+    op = oracle.EffectiveOraclePlan(d["plan"])
+    o = op.options(t0=t0, t1=t1, abstol=1e-9, reltol=1e-7, dt=1e-10, saveat=None, save_start=True, maxiters=100000,
+                   solver="tsit5", output="excited_population", output_indices=None, integral_weights=w,
+                   output_when="final")
+    start = time.perf_counter()
+    ref, _, _ = op.solve_batch(o, d["y0"], [0, 1], pb[:cpu_sample].astype(complex))
+    cpu_s = time.perf_counter() - start
+    vals = np.asarray(out[1])[:cpu_sample]
+    rel = float(np.max(np.abs(vals - ref.reshape(-1)) / np.abs(ref.reshape(-1))))
+    return {"workload": f"{total} trajectories of the 10-state R(0) interpolated effective model, Tsit5, "
+                        "excited-population integral, host arrays in and out",
+            "value": total / best, "unit": "trajectories/s", "ms": 1e3 * best,
+            "accepted_steps": int(out[4]["accepted_steps"]),
+            "cpu_oracle": {"value": cpu_sample / cpu_s, "unit": "trajectories/s", "cores": int(oracle.max_threads()),
+                           "sample": cpu_sample},
+            "max_rel_err_vs_cpu_oracle": rel}
+
+
 def run_gpu(args) -> None:
     import torch
 
@@ -511,6 +559,7 @@ def run_gpu(args) -> None:
     cpu = cpu_oracle_rate(d, params, slots, args.cpu_sample)
     gradient = measure_gradient(torch, d, params, dev) if not args.no_gradient else None
     hetero = measure_heterogeneous(torch, dev, total=args.hetero_instances) if args.hetero_instances > 0 else None
+    effective = measure_effective(torch, dev) if not args.no_effective else None
     gpu_obs = np.asarray(out[1])[: args.cpu_sample]
     obs_rel = float(np.max(np.abs(gpu_obs - cpu["values"]) / np.maximum(np.abs(cpu["values"]), 1e-300)))
     accuracy["observable_max_rel_err_vs_cpu_oracle"] = obs_rel
@@ -551,6 +600,7 @@ def run_gpu(args) -> None:
         "clocks": clocks,
         "gradient": gradient,
         "heterogeneous": hetero,
+        "effective": effective,
     }
     print(json.dumps(line))
     if world > 1:
@@ -633,6 +683,7 @@ def main() -> None:
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 path beside mixed")
     ap.add_argument("--no-gradient", action="store_true", help="skip timing the adjoint beside the forward solve")
+    ap.add_argument("--no-effective", action="store_true", help="skip timing the effective-Hamiltonian path")
     ap.add_argument("--hetero-instances", type=int, default=8192,
                     help="instances of the heterogeneous 16/39/76-state batch timed beside the scan (0 skips it)")
     ap.add_argument("--points", type=int, default=4096)
