@@ -442,8 +442,11 @@ def run_gpu(args) -> None:
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
+    from centrex_tlf_gb300.sharding import max_over_ranks, shard_bounds
+
     d, params_all, slots = workload(args.points * world)
-    params = params_all[rank * args.points:(rank + 1) * args.points]  # weak scaling: one shard per rank
+    lo, hi = shard_bounds(args.points, rank)  # weak scaling: one shard of the scan per rank
+    params = params_all[lo:hi]
     gamma, (t0, t1) = d["gamma"], d["t_span"]
     b = params.shape[0]
     plan = api.prepare_lindblad_problem_py(d["payload"])
@@ -502,10 +505,7 @@ def run_gpu(args) -> None:
         other = (ms64, att64)
     total_s = sum(ms) * 1e-3
     total64_s = sum(other[0]) * 1e-3 if other else 0.0
-    if world > 1:
-        t = torch.tensor([total_s, total64_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s, total64_s = float(t[0].item()), float(t[1].item())
+    total_s, total64_s = max_over_ranks([total_s, total64_s], device=dev)
     value = b * world * args.steps / total_s
     launches = args.steps  # one integrator launch per solve (obe_last_launch_count agrees)
 
