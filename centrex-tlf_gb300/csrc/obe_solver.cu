@@ -45,7 +45,9 @@ int k1_refresh_interval() {
     static int v = 0;
     if (!v) {
         const char* env = std::getenv("OBE_K1_REFRESH");
-        v = env ? std::max(1, std::atoi(env)) : 8;
+        // every 32 accepted steps: measured on the 4096-point 16-state scan, 8 -> 32 is 5 % faster
+        // at a population error against FP64 of 4.3e-9 (8.7e-10 at 8; 9.7e-8 with no refresh)
+        v = env ? std::max(1, std::atoi(env)) : 32;
     }
     return v;
 }
