@@ -8,7 +8,10 @@ derivatives per step).  The backward pass is the exact adjoint of that discrete 
 step sequence frozen -- what central finite differences of the solve with the same steps give --
 for the final weighted integral (``excited_population``, ``photon_integral``,
 ``weighted_integral``) or the final populations, with respect to any scalar base parameter slots
-and the packed initial state.
+and the packed initial state.  A ``stop_event`` (population threshold or runtime expression) may
+end each trajectory: the step that ends on it maps to the dense output at the event time, and the
+event time's own dependence on the state and parameters enters through the event function's
+derivatives.
 
 Example::
 
@@ -34,6 +37,7 @@ __all__ = ["solve_batch_with_grad", "ForwardTape"]
 _ADJ_MESSAGES = {
     1: "a helper function or interpolation table receives an argument that depends on a differentiated parameter",
     2: "the forward trajectory failed or ran past the tape",
+    3: "the stop event's function has a zero time derivative at the crossing",
 }
 
 
@@ -57,6 +61,11 @@ class ForwardTape:
             per = self.plan.grad_tape_doubles_per_step()
             tape = self.tape.view(b, self.max_steps, per)[:, :, :2].cpu().numpy()
         return [tape[k, : int(st[k, 0])] for k in range(b)]
+
+    def event_hits(self) -> np.ndarray:
+        """Per trajectory: 1 where the stop event ended the solve (its last step is the event step)."""
+        st = self.stats.view(-1, 6).cpu().numpy()
+        return (st[:, 3] & 0xFFFFFFFF).astype(np.int32)
 
 
 def _checkpoint_every(plan: NativePlan, b: int, max_steps: int, requested: int | None) -> int:
@@ -126,7 +135,7 @@ def solve_batch_with_grad(plan: NativePlan, rho0, t_span: Sequence[float], param
                           parameter_slot_indices: Sequence[int], *, solver: str = "tsit5", abstol: float = 1e-11,
                           reltol: float = 1e-8, dt: float = 0.0, maxiters: int = 100000,
                           output: str = "excited_population", integral_weights=None, max_steps: int = 4096,
-                          checkpoint_every: int | None = None, return_tape: bool = False):
+                          checkpoint_every: int | None = None, stop_event=None, return_tape: bool = False):
     """Batched double-precision solve whose outputs are differentiable in ``params`` ((B, S) real,
     the values of the base slots ``parameter_slot_indices``) and in ``rho0`` ((B, N) packed).
 
@@ -135,18 +144,20 @@ def solve_batch_with_grad(plan: NativePlan, rho0, t_span: Sequence[float], param
     ``checkpoint_every``: 0 records every step's stage derivatives; C > 0 records the start state
     of every C-th step and the reverse sweep recomputes each segment from it (one more forward's
     work, a tape of 2 + N / C doubles per step); None takes the full tape while it stays under
-    4 GiB.
-    With ``return_tape`` the forward tape comes back too (its ``steps()`` are the frozen steps).
+    4 GiB.  ``stop_event``: as in the solves (``{"kind": "population", "indices", "threshold"}`` or
+    ``{"kind": "runtime_expression", "expression"}``); the outputs end at the event time.
+    With ``return_tape`` the forward tape comes back too (its ``steps()`` are the frozen steps,
+    its ``event_hits()`` which trajectories ended on the event).
     """
     t0, t1 = float(t_span[0]), float(t_span[1])
     if output in INTEGRAL_OUTPUTS:
         opts = plan.options(t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=None, save_start=True,
                             maxiters=maxiters, solver=solver, output=output, output_indices=None, output_when="final",
-                            integral_weights=integral_weights, stop_event=None)
+                            integral_weights=integral_weights, stop_event=stop_event)
     elif output == "populations":
         opts = plan.options(t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=np.array([t1]), save_start=False,
                             maxiters=maxiters, solver=solver, output="populations", output_indices=None,
-                            output_when="final", integral_weights=None, stop_event=None)
+                            output_when="final", integral_weights=None, stop_event=stop_event)
     else:
         raise NotImplementedError("gradients are available for final weighted integrals and final populations")
     dev = params.device

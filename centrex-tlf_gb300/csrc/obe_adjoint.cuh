@@ -29,7 +29,7 @@ namespace obe {
 constexpr int kMaxGrad = 8;
 
 // per-trajectory adjoint status codes
-enum AdjCode : int32_t { ADJ_OK = 0, ADJ_HELPER_DERIVATIVE = 1, ADJ_FORWARD_FAILED = 2 };
+enum AdjCode : int32_t { ADJ_OK = 0, ADJ_HELPER_DERIVATIVE = 1, ADJ_FORWARD_FAILED = 2, ADJ_EVENT_TANGENT = 3 };
 
 struct AdjArgs {
     int n_grad;
@@ -57,17 +57,17 @@ struct AdjArgs {
 // ------------------------------------------------------------------------------------------
 // forward-mode evaluation: value and derivatives with respect to the n_grad parameters
 
-// One program in dual numbers.  slots / dslots: values and derivatives ([slot * n_grad + g]) of
-// the parameter slots; the stack holds values in sv, derivatives in sd ([depth * kMaxGrad]) and
-// tuple ids in tp.  Returns the value and writes the derivatives to out_d[0..n_grad).  A helper
-// or table whose arguments carry a derivative sets *bad (its derivative is not implemented).
-static __device__ __noinline__ double2 vm_eval_dual(const DevPlan& P, int32_t start, int32_t len, const double2* slots,
-                                                    const double2* dslots, int ng, double t, double2* sv, double2* sd,
-                                                    int32_t* tp, double2* out_d, int* bad) {
-    const int32_t* op = P.ins_op;
-    const int32_t* arg = P.ins_arg;
-    const int32_t* fn = P.ins_fn;
-    const double* val = P.ins_val;
+// One program (instruction arrays op/arg/fn/val, entries start..start+len) in dual numbers.
+// slots / dslots: values and derivatives ([slot * n_grad + g]) of the parameter slots; the stack
+// holds values in sv, derivatives in sd ([depth * kMaxGrad]) and tuple ids in tp.  Returns the
+// value and writes the derivatives to out_d[0..n_grad).  tseed >= 0 seeds d(time)/d(variable
+// tseed) = 1 (the time derivative of the program).  A helper or table whose arguments carry a
+// derivative sets *bad (its derivative is not implemented).
+static __device__ __noinline__ double2 vm_eval_dual_prog(const DevPlan& P, const int32_t* op, const int32_t* arg,
+                                                         const int32_t* fn, const double* val, int32_t start, int32_t len,
+                                                         const double2* slots, const double2* dslots, int ng, double t,
+                                                         double2* sv, double2* sd, int32_t* tp, double2* out_d, int* bad,
+                                                         int tseed) {
     int sp = 0;
     auto D = [&](int i, int g) -> double2& { return sd[i * kMaxGrad + g]; };
     for (int32_t k = start; k < start + len; ++k) {
@@ -88,7 +88,7 @@ static __device__ __noinline__ double2 vm_eval_dual(const DevPlan& P, int32_t st
         }
         case OP_TIME:
             sv[sp] = make_double2(t, 0.0);
-            for (int g = 0; g < ng; ++g) D(sp, g) = make_double2(0.0, 0.0);
+            for (int g = 0; g < ng; ++g) D(sp, g) = make_double2(g == tseed ? 1.0 : 0.0, 0.0);
             tp[sp++] = -1;
             break;
         case OP_ADD: case OP_SUB: case OP_MUL: case OP_DIV: case OP_POW: {
@@ -230,17 +230,27 @@ static __device__ __noinline__ double2 vm_eval_dual(const DevPlan& P, int32_t st
     return sv[0];
 }
 
+// a program of the plan's expression pool, derivatives with respect to the parameters
+static __device__ __forceinline__ double2 vm_eval_dual(const DevPlan& P, int32_t start, int32_t len, const double2* slots,
+                                                       const double2* dslots, int ng, double t, double2* sv, double2* sd,
+                                                       int32_t* tp, double2* out_d, int* bad) {
+    return vm_eval_dual_prog(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, start, len, slots, dslots, ng, t, sv, sd, tp, out_d,
+                             bad, -1);
+}
+
 // ------------------------------------------------------------------------------------------
 // shared-memory layout of one adjoint trajectory group (tpt threads)
 
 struct AdjLayout {
-    size_t tab, G, LS, MU, YB, slots, dslots, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, red, traj, bytes;
+    size_t tab, G, LS, MU, YB, slots, dslots, dts, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, red, traj, bytes;
     size_t gbytes;  // large systems: bytes of the group's device-memory slice (MU, YB, S)
     bool glob;
 };
 
+// stages: 6, or 7 when a stop event can end the solve (the event step's dense output reads the
+// first-same-as-last stage too)
 __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int n_coeff, int n_dyn, int n_slots, int vm_depth,
-                                                int tpt) {
+                                                int tpt, int stages) {
     const size_t U = static_cast<size_t>(n) * (n + 1) / 2;
     const size_t nc = n_coeff > 0 ? n_coeff : 1, nd = n_dyn > 0 ? n_dyn : 1, ns = n_slots > 0 ? n_slots : 1;
     AdjLayout L{};
@@ -250,10 +260,11 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     L.tab = o; o = align16(o + (1 + n_formula) * 16);
     L.G = o; o = align16(o + U * 16);
     L.LS = o; o = align16(o + U * 16);
-    L.MU = om; om = align16(om + 6 * static_cast<size_t>(N) * 8);
+    L.MU = om; om = align16(om + static_cast<size_t>(stages) * N * 8);
     L.YB = om; om = align16(om + static_cast<size_t>(N) * 8);
     L.slots = o; o = align16(o + 6 * ns * 16);
     L.dslots = o; o = align16(o + 6 * ns * kMaxGrad * 16);
+    L.dts = o; o = align16(o + ns * 16);
     L.sv = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 16);
     L.sd = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * kMaxGrad * 16);
     L.tp = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 4);
@@ -273,6 +284,35 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
 // the record streams staged per CTA (large systems read them from the plan's device image)
 __host__ __device__ inline size_t adj_plan_smem_bytes(const DevPlan& P, int tpt) {
     return tpt >= 256 ? 0 : align16(static_cast<size_t>(P.n_biter + P.n_titer + P.n_tin) * tpt * 4);
+}
+
+// The dense output of a step as stage weights: y(theta) = y_n + h sum_{j<7} w_j(theta) K_j, and
+// dw_j = d w_j / d theta.  Dopri5 (M = 0, dopri5.rs:104-143): theta dd + theta(1-theta) bb +
+// theta^2 (1-theta) r3 + theta^2 (1-theta)^2 r4 with dd = h sum b_j K_j, bb = h K_1 - dd,
+// r3 = -h K_7 + dd - bb, r4 = h sum d_j K_j.  Tsit5 (M = 1, tsit5.rs:121-143): the interpolant's
+// quartic polynomials.  b: the solution weights (b_7 = 0).
+__device__ __forceinline__ void dense_weights(int M, double th, const double* b, double* w, double* dw) {
+    if (M == 0) {
+        const double t1 = 1.0 - th;
+        const double p1 = th, p2 = th * t1, p3 = th * th * t1, p4 = th * th * t1 * t1;
+        const double q1 = 1.0, q2 = 1.0 - 2.0 * th, q3 = th * (2.0 - 3.0 * th), q4 = 2.0 * th * t1 * (1.0 - 2.0 * th);
+#pragma unroll
+        for (int j = 0; j < 7; ++j) {
+            const double bj = j < 6 ? b[j] : 0.0;
+            const double e0 = j == 0 ? 1.0 : 0.0, e6 = j == 6 ? 1.0 : 0.0;
+            const double dj = j == 1 ? 0.0 : kTab.dd[j];
+            const double c2 = e0 - bj, c3 = 2.0 * bj - e0 - e6;
+            w[j] = p1 * bj + p2 * c2 + p3 * c3 + p4 * dj;
+            dw[j] = q1 * bj + q2 * c2 + q3 * c3 + q4 * dj;
+        }
+    } else {
+        const double t2 = th * th, t3 = t2 * th, t4 = t3 * th;
+#pragma unroll
+        for (int j = 0; j < 7; ++j) {
+            w[j] = kTab.r[j][0] * th + kTab.r[j][1] * t2 + kTab.r[j][2] * t3 + kTab.r[j][3] * t4;
+            dw[j] = kTab.r[j][0] + 2.0 * kTab.r[j][1] * th + 3.0 * kTab.r[j][2] * t2 + 4.0 * kTab.r[j][3] * t3;
+        }
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -303,7 +343,8 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     __syncthreads();
     if (g >= gpb) return;
 
-    const AdjLayout Lay = adj_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, TPT);
+    const int n_stage_max = A.ev_kind != OBE_EVENT_NONE ? 7 : 6;
+    const AdjLayout Lay = adj_layout(n, N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, TPT, n_stage_max);
     unsigned char* gb = smem + adj_plan_smem_bytes(P, TPT) + static_cast<size_t>(g) * group_bytes;
     unsigned char* gm = Lay.glob ? J.gscratch + (static_cast<size_t>(blockIdx.x) * gpb + g) * J.gstride : gb;
     double2* s_tab = reinterpret_cast<double2*>(gb + Lay.tab);
@@ -332,6 +373,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     double2* sv = reinterpret_cast<double2*>(gb + Lay.sv) + vl * A.vm_depth;
     double2* sd = reinterpret_cast<double2*>(gb + Lay.sd) + static_cast<size_t>(vl) * A.vm_depth * kMaxGrad;
     int32_t* tp = reinterpret_cast<int32_t*>(gb + Lay.tp) + vl * A.vm_depth;
+    double2* dts = reinterpret_cast<double2*>(gb + Lay.dts);
     const bool integral = A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL;
     // solution weights b (row 5 of the stage table) and stage times c_s
     double bw[6], cs[6];
@@ -351,6 +393,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         int bad = 0;
         const obe_traj_stats fst = J.fwd_stats[traj];
         const long long n_acc = fst.accepted_steps;
+        const bool ev_hit = A.ev_kind != OBE_EVENT_NONE && fst.event_triggered != 0 && n_acc > 0;
         if (fst.status != 0 || n_acc > J.tape_cap) {
             if (lt == 0) J.adj_status[traj] = ADJ_FORWARD_FAILED;
             for (int q = lt; q < ng; q += TPT) J.param_grad[traj * ng + q] = CUDART_NAN;
@@ -454,6 +497,18 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, K_r + static_cast<size_t>(s) * N, lt);
                     gsync<TPT>(g);
                 }
+                if (ev_hit && st == n_acc - 1) {
+                    // the event step's seventh stage K_7 = L(t_n + h) y_{n+1}, into the next record's
+                    // state slot (the segment buffer holds one record more than a segment)
+                    for (int i = lt; i < N; i += TPT) {
+                        double acc = 0.0;
+                        for (int s = 0; s < 6; ++s) acc += bw[s] * K_r[static_cast<size_t>(s) * N + i];
+                        s_G64[gslot64(i, n)] = yn_r[i] + h * acc;
+                    }
+                    gsync<TPT>(g);
+                    gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, rec + J.rec_stride + 2, lt);
+                    gsync<TPT>(g);
+                }
                 if (st + 1 < s1) {
                     double* yn_next = rec + J.rec_stride + 2;
                     for (int i = lt; i < N; i += TPT) {
@@ -471,10 +526,100 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
             const double tn = rec[0], h = rec[1];
             const double* yn_t = rec + 2;
             const double* Kt = rec + 2 + N;
-            const double dt = (tn + h) - tn;
+            // The step that ended on the stop event maps y_n to the dense output at theta =
+            // (t_e - t_n) / h: y(t_e) = y_n + h sum_{j<7} W_j(theta) K_j, a seven-stage explicit map
+            // whose seventh stage K_7 = L(t_n + h) y_{n+1} has the input weights b.  Its final
+            // weights W replace b; otherwise wgt = b.
+            const bool ev_step = ev_hit && st == n_acc - 1;
+            const int n_st = ev_step ? 7 : 6;
+            const double* K7 = rec + J.rec_stride + 2;
+            double wgt[7], dwgt[7];
+            double te = tn + h;
+#pragma unroll
+            for (int s = 0; s < 7; ++s) {
+                wgt[s] = s < 6 ? bw[s] : 0.0;
+                dwgt[s] = 0.0;
+            }
+            if (ev_step) {
+                te = fst.event_time;
+                double th = (te - tn) / h;
+                th = th < 0.0 ? 0.0 : (th > 1.0 ? 1.0 : th);
+                dense_weights(M, th, bw, wgt, dwgt);
+            }
+            const double dt = ev_step ? te - tn : (tn + h) - tn;
             const bool segment = integral && (st > 0 || A.save_start);
-            if (segment) add_quadrature(dt);  // the end state y_{n+1}
-            // coefficient values and derivatives at the six stage times, one VM lane each
+            if (segment) add_quadrature(dt);  // the end state y_{n+1} (or y(t_e))
+            if (ev_step) {
+                // t_e moves with the state and the parameters (g(t_e, y(t_e), p) = 0).  With
+                // J_t = dJ/dt_e at fixed stages (the integral's end-point term plus ybar . y'(t_e)),
+                // a population event g = e.y - threshold adds -J_t / (e.y'(t_e)) e to ybar(t_e); an
+                // event program g(t, p) adds -J_t (dg/dp) / (dg/dt) to the parameter gradient.
+                double part = 0.0;
+                for (int i = lt; i < N; i += TPT) {
+                    double yd = 0.0;
+                    for (int j = 0; j < 6; ++j) yd += dwgt[j] * Kt[static_cast<size_t>(j) * N + i];
+                    yd += dwgt[6] * K7[i];
+                    part += s_YB[i] * yd;
+                }
+                double jt = group_sum<TPT>(part, s_red, lt, g);
+                if (lt == 0) {
+                    auto y_te = [&](int i) {
+                        double acc = 0.0;
+                        for (int j = 0; j < 6; ++j) acc += wgt[j] * Kt[static_cast<size_t>(j) * N + i];
+                        return yn_t[i] + h * (acc + wgt[6] * K7[i]);
+                    };
+                    auto yd_te = [&](int i) {
+                        double acc = dwgt[6] * K7[i];
+                        for (int j = 0; j < 6; ++j) acc += dwgt[j] * Kt[static_cast<size_t>(j) * N + i];
+                        return acc;
+                    };
+                    if (segment) {
+                        double wy = 0.0;
+                        for (int k = 0; k < A.n_weights; ++k) wy += A.w_val[k] * (yn_t[A.w_idx[k]] + y_te(A.w_idx[k]));
+                        jt += 0.5 * gbar * wy;
+                    }
+                    if (A.ev_kind == OBE_EVENT_POPULATION) {
+                        double ey = 0.0;
+                        for (int k = 0; k < A.n_ev; ++k) ey += yd_te(A.ev_idx[k]);
+                        const double c = -jt / ey;
+                        if (!isfinite(c)) bad = ADJ_EVENT_TANGENT;
+                        else
+                            for (int k = 0; k < A.n_ev; ++k) s_YB[A.ev_idx[k]] += c;
+                    } else if (ng > 0) {
+                        // dg/dp: the time-dependent compounds and the event program at t_e in dual numbers
+                        double2 dtmp[kMaxGrad], gp[kMaxGrad], gt;
+                        int hb = 0;
+                        for (int c = 0; c < P.n_comp; ++c) {
+                            if (!P.comp_dynamic[c]) continue;
+                            const DevExpr e = P.comp_expr[c];
+                            const int slot = P.comp_slot[c];
+                            slots[slot] = vm_eval_dual(P, e.start, e.len, slots, dslots, ng, te, sv, sd, tp, dtmp, &hb);
+                            for (int q = 0; q < ng; ++q) dslots[slot * ng + q] = dtmp[q];
+                        }
+                        vm_eval_dual_prog(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, slots, dslots, ng, te, sv, sd,
+                                          tp, gp, &hb, -1);
+                        // dg/dt: the same programs with the time seeded
+                        for (int q = 0; q < P.n_slots; ++q) dts[q] = make_double2(0.0, 0.0);
+                        for (int c = 0; c < P.n_comp; ++c) {
+                            if (!P.comp_dynamic[c]) continue;
+                            const DevExpr e = P.comp_expr[c];
+                            vm_eval_dual_prog(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, e.start, e.len, slots, dts, 1, te, sv,
+                                              sd, tp, &dts[P.comp_slot[c]], &hb, 0);
+                        }
+                        vm_eval_dual_prog(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, slots, dts, 1, te, sv, sd, tp, &gt,
+                                          &hb, 0);
+                        if (hb) bad = ADJ_HELPER_DERIVATIVE;
+                        for (int q = 0; q < ng; ++q) {
+                            const double c = -jt * gp[q].x / gt.x;
+                            if (!isfinite(c)) bad = ADJ_EVENT_TANGENT;
+                            else pbar[q] += c;
+                        }
+                    }
+                }
+                gsync<TPT>(g);
+            }
+            // coefficient values and derivatives at the six stage times, one VM lane each (the
+            // seventh stage of an event step sits at t_n + h, as the sixth)
             if (lt < 6) {
                 const double ts = tn + h * cs[lt];
                 double2 dtmp[kMaxGrad];
@@ -502,18 +647,23 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 s_dcls[(row * nc2 + cls) * kMaxGrad + gi] = d;
             }
             gsync<TPT>(g);
-            for (int s = 5; s >= 0; --s) {
+            for (int s = n_st - 1; s >= 0; --s) {
+                const int row = s < 6 ? s : 5;
                 // lambda_s (adjoint of K_s) into the lambda slot buffer; Y_s into the input buffer
                 for (int i = lt; i < N; i += TPT) {
-                    double lam = h * bw[s] * s_YB[i];
+                    double lam = h * wgt[s] * s_YB[i];
                     for (int m = s + 1; m < 6; ++m) lam += h * kTab.a[M][m - 1][s] * s_MU[static_cast<size_t>(m) * N + i];
+                    if (n_st == 7 && s < 6) lam += h * bw[s] * s_MU[static_cast<size_t>(6) * N + i];
                     s_LS64[gslot64(i, n)] = lam;
                     double acc = 0.0;
-                    for (int l = 0; l < s; ++l) acc += kTab.a[M][s - 1][l] * Kt[static_cast<size_t>(l) * N + i];
+                    if (s < 6)
+                        for (int l = 0; l < s; ++l) acc += kTab.a[M][s - 1][l] * Kt[static_cast<size_t>(l) * N + i];
+                    else
+                        for (int l = 0; l < 6; ++l) acc += bw[l] * Kt[static_cast<size_t>(l) * N + i];
                     s_G64[gslot64(i, n)] = s > 0 ? yn_t[i] + h * acc : yn_t[i];
                 }
                 gsync<TPT>(g);
-                if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + s * nd, s_tab, lt);
+                if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
                 gsync<TPT>(g);
                 // mu_s = L(t_s)^T lambda_s on the input-major stream
                 {
@@ -570,7 +720,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 for (int c = 0; c < nc2; ++c) {
                     const double2 Sv = s_S[c * TPT + lt];
                     for (int q = 0; q < ng; ++q) {
-                        const double2 d = s_dcls[(s * nc2 + c) * kMaxGrad + q];
+                        const double2 d = s_dcls[(row * nc2 + c) * kMaxGrad + q];
                         pbar[q] += d.x * Sv.x - d.y * Sv.y;
                     }
                 }
@@ -579,7 +729,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
             // ybar_n = ybar_{n+1} + sum_s mu_s
             for (int i = lt; i < N; i += TPT) {
                 double acc = s_YB[i];
-                for (int s = 0; s < 6; ++s) acc += s_MU[static_cast<size_t>(s) * N + i];
+                for (int s = 0; s < n_st; ++s) acc += s_MU[static_cast<size_t>(s) * N + i];
                 s_YB[i] = acc;
             }
             gsync<TPT>(g);
@@ -595,7 +745,8 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         if (J.rho0_grad)
             for (int i = lt; i < N; i += TPT) J.rho0_grad[traj * N + i] = s_YB[i];
         const double any_bad = group_sum<TPT>(bad ? 1.0 : 0.0, s_red, lt, g);
-        if (lt == 0) J.adj_status[traj] = any_bad > 0.0 ? ADJ_HELPER_DERIVATIVE : ADJ_OK;
+        const double tangent = group_sum<TPT>(bad == ADJ_EVENT_TANGENT ? 1.0 : 0.0, s_red, lt, g);
+        if (lt == 0) J.adj_status[traj] = tangent > 0.0 ? ADJ_EVENT_TANGENT : any_bad > 0.0 ? ADJ_HELPER_DERIVATIVE : ADJ_OK;
         gsync<TPT>(g);
     }
 }

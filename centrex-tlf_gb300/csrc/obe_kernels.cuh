@@ -1438,24 +1438,14 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                     stage_registers_to_buf(yn);
                     push(x);
                 }
-                if (hit) {
-                    // push_unique (dopri5.rs:150-158)
-                    if (!(count > 0 && fabs(last_time - te) <= time_tol(te))) {
-                        if (ev_state == 0) stage_registers_to_buf(y);
-                        else if (ev_state == 1) stage_registers_to_buf(yn);
-                        else dense_to_buf(ev_theta);
-                        push(te);
-                    }
-                    ev_triggered = 1;
-                    ev_time = te;
-                    break;
-                }
-                // accept: y <- yn; K_1 <- K_7
+                // the step for the adjoint: start time, size, start state and stages 1-6 (or,
+                // checkpointed, the step and every tape_ckpt-th start state).  The step that ends on
+                // a stop event also leaves its seventh stage (the dense output's first-same-as-last
+                // derivative) in the next record's state slot.
                 if constexpr (!MIXED) {
                     if (A.tape) {
-                        // the step for the adjoint: start time, size, start state and stages 1-6
-                        // (or, checkpointed, the step and every tape_ckpt-th start state)
-                        if (accepted > A.tape_cap) { status = ST_TAPE; err_a = A.tape_cap; break; }
+                        const bool k7 = hit && A.tape_ckpt == 0;
+                        if (accepted + (k7 ? 1 : 0) > A.tape_cap) { status = ST_TAPE; err_a = A.tape_cap; break; }
                         const long long j = accepted - 1;
                         double* rec;
                         bool keep_y = true;
@@ -1463,7 +1453,8 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             rec = A.tape + (static_cast<size_t>(traj) * A.tape_cap + j) * A.tape_stride;
                             if (lt == 0) { rec[0] = xo; rec[1] = h; }
                             rec += 2;
-                            for (int i = lt; i < 6 * N; i += TPT) rec[N + i] = s_K[i];
+                            for (int i = lt; i < (k7 ? 7 : 6) * N; i += TPT)
+                                rec[i < 6 * N ? N + i : A.tape_stride + (i - 6 * N)] = s_K[i];
                         } else {
                             double* base = A.tape + static_cast<size_t>(traj) * A.tape_stride;
                             if (lt == 0) { base[2 * j] = xo; base[2 * j + 1] = h; }
@@ -1478,6 +1469,21 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             }
                         }
                     }
+                }
+                if (hit) {
+                    // push_unique (dopri5.rs:150-158)
+                    if (!(count > 0 && fabs(last_time - te) <= time_tol(te))) {
+                        if (ev_state == 0) stage_registers_to_buf(y);
+                        else if (ev_state == 1) stage_registers_to_buf(yn);
+                        else dense_to_buf(ev_theta);
+                        push(te);
+                    }
+                    ev_triggered = 1;
+                    ev_time = te;
+                    break;
+                }
+                // accept: y <- yn; K_1 <- K_7
+                if constexpr (!MIXED) {
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;

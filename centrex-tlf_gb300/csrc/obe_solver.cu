@@ -1092,10 +1092,6 @@ static obe_status grad_check(const obe_plan* p, const obe_solve_options* o, int6
         set_error("gradients are implemented for the adaptive solvers 'dopri5' and 'tsit5'");
         return OBE_ERR_UNSUPPORTED;
     }
-    if (o->event_kind != OBE_EVENT_NONE) {
-        set_error("gradients through a stop_event are not supported");
-        return OBE_ERR_UNSUPPORTED;
-    }
     if (p->packed.tpt > 256) {
         set_error("gradients need the plan at 256 threads per trajectory or fewer: call obe_plan_set_shape");
         return OBE_ERR_UNSUPPORTED;
@@ -1205,7 +1201,7 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     A.n_param = d_param_values ? n_param_slots : 0;
     for (int k = 0; k < A.n_param; ++k) A.param_slot[k] = static_cast<int>(param_slots[k]);
     A.param_values = d_param_values;
-    A.vm_depth = std::max(p->dev.max_stack, 1);
+    A.vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
     AdjArgs J{};
     J.n_grad = n_grad;
     for (int q = 0; q < n_grad; ++q) J.grad_slot[q] = static_cast<int>(grad_slots[q]);
@@ -1223,7 +1219,8 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     const DevPlan& P = p->dev;
     const int tpt = P.tpt;
     const size_t plan_bytes = adj_plan_smem_bytes(P, tpt);
-    const AdjLayout AL = adj_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, tpt);
+    const bool events = opt->event_kind != OBE_EVENT_NONE;
+    const AdjLayout AL = adj_layout(P.n, P.N, P.n_formula, P.n_coeff, P.n_dyn, P.n_slots, A.vm_depth, tpt, events ? 7 : 6);
     const size_t group = AL.bytes;
     const size_t limit = 227 * 1024;
     int gpb = 256 / tpt;
@@ -1234,9 +1231,11 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     const size_t smem = plan_bytes + gpb * group;
     const int blocks = static_cast<int>(std::max<long long>(1, std::min<long long>((n_traj + gpb - 1) / gpb, sm_count())));
     // per resident trajectory group, in the plan's device scratch: one segment of full records
-    // (checkpointed tape) and the large systems' slice
+    // (checkpointed tape; one record more with a stop event, whose step's seventh stage goes
+    // there) and the large systems' slice
     const size_t groups = static_cast<size_t>(blocks) * gpb;
-    const size_t seg_bytes = checkpoint_every > 0 ? align16(static_cast<size_t>(checkpoint_every) * J.rec_stride * 8) : 0;
+    const size_t seg_bytes =
+        checkpoint_every > 0 ? align16(static_cast<size_t>(checkpoint_every + (events ? 1 : 0)) * J.rec_stride * 8) : 0;
     if (seg_bytes + AL.gbytes > 0) {
         unsigned char* gk = nullptr;
         if ((st = kscratch(p, groups * (seg_bytes + AL.gbytes), &gk)) != OBE_OK) return st;

@@ -2311,11 +2311,15 @@ int32_t orc_max_threads(void) {
 /* Replay of a frozen step sequence (test support for the GPU adjoint): for each trajectory, the
  * given accepted steps (t_n, h_n) of Dopri5 (dopri5.rs:60-86) or Tsit5 (tsit5.rs:70-103), no step
  * control, no error estimate; outputs the weighted trapezoid integral of the pushed points
- * (output.rs:314-330; t0 pushed when save_start) or the final populations.  Central finite
- * differences of this map check the adjoint of the same frozen sequence. */
+ * (output.rs:314-330; t0 pushed when save_start) or the final populations.  With event_hit[t] set
+ * the last step is the one that ended on opt's stop event: its crossing is found again as the
+ * solver finds it (dopri5.rs:280-317: the seventh stage, the 60-step bisection on the dense
+ * output) and the output ends at that time and state (push_unique, dopri5.rs:149-158).  Central
+ * finite differences of this map check the adjoint of the same frozen sequence. */
 int orc_solve_replay(const orc_plan* plan, const obe_solve_options* opt, int64_t n_traj, const double* rho0, int64_t rho0_stride,
                      int32_t n_param_slots, const int64_t* param_slots, const double* param_values, const int64_t* n_steps,
-                     const double* steps, int64_t max_steps, int64_t width, double* values, char* err, size_t err_len) {
+                     const double* steps, int64_t max_steps, const int32_t* event_hit, int64_t width, double* values, char* err,
+                     size_t err_len) {
     errbuf e = {{0}, 0};
     const int tsit = opt->solver == OBE_SOLVER_TSIT5;
     if (opt->solver != OBE_SOLVER_DOPRI5 && !tsit) { fail(&e, "replay supports dopri5 and tsit5"); copy_err(&e, err, err_len); return 1; }
@@ -2324,10 +2328,13 @@ int orc_solve_replay(const orc_plan* plan, const obe_solve_options* opt, int64_t
     if (width != (integral ? 1 : n)) { fail(&e, "replay output width mismatch"); copy_err(&e, err, err_len); return 1; }
     workspace w;
     ws_init(&w, plan, 1);
+    setup_event(&w, opt);
     rk_buf b;
     rkb_init(&b, N);
     int rc = 0;
     for (int64_t t = 0; t < n_traj && !rc; ++t) {
+        const int ev_step = event_hit && event_hit[t] && opt->event_kind != OBE_EVENT_NONE && n_steps[t] > 0;
+        const double* yout = NULL;
         if (n_param_slots > 0) ws_set_overrides(&w, n_param_slots, param_slots, param_values + 2 * t * n_param_slots);
         else w.valid = 0;
         double* y = b.y, *yt = b.yt, *yn = b.yn, *k = b.k;
@@ -2369,6 +2376,44 @@ int orc_solve_replay(const orc_plan* plan, const obe_solve_options* opt, int64_t
                 for (int64_t i = 0; i < N; ++i) yn[i] = y[i] + h * (T_A71 * k[i] + T_A72 * k[N + i] + T_A73 * k[2 * N + i] + T_A74 * k[3 * N + i] + T_A75 * k[4 * N + i] + T_A76 * k[5 * N + i]);
             }
             const double xn = x + h;
+            if (ev_step && s == n_steps[t] - 1) {
+                b.y = y;
+                b.yn = yn;
+                if ((rc = ws_rhs(&w, xn, yn, k + 6 * N, &e))) break;
+                int has0, has1;
+                double g0, g1, te;
+                if ((rc = ws_event(&w, x, y, &has0, &g0, &e))) break;
+                if ((rc = ws_event(&w, xn, yn, &has1, &g1, &e))) break;
+                if (!has0 || !has1 || !crossed_zero(g0, g1)) { rc = fail(&e, "the replayed event step does not cross zero"); break; }
+                if (g0 == 0.0) { te = x; yout = y; }
+                else if (g1 == 0.0) { te = xn; yout = yn; }
+                else {
+                    if (!tsit) dopri_dense_prep(&b, h);
+                    double lo = 0.0, hi = 1.0, glo = g0;
+                    for (int it = 0; it < 60; ++it) {
+                        double mid = 0.5 * (lo + hi);
+                        if (!tsit) dopri_dense_out(&b, mid, b.ds); else tsit_dense_out(&b, mid, h, b.ds);
+                        int has;
+                        double gm;
+                        if ((rc = ws_event(&w, x + mid * h, b.ds, &has, &gm, &e))) break;
+                        if (!has) { rc = fail(&e, "event disappeared during root finding"); break; }
+                        if (gm == 0.0) { lo = mid; hi = mid; break; }
+                        if ((glo < 0.0 && gm > 0.0) || (glo > 0.0 && gm < 0.0)) hi = mid;
+                        else { lo = mid; glo = gm; }
+                    }
+                    if (rc) break;
+                    double theta = 0.5 * (lo + hi);
+                    if (!tsit) dopri_dense_out(&b, theta, b.ds); else tsit_dense_out(&b, theta, h, b.ds);
+                    te = x + theta * h;
+                    yout = b.ds;
+                }
+                if (integral && !(have_last && fabs(last_t - te) <= time_tol(te))) {
+                    double v = 0.0;
+                    for (int32_t q = 0; q < opt->n_weights; ++q) v += opt->weight_value[q] * yout[opt->weight_index[q]];
+                    if (have_last) integ += 0.5 * (last_v + v) * (te - last_t);
+                }
+                break;
+            }
             if (integral) {
                 double v = 0.0;
                 for (int32_t q = 0; q < opt->n_weights; ++q) v += opt->weight_value[q] * yn[opt->weight_index[q]];
@@ -2381,8 +2426,9 @@ int orc_solve_replay(const orc_plan* plan, const obe_solve_options* opt, int64_t
             b.y = y; b.yn = yn;
         }
         if (rc) break;
+        if (!yout) yout = y;
         if (integral) values[t] = integ;
-        else memcpy(values + t * n, y, sizeof(double) * (size_t)n);
+        else memcpy(values + t * n, yout, sizeof(double) * (size_t)n);
     }
     if (rc) copy_err(&e, err, err_len);
     rkb_free(&b);

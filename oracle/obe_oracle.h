@@ -76,10 +76,12 @@ orc_plan* orc_effective_plan_create(const obe_plan_desc* graph, const obe_effect
 int32_t orc_max_threads(void);
 
 /* Frozen-step replay (test support for gradients): steps[traj][max_steps][2] = (t_n, h_n),
- * n_steps[traj] of them; width 1 (weighted integral) or n (final populations). */
+ * n_steps[traj] of them; event_hit[traj] (or null): the last step ended on the stop event;
+ * width 1 (weighted integral) or n (final populations). */
 int orc_solve_replay(const orc_plan* plan, const obe_solve_options* opt, int64_t n_traj, const double* rho0, int64_t rho0_stride,
                      int32_t n_param_slots, const int64_t* param_slots, const double* param_values, const int64_t* n_steps,
-                     const double* steps, int64_t max_steps, int64_t width, double* values, char* err, size_t err_len);
+                     const double* steps, int64_t max_steps, const int32_t* event_hit, int64_t width, double* values, char* err,
+                     size_t err_len);
 
 #ifdef __cplusplus
 }

@@ -68,7 +68,7 @@ def _lib():
     lib.orc_effective_plan_create.restype = vp
     lib.orc_solve_replay.argtypes = [
         vp, ctypes.POINTER(ObeSolveOptions), ctypes.c_int64, f64p, ctypes.c_int64, ctypes.c_int32, i64p, f64p, i64p, f64p,
-        ctypes.c_int64, ctypes.c_int64, f64p, ctypes.c_char_p, ctypes.c_size_t,
+        ctypes.c_int64, ctypes.POINTER(ctypes.c_int32), ctypes.c_int64, f64p, ctypes.c_char_p, ctypes.c_size_t,
     ]
     lib.orc_solve_replay.restype = ctypes.c_int
     _LIB = lib
@@ -167,9 +167,10 @@ class OraclePlan:
             values = values.view(np.complex128)
         return values.reshape(b, time_count, width), times[:time_count], stats
 
-    def solve_replay(self, opts: SolveOptions, rho0, param_slots, param_values, steps):
-        """Replay frozen step sequences: steps[b] is an (n_b, 2) array of (t_n, h_n).  Returns the
-        weighted integral (B,) or the final populations (B, n) of opts' output."""
+    def solve_replay(self, opts: SolveOptions, rho0, param_slots, param_values, steps, event_hit=None):
+        """Replay frozen step sequences: steps[b] is an (n_b, 2) array of (t_n, h_n); event_hit[b]:
+        its last step ended on opts' stop event (found again by bisection).  Returns the weighted
+        integral (B,) or the final populations (B, n) of opts' output."""
         rho0 = np.ascontiguousarray(rho0, dtype=np.float64)
         pv = np.asarray(param_values, dtype=np.complex128)
         b = pv.shape[0]
@@ -186,10 +187,12 @@ class OraclePlan:
         width = opts.width
         values = np.zeros(b * width)
         err = ctypes.create_string_buffer(1024)
+        hits = None if event_hit is None else np.ascontiguousarray(np.asarray(event_hit, dtype=np.int32).reshape(b))
         rc = _lib().orc_solve_replay(
             self.handle, ctypes.byref(opts.opts), b, _abi.ptr(rho0, ctypes.c_double), stride, int(slots.size),
             _abi.ptr(slots, ctypes.c_int64), _abi.ptr(pvals, ctypes.c_double), _abi.ptr(counts, ctypes.c_int64),
-            _abi.ptr(np.ascontiguousarray(flat.reshape(-1)), ctypes.c_double), max_steps, width,
+            _abi.ptr(np.ascontiguousarray(flat.reshape(-1)), ctypes.c_double), max_steps,
+            None if hits is None else hits.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), width,
             _abi.ptr(values, ctypes.c_double), err, 1024,
         )
         if rc:

@@ -246,3 +246,91 @@ def test_gradient_errors(golden, q1):
                                 output="populations")
     out[:, 1].sum().backward()
     assert np.isfinite(p.grad.cpu().numpy()).all() and abs(float(p.grad)) > 0
+
+
+def _t_end_event(names):
+    return {"kind": "runtime_expression",
+            "expression": {"instructions": [{"op": 4}, {"op": 2, "index": names.index("t_end")}, {"op": 6}],
+                           "scalar_only": True, "output_is_tuple": False}}
+
+
+def _event_fd_check(d, p0, slots, ev, hits_expected, solver="tsit5", output="excited_population", checkpoint_every=0,
+                    t1=None):
+    """Gradients of a solve that a stop event ends against central differences of the oracle's
+    replay of the frozen steps, whose last step finds the event again at p +- eps (the same bar as
+    the event-free checks).  The forward values equal the plain solve's with the same event."""
+    g = d["gamma"]
+    t1 = 200.0 / g if t1 is None else t1
+    plan = NativePlan(d["payload"])
+    op = oracle.OraclePlan(d["payload"])
+    w = [(i, 1.0) for i in d["excited_indices"]]
+    integral = output != "populations"
+    b = p0.shape[0]
+    params = torch.tensor(p0, dtype=torch.float64, device="cuda", requires_grad=True)
+    out, tape = solve_batch_with_grad(plan, d["rho0_packed"], (0.0, t1), params, slots, solver=solver, dt=1e-3 / g,
+                                      output=output, integral_weights=w if integral else None, return_tape=True,
+                                      checkpoint_every=checkpoint_every, stop_event=ev)
+    hits = tape.event_hits()
+    assert hits.tolist() == hits_expected
+    rng = np.random.default_rng(11)
+    wout = np.ones((b, 1)) if integral else rng.normal(size=(b, d["payload"]["n_states"]))
+    (out.reshape(b, -1) * torch.tensor(wout, device="cuda")).sum().backward()
+    grad = params.grad.cpu().numpy()
+    _, ref_vals, _, _, _ = api.solve_lindblad_batch_ode_py(
+        api.prepare_lindblad_problem_py(d["payload"]), np.repeat(d["rho0_packed"].reshape(1, -1), b, axis=0), 0.0, t1,
+        1e-11, 1e-8, 1e-3 / g, saveat=None if integral else np.array([t1]), save_start=integral, solver=solver,
+        output=output, integral_weights=w if integral else None, parameter_slot_indices=slots,
+        parameter_batch=p0.astype(complex), stop_event=ev)
+    np.testing.assert_allclose(out.detach().cpu().numpy().reshape(-1), np.asarray(ref_vals).reshape(-1), rtol=1e-12, atol=1e-20)
+    o = op.options(t0=0.0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=None if integral else np.array([t1]),
+                   save_start=integral, maxiters=100000, solver=solver, output=output, output_indices=None,
+                   output_when="final", integral_weights=w if integral else None, stop_event=ev)
+    steps = tape.steps()
+
+    def replay(p):
+        v = op.solve_replay(o, d["rho0_packed"], slots, p.astype(complex), steps, event_hit=hits)
+        return (np.asarray(v).reshape(b, -1) * wout).sum(axis=1)
+
+    base = replay(p0)
+    np.testing.assert_allclose(base, (out.detach().cpu().numpy().reshape(b, -1) * wout).sum(axis=1), rtol=1e-10, atol=1e-22)
+    for k in range(p0.shape[1]):
+        eps = 1e-6 * np.abs(p0[:, k])
+        eps[eps == 0] = 1e-6 * g
+        pp, pm = p0.copy(), p0.copy()
+        pp[:, k] += eps
+        pm[:, k] -= eps
+        fd = (replay(pp) - replay(pm)) / (2 * eps)
+        tol = 1e-5 * np.abs(fd) + 1e-8 * np.abs(base) / np.maximum(np.abs(p0[:, k]), 1e-300)
+        assert np.all(np.abs(grad[:, k] - fd) <= tol), (k, grad[:, k], fd, tol)
+    return grad
+
+
+@pytest.mark.parametrize("solver,output,ck", [("tsit5", "excited_population", 0), ("dopri5", "excited_population", 0),
+                                              ("tsit5", "populations", 0), ("dopri5", "populations", 0),
+                                              ("tsit5", "excited_population", 7)])
+def test_gradients_through_a_time_event(golden, solver, output, ck):
+    """A `Time() - t_end` stop event with t_end a differentiated base slot (the ragged end times of
+    the heterogeneous scan): gradients with respect to the Rabi rate, detuning, angle and the end
+    time itself (the event time's own derivative); one trajectory's t_end lies past t1."""
+    d = golden("plan_q1_16_tend")
+    g = d["gamma"]
+    names = d["payload"]["parameter_graph"]["slot_names"]
+    slots = [names.index(s) for s in ("rabi", "detuning", "theta", "t_end")]
+    p0 = np.array([[1.0 * g, 0.0, 0.3, 123.4 / g], [3.0 * g, -2.0 * g, 1.1, 60.3 / g], [0.4 * g, 1.5 * g, 2.5, 250.0 / g],
+                   [6.0 * g, 4.0 * g, 0.8, 170.7 / g]])
+    grad = _event_fd_check(d, p0, slots, _t_end_event(names), [1, 1, 0, 1], solver=solver, output=output,
+                           checkpoint_every=ck)
+    assert grad[2, 3] == 0.0  # no event, no dependence on t_end
+    assert np.all(np.abs(grad[[0, 1, 3], 3]) > 0.0)
+
+
+@pytest.mark.parametrize("output,ck", [("excited_population", 0), ("populations", 0), ("excited_population", 5)])
+def test_gradients_through_a_population_event(golden, output, ck):
+    """A threshold on the excited populations ends each trajectory at a state-dependent time: the
+    implicit-function term moves ybar at the crossing along the event's population vector."""
+    d = golden("plan_q1_16")
+    g = d["gamma"]
+    slots = _slots(d)
+    ev = {"kind": "population", "indices": list(d["excited_indices"]), "threshold": 0.004}
+    p0 = np.array([[1.3 * g, 0.7 * g, 0.4, 100.0 / g], [3.0 * g, -2.0 * g, 1.1, 95.0 / g], [0.1 * g, 4.5 * g, 2.5, 104.0 / g]])
+    _event_fd_check(d, p0, slots, ev, [1, 1, 0], output=output, checkpoint_every=ck)
