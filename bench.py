@@ -228,11 +228,12 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
         plan.solve_batch_device(opts, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, d_val.data_ptr(),
                                 d_st.data_ptr(), stream.cuda_stream)
 
-    def grad(checkpoint_every=0):
+    def grad(checkpoint_every=0, precision="fp64"):
         pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
         j = solve_batch_with_grad(plan, d["rho0_packed"], (t0, t1), pt, slots, dt=1e-3 / gamma, integral_weights=W_EXCITED,
-                                  max_steps=2048, checkpoint_every=checkpoint_every)
+                                  max_steps=2048, checkpoint_every=checkpoint_every, precision=precision)
         j.sum().backward()
+        grad.last_values = j.detach()
         return pt.grad
 
     def timed(fn):
@@ -255,16 +256,49 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
     t_fwd_t = timed(fwd)
     t_grad_t = timed(grad)
     t_grad_ck = timed(lambda: grad(512))
+    g64 = grad().cpu().numpy()
+    j64 = grad.last_values.cpu().numpy()
+    # the mixed form (FP32-RHS forward with a single-precision tape, single-precision transposed
+    # and parameter products in the reverse sweep, FP64 accumulation) at the shape the autotuner
+    # picks for the mixed forward
+    opts_m = plan.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=None, save_start=True,
+                          maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
+                          output_when="final", integral_weights=W_EXCITED, stop_event=None, precision="mixed")
+
+    def fwd_m():
+        plan.solve_batch_device(opts_m, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, d_val.data_ptr(),
+                                d_st.data_ptr(), stream.cuda_stream)
+
+    cands_m = plan.autotune(opts_m, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, probe_steps=64,
+                            stream=stream.cuda_stream)
+    t_fwd_m = timed(fwd_m)
+    t_grad_m = timed(lambda: grad(precision="mixed"))
+    t_grad_m_ck = timed(lambda: grad(512, precision="mixed"))
+    gm = grad(precision="mixed").cpu().numpy()
     plan.set_shape(0, 0)
+    # the mixed gradients against the FP64 ones (each form on its own frozen step sequence), on
+    # each derivative's natural scale |J| / |p|
+    natural = np.abs(j64)[:, None] / np.maximum(np.abs(p), 1e-300)
+    mixed_vs_64 = float(np.max(np.abs(gm - g64) / natural))
     return {"workload": f"{n_traj} scan points, d(excited-population integral)/d(rabi, detuning, theta, t_center), "
-                        "FP64 Tsit5 discrete adjoint", "fwd_ms": 1e3 * t_fwd, "fwd_plus_grad_ms": 1e3 * t_grad,
+                        "Tsit5 discrete adjoint", "fwd_ms": 1e3 * t_fwd, "fwd_plus_grad_ms": 1e3 * t_grad,
             "grad_over_fwd": t_grad / t_fwd,
             "autotuned": {"threads_per_trajectory": cands[0]["threads_per_trajectory"],
                           "trajectories_per_cta": cands[0]["trajectories_per_cta"], "fwd_ms": 1e3 * t_fwd_t,
                           "fwd_plus_grad_ms": 1e3 * t_grad_t, "grad_over_fwd": t_grad_t / t_fwd_t,
                           "checkpointed_512": {"fwd_plus_grad_ms": 1e3 * t_grad_ck, "grad_over_fwd": t_grad_ck / t_fwd_t,
                                                "tape_bytes_per_trajectory": 8 * plan.grad_tape_doubles(2048, 512),
-                                               "full_tape_bytes_per_trajectory": 8 * plan.grad_tape_doubles(2048, 0)}}}
+                                               "full_tape_bytes_per_trajectory": 8 * plan.grad_tape_doubles(2048, 0)}},
+            "mixed": {"threads_per_trajectory": cands_m[0]["threads_per_trajectory"],
+                      "trajectories_per_cta": cands_m[0]["trajectories_per_cta"], "fwd_ms": 1e3 * t_fwd_m,
+                      "fwd_plus_grad_ms": 1e3 * t_grad_m, "grad_over_fwd": t_grad_m / t_fwd_m,
+                      "grad_vs_fp64_fwd": t_grad_m / t_fwd_t,
+                      "checkpointed_512": {"fwd_plus_grad_ms": 1e3 * t_grad_m_ck, "grad_over_fwd": t_grad_m_ck / t_fwd_m},
+                      "max_grad_diff_vs_fp64_natural_scale": mixed_vs_64,
+                      "note": "difference on the scale |J|/|p|, each form on its own step sequence; against central "
+                              "differences of its own frozen steps the mixed adjoint agrees to <= 3e-6 relative for "
+                              "rabi, detuning and angle, and to ~5e-9 of |J|/|p| for the pulse centre (a derivative "
+                              "that cancels to ~1e-7 of that scale) (tests/test_gpu_adjoint.py)"}}
 
 
 HETERO_PLANS = (("plan_q1_16_tend", 6), ("plan_r0_39", 3), ("plan_rc_76", 1))
@@ -377,6 +411,75 @@ def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
         "max_time_averaged_population_error_vs_fp64": err,
         "note": "fp64 timed on its first call (plans already on the device); the error is |integral difference| / t_end",
     }
+
+
+def measure_hetero_gradient(torch, dev, total: int = 8192, precision: str = "mixed", reps: int = 1) -> dict:
+    """Forward plus adjoint of the heterogeneous batch: for each of the three plans,
+    d(excited-population integral)/d(its scanned slots, the end time included) through the
+    discrete adjoint (the event step and the event time's derivative included), checkpointed tape
+    (a start state every 512 steps) where the full one would pass 4 GiB; against the same plans'
+    plain forward solves, one call per plan."""
+    from centrex_tlf_gb300.autograd import solve_batch_with_grad
+    from centrex_tlf_gb300.native import NativePlan
+
+    spec = hetero_jobs(total)
+    stream = torch.cuda.current_stream(dev)
+    runs = []
+    for j in spec:
+        d = j["d"]
+        plan = NativePlan(d["payload"])
+        g = d["gamma"]
+        opts = plan.options(t0=0.0, t1=j["t1"], abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=None, save_start=True,
+                            maxiters=1000000, solver="tsit5", output="excited_population", output_indices=None,
+                            output_when="final", integral_weights=j["weights"], stop_event=j["event"], precision=precision)
+        b = j["count"]
+        rho = torch.from_numpy(np.repeat(d["rho0_packed"].reshape(1, -1), b, axis=0)).to(dev)
+        par = torch.from_numpy(np.ascontiguousarray(j["params"]).view(np.float64).reshape(-1)).to(dev)
+        val = torch.zeros(b, dtype=torch.float64, device=dev)
+        st = torch.zeros(b * 6, dtype=torch.int64, device=dev)
+        runs.append((j, plan, opts, b, rho, par, val, st))
+
+    def fwd():
+        for j, plan, opts, b, rho, par, val, st in runs:
+            plan.solve_batch_device(opts, b, rho.data_ptr(), j["slots"], par.data_ptr(), 1, val.data_ptr(), st.data_ptr(),
+                                    stream.cuda_stream)
+
+    per_plan = {}
+
+    def grad():
+        for j, plan, opts, b, rho, par, val, st in runs:
+            t = time.perf_counter()
+            pt = torch.tensor(j["params"].real, dtype=torch.float64, device=dev, requires_grad=True)
+            out = solve_batch_with_grad(plan, rho, (0.0, j["t1"]), pt, j["slots"], dt=1e-3 / j["d"]["gamma"],
+                                        maxiters=1000000, integral_weights=j["weights"], stop_event=j["event"],
+                                        precision=precision, max_steps=8192)
+            out.sum().backward()
+            torch.cuda.synchronize()
+            assert bool(torch.isfinite(pt.grad).all()), j["name"]
+            per_plan[j["name"]] = 1e3 * (time.perf_counter() - t)
+
+    def timed(fn):
+        best = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t)
+        return best
+
+    fwd()
+    torch.cuda.synchronize()
+    t_fwd = timed(fwd)
+    t_grad = timed(grad)
+    return {"workload": f"{total} instances of the heterogeneous batch (16/39/76-state plans 6:3:1, end times "
+                        "U[50, 300]/Γ by a Time() - t_end stop event); d(excited-population integral)/d(Rabi rates, "
+                        "detunings, angle, t_end) per instance, Tsit5 discrete adjoint, " + precision,
+            "instances": {j["name"]: j["count"] for j in spec}, "fwd_ms": 1e3 * t_fwd, "fwd_plus_grad_ms": 1e3 * t_grad,
+            "grad_over_fwd": t_grad / t_fwd, "fwd_plus_grad_ms_per_plan": per_plan,
+            "note": "forward = the three plans' plain solves one call each (device-resident); gradient = "
+                    "solve_batch_with_grad + backward per plan (host-synchronised between the tape check and the "
+                    "reverse sweep); the 76-state trajectories dominate both"}
 
 
 def measure_effective(torch, dev, total: int = 4096, cpu_sample: int = 256, reps: int = 2) -> dict:
@@ -560,6 +663,8 @@ def run_gpu(args) -> None:
     gradient = measure_gradient(torch, d, params, dev) if not args.no_gradient else None
     hetero = measure_heterogeneous(torch, dev, total=args.hetero_instances) if args.hetero_instances > 0 else None
     effective = measure_effective(torch, dev) if not args.no_effective else None
+    hetero_grad = (measure_hetero_gradient(torch, dev, total=args.hetero_grad_instances)
+                   if args.hetero_grad_instances > 0 else None)
     gpu_obs = np.asarray(out[1])[: args.cpu_sample]
     obs_rel = float(np.max(np.abs(gpu_obs - cpu["values"]) / np.maximum(np.abs(cpu["values"]), 1e-300)))
     accuracy["observable_max_rel_err_vs_cpu_oracle"] = obs_rel
@@ -600,6 +705,7 @@ def run_gpu(args) -> None:
         "clocks": clocks,
         "gradient": gradient,
         "heterogeneous": hetero,
+        "heterogeneous_gradient": hetero_grad,
         "effective": effective,
     }
     print(json.dumps(line))
@@ -618,6 +724,10 @@ def run_case(args) -> None:
     times = []
     if args.case == "heterogeneous":
         r = measure_heterogeneous(torch, dev, total=args.points, reps=max(1, args.steps))
+        print(json.dumps({"case": args.case, **r}))
+        return
+    if args.case == "hetero-gradient":
+        r = measure_hetero_gradient(torch, dev, total=args.points, precision=args.precision, reps=max(1, args.steps))
         print(json.dumps({"case": args.case, **r}))
         return
     if args.case == "gradient":
@@ -686,10 +796,13 @@ def main() -> None:
     ap.add_argument("--no-effective", action="store_true", help="skip timing the effective-Hamiltonian path")
     ap.add_argument("--hetero-instances", type=int, default=8192,
                     help="instances of the heterogeneous 16/39/76-state batch timed beside the scan (0 skips it)")
+    ap.add_argument("--hetero-grad-instances", type=int, default=512,
+                    help="instances of the heterogeneous batch timed forward plus adjoint (0: skip; the full "
+                         "8192-instance batch: --case hetero-gradient --points 8192)")
     ap.add_argument("--points", type=int, default=4096)
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--ref-sample", type=int, default=256)
-    ap.add_argument("--case", choices=["scan", "gradient", "heterogeneous", "large"], default="scan",
+    ap.add_argument("--case", choices=["scan", "gradient", "heterogeneous", "hetero-gradient", "large"], default="scan",
                     help="scan: the benchmark line; the others run one workload alone (profiling)")
     ap.add_argument("--threads-per-trajectory", type=int, default=0,
                     help="launch width of the gradient and large cases (0: automatic)")

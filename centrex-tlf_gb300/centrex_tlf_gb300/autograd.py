@@ -2,9 +2,11 @@
 adjoint (obe_grad_forward / obe_grad_backward).
 
 The reference has no gradient path (its ``lindblad_jvp_py`` is the linear RHS itself), so this
-module has no counterpart there.  The forward pass is the double-precision adaptive solve; it
-records every accepted step on the device (the tape: start time, size, start state and six stage
-derivatives per step).  The backward pass is the exact adjoint of that discrete solve with the
+module has no counterpart there.  The forward pass is the adaptive solve, double precision or
+the mixed form (single-precision RHS, double-precision state); it records every accepted step on
+the device (the tape: start time, size, start state and six stage derivatives per step; the mixed
+form's in single precision, and its reverse sweep runs the transposed and parameter products in
+single precision with double-precision accumulation).  The backward pass is the exact adjoint of that discrete solve with the
 step sequence frozen -- what central finite differences of the solve with the same steps give --
 for the final weighted integral (``excited_population``, ``photon_integral``,
 ``weighted_integral``) or the final populations, with respect to any scalar base parameter slots
@@ -68,11 +70,15 @@ class ForwardTape:
         return (st[:, 3] & 0xFFFFFFFF).astype(np.int32)
 
 
-def _checkpoint_every(plan: NativePlan, b: int, max_steps: int, requested: int | None) -> int:
-    """The full tape while it stays under 4 GiB, else a start state every 512 steps."""
+def _checkpoint_every(plan: NativePlan, b: int, max_steps: int, requested: int | None, device=None) -> int:
+    """The full tape while it takes at most a quarter of the device's free memory (at least
+    4 GiB), else a start state every 512 steps."""
     if requested is not None:
         return int(requested)
-    return 0 if b * plan.grad_tape_doubles(max_steps, 0) * 8 <= (4 << 30) else 512
+    budget = 4 << 30
+    if device is not None and device.type == "cuda":
+        budget = max(budget, torch.cuda.mem_get_info(device)[0] // 4)
+    return 0 if b * plan.grad_tape_doubles(max_steps, 0) * 8 <= budget else 512
 
 
 def _forward(plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals: torch.Tensor, max_steps: int,
@@ -80,7 +86,7 @@ def _forward(plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals
     b = rho0.shape[0]
     stream = torch.cuda.current_stream(rho0.device).cuda_stream
     while True:
-        ck = _checkpoint_every(plan, b, max_steps, checkpoint_every)
+        ck = _checkpoint_every(plan, b, max_steps, checkpoint_every, rho0.device)
         tape = torch.empty(b * plan.grad_tape_doubles(max_steps, ck), dtype=torch.float64, device=rho0.device)
         values = torch.empty(b * opts.width, dtype=torch.float64, device=rho0.device)
         stats = torch.zeros(b * 6, dtype=torch.int64, device=rho0.device)
@@ -135,7 +141,8 @@ def solve_batch_with_grad(plan: NativePlan, rho0, t_span: Sequence[float], param
                           parameter_slot_indices: Sequence[int], *, solver: str = "tsit5", abstol: float = 1e-11,
                           reltol: float = 1e-8, dt: float = 0.0, maxiters: int = 100000,
                           output: str = "excited_population", integral_weights=None, max_steps: int = 4096,
-                          checkpoint_every: int | None = None, stop_event=None, return_tape: bool = False):
+                          checkpoint_every: int | None = None, stop_event=None, precision: str = "fp64",
+                          return_tape: bool = False):
     """Batched double-precision solve whose outputs are differentiable in ``params`` ((B, S) real,
     the values of the base slots ``parameter_slot_indices``) and in ``rho0`` ((B, N) packed).
 
@@ -143,9 +150,10 @@ def solve_batch_with_grad(plan: NativePlan, rho0, t_span: Sequence[float], param
     populations, shape (B, n)).  ``max_steps`` sizes the tape (doubled and retried on overflow).
     ``checkpoint_every``: 0 records every step's stage derivatives; C > 0 records the start state
     of every C-th step and the reverse sweep recomputes each segment from it (one more forward's
-    work, a tape of 2 + N / C doubles per step); None takes the full tape while it stays under
-    4 GiB.  ``stop_event``: as in the solves (``{"kind": "population", "indices", "threshold"}`` or
+    work, a tape of 2 + N / C doubles per step); None takes the full tape while it fits in a
+    quarter of the device's free memory.  ``stop_event``: as in the solves (``{"kind": "population", "indices", "threshold"}`` or
     ``{"kind": "runtime_expression", "expression"}``); the outputs end at the event time.
+    ``precision``: ``"fp64"`` or ``"mixed"`` (the forward and the reverse sweep in the mixed form).
     With ``return_tape`` the forward tape comes back too (its ``steps()`` are the frozen steps,
     its ``event_hits()`` which trajectories ended on the event).
     """
@@ -153,11 +161,11 @@ def solve_batch_with_grad(plan: NativePlan, rho0, t_span: Sequence[float], param
     if output in INTEGRAL_OUTPUTS:
         opts = plan.options(t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=None, save_start=True,
                             maxiters=maxiters, solver=solver, output=output, output_indices=None, output_when="final",
-                            integral_weights=integral_weights, stop_event=stop_event)
+                            integral_weights=integral_weights, stop_event=stop_event, precision=precision)
     elif output == "populations":
         opts = plan.options(t0=t0, t1=t1, abstol=abstol, reltol=reltol, dt=dt, saveat=np.array([t1]), save_start=False,
                             maxiters=maxiters, solver=solver, output="populations", output_indices=None,
-                            output_when="final", integral_weights=None, stop_event=stop_event)
+                            output_when="final", integral_weights=None, stop_event=stop_event, precision=precision)
     else:
         raise NotImplementedError("gradients are available for final weighted integrals and final populations")
     dev = params.device

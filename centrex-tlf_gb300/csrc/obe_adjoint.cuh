@@ -243,6 +243,7 @@ static __device__ __forceinline__ double2 vm_eval_dual(const DevPlan& P, int32_t
 
 struct AdjLayout {
     size_t tab, G, LS, MU, YB, slots, dslots, dts, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, red, traj, bytes;
+    size_t tab32, YB32, dcls32;  // the mixed sweep's single-precision formula table, ybar copy, class derivatives
     size_t gbytes;  // large systems: bytes of the group's device-memory slice (MU, YB, S)
     bool glob;
 };
@@ -258,10 +259,12 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     size_t o = 0, og = 0;
     size_t& om = L.glob ? og : o;  // cursor of the buffers that move to device memory
     L.tab = o; o = align16(o + (1 + n_formula) * 16);
+    L.tab32 = o; o = align16(o + (1 + n_formula) * 8);
     L.G = o; o = align16(o + U * 16);
     L.LS = o; o = align16(o + U * 16);
     L.MU = om; om = align16(om + static_cast<size_t>(stages) * N * 8);
     L.YB = om; om = align16(om + static_cast<size_t>(N) * 8);
+    L.YB32 = om; om = align16(om + static_cast<size_t>(N) * 4);
     L.slots = o; o = align16(o + 6 * ns * 16);
     L.dslots = o; o = align16(o + 6 * ns * kMaxGrad * 16);
     L.dts = o; o = align16(o + ns * 16);
@@ -273,6 +276,7 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     L.cdyn = o; o = align16(o + 6 * nd * 16);
     L.ddyn = o; o = align16(o + 6 * nd * kMaxGrad * 16);
     L.dcls = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 16);
+    L.dcls32 = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 8);
     L.S = om; om = align16(om + 2 * nc * static_cast<size_t>(tpt) * 16);
     L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
     L.traj = o; o = align16(o + 16);
@@ -318,7 +322,11 @@ __device__ __forceinline__ void dense_weights(int M, double th, const double* b,
 // ------------------------------------------------------------------------------------------
 // the reverse sweep
 
-template <int TPT, int EPT>
+// MIXED: the sweep of the mixed form's tape (single-precision records [y_n, k_1, d_2..d_7], the
+// stage derivatives K_s = k_1 + d_s): stage inputs, adjoints lambda_s and mu_s, the transposed and
+// bilinear products in single precision; ybar and the parameter gradient accumulate in double
+// (each step's mu sum and class sums are added to them once, exactly converted).
+template <int TPT, int EPT, bool MIXED>
 __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const CallArgs A, const AdjArgs J, int gpb,
                                                          size_t group_bytes, int M) {
     static_assert(TPT >= 32 && TPT <= 256, "the adjoint runs 32, 64, 128 or 256 threads per trajectory");
@@ -374,6 +382,16 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     double2* sd = reinterpret_cast<double2*>(gb + Lay.sd) + static_cast<size_t>(vl) * A.vm_depth * kMaxGrad;
     int32_t* tp = reinterpret_cast<int32_t*>(gb + Lay.tp) + vl * A.vm_depth;
     double2* dts = reinterpret_cast<double2*>(gb + Lay.dts);
+    // single-precision views (mixed form)
+    float2* s_tab32 = reinterpret_cast<float2*>(gb + Lay.tab32);
+    float2* s_G32 = reinterpret_cast<float2*>(gb + Lay.G);
+    float* s_G32f = reinterpret_cast<float*>(gb + Lay.G);
+    float2* s_LS32 = reinterpret_cast<float2*>(gb + Lay.LS);
+    float* s_LS32f = reinterpret_cast<float*>(gb + Lay.LS);
+    float* s_MU32 = reinterpret_cast<float*>(gm + Lay.MU);
+    float* s_YB32 = reinterpret_cast<float*>(gm + Lay.YB32);
+    float2* s_dcls32 = reinterpret_cast<float2*>(gb + Lay.dcls32);
+    float2* s_S32 = reinterpret_cast<float2*>(gm + Lay.S);
     const bool integral = A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL;
     // solution weights b (row 5 of the stage table) and stage times c_s
     double bw[6], cs[6];
@@ -436,20 +454,34 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         for (int i = lt; i < N; i += TPT) s_YB[i] = 0.0;
         gsync<TPT>(g);
         fill_formulas<TPT>(P, 1, 1 + S, s_cstat, s_cdyn, s_tab, lt);  // static entries: once
+        if constexpr (MIXED) {
+            gsync<TPT>(g);
+            for (int f = lt; f < 1 + S; f += TPT) s_tab32[f] = make_float2(d2f(s_tab[f].x), d2f(s_tab[f].y));
+        }
 
         // ---- the loss gradient at the final state ----
         const double* og = J.out_grad + traj * (integral ? 1 : n);
         const double gbar = integral ? og[0] : 0.0;
         if (!integral)
             for (int i = lt; i < n; i += TPT) s_YB[i] = og[i];
+        if constexpr (MIXED) {
+            gsync<TPT>(g);
+            for (int i = lt; i < N; i += TPT) s_YB32[i] = d2f(s_YB[i]);
+        }
         double pbar[kMaxGrad];
 #pragma unroll
         for (int q = 0; q < kMaxGrad; ++q) pbar[q] = 0.0;
         gsync<TPT>(g);
+        // ybar[i] += v on one thread (the mixed form keeps its single-precision copy in step)
+        auto ybar_add = [&](int i, double v) {
+            const double r = s_YB[i] + v;
+            s_YB[i] = r;
+            if constexpr (MIXED) s_YB32[i] = d2f(r);
+        };
         // the trapezoid weight of a segment of length dt on one of its end states
         auto add_quadrature = [&](double dt) {
             if (lt == 0)
-                for (int k = 0; k < A.n_weights; ++k) s_YB[A.w_idx[k]] += gbar * A.w_val[k] * (0.5 * dt);
+                for (int k = 0; k < A.n_weights; ++k) ybar_add(A.w_idx[k], gbar * A.w_val[k] * (0.5 * dt));
             gsync<TPT>(g);
         };
 
@@ -462,11 +494,14 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         const long long s0 = sg * seg_len, s1 = s0 + seg_len < n_acc ? s0 + seg_len : n_acc;
         if (J.ckpt > 0) {
             // replay the segment's steps from its checkpointed start state with the recorded
-            // (t_n, h_n): the stage derivatives of the frozen steps, as the forward solve took them
+            // (t_n, h_n): the stage derivatives of the frozen steps, as the forward solve took them.
+            // The mixed form replays in double precision into a scratch record (after the segment's
+            // records) and stores each step as a single-precision record [y_n, k_1, d_2..d_7].
             const double* ck = tbase + 2 * J.tape_cap + static_cast<size_t>(sg) * N;
-            for (int i = lt; i < N; i += TPT) segbuf[2 + i] = ck[i];
+            double* xrec = MIXED ? segbuf + static_cast<size_t>(J.ckpt + 1) * J.rec_stride : segbuf;
+            for (int i = lt; i < N; i += TPT) xrec[2 + i] = ck[i];
             for (long long st = s0; st < s1; ++st) {
-                double* rec = segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
+                double* rec = MIXED ? xrec : segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
                 const double tn = tbase[2 * st], h = tbase[2 * st + 1];
                 if (lt == 0) { rec[0] = tn; rec[1] = h; }
                 if (lt < 6) {
@@ -489,7 +524,10 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     for (int i = lt; i < N; i += TPT) {
                         double acc = 0.0;
                         for (int l = 0; l < s; ++l) acc += kTab.a[M][s - 1][l] * K_r[static_cast<size_t>(l) * N + i];
-                        s_G64[gslot64(i, n)] = s > 0 ? yn_r[i] + h * acc : yn_r[i];
+                        const double v = s > 0 ? yn_r[i] + h * acc : yn_r[i];
+                        // diagonal entries fill the whole complex slot (the mixed sweep reuses the buffer)
+                        if (i < n) s_G[i] = make_double2(v, 0.0);
+                        else s_G64[gslot64(i, n)] = v;
                     }
                     gsync<TPT>(g);
                     if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + s * nd, s_tab, lt);
@@ -497,19 +535,41 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, K_r + static_cast<size_t>(s) * N, lt);
                     gsync<TPT>(g);
                 }
-                if (ev_hit && st == n_acc - 1) {
+                const bool ev_last = ev_hit && st == n_acc - 1;
+                if (ev_last) {
                     // the event step's seventh stage K_7 = L(t_n + h) y_{n+1}, into the next record's
-                    // state slot (the segment buffer holds one record more than a segment)
+                    // state slot (the segment buffer holds one record more than a segment), or, mixed,
+                    // into the scratch record's seventh row
                     for (int i = lt; i < N; i += TPT) {
                         double acc = 0.0;
                         for (int s = 0; s < 6; ++s) acc += bw[s] * K_r[static_cast<size_t>(s) * N + i];
-                        s_G64[gslot64(i, n)] = yn_r[i] + h * acc;
+                        const double v = yn_r[i] + h * acc;
+                        if (i < n) s_G[i] = make_double2(v, 0.0);
+                        else s_G64[gslot64(i, n)] = v;
                     }
                     gsync<TPT>(g);
-                    gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, rec + J.rec_stride + 2, lt);
+                    gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G,
+                                                     MIXED ? K_r + static_cast<size_t>(6) * N : rec + J.rec_stride + 2, lt);
                     gsync<TPT>(g);
                 }
-                if (st + 1 < s1) {
+                if constexpr (MIXED) {
+                    double* out = segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
+                    if (lt == 0) { out[0] = tn; out[1] = h; }
+                    float* fo = reinterpret_cast<float*>(out + 2);
+                    const int nd_rows = ev_last ? 6 : 5;
+                    for (int i = lt; i < N; i += TPT) {
+                        const double k1 = K_r[i];
+                        fo[i] = d2f(yn_r[i]);
+                        fo[N + i] = d2f(k1);
+                        for (int l = 1; l <= nd_rows; ++l)
+                            fo[static_cast<size_t>(l + 1) * N + i] = d2f(K_r[static_cast<size_t>(l) * N + i] - k1);
+                        if (st + 1 < s1) {
+                            double acc = 0.0;
+                            for (int s = 0; s < 6; ++s) acc += bw[s] * K_r[static_cast<size_t>(s) * N + i];
+                            xrec[2 + i] = yn_r[i] + h * acc;  // y_{n+1} in place (element i is this thread's)
+                        }
+                    }
+                } else if (st + 1 < s1) {
                     double* yn_next = rec + J.rec_stride + 2;
                     for (int i = lt; i < N; i += TPT) {
                         double acc = 0.0;
@@ -533,6 +593,19 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
             const bool ev_step = ev_hit && st == n_acc - 1;
             const int n_st = ev_step ? 7 : 6;
             const double* K7 = rec + J.rec_stride + 2;
+            // single-precision record of the mixed form: y_n, k_1, d_2..d_7 (K_s = k_1 + d_s)
+            const float* yf = reinterpret_cast<const float*>(rec + 2);
+            const float* k1f = yf + N;
+            const float* df = yf + 2 * static_cast<size_t>(N);
+            // stage j's derivative and the start state as doubles, either record
+            auto kv = [&](int j, int i) -> double {
+                if constexpr (MIXED) return f2d(k1f[i]) + (j > 0 ? f2d(df[static_cast<size_t>(j - 1) * N + i]) : 0.0);
+                else return j < 6 ? Kt[static_cast<size_t>(j) * N + i] : K7[i];
+            };
+            auto yv = [&](int i) -> double {
+                if constexpr (MIXED) return f2d(yf[i]);
+                else return yn_t[i];
+            };
             double wgt[7], dwgt[7];
             double te = tn + h;
 #pragma unroll
@@ -557,25 +630,24 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 double part = 0.0;
                 for (int i = lt; i < N; i += TPT) {
                     double yd = 0.0;
-                    for (int j = 0; j < 6; ++j) yd += dwgt[j] * Kt[static_cast<size_t>(j) * N + i];
-                    yd += dwgt[6] * K7[i];
+                    for (int j = 0; j < 7; ++j) yd += dwgt[j] * kv(j, i);
                     part += s_YB[i] * yd;
                 }
                 double jt = group_sum<TPT>(part, s_red, lt, g);
                 if (lt == 0) {
                     auto y_te = [&](int i) {
                         double acc = 0.0;
-                        for (int j = 0; j < 6; ++j) acc += wgt[j] * Kt[static_cast<size_t>(j) * N + i];
-                        return yn_t[i] + h * (acc + wgt[6] * K7[i]);
+                        for (int j = 0; j < 7; ++j) acc += wgt[j] * kv(j, i);
+                        return yv(i) + h * acc;
                     };
                     auto yd_te = [&](int i) {
-                        double acc = dwgt[6] * K7[i];
-                        for (int j = 0; j < 6; ++j) acc += dwgt[j] * Kt[static_cast<size_t>(j) * N + i];
+                        double acc = 0.0;
+                        for (int j = 0; j < 7; ++j) acc += dwgt[j] * kv(j, i);
                         return acc;
                     };
                     if (segment) {
                         double wy = 0.0;
-                        for (int k = 0; k < A.n_weights; ++k) wy += A.w_val[k] * (yn_t[A.w_idx[k]] + y_te(A.w_idx[k]));
+                        for (int k = 0; k < A.n_weights; ++k) wy += A.w_val[k] * (yv(A.w_idx[k]) + y_te(A.w_idx[k]));
                         jt += 0.5 * gbar * wy;
                     }
                     if (A.ev_kind == OBE_EVENT_POPULATION) {
@@ -584,7 +656,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                         const double c = -jt / ey;
                         if (!isfinite(c)) bad = ADJ_EVENT_TANGENT;
                         else
-                            for (int k = 0; k < A.n_ev; ++k) s_YB[A.ev_idx[k]] += c;
+                            for (int k = 0; k < A.n_ev; ++k) ybar_add(A.ev_idx[k], c);
                     } else if (ng > 0) {
                         // dg/dp: the time-dependent compounds and the event program at t_e in dual numbers
                         double2 dtmp[kMaxGrad], gp[kMaxGrad], gt;
@@ -598,17 +670,22 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                         }
                         vm_eval_dual_prog(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, slots, dslots, ng, te, sv, sd,
                                           tp, gp, &hb, -1);
-                        // dg/dt: the same programs with the time seeded
+                        // dg/dt: the same programs with the time seeded (a compound whose time derivative
+                        // goes through a helper, e.g. a square wave, gets NaN, which matters only if the
+                        // event program reads it)
                         for (int q = 0; q < P.n_slots; ++q) dts[q] = make_double2(0.0, 0.0);
                         for (int c = 0; c < P.n_comp; ++c) {
                             if (!P.comp_dynamic[c]) continue;
                             const DevExpr e = P.comp_expr[c];
+                            int hc = 0;
+                            double2& dt_slot = dts[P.comp_slot[c]];
                             vm_eval_dual_prog(P, P.ins_op, P.ins_arg, P.ins_fn, P.ins_val, e.start, e.len, slots, dts, 1, te, sv,
-                                              sd, tp, &dts[P.comp_slot[c]], &hb, 0);
+                                              sd, tp, &dt_slot, &hc, 0);
+                            if (hc) dt_slot = make_double2(CUDART_NAN, CUDART_NAN);
                         }
                         vm_eval_dual_prog(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, slots, dts, 1, te, sv, sd, tp, &gt,
                                           &hb, 0);
-                        if (hb) bad = ADJ_HELPER_DERIVATIVE;
+                        if (hb || !isfinite(gt.x)) bad = ADJ_HELPER_DERIVATIVE;
                         for (int q = 0; q < ng; ++q) {
                             const double c = -jt * gp[q].x / gt.x;
                             if (!isfinite(c)) bad = ADJ_EVENT_TANGENT;
@@ -645,8 +722,113 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 double2 d = pos >= 0 ? s_ddyn[(row * nd + pos) * kMaxGrad + gi] : s_dcstat[k * kMaxGrad + gi];
                 if (cls & 1) d.y = -d.y;
                 s_dcls[(row * nc2 + cls) * kMaxGrad + gi] = d;
+                if constexpr (MIXED) s_dcls32[(row * nc2 + cls) * kMaxGrad + gi] = make_float2(d2f(d.x), d2f(d.y));
             }
             gsync<TPT>(g);
+            if constexpr (MIXED) {
+                const float hf = d2f(h);
+                float wf[7];
+#pragma unroll
+                for (int s = 0; s < 7; ++s) wf[s] = d2f(wgt[s]);
+                float pst[kMaxGrad];  // this step's parameter-gradient terms
+#pragma unroll
+                for (int q = 0; q < kMaxGrad; ++q) pst[q] = 0.f;
+                for (int s = n_st - 1; s >= 0; --s) {
+                    const int row = s < 6 ? s : 5;
+                    // lambda_s and the stage input Y_s = y_n + h (c_s k_1 + sum_l a_sl d_l) (the seventh
+                    // stage's input is y_{n+1}: row 5, the solution weights)
+                    for (int i = lt; i < N; i += TPT) {
+                        float lam = hf * wf[s] * s_YB32[i];
+                        for (int m = s + 1; m < 6; ++m) lam = fmaf(hf * kTabF.a[M][m - 1][s], s_MU32[static_cast<size_t>(m) * N + i], lam);
+                        if (n_st == 7 && s < 6) lam = fmaf(hf * kTabF.a[M][5][s], s_MU32[static_cast<size_t>(6) * N + i], lam);
+                        // diagonal entries (i < n) fill the whole complex slot: the double-precision
+                        // replay reuses these buffers
+                        if (i < n) s_LS32[i] = make_float2(lam, 0.f);
+                        else s_LS32f[gslot64(i, n)] = lam;
+                        float yin = yf[i];
+                        if (s > 0) {
+                            const int r = s - 1;
+                            float acc = kTabF.csum[M][r] * k1f[i];
+                            for (int l = 1; l < s; ++l) acc = fmaf(kTabF.a[M][r][l], df[static_cast<size_t>(l - 1) * N + i], acc);
+                            yin = fmaf(hf, acc, yin);
+                        }
+                        if (i < n) s_G32[i] = make_float2(yin, 0.f);
+                        else s_G32f[gslot64(i, n)] = yin;
+                    }
+                    if (F > S) {
+                        fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
+                        gsync<TPT>(g);
+                        for (int f = 1 + S + lt; f < 1 + F; f += TPT) s_tab32[f] = make_float2(d2f(s_tab[f].x), d2f(s_tab[f].y));
+                    }
+                    gsync<TPT>(g);
+                    // mu_s = L(t_s)^T lambda_s
+                    {
+                        float br = 0.f, bi = 0.f;
+                        int o = 0;
+                        for (int it = 0; it < P.n_titer; ++it) {
+                            const uint32_t w = s_trec[it * TPT + lt];
+                            const float2 c = s_tab32[w >> kRecCoefShift];
+                            const float2 u = s_LS32[w & kRecIndexMask];
+                            const float tr = fmaf(c.x, u.x, c.y * u.y);
+                            float ti = fmaf(c.x, u.y, -c.y * u.x);
+                            if (w & kRecConj) ti = -ti;
+                            br += tr;
+                            bi += ti;
+                            if (w & kRecFlush) {
+                                const uint32_t d = s_lin[o * TPT + lt];
+                                s_MU32[static_cast<size_t>(s) * N + (d & 0xFFFFu)] = br;
+                                if ((d >> 16) != kNoImag) s_MU32[static_cast<size_t>(s) * N + (d >> 16)] = bi;
+                                br = 0.f;
+                                bi = 0.f;
+                                ++o;
+                            }
+                        }
+                    }
+                    // lambda_s^T (dL/dp) Y_s, formula by formula
+                    for (int c = 0; c < nc2; ++c) s_S32[c * TPT + lt] = make_float2(0.f, 0.f);
+                    {
+                        float zr = 0.f, zi = 0.f;
+                        for (int it = 0; it < P.n_biter; ++it) {
+                            const uint32_t w = s_bil[it * TPT + lt];
+                            if (w & kBilEnd) {
+                                const int f = static_cast<int>(w & ~kBilEnd);
+                                for (int p = P.formula_ptr[f - 1]; p < P.formula_ptr[f]; ++p) {
+                                    const int cls = P.prod_class[p];
+                                    if (cls < 0) continue;
+                                    const float fr = P.prod_factor32[2 * p], fi = P.prod_factor32[2 * p + 1];
+                                    float2& acc = s_S32[cls * TPT + lt];
+                                    acc.x += fr * zr - fi * zi;
+                                    acc.y += fr * zi + fi * zr;
+                                }
+                                zr = 0.f;
+                                zi = 0.f;
+                            } else {
+                                float2 a = s_G32[w & kBilSlotMask];
+                                if (w & kBilConj) a.y = -a.y;
+                                const float2 lam = s_LS32[(w >> kBilOutShift) & kBilSlotMask];
+                                zr = fmaf(a.x, lam.x, fmaf(a.y, lam.y, zr));
+                                zi = fmaf(a.y, lam.x, fmaf(-a.x, lam.y, zi));
+                            }
+                        }
+                    }
+                    for (int c = 0; c < nc2; ++c) {
+                        const float2 Sv = s_S32[c * TPT + lt];
+                        for (int q = 0; q < ng; ++q) {
+                            const float2 d = s_dcls32[(row * nc2 + c) * kMaxGrad + q];
+                            pst[q] = fmaf(d.x, Sv.x, fmaf(-d.y, Sv.y, pst[q]));
+                        }
+                    }
+                    gsync<TPT>(g);
+                }
+                for (int q = 0; q < ng; ++q) pbar[q] += f2d(pst[q]);
+                // ybar_n = ybar_{n+1} + sum_s mu_s (the stage sum in single precision)
+                for (int i = lt; i < N; i += TPT) {
+                    float acc = 0.f;
+                    for (int s = 0; s < n_st; ++s) acc += s_MU32[static_cast<size_t>(s) * N + i];
+                    ybar_add(i, f2d(acc));
+                }
+                gsync<TPT>(g);
+            } else {
             for (int s = n_st - 1; s >= 0; --s) {
                 const int row = s < 6 ? s : 5;
                 // lambda_s (adjoint of K_s) into the lambda slot buffer; Y_s into the input buffer
@@ -733,6 +915,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 s_YB[i] = acc;
             }
             gsync<TPT>(g);
+            }  // double-precision stages
             if (segment) add_quadrature(dt);  // the start state y_n
         }
         }  // segments
@@ -751,10 +934,10 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     }
 }
 
-template <int TPT, int EPT>
+template <int TPT, int EPT, bool MIXED>
 cudaError_t launch_adjoint_shape(const DevPlan& P, const CallArgs& A, const AdjArgs& J, int blocks, int gpb, size_t smem,
                                  size_t group_bytes, int method, cudaStream_t stream) {
-    auto k = adjoint_kernel<TPT, EPT>;
+    auto k = adjoint_kernel<TPT, EPT, MIXED>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     k<<<blocks, gpb * TPT, smem, stream>>>(P, A, J, gpb, group_bytes, method);
@@ -764,9 +947,11 @@ cudaError_t launch_adjoint_shape(const DevPlan& P, const CallArgs& A, const AdjA
 // the adjoint widths (the integrator shapes up to 256 threads per trajectory)
 #define OBE_FOR_EACH_ADJOINT(X) X(32, 8) X(32, 16) X(64, 16) X(128, 16) X(256, 32)
 #ifndef OBE_INSTANCE_TU
-#define OBE_EXTERN_ADJOINT(T, E)                                                                                      \
-    extern template cudaError_t launch_adjoint_shape<T, E>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, \
-                                                           size_t, size_t, int, cudaStream_t);
+#define OBE_EXTERN_ADJOINT(T, E)                                                                                             \
+    extern template cudaError_t launch_adjoint_shape<T, E, false>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, \
+                                                                  size_t, size_t, int, cudaStream_t);                      \
+    extern template cudaError_t launch_adjoint_shape<T, E, true>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int,  \
+                                                                 size_t, size_t, int, cudaStream_t);
 OBE_FOR_EACH_ADJOINT(OBE_EXTERN_ADJOINT)
 #undef OBE_EXTERN_ADJOINT
 #endif

@@ -24,7 +24,9 @@ template cudaError_t launch_rhs_shape<OBE_TPT, true>(const DevPlan&, long long, 
                                                      size_t, double*);
 #endif
 #if OBE_TPT <= 256
-template cudaError_t launch_adjoint_shape<OBE_TPT, OBE_EPT>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, size_t,
-                                                            size_t, int, cudaStream_t);
+template cudaError_t launch_adjoint_shape<OBE_TPT, OBE_EPT, false>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int,
+                                                                   size_t, size_t, int, cudaStream_t);
+template cudaError_t launch_adjoint_shape<OBE_TPT, OBE_EPT, true>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int,
+                                                                  size_t, size_t, int, cudaStream_t);
 #endif
 }  // namespace obe

@@ -1469,6 +1469,37 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             }
                         }
                     }
+                } else {
+                    // the mixed form's tape: single-precision records [t_n, h_n | y_n, k_1, d_2..d_7]
+                    // (the stage derivatives as this step used them, K_s = k_1 + d_s); checkpointed,
+                    // the step log and every tape_ckpt-th start state in double, as above
+                    if (A.tape) {
+                        if (accepted > A.tape_cap) { status = ST_TAPE; err_a = A.tape_cap; break; }
+                        const long long j = accepted - 1;
+                        if (A.tape_ckpt == 0) {
+                            double* rec = A.tape + (static_cast<size_t>(traj) * A.tape_cap + j) * A.tape_stride;
+                            if (lt == 0) { rec[0] = xo; rec[1] = h; }
+                            float* fo = reinterpret_cast<float*>(rec + 2);
+#pragma unroll
+                            for (int e = 0; e < EPT; ++e) {
+                                int i = lt + e * TPT;
+                                if (i < N) fo[i] = d2f(y[e]);
+                            }
+                            for (int i = lt; i < N; i += TPT) fo[N + i] = s_k1f[i];
+                            for (int i = lt; i < 6 * N; i += TPT) fo[2 * N + i] = s_K32[i];
+                        } else {
+                            double* base = A.tape + static_cast<size_t>(traj) * A.tape_stride;
+                            if (lt == 0) { base[2 * j] = xo; base[2 * j + 1] = h; }
+                            if (j % A.tape_ckpt == 0) {
+                                double* rec = base + 2 * A.tape_cap + static_cast<size_t>(j / A.tape_ckpt) * N;
+#pragma unroll
+                                for (int e = 0; e < EPT; ++e) {
+                                    int i = lt + e * TPT;
+                                    if (i < N) rec[i] = y[e];
+                                }
+                            }
+                        }
+                    }
                 }
                 if (hit) {
                     // push_unique (dopri5.rs:150-158)

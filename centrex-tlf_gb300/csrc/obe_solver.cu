@@ -1084,8 +1084,8 @@ static obe_status grad_check(const obe_plan* p, const obe_solve_options* o, int6
         set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan");
         return OBE_ERR_INVALID;
     }
-    if (o->precision != OBE_PRECISION_FP64) {
-        set_error("gradients are implemented for the double-precision form (precision='fp64')");
+    if (o->precision != OBE_PRECISION_FP64 && o->precision != OBE_PRECISION_MIXED) {
+        set_error("gradients are implemented for precision='fp64' and precision='mixed'");
         return OBE_ERR_UNSUPPORTED;
     }
     if (o->solver != OBE_SOLVER_DOPRI5 && o->solver != OBE_SOLVER_TSIT5) {
@@ -1234,8 +1234,12 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     // (checkpointed tape; one record more with a stop event, whose step's seventh stage goes
     // there) and the large systems' slice
     const size_t groups = static_cast<size_t>(blocks) * gpb;
+    // (the mixed form: single-precision records, then the double-precision replay's scratch record)
+    const size_t seg_recs = static_cast<size_t>(checkpoint_every) + (events || opt->precision == OBE_PRECISION_MIXED ? 1 : 0);
     const size_t seg_bytes =
-        checkpoint_every > 0 ? align16(static_cast<size_t>(checkpoint_every + (events ? 1 : 0)) * J.rec_stride * 8) : 0;
+        checkpoint_every > 0
+            ? align16((seg_recs * J.rec_stride + (opt->precision == OBE_PRECISION_MIXED ? 2 + 8 * static_cast<size_t>(P.N) : 0)) * 8)
+            : 0;
     if (seg_bytes + AL.gbytes > 0) {
         unsigned char* gk = nullptr;
         if ((st = kscratch(p, groups * (seg_bytes + AL.gbytes), &gk)) != OBE_OK) return st;
@@ -1248,8 +1252,11 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     const int method = opt->solver == OBE_SOLVER_TSIT5 ? 1 : 0;
     const int ept = ept_for(P.N, tpt);
     cudaError_t e = cudaErrorInvalidConfiguration;
-#define OBE_ADJ_DISPATCH(T, E) \
-    if (tpt == T && ept == E) e = launch_adjoint_shape<T, E>(P, A, J, blocks, gpb, smem, group, method, s);
+    const bool mixed = opt->precision == OBE_PRECISION_MIXED;
+#define OBE_ADJ_DISPATCH(T, E)                                                                                    \
+    if (tpt == T && ept == E)                                                                                     \
+        e = mixed ? launch_adjoint_shape<T, E, true>(P, A, J, blocks, gpb, smem, group, method, s)               \
+                  : launch_adjoint_shape<T, E, false>(P, A, J, blocks, gpb, smem, group, method, s);
     OBE_FOR_EACH_ADJOINT(OBE_ADJ_DISPATCH)
 #undef OBE_ADJ_DISPATCH
     if (!cuda_ok(e, "adjoint kernel launch")) return OBE_ERR_CUDA;

@@ -334,3 +334,103 @@ def test_gradients_through_a_population_event(golden, output, ck):
     ev = {"kind": "population", "indices": list(d["excited_indices"]), "threshold": 0.004}
     p0 = np.array([[1.3 * g, 0.7 * g, 0.4, 100.0 / g], [3.0 * g, -2.0 * g, 1.1, 95.0 / g], [0.1 * g, 4.5 * g, 2.5, 104.0 / g]])
     _event_fd_check(d, p0, slots, ev, [1, 1, 0], output=output, checkpoint_every=ck)
+
+
+def _mixed_fd_check(d, plan, op, p0, slots, t_span, output="excited_population", checkpoint_every=0, stop_event=None,
+                    hits_expected=None, rel=1e-5, floor=1e-6):
+    """The mixed form (single-precision RHS and reverse-sweep products, double-precision state and
+    accumulation) against central differences of the double-precision replay of the mixed
+    forward's own frozen steps: 1e-5 relative, with a floor of 1e-6 of the natural scale |J|/|p|
+    for the single-precision products' rounding.  The costate is integrated with single-precision
+    transposed products, so a derivative that cancels to ~1e-4 of its natural scale (the pulse
+    centre's) carries relative errors up to ~1e-2 (measured 4e-7 of |J|/|p|); the Rabi rate,
+    detuning and angle derivatives agree to ~3e-6 relative."""
+    g = d["gamma"]
+    integral = output != "populations"
+    w = [(i, 1.0) for i in d["excited_indices"]]
+    b = p0.shape[0]
+    params = torch.tensor(p0, dtype=torch.float64, device="cuda", requires_grad=True)
+    out, tape = solve_batch_with_grad(plan, d["rho0_packed"], t_span, params, slots, solver="tsit5", dt=1e-3 / g,
+                                      output=output, integral_weights=w if integral else None, return_tape=True,
+                                      checkpoint_every=checkpoint_every, stop_event=stop_event, precision="mixed")
+    hits = tape.event_hits()
+    if hits_expected is not None:
+        assert hits.tolist() == hits_expected
+    rng = np.random.default_rng(5)
+    wout = np.ones((b, 1)) if integral else rng.normal(size=(b, d["payload"]["n_states"]))
+    (out.reshape(b, -1) * torch.tensor(wout, device="cuda")).sum().backward()
+    grad = params.grad.cpu().numpy()
+    # the forward values are the mixed solve's (the same plan, so the same launch shape)
+    _, ref_vals, _, _, _ = api.solve_lindblad_batch_ode_py(
+        plan, np.repeat(d["rho0_packed"].reshape(1, -1), b, axis=0), t_span[0],
+        t_span[1], 1e-11, 1e-8, 1e-3 / g, saveat=None if integral else np.array([t_span[1]]), save_start=integral,
+        solver="tsit5", output=output, integral_weights=w if integral else None, parameter_slot_indices=slots,
+        parameter_batch=p0.astype(complex), stop_event=stop_event, precision="mixed")
+    np.testing.assert_array_equal(out.detach().cpu().numpy().reshape(-1), np.asarray(ref_vals).reshape(-1))
+    o = op.options(t0=t_span[0], t1=t_span[1], abstol=1e-11, reltol=1e-8, dt=1e-3 / g,
+                   saveat=None if integral else np.array([t_span[1]]), save_start=integral, maxiters=100000,
+                   solver="tsit5", output=output, output_indices=None, output_when="final",
+                   integral_weights=w if integral else None, stop_event=stop_event)
+    steps = tape.steps()
+
+    def replay(p):
+        v = op.solve_replay(o, d["rho0_packed"], slots, p.astype(complex), steps, event_hit=hits)
+        return (np.asarray(v).reshape(b, -1) * wout).sum(axis=1)
+
+    base = replay(p0)
+    # the double-precision replay of the mixed steps is within the mixed form's error of its values
+    np.testing.assert_allclose(base, (out.detach().cpu().numpy().reshape(b, -1) * wout).sum(axis=1), rtol=1e-6,
+                               atol=1e-6 * np.max(np.abs(base)))
+    worst = 0.0
+    for k in range(p0.shape[1]):
+        eps = 1e-6 * np.abs(p0[:, k])
+        eps[eps == 0] = 1e-6 * g
+        pp, pm = p0.copy(), p0.copy()
+        pp[:, k] += eps
+        pm[:, k] -= eps
+        fd = (replay(pp) - replay(pm)) / (2 * eps)
+        natural = np.abs(base) / np.maximum(np.abs(p0[:, k]), 1e-300)
+        tol = rel * np.abs(fd) + floor * natural
+        assert np.all(np.abs(grad[:, k] - fd) <= tol), (k, grad[:, k], fd, tol)
+        worst = max(worst, float(np.max(np.abs(grad[:, k] - fd) / np.maximum(np.abs(fd), 1e-300))))
+    return grad, worst
+
+
+@pytest.mark.parametrize("output,ck", [("excited_population", 0), ("populations", 0), ("excited_population", 7),
+                                       ("excited_population", 512)])
+def test_mixed_form_gradients(q1, output, ck):
+    """The mixed form's gradients (forward with a single-precision tape, single-precision reverse
+    products): full and checkpointed tapes, integral and final populations."""
+    d, plan, op = q1
+    _mixed_fd_check(d, plan, op, _params(d), _slots(d), d["t_span"], output=output, checkpoint_every=ck)
+
+
+@pytest.mark.parametrize("tpt", [32, 128])
+def test_mixed_form_gradients_at_other_widths(q1, tpt):
+    d, plan, op = q1
+    plan.set_shape(tpt, 0)
+    try:
+        _mixed_fd_check(d, plan, op, _params(d)[:3], _slots(d), d["t_span"])
+    finally:
+        plan.set_shape(0, 0)
+
+
+def test_mixed_form_gradients_through_a_time_event(golden):
+    d = golden("plan_q1_16_tend")
+    g = d["gamma"]
+    names = d["payload"]["parameter_graph"]["slot_names"]
+    slots = [names.index(s) for s in ("rabi", "detuning", "theta", "t_end")]
+    p0 = np.array([[1.0 * g, 0.0, 0.3, 123.4 / g], [3.0 * g, -2.0 * g, 1.1, 60.3 / g], [0.4 * g, 1.5 * g, 2.5, 250.0 / g]])
+    for ck in (0, 9):
+        _mixed_fd_check(d, NativePlan(d["payload"]), oracle.OraclePlan(d["payload"]), p0, slots, (0.0, 200.0 / g),
+                        checkpoint_every=ck, stop_event=_t_end_event(names), hits_expected=[1, 1, 0])
+
+
+def test_mixed_form_gradients_of_the_76_state_system(golden):
+    """256 threads per trajectory (the sweep's buffers in device memory), checkpointed."""
+    d = golden("plan_rc_76")
+    g = d["gamma"]
+    plan = NativePlan(d["payload"])
+    op = oracle.OraclePlan(d["payload"])
+    p0 = np.array([[1.2 * g, 2.0 * g, 0.3 * g, -0.2 * g], [2.5 * g, 0.8 * g, -0.4 * g, 0.6 * g]])
+    _mixed_fd_check(d, plan, op, p0, _slots(d, ("Ω0", "Ω1", "δ0", "δ1")), (0.0, 6.0 / g), checkpoint_every=16)

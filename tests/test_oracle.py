@@ -283,3 +283,39 @@ def test_r2_38_state_known_answer(golden):
     assert abs(int(gst["accepted_steps"].sum()) - kg["accepted_steps"]) <= 2
     assert int(gst["rejected_steps"].sum()) == 0
     assert abs(int(gst["rhs_calls"].sum()) - kg["rhs_calls"]) <= 12
+
+
+@pytest.mark.parametrize("solver", ["tsit5", "dopri5"])
+def test_replay_of_an_event_ended_solve(golden, solver):
+    """The frozen-step replay (the gradient tests' finite differences) given the steps of an
+    event-free solve up to the crossing and `event_hit` reproduces the solve that the stop event
+    ends: the same crossing by bisection, the same final integral and populations."""
+    d = golden("plan_q1_16_tend")
+    op = oracle.OraclePlan(d["payload"])
+    g = d["gamma"]
+    names = d["payload"]["parameter_graph"]["slot_names"]
+    slots = [names.index(s) for s in ("rabi", "detuning", "theta", "t_end")]
+    w = [(i, 1.0) for i in d["excited_indices"]]
+    p = np.array([[1.3 * g, 0.7 * g, 0.4, 123.4 / g]], dtype=complex)
+    common = dict(t0=0.0, t1=200 / g, abstol=1e-11, reltol=1e-8, dt=1e-3 / g, maxiters=100000, solver=solver,
+                  output_indices=None)
+    tt, _, _ = op.solve_single(op.options(saveat=None, save_start=True, output="populations", output_when="saveat",
+                                          integral_weights=None, stop_event=None, **common),
+                               d["rho0_packed"], slots, p[0], capacity=100000)
+    tt = np.asarray(tt)
+    steps = np.stack([tt[:-1], np.diff(tt)], axis=1)
+    events = [{"kind": "runtime_expression",
+               "expression": {"instructions": [{"op": 4}, {"op": 2, "index": names.index("t_end")}, {"op": 6}],
+                              "scalar_only": True, "output_is_tuple": False}},
+              {"kind": "population", "indices": list(d["excited_indices"]), "threshold": 0.004}]
+    for ev in events:
+        for integral in (True, False):
+            o = op.options(saveat=None if integral else np.array([200 / g]), save_start=integral,
+                           output="excited_population" if integral else "populations", output_when="final",
+                           integral_weights=w if integral else None, stop_event=ev, **common)
+            vals, _, st = op.solve_batch(o, d["rho0_packed"].reshape(1, -1), slots, p)
+            assert st["event_triggered"][0]
+            k = int(np.searchsorted(tt, float(st["event_time"][0]), side="left"))
+            r = op.solve_replay(o, d["rho0_packed"], slots, p, [steps[:k]], event_hit=[1])
+            ref = np.asarray(vals).reshape(-1)
+            np.testing.assert_allclose(np.asarray(r).reshape(-1), ref, rtol=1e-13, atol=1e-15 * np.max(np.abs(ref)))
