@@ -297,8 +297,8 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
                       "max_grad_diff_vs_fp64_natural_scale": mixed_vs_64,
                       "note": "difference on the scale |J|/|p|, each form on its own step sequence; against central "
                               "differences of its own frozen steps the mixed adjoint agrees to <= 3e-6 relative for "
-                              "rabi, detuning and angle, and to ~5e-9 of |J|/|p| for the pulse centre (a derivative "
-                              "that cancels to ~1e-7 of that scale) (tests/test_gpu_adjoint.py)"}}
+                              "rabi, detuning and angle, and to ~4e-7 of |J|/|p| for the pulse centre (a derivative "
+                              "that cancels to ~1e-4 of that scale) (tests/test_gpu_adjoint.py)"}}
 
 
 HETERO_PLANS = (("plan_q1_16_tend", 6), ("plan_r0_39", 3), ("plan_rc_76", 1))
@@ -452,7 +452,7 @@ def measure_hetero_gradient(torch, dev, total: int = 8192, precision: str = "mix
             pt = torch.tensor(j["params"].real, dtype=torch.float64, device=dev, requires_grad=True)
             out = solve_batch_with_grad(plan, rho, (0.0, j["t1"]), pt, j["slots"], dt=1e-3 / j["d"]["gamma"],
                                         maxiters=1000000, integral_weights=j["weights"], stop_event=j["event"],
-                                        precision=precision, max_steps=8192)
+                                        precision=precision, max_steps=8192 if j["name"] == "plan_rc_76" else 2048)
             out.sum().backward()
             torch.cuda.synchronize()
             assert bool(torch.isfinite(pt.grad).all()), j["name"]
@@ -471,6 +471,7 @@ def measure_hetero_gradient(torch, dev, total: int = 8192, precision: str = "mix
     fwd()
     torch.cuda.synchronize()
     t_fwd = timed(fwd)
+    grad()  # untimed: device buffers (tapes, segment buffers) allocated once
     t_grad = timed(grad)
     return {"workload": f"{total} instances of the heterogeneous batch (16/39/76-state plans 6:3:1, end times "
                         "U[50, 300]/Γ by a Time() - t_end stop event); d(excited-population integral)/d(Rabi rates, "
@@ -479,7 +480,8 @@ def measure_hetero_gradient(torch, dev, total: int = 8192, precision: str = "mix
             "grad_over_fwd": t_grad / t_fwd, "fwd_plus_grad_ms_per_plan": per_plan,
             "note": "forward = the three plans' plain solves one call each (device-resident); gradient = "
                     "solve_batch_with_grad + backward per plan (host-synchronised between the tape check and the "
-                    "reverse sweep); the 76-state trajectories dominate both"}
+                    "reverse sweep), timed after one untimed call; the 76-state trajectories (checkpointed tape) "
+                    "dominate both"}
 
 
 def measure_effective(torch, dev, total: int = 4096, cpu_sample: int = 256, reps: int = 2) -> dict:

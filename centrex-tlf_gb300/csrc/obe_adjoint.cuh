@@ -244,6 +244,7 @@ static __device__ __forceinline__ double2 vm_eval_dual(const DevPlan& P, int32_t
 struct AdjLayout {
     size_t tab, G, LS, MU, YB, slots, dslots, dts, sv, sd, tp, cstat, dcstat, cdyn, ddyn, dcls, S, red, traj, bytes;
     size_t tab32, YB32, dcls32;  // the mixed sweep's single-precision formula table, ybar copy, class derivatives
+    size_t T4, cv;               // the mixed replay's deviation-form formula table and stage class values
     size_t gbytes;  // large systems: bytes of the group's device-memory slice (MU, YB, S)
     bool glob;
 };
@@ -265,6 +266,7 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     L.MU = om; om = align16(om + static_cast<size_t>(stages) * N * 8);
     L.YB = om; om = align16(om + static_cast<size_t>(N) * 8);
     L.YB32 = om; om = align16(om + static_cast<size_t>(N) * 4);
+    L.T4 = om; om = align16(om + static_cast<size_t>(1 + n_formula) * 16);
     L.slots = o; o = align16(o + 6 * ns * 16);
     L.dslots = o; o = align16(o + 6 * ns * kMaxGrad * 16);
     L.dts = o; o = align16(o + ns * 16);
@@ -277,6 +279,7 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     L.ddyn = o; o = align16(o + 6 * nd * kMaxGrad * 16);
     L.dcls = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 16);
     L.dcls32 = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 8);
+    L.cv = o; o = align16(o + 5 * 2 * nc * 16);
     L.S = om; om = align16(om + 2 * nc * static_cast<size_t>(tpt) * 16);
     L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
     L.traj = o; o = align16(o + 16);
@@ -492,16 +495,104 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         const double* tbase = J.tape + static_cast<size_t>(traj) * (J.ckpt > 0 ? J.tape_stride : J.tape_cap * J.tape_stride);
         for (long long sg = n_seg - 1; sg >= 0; --sg) {
         const long long s0 = sg * seg_len, s1 = s0 + seg_len < n_acc ? s0 + seg_len : n_acc;
-        if (J.ckpt > 0) {
-            // replay the segment's steps from its checkpointed start state with the recorded
-            // (t_n, h_n): the stage derivatives of the frozen steps, as the forward solve took them.
-            // The mixed form replays in double precision into a scratch record (after the segment's
-            // records) and stores each step as a single-precision record [y_n, k_1, d_2..d_7].
+        if (J.ckpt > 0 && MIXED) {
+            // replay the segment's steps from its checkpointed start state as the mixed forward took
+            // them: single-precision stage deviations d_2..d_7 (the same deviation-form gather), the
+            // solution and k_1 (first same as last, refreshed in double precision at the segment start
+            // and every k1_refresh steps) in double; each step stored as a single-precision record
+            // [y_n, k_1, d_2..d_7].  Scratch after the segment's records: y, k_1 (double), k_1 (single).
+            double* yx = segbuf + static_cast<size_t>(J.ckpt + 1) * J.rec_stride;
+            double* k1x = yx + N;
+            float* k1fx = reinterpret_cast<float*>(yx + 2 * static_cast<size_t>(N));
+            float* K32 = s_MU32;  // the step's stage deviations (the mu buffer is free here)
+            float4* G4 = reinterpret_cast<float4*>(gb + Lay.G);
+            float* G4f = reinterpret_cast<float*>(gb + Lay.G);
+            float4* T4 = reinterpret_cast<float4*>(gm + Lay.T4);
+            float4* cv = reinterpret_cast<float4*>(gb + Lay.cv);
             const double* ck = tbase + 2 * J.tape_cap + static_cast<size_t>(sg) * N;
-            double* xrec = MIXED ? segbuf + static_cast<size_t>(J.ckpt + 1) * J.rec_stride : segbuf;
-            for (int i = lt; i < N; i += TPT) xrec[2 + i] = ck[i];
+            for (int i = lt; i < N; i += TPT) yx[i] = ck[i];
+            // the table's fixed part: the records' zero coefficient and the time-independent formulas
+            // (no change within a step); the formula stream refreshes the time-dependent ones per stage
+            if (lt == 0) T4[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int f = 1 + lt; f < 1 + S; f += TPT) T4[f] = make_float4(d2f(s_tab[f].x), d2f(s_tab[f].y), 0.f, 0.f);
+            int since = 0;
             for (long long st = s0; st < s1; ++st) {
-                double* rec = MIXED ? xrec : segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
+                const double tn = tbase[2 * st], h = tbase[2 * st + 1];
+                // coefficient rows as the mixed forward keeps them: 0..4 at c_2..c_5, 1; 5 at t_n
+                if (lt < 6) {
+                    const double ts = lt < 5 ? tn + h * (lt < 4 ? kTab.c[M][lt] : 1.0) : tn;
+                    double2 dtmp[kMaxGrad];
+                    for (int c = 0; c < P.n_comp; ++c) {
+                        if (!P.comp_dynamic[c]) continue;
+                        const DevExpr e = P.comp_expr[c];
+                        slots[P.comp_slot[c]] = vm_eval_dual(P, e.start, e.len, slots, dslots, 0, ts, sv, sd, tp, dtmp, &bad);
+                    }
+                    for (int j = 0; j < P.n_dyn; ++j) {
+                        const DevExpr e = P.coeff_expr[P.dyn_ids[j]];
+                        s_cdyn[lt * nd + j] = vm_eval_dual(P, e.start, e.len, slots, dslots, 0, ts, sv, sd, tp, dtmp, &bad);
+                    }
+                }
+                gsync<TPT>(g);
+                if (st == s0 || since >= A.k1_refresh) {
+                    // k_1 = L(t_n) y_n in double precision
+                    if (F > S) fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + 5 * nd, s_tab, lt);
+                    for (int i = lt; i < N; i += TPT) {
+                        if (i < n) s_G[i] = make_double2(yx[i], 0.0);
+                        else s_G64[gslot64(i, n)] = yx[i];
+                    }
+                    gsync<TPT>(g);
+                    gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, k1x, lt);
+                    gsync<TPT>(g);
+                    for (int i = lt; i < N; i += TPT) k1fx[i] = d2f(k1x[i]);
+                    since = 0;
+                }
+                stage_classes<TPT>(P, s_cstat, s_cdyn, nd, cv, lt);
+                const float hf = d2f(h);
+                for (int s = 0; s < 6; ++s) {
+                    for (int i = lt; i < N; i += TPT) {
+                        float acc = 0.f;
+                        for (int j = 1; j <= s; ++j) acc = fmaf(kTabF.a[M][s][j], K32[static_cast<size_t>(j - 1) * N + i], acc);
+                        const float dv = hf * fmaf(kTabF.csum[M][s], k1fx[i], acc);
+                        const float yv32 = d2f(yx[i]);
+                        if (i < n) {
+                            G4[i] = make_float4(dv, 0.f, yv32, 0.f);
+                        } else {
+                            const int q = gslot32(i, n);
+                            G4f[q] = dv;
+                            G4f[q + 2] = yv32;
+                        }
+                    }
+                    gsync<TPT>(g);
+                    fill_formulas_dev<TPT>(P.n_fiter, reinterpret_cast<const float4*>(P.fstream), cv + (s < 5 ? s : 4) * 2 * P.n_coeff,
+                                           T4, lt);
+                    gsync<TPT>(g);
+                    gather_dev<TPT>(P, P.rec, P.lane_out, T4, G4, K32 + static_cast<size_t>(s) * N, lt);
+                    gsync<TPT>(g);
+                }
+                double* out = segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
+                if (lt == 0) { out[0] = tn; out[1] = h; }
+                float* fo = reinterpret_cast<float*>(out + 2);
+                for (int i = lt; i < N; i += TPT) {
+                    fo[i] = d2f(yx[i]);
+                    fo[N + i] = k1fx[i];
+                    for (int r = 0; r < 6; ++r) fo[static_cast<size_t>(2 + r) * N + i] = K32[static_cast<size_t>(r) * N + i];
+                    float acc = 0.f;
+                    for (int j = 1; j < 6; ++j) acc = fmaf(kTabF.a[M][5][j], K32[static_cast<size_t>(j - 1) * N + i], acc);
+                    yx[i] = yx[i] + h * (k1x[i] + f2d(acc));
+                    const double k = k1x[i] + f2d(K32[static_cast<size_t>(5) * N + i]);
+                    k1x[i] = k;
+                    k1fx[i] = d2f(k);
+                }
+                ++since;
+                gsync<TPT>(g);
+            }
+        } else if (J.ckpt > 0) {
+            // replay the segment's steps from its checkpointed start state with the recorded
+            // (t_n, h_n): the stage derivatives of the frozen steps, as the forward solve took them
+            const double* ck = tbase + 2 * J.tape_cap + static_cast<size_t>(sg) * N;
+            for (int i = lt; i < N; i += TPT) segbuf[2 + i] = ck[i];
+            for (long long st = s0; st < s1; ++st) {
+                double* rec = segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
                 const double tn = tbase[2 * st], h = tbase[2 * st + 1];
                 if (lt == 0) { rec[0] = tn; rec[1] = h; }
                 if (lt < 6) {
@@ -525,7 +616,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                         double acc = 0.0;
                         for (int l = 0; l < s; ++l) acc += kTab.a[M][s - 1][l] * K_r[static_cast<size_t>(l) * N + i];
                         const double v = s > 0 ? yn_r[i] + h * acc : yn_r[i];
-                        // diagonal entries fill the whole complex slot (the mixed sweep reuses the buffer)
+                        // diagonal entries fill the whole complex slot (the buffer is shared)
                         if (i < n) s_G[i] = make_double2(v, 0.0);
                         else s_G64[gslot64(i, n)] = v;
                     }
@@ -535,11 +626,9 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, K_r + static_cast<size_t>(s) * N, lt);
                     gsync<TPT>(g);
                 }
-                const bool ev_last = ev_hit && st == n_acc - 1;
-                if (ev_last) {
+                if (ev_hit && st == n_acc - 1) {
                     // the event step's seventh stage K_7 = L(t_n + h) y_{n+1}, into the next record's
-                    // state slot (the segment buffer holds one record more than a segment), or, mixed,
-                    // into the scratch record's seventh row
+                    // state slot (the segment buffer holds one record more than a segment)
                     for (int i = lt; i < N; i += TPT) {
                         double acc = 0.0;
                         for (int s = 0; s < 6; ++s) acc += bw[s] * K_r[static_cast<size_t>(s) * N + i];
@@ -548,28 +637,10 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                         else s_G64[gslot64(i, n)] = v;
                     }
                     gsync<TPT>(g);
-                    gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G,
-                                                     MIXED ? K_r + static_cast<size_t>(6) * N : rec + J.rec_stride + 2, lt);
+                    gather_rhs<TPT, double, double2>(P, P.rec, P.lane_out, s_tab, s_G, rec + J.rec_stride + 2, lt);
                     gsync<TPT>(g);
                 }
-                if constexpr (MIXED) {
-                    double* out = segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
-                    if (lt == 0) { out[0] = tn; out[1] = h; }
-                    float* fo = reinterpret_cast<float*>(out + 2);
-                    const int nd_rows = ev_last ? 6 : 5;
-                    for (int i = lt; i < N; i += TPT) {
-                        const double k1 = K_r[i];
-                        fo[i] = d2f(yn_r[i]);
-                        fo[N + i] = d2f(k1);
-                        for (int l = 1; l <= nd_rows; ++l)
-                            fo[static_cast<size_t>(l + 1) * N + i] = d2f(K_r[static_cast<size_t>(l) * N + i] - k1);
-                        if (st + 1 < s1) {
-                            double acc = 0.0;
-                            for (int s = 0; s < 6; ++s) acc += bw[s] * K_r[static_cast<size_t>(s) * N + i];
-                            xrec[2 + i] = yn_r[i] + h * acc;  // y_{n+1} in place (element i is this thread's)
-                        }
-                    }
-                } else if (st + 1 < s1) {
+                if (st + 1 < s1) {
                     double* yn_next = rec + J.rec_stride + 2;
                     for (int i = lt; i < N; i += TPT) {
                         double acc = 0.0;

@@ -1202,6 +1202,7 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     for (int k = 0; k < A.n_param; ++k) A.param_slot[k] = static_cast<int>(param_slots[k]);
     A.param_values = d_param_values;
     A.vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
+    A.k1_refresh = k1_refresh_interval();  // the mixed form's checkpoint replay
     AdjArgs J{};
     J.n_grad = n_grad;
     for (int q = 0; q < n_grad; ++q) J.grad_slot[q] = static_cast<int>(grad_slots[q]);
