@@ -747,12 +747,14 @@ def run_case(args) -> None:
             pt = torch.tensor(p, dtype=torch.float64, device=dev, requires_grad=True)
             start = time.perf_counter()
             j = solve_batch_with_grad(plan, d["rho0_packed"], (t0, t1), pt, slots, dt=1e-3 / gamma,
-                                      integral_weights=W_EXCITED, max_steps=2048)
+                                      integral_weights=W_EXCITED, max_steps=2048, precision=args.precision,
+                                      checkpoint_every=args.checkpoint_every)
             j.sum().backward()
             torch.cuda.synchronize()
             times.append(1e3 * (time.perf_counter() - start))
             assert bool(torch.isfinite(pt.grad).all())
         print(json.dumps({"case": args.case, "points": p.shape[0], "threads_per_trajectory": plan.shape()[0],
+                          "precision": args.precision, "checkpoint_every": args.checkpoint_every,
                           "fwd_plus_grad_ms": times}))
         return
     # large: one wave of the 76-state system through the device entry point
@@ -802,6 +804,8 @@ def main() -> None:
                     help="instances of the heterogeneous batch timed forward plus adjoint (0: skip; the full "
                          "8192-instance batch: --case hetero-gradient --points 8192)")
     ap.add_argument("--points", type=int, default=4096)
+    ap.add_argument("--checkpoint-every", type=int, default=None,
+                    help="--case gradient: the tape's checkpoint interval (default: full tape while it fits)")
     ap.add_argument("--cpu-sample", type=int, default=128)
     ap.add_argument("--ref-sample", type=int, default=256)
     ap.add_argument("--case", choices=["scan", "gradient", "heterogeneous", "hetero-gradient", "large"], default="scan",
