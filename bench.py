@@ -344,7 +344,7 @@ def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
     three plans' kernels concurrent): the mixed form timed after one untimed call, the same jobs
     as three single-plan calls in a row on one stream (what a caller of the reference's
     one-plan-per-call API does), and the FP64 form once, for the error of the mixed form."""
-    from centrex_tlf_gb300.native import NativePlan, multi_solve_device
+    from centrex_tlf_gb300.native import MultiGraph, NativePlan, multi_solve_device
 
     spec = hetero_jobs(total)
     stream = torch.cuda.current_stream(dev)
@@ -393,6 +393,11 @@ def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
     failed = sum(int(np.count_nonzero(s.view(-1, 6)[:, 3].cpu().numpy() >> 32)) for *_, s in prepared)
     steps = [int(s.view(-1, 6)[:, 0].sum().item()) for *_, s in prepared]
     t_seq, _ = timed(sequential, "mixed", warm=False)
+    # the same batch recorded once as a CUDA graph (obe_multi_graph), replayed as one launch
+    graph = MultiGraph([(pl, o["mixed"], b, r.data_ptr(), sl, pa.data_ptr(), 1, v["mixed"].data_ptr(), s.data_ptr())
+                        for pl, o, b, r, sl, pa, v, s in prepared])
+    t_graph, _ = timed(lambda prec: graph.launch(stream.cuda_stream), "mixed")
+    graph.close()
     t_64, _ = timed(multi, "fp64", warm=False)
     err = 0.0
     for j, (*_, val, _) in zip(spec, prepared):
@@ -407,6 +412,7 @@ def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
         "accepted_steps": {j["name"]: n for j, n in zip(spec, steps)},
         "failed_trajectories": failed,
         "one_call_per_plan_ms": 1e3 * t_seq, "concurrency_gain": t_seq / t_multi,
+        "cuda_graph_ms": 1e3 * t_graph,
         "fp64_ms": 1e3 * t_64, "speedup_of_mixed": t_64 / t_multi,
         "max_time_averaged_population_error_vs_fp64": err,
         "note": "fp64 timed on its first call (plans already on the device); the error is |integral difference| / t_end",

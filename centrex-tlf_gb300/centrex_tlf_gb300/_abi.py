@@ -260,6 +260,12 @@ def load_library() -> ctypes.CDLL:
     lib.obe_last_launch_count.restype = ctypes.c_int64
     lib.obe_solve_multi_device.argtypes = [ctypes.c_int32, ctypes.POINTER(ObeBatchJob), ctypes.c_void_p]
     lib.obe_solve_multi_device.restype = ctypes.c_int
+    lib.obe_multi_graph_create.argtypes = [ctypes.c_int32, ctypes.POINTER(ObeBatchJob), ctypes.POINTER(ctypes.c_void_p)]
+    lib.obe_multi_graph_create.restype = ctypes.c_int
+    lib.obe_multi_graph_launch.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.obe_multi_graph_launch.restype = ctypes.c_int
+    lib.obe_multi_graph_destroy.argtypes = [ctypes.c_void_p]
+    lib.obe_multi_graph_destroy.restype = None
     lib.obe_effective_plan_create.argtypes = [ctypes.POINTER(ObePlanDesc), ctypes.POINTER(ObeEffectiveDesc),
                                               ctypes.POINTER(ctypes.c_void_p)]
     lib.obe_effective_plan_create.restype = ctypes.c_int

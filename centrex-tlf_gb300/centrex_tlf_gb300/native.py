@@ -289,15 +289,7 @@ class NativePlan:
         return int(self.lib.obe_last_launch_count())
 
 
-def multi_solve_device(jobs, stream: int = 0) -> int:
-    """obe_solve_multi_device over device-resident batches on different plans.
-
-    ``jobs``: sequence of ``(plan: NativePlan, opts: SolveOptions, n_traj, d_rho0, param_slots or
-    None, d_param_values or None, time_count, d_values, d_stats)``, data pointers as ints.  The
-    jobs' kernels run concurrently, asynchronous on ``stream``.  Returns the kernel launch count."""
-    if not jobs:
-        return 0
-    lib = load_library()
+def _job_array(jobs):
     arr = (_abi.ObeBatchJob * len(jobs))()
     keep = []
     for k, (plan, opts, n_traj, d_rho0, slots, d_params, time_count, d_values, d_stats) in enumerate(jobs):
@@ -307,10 +299,57 @@ def multi_solve_device(jobs, stream: int = 0) -> int:
         arr[k] = _abi.ObeBatchJob(plan.handle.value, ctypes.pointer(opts.opts), int(n_traj), d_rho0, n_param,
                                   _abi.ptr(sl, ctypes.c_int64), d_params or 0, int(time_count), opts.width,
                                   d_values, d_stats)
+    return arr, keep
+
+
+def multi_solve_device(jobs, stream: int = 0) -> int:
+    """obe_solve_multi_device over device-resident batches on different plans.
+
+    ``jobs``: sequence of ``(plan: NativePlan, opts: SolveOptions, n_traj, d_rho0, param_slots or
+    None, d_param_values or None, time_count, d_values, d_stats)``, data pointers as ints.  The
+    jobs' kernels run concurrently, asynchronous on ``stream``.  Returns the kernel launch count."""
+    if not jobs:
+        return 0
+    lib = load_library()
+    arr, _keep = _job_array(jobs)
     st = lib.obe_solve_multi_device(len(jobs), arr, ctypes.c_void_p(stream))
     if st != _abi.OBE_OK:
         _raise(lib, st)
     return int(lib.obe_last_launch_count())
+
+
+class MultiGraph:
+    """obe_multi_graph: the jobs of ``multi_solve_device`` recorded once as a CUDA graph; each
+    ``launch(stream)`` replays the whole heterogeneous batch as one graph launch (refill the
+    jobs' device inputs between launches, read their outputs after).  Holds its plans."""
+
+    def __init__(self, jobs) -> None:
+        lib = load_library()
+        self._plans = [j[0] for j in jobs]
+        arr, _keep = _job_array(jobs)
+        h = ctypes.c_void_p()
+        st = lib.obe_multi_graph_create(len(jobs), arr, ctypes.byref(h))
+        if st != _abi.OBE_OK:
+            _raise(lib, st)
+        self.handle = h
+
+    def launch(self, stream: int = 0) -> int:
+        lib = load_library()
+        st = lib.obe_multi_graph_launch(self.handle, ctypes.c_void_p(stream))
+        if st != _abi.OBE_OK:
+            _raise(lib, st)
+        return int(lib.obe_last_launch_count())
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) and self.handle.value:
+            load_library().obe_multi_graph_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def _stats_dict(st: ObeTrajStats) -> dict:

@@ -824,9 +824,67 @@ struct PreparedJob {
     std::vector<double> save_times;
     CallBlob cb;
     int cplx = 0;
+    LaunchShape shape;
     unsigned char* d = nullptr;
-    size_t errs_off = 0;
+    size_t errs_off = 0, need = 0;
 };
+
+obe_status job_fail(int k, obe_status st) {
+    set_error("job " + std::to_string(k) + ": " + last_error_cstr());
+    return st;
+}
+
+// Validation shared by the immediate and the graph-recorded heterogeneous batch (under the plan
+// mutex): plans on the device, options checked, each job's argument block built and launch shape
+// chosen; q.need = bytes of its argument block and error records.
+obe_status prepare_jobs(int32_t n_jobs, const obe_batch_job* jobs, std::vector<PreparedJob>& pj) {
+    for (int k = 0; k < n_jobs; ++k) {
+        if (!jobs[k].plan || !jobs[k].opt) { set_error("null argument"); return job_fail(k, OBE_ERR_INVALID); }
+        if (jobs[k].n_traj < 0) { set_error("n_traj must be non-negative"); return job_fail(k, OBE_ERR_INVALID); }
+        for (int m = 0; m < k; ++m)
+            if (jobs[m].plan == jobs[k].plan) {
+                set_error("plan already used by job " + std::to_string(m) + " (one job per plan)");
+                return job_fail(k, OBE_ERR_INVALID);
+            }
+    }
+    pj.assign(n_jobs, PreparedJob{});
+    for (int k = 0; k < n_jobs; ++k) {
+        PreparedJob& q = pj[k];
+        q.j = &jobs[k];
+        q.p = const_cast<obe_plan*>(jobs[k].plan);
+        obe_status st = ensure_ready(q.p);
+        if (st != OBE_OK) return job_fail(k, st);
+        if ((st = check_params(q.p, q.j->n_param_slots, q.j->param_slots)) != OBE_OK) return job_fail(k, st);
+        int64_t w = 0;
+        if ((st = validate_options(q.p, q.j->opt, q.save_times, q.cb, &w, &q.cplx)) != OBE_OK) return job_fail(k, st);
+        if (w != q.j->width) { set_error("output width mismatch"); return job_fail(k, OBE_ERR_INVALID); }
+        const int vm_depth = std::max(q.p->dev.max_stack, std::max(q.cb.ev_len, 1));
+        if ((st = plan_launch(q.p->dev, q.j->opt->precision == OBE_PRECISION_MIXED, std::max<int64_t>(q.j->n_traj, 1), vm_depth,
+                              &q.shape, q.p->shape_gpb)) != OBE_OK)
+            return job_fail(k, st);
+        q.errs_off = align16(q.cb.bytes.size());
+        q.need = q.errs_off + sizeof(TrajErr) * static_cast<size_t>(std::max<int64_t>(q.j->n_traj, 1));
+    }
+    return OBE_OK;
+}
+
+// largest systems first: their trajectories are the longest single pieces of work, so they take
+// the SMs first and the small systems fill in behind them (longest-processing-time order)
+std::vector<int> job_order(const std::vector<PreparedJob>& pj) {
+    std::vector<int> order(pj.size());
+    for (size_t k = 0; k < pj.size(); ++k) order[k] = static_cast<int>(k);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pj[a].p->N > pj[b].p->N; });
+    return order;
+}
+
+// job q's solve on stream js (its argument block already at q.d)
+obe_status launch_job(PreparedJob& q, cudaStream_t js) {
+    return solve_device(q.p, q.j->opt, q.j->n_traj, q.j->d_rho0, q.p->N, q.j->n_param_slots, q.j->param_slots,
+                        q.j->d_param_values, 0, nullptr, nullptr, q.j->time_count,
+                        q.j->time_count * q.j->width * (q.cplx ? 2 : 1), q.j->d_values, nullptr, q.j->d_stats,
+                        reinterpret_cast<TrajErr*>(q.d + q.errs_off), q.d, q.cb, q.save_times,
+                        static_cast<unsigned long long*>(q.p->d_counter), js);
+}
 }  // namespace
 
 obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, void* stream) {
@@ -837,50 +895,18 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
     }
     if (n_jobs == 0) return OBE_OK;
     if (!jobs) { set_error("null argument"); return OBE_ERR_INVALID; }
-    auto fail = [](int k, obe_status st) {
-        set_error("job " + std::to_string(k) + ": " + last_error_cstr());
-        return st;
-    };
-    for (int k = 0; k < n_jobs; ++k) {
-        if (!jobs[k].plan || !jobs[k].opt) { set_error("null argument"); return fail(k, OBE_ERR_INVALID); }
-        if (jobs[k].n_traj < 0) { set_error("n_traj must be non-negative"); return fail(k, OBE_ERR_INVALID); }
-        for (int m = 0; m < k; ++m)
-            if (jobs[m].plan == jobs[k].plan) {
-                set_error("plan already used by job " + std::to_string(m) + " (one job per plan)");
-                return fail(k, OBE_ERR_INVALID);
-            }
-    }
     std::lock_guard<std::mutex> lock(g_plan_mutex);
-    std::vector<PreparedJob> pj(n_jobs);
-    for (int k = 0; k < n_jobs; ++k) {
-        PreparedJob& q = pj[k];
-        q.j = &jobs[k];
-        q.p = const_cast<obe_plan*>(jobs[k].plan);
-        obe_status st = ensure_ready(q.p);
-        if (st != OBE_OK) return fail(k, st);
-        if ((st = check_params(q.p, q.j->n_param_slots, q.j->param_slots)) != OBE_OK) return fail(k, st);
-        int64_t w = 0;
-        if ((st = validate_options(q.p, q.j->opt, q.save_times, q.cb, &w, &q.cplx)) != OBE_OK) return fail(k, st);
-        if (w != q.j->width) { set_error("output width mismatch"); return fail(k, OBE_ERR_INVALID); }
-        LaunchShape s;
-        const int vm_depth = std::max(q.p->dev.max_stack, std::max(q.cb.ev_len, 1));
-        if ((st = plan_launch(q.p->dev, q.j->opt->precision == OBE_PRECISION_MIXED, std::max<int64_t>(q.j->n_traj, 1), vm_depth, &s,
-                              q.p->shape_gpb)) != OBE_OK)
-            return fail(k, st);
-        q.errs_off = align16(q.cb.bytes.size());
-        size_t need = q.errs_off + sizeof(TrajErr) * static_cast<size_t>(std::max<int64_t>(q.j->n_traj, 1));
-        if ((st = scratch(q.p, need, &q.d)) != OBE_OK) return fail(k, st);
-    }
+    std::vector<PreparedJob> pj;
+    obe_status pst = prepare_jobs(n_jobs, jobs, pj);
+    if (pst != OBE_OK) return pst;
+    for (int k = 0; k < n_jobs; ++k)
+        if ((pst = scratch(pj[k].p, pj[k].need, &pj[k].d)) != OBE_OK) return job_fail(k, pst);
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
     JobStreams* J = nullptr;
     obe_status st = job_streams(dev, &J);
     if (st != OBE_OK) return st;
-    // largest systems first: their trajectories are the longest single pieces of work, so they
-    // take the SMs first and the small systems fill in behind them (longest-processing-time order)
-    std::vector<int> order(n_jobs);
-    for (int k = 0; k < n_jobs; ++k) order[k] = k;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pj[a].p->N > pj[b].p->N; });
+    const std::vector<int> order = job_order(pj);
     cudaStream_t caller = static_cast<cudaStream_t>(stream);
     if (!cuda_ok(cudaEventRecord(J->start, caller), "cudaEventRecord")) return OBE_ERR_CUDA;
     long long launches = 0;
@@ -892,12 +918,8 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
         if (q.j->n_traj > 0) {
             if (!cuda_ok(cudaMemcpyAsync(q.d, q.cb.bytes.data(), q.cb.bytes.size(), cudaMemcpyHostToDevice, js), "cudaMemcpyAsync(args)"))
                 return OBE_ERR_CUDA;
-            st = solve_device(q.p, q.j->opt, q.j->n_traj, q.j->d_rho0, q.p->N, q.j->n_param_slots, q.j->param_slots,
-                              q.j->d_param_values, 0, nullptr, nullptr, q.j->time_count,
-                              q.j->time_count * q.j->width * (q.cplx ? 2 : 1), q.j->d_values, nullptr, q.j->d_stats,
-                              reinterpret_cast<TrajErr*>(q.d + q.errs_off), q.d, q.cb, q.save_times,
-                              static_cast<unsigned long long*>(q.p->d_counter), js);
-            if (st != OBE_OK) return fail(k, st);
+            st = launch_job(q, js);
+            if (st != OBE_OK) return job_fail(k, st);
             launches += g_launches;
             g_launches = 0;
         }
@@ -905,6 +927,124 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
         if (!cuda_ok(cudaStreamWaitEvent(caller, J->done[r], 0), "cudaStreamWaitEvent")) return OBE_ERR_CUDA;
     }
     g_launches = launches;
+    return OBE_OK;
+}
+
+// The heterogeneous batch recorded once as a CUDA graph: argument blocks in graph-owned device
+// memory, the queue resets and per-plan kernels captured on forked branches.
+struct obe_multi_graph {
+    int device = 0;
+    std::vector<void*> bufs;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+};
+
+void obe_multi_graph_destroy(obe_multi_graph* G) {
+    if (!G) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(G->device);
+    if (G->exec) cudaGraphExecDestroy(G->exec);
+    if (G->graph) cudaGraphDestroy(G->graph);
+    for (cudaEvent_t e : G->events) cudaEventDestroy(e);
+    for (cudaStream_t st : G->streams) cudaStreamDestroy(st);
+    for (void* b : G->bufs) cudaFree(b);
+    cudaSetDevice(cur);
+    delete G;
+}
+
+obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe_multi_graph** out) {
+    g_launches = 0;
+    if (!out) { set_error("null argument"); return OBE_ERR_INVALID; }
+    *out = nullptr;
+    if (n_jobs < 1 || n_jobs > OBE_MAX_JOBS) {
+        set_error("n_jobs must be between 1 and " + std::to_string(OBE_MAX_JOBS));
+        return OBE_ERR_INVALID;
+    }
+    if (!jobs) { set_error("null argument"); return OBE_ERR_INVALID; }
+    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::vector<PreparedJob> pj;
+    obe_status st = prepare_jobs(n_jobs, jobs, pj);
+    if (st != OBE_OK) return st;
+    auto* G = new obe_multi_graph();
+    auto bail = [&](obe_status code) {
+        obe_multi_graph_destroy(G);
+        return code;
+    };
+    if (!cuda_ok(cudaGetDevice(&G->device), "cudaGetDevice")) return bail(OBE_ERR_CUDA);
+    // argument blocks copied once into memory the graph owns; the large systems' per-trajectory
+    // stage buffers allocated now, so that nothing allocates while the launches are recorded
+    for (int k = 0; k < n_jobs; ++k) {
+        PreparedJob& q = pj[k];
+        void* b = nullptr;
+        if (!cuda_ok(cudaMalloc(&b, q.need), "cudaMalloc(graph arguments)")) return bail(OBE_ERR_CUDA);
+        G->bufs.push_back(b);
+        q.d = static_cast<unsigned char*>(b);
+        if (!cuda_ok(cudaMemcpy(q.d, q.cb.bytes.data(), q.cb.bytes.size(), cudaMemcpyHostToDevice), "cudaMemcpy(graph arguments)"))
+            return bail(OBE_ERR_CUDA);
+        if (q.shape.gstride > 0 && q.j->n_traj > 0) {
+            unsigned char* gk = nullptr;
+            if ((st = kscratch(q.p, q.shape.gstride * static_cast<size_t>(q.shape.blocks) * q.shape.gpb, &gk)) != OBE_OK)
+                return bail(job_fail(k, st));
+        }
+    }
+    cudaStream_t cs = nullptr;
+    if (!cuda_ok(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate")) return bail(OBE_ERR_CUDA);
+    G->streams.push_back(cs);
+    cudaEvent_t start = nullptr;
+    if (!cuda_ok(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "cudaEventCreate")) return bail(OBE_ERR_CUDA);
+    G->events.push_back(start);
+    for (int k = 0; k < n_jobs; ++k) {
+        cudaStream_t js = nullptr;
+        cudaEvent_t done = nullptr;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&js, cudaStreamNonBlocking), "cudaStreamCreate")) return bail(OBE_ERR_CUDA);
+        G->streams.push_back(js);
+        if (!cuda_ok(cudaEventCreateWithFlags(&done, cudaEventDisableTiming), "cudaEventCreate")) return bail(OBE_ERR_CUDA);
+        G->events.push_back(done);
+    }
+    const std::vector<int> order = job_order(pj);
+    if (!cuda_ok(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture")) return bail(OBE_ERR_CUDA);
+    obe_status rec = OBE_OK;
+    long long launches = 0;
+    if (!cuda_ok(cudaEventRecord(start, cs), "cudaEventRecord")) rec = OBE_ERR_CUDA;
+    for (int r = 0; r < n_jobs && rec == OBE_OK; ++r) {
+        const int k = order[r];
+        cudaStream_t js = G->streams[1 + r];
+        cudaEvent_t done = G->events[1 + r];
+        if (!cuda_ok(cudaStreamWaitEvent(js, start, 0), "cudaStreamWaitEvent")) { rec = OBE_ERR_CUDA; break; }
+        if (pj[k].j->n_traj > 0) {
+            g_launches = 0;
+            if ((rec = launch_job(pj[k], js)) != OBE_OK) { rec = job_fail(k, rec); break; }
+            launches += g_launches;
+        }
+        if (!cuda_ok(cudaEventRecord(done, js), "cudaEventRecord") || !cuda_ok(cudaStreamWaitEvent(cs, done, 0), "cudaStreamWaitEvent"))
+            rec = OBE_ERR_CUDA;
+    }
+    const std::string rec_msg = last_error_cstr();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+    G->graph = graph;
+    if (rec != OBE_OK) {
+        set_error(rec_msg);
+        return bail(rec);
+    }
+    if (!cuda_ok(ce, "cudaStreamEndCapture")) return bail(OBE_ERR_CUDA);
+    if (!cuda_ok(cudaGraphInstantiate(&G->exec, G->graph, 0ull), "cudaGraphInstantiate")) return bail(OBE_ERR_CUDA);
+    G->launches = launches;
+    *out = G;
+    g_launches = 0;
+    set_error("");
+    return OBE_OK;
+}
+
+obe_status obe_multi_graph_launch(obe_multi_graph* G, void* stream) {
+    g_launches = 0;
+    if (!G || !G->exec) { set_error("null argument"); return OBE_ERR_INVALID; }
+    if (!cuda_ok(cudaGraphLaunch(G->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch")) return OBE_ERR_CUDA;
+    g_launches = G->launches;
     return OBE_OK;
 }
 

@@ -343,28 +343,54 @@ typedef struct {
 obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, void* stream);
 
 /*
+ * The heterogeneous batch recorded once as a CUDA graph (no counterpart in the reference):
+ * obe_multi_graph_create validates the jobs as obe_solve_multi_device does (same messages),
+ * copies their per-call arguments into device memory the graph owns and records the work-queue
+ * resets and the per-plan kernels (each plan on its own branch, largest systems first);
+ * obe_multi_graph_launch replays the whole batch as one graph launch on `stream`.  The graph
+ * keeps the jobs' device buffers by address: refill d_rho0 / d_param_values between launches and
+ * read d_values / d_stats after them (a trajectory's failure is its stats' status).  The jobs'
+ * host arrays (options, parameter slots) are read at creation only.  The plans must outlive the
+ * graph, and a plan's queue counter and stage buffers serve one solve at a time: no other call
+ * may use its plans while a launch is in flight.  obe_last_launch_count() after a launch: the
+ * kernels it ran.
+ */
+typedef struct obe_multi_graph obe_multi_graph;
+obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe_multi_graph** out_graph);
+obe_status obe_multi_graph_launch(obe_multi_graph* graph, void* stream);
+void obe_multi_graph_destroy(obe_multi_graph* graph);
+
+/*
  * Gradients (no counterpart in the reference, whose Rust crate has no gradient path): the
- * discrete adjoint of the double-precision adaptive solve with its step sequence frozen, for
- * final weighted integrals (output_when="final", saveat None) and final populations, with
- * respect to base parameter slots and the initial state.  Device pointers, asynchronous on
- * `stream`; every system the solver takes (up to 90 states, a plan width of 256 threads or
- * fewer), dopri5/tsit5, no stop event.
+ * discrete adjoint of the adaptive solve with its step sequence frozen, for final weighted
+ * integrals (output_when="final", saveat None) and final populations, with respect to base
+ * parameter slots and the initial state.  Device pointers, asynchronous on `stream`; every
+ * system the solver takes (up to 90 states, a plan width of 256 threads or fewer), dopri5/tsit5,
+ * precision fp64 or mixed (the mixed form's tape holds single-precision records and its reverse
+ * sweep runs the transposed and parameter products in single precision, accumulating in double),
+ * with or without a stop event (the event step maps to the dense output at the event time; the
+ * event time's own dependence on the state and parameters is included).
  *
  * obe_grad_forward is obe_solve_batch_device that also records a tape per trajectory into d_tape
  * (caller-owned, n_traj * obe_grad_tape_doubles(plan, max_steps, checkpoint_every) doubles).
  * checkpoint_every = 0: every accepted step with its start time, size, start state and stage
- * derivatives 1-6 (obe_grad_tape_doubles_per_step doubles each).  checkpoint_every = C > 0: the
- * start time and size of every step and the start state of every C-th step; the reverse sweep
- * then replays each segment of C steps from its start state (frozen steps, double precision)
- * into a library-owned buffer of C full records per resident trajectory before sweeping it --
- * one more forward's arithmetic for a tape of 2 + N / C doubles per step.  A trajectory with more
- * than max_steps accepted steps ends with a status whose message asks for a larger max_steps.
- * obe_grad_backward runs the reverse sweep on that tape (same max_steps and checkpoint_every):
- * given d(loss)/d(outputs) in d_out_grad ([n_traj][width]), it writes d(loss)/d(parameter) to
- * d_param_grad ([n_traj][n_grad], for the base slots grad_slots, at most 8) and, if d_rho0_grad
- * is not NULL, d(loss)/d(packed rho0) to d_rho0_grad ([n_traj][N]).  d_adj_status ([n_traj]):
- * 0 = ok, 1 = a helper function or table received an argument that depends on a differentiated
- * parameter (not differentiable here), 2 = the forward trajectory failed or overflowed the tape.
+ * derivatives 1-6 (obe_grad_tape_doubles_per_step doubles each; a double-precision trajectory
+ * that a stop event ends also keeps that step's seventh stage in the next record, so it needs
+ * one record more).  checkpoint_every = C > 0: the start time and size of every step and the
+ * start state of every C-th step; the reverse sweep then replays each segment of C steps from
+ * its start state (frozen steps; double precision, or the mixed form's own single-precision
+ * deviation form) into a library-owned buffer of C records per resident trajectory before
+ * sweeping it -- one more forward's arithmetic for a tape of 2 + N / C doubles per step.  A
+ * trajectory with more than max_steps accepted steps ends with a status whose message asks for a
+ * larger max_steps.
+ * obe_grad_backward runs the reverse sweep on that tape (same options, max_steps and
+ * checkpoint_every): given d(loss)/d(outputs) in d_out_grad ([n_traj][width]), it writes
+ * d(loss)/d(parameter) to d_param_grad ([n_traj][n_grad], for the base slots grad_slots, at most
+ * 8) and, if d_rho0_grad is not NULL, d(loss)/d(packed rho0) to d_rho0_grad ([n_traj][N]).
+ * d_adj_status ([n_traj]): 0 = ok, 1 = a helper function or table received an argument that
+ * depends on a differentiated parameter (not differentiable here), 2 = the forward trajectory
+ * failed or overflowed the tape, 3 = the stop event's function has a zero time derivative at the
+ * crossing.
  * The parameter arguments must be those of the forward call.
  */
 int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan);

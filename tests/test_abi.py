@@ -137,6 +137,13 @@ def test_multi_batch_validation_before_device_work(golden):
     assert _abi.last_error(lib) == "job 1: plan already used by job 0 (one job per plan)"
     assert lib.obe_solve_multi_device(_abi.MAX_JOBS + 1, arr, None) == _abi.OBE_ERR_INVALID
     assert lib.obe_solve_multi_device(0, None, None) == _abi.OBE_OK
+    # the graph-recorded form validates the same way before touching the device
+    h = ctypes.c_void_p()
+    assert lib.obe_multi_graph_create(2, arr, ctypes.byref(h)) == _abi.OBE_ERR_INVALID and not h.value
+    assert _abi.last_error(lib) == "job 1: plan already used by job 0 (one job per plan)"
+    assert lib.obe_multi_graph_create(0, arr, ctypes.byref(h)) == _abi.OBE_ERR_INVALID and not h.value
+    assert lib.obe_multi_graph_launch(None, None) == _abi.OBE_ERR_INVALID
+    lib.obe_multi_graph_destroy(None)
 
 
 def test_launch_shape_validation_on_host(golden):

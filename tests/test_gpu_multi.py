@@ -116,3 +116,48 @@ def test_multi_batch_errors(jobs):
     empty = dict(j16, packed_rho0_batch=np.zeros((0, 256)), parameter_batch=np.zeros((0, 4), complex))
     out = api.solve_lindblad_multi_batch_ode_py([empty, j39])
     assert out[0][3] == 0 and out[1][2] == 1
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_multi_graph_replays_the_batch(jobs, precision):
+    """obe_multi_graph: the batch recorded once as a CUDA graph gives the immediate call's values
+    and statistics bit for bit, and a second launch after the inputs changed in place gives the
+    immediate call's results for the new inputs."""
+    torch = pytest.importorskip("torch")
+    from centrex_tlf_gb300.native import MultiGraph, multi_solve_device
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    built = []
+    for _, job, _ in jobs:
+        plan = job["plan"].native
+        opts = plan.options(t0=job["t0"], t1=job["t1"], abstol=job["abstol"], reltol=job["reltol"], dt=job["dt"],
+                            saveat=None, save_start=True, maxiters=100000, solver="tsit5", output="excited_population",
+                            output_indices=None, output_when="final", integral_weights=job["integral_weights"],
+                            stop_event=job["stop_event"], precision=precision)
+        b = job["packed_rho0_batch"].shape[0]
+        built.append(dict(plan=plan, opts=opts, b=b, slots=job["parameter_slot_indices"],
+                          rho=torch.from_numpy(job["packed_rho0_batch"]).to(dev),
+                          par=torch.from_numpy(np.ascontiguousarray(job["parameter_batch"]).view(np.float64).reshape(-1)).to(dev),
+                          val=torch.zeros(b, dtype=torch.float64, device=dev), st=torch.zeros(b * 6, dtype=torch.int64, device=dev),
+                          ref=torch.zeros(b, dtype=torch.float64, device=dev), rst=torch.zeros(b * 6, dtype=torch.int64, device=dev)))
+
+    def spec(out, stats):
+        return [(x["plan"], x["opts"], x["b"], x["rho"].data_ptr(), x["slots"], x["par"].data_ptr(), 1, x[out].data_ptr(),
+                 x[stats].data_ptr()) for x in built]
+
+    graph = MultiGraph(spec("val", "st"))
+    try:
+        for rep in range(2):
+            if rep == 1:
+                for x in built:
+                    x["par"].view(x["b"], -1, 2)[:, 0, 0] *= 1.3  # the first scanned slot: a Rabi rate
+            assert graph.launch(stream) == len(built)
+            multi_solve_device(spec("ref", "rst"), stream)
+            torch.cuda.synchronize()
+            for x in built:
+                assert torch.equal(x["val"], x["ref"])
+                assert torch.equal(x["st"], x["rst"])
+                assert not bool((x["st"].view(-1, 6)[:, 3] >> 32).any())
+    finally:
+        graph.close()
