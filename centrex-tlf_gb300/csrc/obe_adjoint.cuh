@@ -247,6 +247,7 @@ struct AdjLayout {
     size_t T4, cv;               // the mixed replay's deviation-form formula table and stage class values
     size_t gbytes;  // large systems: bytes of the group's device-memory slice (MU, YB, S)
     bool glob;
+    bool s_shared;  // the class sums S in shared memory (always below 256 threads; above, when they fit)
 };
 
 // stages: 6, or 7 when a stop event can end the solve (the event step's dense output reads the
@@ -280,9 +281,19 @@ __host__ __device__ inline AdjLayout adj_layout(int n, int N, int n_formula, int
     L.dcls = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 16);
     L.dcls32 = o; o = align16(o + 6 * 2 * nc * kMaxGrad * 8);
     L.cv = o; o = align16(o + 5 * 2 * nc * 16);
-    L.S = om; om = align16(om + 2 * nc * static_cast<size_t>(tpt) * 16);
     L.red = o; o = align16(o + (tpt / 32 + 4) * 8);
     L.traj = o; o = align16(o + 16);
+    // the class sums take read-modify-writes at every formula end: shared memory whenever they fit
+    // (large systems: within a 200 KB group, one group per CTA)
+    const size_t s_bytes = align16(2 * nc * static_cast<size_t>(tpt) * 16);
+    L.s_shared = !L.glob || o + s_bytes <= 200 * 1024;
+    if (L.s_shared) {
+        L.S = o;
+        o += s_bytes;
+    } else {
+        L.S = og;
+        og += s_bytes;
+    }
     L.bytes = o;
     L.gbytes = og;
     return L;
@@ -370,7 +381,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     double2* s_cdyn = reinterpret_cast<double2*>(gb + Lay.cdyn);
     double2* s_ddyn = reinterpret_cast<double2*>(gb + Lay.ddyn);
     double2* s_dcls = reinterpret_cast<double2*>(gb + Lay.dcls);
-    double2* s_S = reinterpret_cast<double2*>(gm + Lay.S);
+    double2* s_S = reinterpret_cast<double2*>((Lay.s_shared ? gb : gm) + Lay.S);
     double* s_red = reinterpret_cast<double*>(gb + Lay.red);
     long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
     const int ns = P.n_slots > 0 ? P.n_slots : 1;
@@ -394,7 +405,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
     float* s_MU32 = reinterpret_cast<float*>(gm + Lay.MU);
     float* s_YB32 = reinterpret_cast<float*>(gm + Lay.YB32);
     float2* s_dcls32 = reinterpret_cast<float2*>(gb + Lay.dcls32);
-    float2* s_S32 = reinterpret_cast<float2*>(gm + Lay.S);
+    float2* s_S32 = reinterpret_cast<float2*>((Lay.s_shared ? gb : gm) + Lay.S);
     const bool integral = A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL;
     // solution weights b (row 5 of the stage table) and stage times c_s
     double bw[6], cs[6];
@@ -808,23 +819,64 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     const int row = s < 6 ? s : 5;
                     // lambda_s and the stage input Y_s = y_n + h (c_s k_1 + sum_l a_sl d_l) (the seventh
                     // stage's input is y_{n+1}: row 5, the solution weights)
-                    for (int i = lt; i < N; i += TPT) {
-                        float lam = hf * wf[s] * s_YB32[i];
-                        for (int m = s + 1; m < 6; ++m) lam = fmaf(hf * kTabF.a[M][m - 1][s], s_MU32[static_cast<size_t>(m) * N + i], lam);
-                        if (n_st == 7 && s < 6) lam = fmaf(hf * kTabF.a[M][5][s], s_MU32[static_cast<size_t>(6) * N + i], lam);
+                    // element i's lambda_s and Y_s; with the buffers in device memory (256 threads) the
+                    // loads of kCh elements are issued before their first use (same arithmetic)
+                    auto stage_in = [&](int i, float ybv, const float* muv, float yv, float k1v, const float* dfv) {
+                        float lam = hf * wf[s] * ybv;
+                        for (int m = s + 1; m < 6; ++m) lam = fmaf(hf * kTabF.a[M][m - 1][s], muv[m - 1], lam);
+                        if (n_st == 7 && s < 6) lam = fmaf(hf * kTabF.a[M][5][s], muv[5], lam);
                         // diagonal entries (i < n) fill the whole complex slot: the double-precision
                         // replay reuses these buffers
                         if (i < n) s_LS32[i] = make_float2(lam, 0.f);
                         else s_LS32f[gslot64(i, n)] = lam;
-                        float yin = yf[i];
+                        float yin = yv;
                         if (s > 0) {
                             const int r = s - 1;
-                            float acc = kTabF.csum[M][r] * k1f[i];
-                            for (int l = 1; l < s; ++l) acc = fmaf(kTabF.a[M][r][l], df[static_cast<size_t>(l - 1) * N + i], acc);
+                            float acc = kTabF.csum[M][r] * k1v;
+                            for (int l = 1; l < s; ++l) acc = fmaf(kTabF.a[M][r][l], dfv[l - 1], acc);
                             yin = fmaf(hf, acc, yin);
                         }
                         if (i < n) s_G32[i] = make_float2(yin, 0.f);
                         else s_G32f[gslot64(i, n)] = yin;
+                    };
+                    if constexpr (TPT >= 256) {
+                        constexpr int kCh = 4;
+                        for (int i0 = lt; i0 < N; i0 += kCh * TPT) {
+                            float muv[kCh][6], dfv[kCh][5], ybv[kCh], yv[kCh], k1v[kCh];
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c) {
+                                const int i = i0 + c * TPT;
+                                const bool in = i < N;
+                                ybv[c] = in ? s_YB32[i] : 0.f;
+                                yv[c] = in ? yf[i] : 0.f;
+                                k1v[c] = in ? k1f[i] : 0.f;
+#pragma unroll
+                                for (int m = 1; m < 7; ++m)
+                                    muv[c][m - 1] = (in && m > s && (m < 6 || n_st == 7)) ? s_MU32[static_cast<size_t>(m) * N + i] : 0.f;
+#pragma unroll
+                                for (int l = 1; l < 6; ++l) dfv[c][l - 1] = (in && l < s) ? df[static_cast<size_t>(l - 1) * N + i] : 0.f;
+                            }
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c)
+                                if (i0 + c * TPT < N) stage_in(i0 + c * TPT, ybv[c], muv[c], yv[c], k1v[c], dfv[c]);
+                        }
+                    } else {
+                        for (int i = lt; i < N; i += TPT) {
+                            float lam = hf * wf[s] * s_YB32[i];
+                            for (int m = s + 1; m < 6; ++m) lam = fmaf(hf * kTabF.a[M][m - 1][s], s_MU32[static_cast<size_t>(m) * N + i], lam);
+                            if (n_st == 7 && s < 6) lam = fmaf(hf * kTabF.a[M][5][s], s_MU32[static_cast<size_t>(6) * N + i], lam);
+                            if (i < n) s_LS32[i] = make_float2(lam, 0.f);
+                            else s_LS32f[gslot64(i, n)] = lam;
+                            float yin = yf[i];
+                            if (s > 0) {
+                                const int r = s - 1;
+                                float acc = kTabF.csum[M][r] * k1f[i];
+                                for (int l = 1; l < s; ++l) acc = fmaf(kTabF.a[M][r][l], df[static_cast<size_t>(l - 1) * N + i], acc);
+                                yin = fmaf(hf, acc, yin);
+                            }
+                            if (i < n) s_G32[i] = make_float2(yin, 0.f);
+                            else s_G32f[gslot64(i, n)] = yin;
+                        }
                     }
                     if (F > S) {
                         fill_formulas<TPT>(P, 1 + S, 1 + F, s_cstat, s_cdyn + row * nd, s_tab, lt);
@@ -893,10 +945,37 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 }
                 for (int q = 0; q < ng; ++q) pbar[q] += f2d(pst[q]);
                 // ybar_n = ybar_{n+1} + sum_s mu_s (the stage sum in single precision)
-                for (int i = lt; i < N; i += TPT) {
-                    float acc = 0.f;
-                    for (int s = 0; s < n_st; ++s) acc += s_MU32[static_cast<size_t>(s) * N + i];
-                    ybar_add(i, f2d(acc));
+                if constexpr (TPT >= 256) {
+                    constexpr int kCh = 4;
+                    for (int i0 = lt; i0 < N; i0 += kCh * TPT) {
+                        float muv[kCh][7];
+                        double ybv[kCh];
+#pragma unroll
+                        for (int c = 0; c < kCh; ++c) {
+                            const int i = i0 + c * TPT;
+#pragma unroll
+                            for (int st7 = 0; st7 < 7; ++st7)
+                                muv[c][st7] = (i < N && st7 < n_st) ? s_MU32[static_cast<size_t>(st7) * N + i] : 0.f;
+                            ybv[c] = i < N ? s_YB[i] : 0.0;
+                        }
+#pragma unroll
+                        for (int c = 0; c < kCh; ++c) {
+                            const int i = i0 + c * TPT;
+                            if (i < N) {
+                                float acc = 0.f;
+                                for (int st7 = 0; st7 < n_st; ++st7) acc += muv[c][st7];
+                                const double r = ybv[c] + f2d(acc);
+                                s_YB[i] = r;
+                                s_YB32[i] = d2f(r);
+                            }
+                        }
+                    }
+                } else {
+                    for (int i = lt; i < N; i += TPT) {
+                        float acc = 0.f;
+                        for (int s = 0; s < n_st; ++s) acc += s_MU32[static_cast<size_t>(s) * N + i];
+                        ybar_add(i, f2d(acc));
+                    }
                 }
                 gsync<TPT>(g);
             } else {

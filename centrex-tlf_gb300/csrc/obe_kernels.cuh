@@ -1231,6 +1231,40 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                     // stage input deviation y_s - y_n = h (c_s k_1 + sum_j a_sj d_j), in single
                     // precision (small next to y_n); the solution y_{n+1} itself in double
                     const float csum = kTabF.csum[M][s];
+                    if constexpr (TPT >= 256) {
+                        // the stage buffers live in device memory here: each batch of kCh elements
+                        // issues all its loads before the first use, so the L2 round trips overlap
+                        // (the same arithmetic as below)
+                        constexpr int kCh = EPT < 8 ? EPT : 8;
+#pragma unroll
+                        for (int e0 = 0; e0 < EPT; e0 += kCh) {
+                            float kv[kCh][5], k1v[kCh];
+                            double k1d[kCh];
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c) {
+                                const int i = lt + (e0 + c) * TPT;
+                                const bool in = i < N;
+#pragma unroll
+                                for (int j = 1; j < 6; ++j)
+                                    kv[c][j - 1] = (in && j <= s) ? s_K32[static_cast<size_t>(j - 1) * N + i] : 0.f;
+                                k1v[c] = in ? s_k1f[i] : 0.f;
+                                k1d[c] = (in && s == 5) ? s_k1[i] : 0.0;
+                            }
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c) {
+                                const int e = e0 + c;
+                                const int i = lt + e * TPT;
+                                if (i < N) {
+                                    float acc = 0.f;
+#pragma unroll
+                                    for (int j = 1; j < 6; ++j)
+                                        if (j <= s) acc = fmaf(kTabF.a[M][s][j], kv[c][j - 1], acc);
+                                    if (s == 5) yn[e] = y[e] + h * (k1d[c] + f2d(acc));
+                                    s_G4f[gslot32(i, n)] = hf * fmaf(csum, k1v[c], acc);
+                                }
+                            }
+                        }
+                    } else {
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
@@ -1244,6 +1278,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             s_G4f[gslot32(i, n)] = hf * fmaf(csum, k1f, acc);
                         }
                     }
+                    }
                     if (s < 5) {  // stage 7 shares stage 6's time
                         gsync<TPT>(g);
                         fill_formulas_dev<TPT>(P.n_fiter, reinterpret_cast<const float4*>(s_fstream), s_cv + s * 2 * P.n_coeff,
@@ -1256,6 +1291,36 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 // error estimate from the deviations alone (the error weights sum to zero); the
                 // per-element ratios in single precision, their sum and the controller in double
                 float errf = 0.f;
+                if constexpr (TPT >= 256) {
+                    // device-memory stage buffers: batched loads, as in the stage inputs
+                    constexpr int kCh = EPT < 8 ? EPT : 8;
+#pragma unroll
+                    for (int e0 = 0; e0 < EPT; e0 += kCh) {
+                        float kv[kCh][6];
+#pragma unroll
+                        for (int c = 0; c < kCh; ++c) {
+                            const int i = lt + (e0 + c) * TPT;
+#pragma unroll
+                            for (int j = 1; j < 7; ++j) kv[c][j - 1] = i < N ? s_K32[static_cast<size_t>(j - 1) * N + i] : 0.f;
+                        }
+#pragma unroll
+                        for (int c = 0; c < kCh; ++c) {
+                            const int i = lt + (e0 + c) * TPT;
+                            if (i < N) {
+                                float acc = 0.f;
+#pragma unroll
+                                for (int j = 1; j < 7; ++j)
+                                    if (M == 1 || j != 1) acc = fmaf(kTabF.e[M][j], kv[c][j - 1], acc);
+                                const int gi = gslot32(i, n);
+                                const float yf = s_G4f[gi + 2];
+                                const float ynf = yf + s_G4f[gi];
+                                const float sc = fmaf(fmaxf(fabsf(yf), fabsf(ynf)), rtolf, atolf);
+                                const float q = __fdividef(hf * acc, sc);
+                                errf = fmaf(q, q, errf);
+                            }
+                        }
+                    }
+                } else {
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
@@ -1271,6 +1336,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                         const float q = __fdividef(hf * acc, sc);
                         errf = fmaf(q, q, errf);
                     }
+                }
                 }
                 // warp-level sum in single precision, broadcast from lane 0 (fixed order)
 #pragma unroll
@@ -1526,6 +1592,33 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                     if (lt < P.n_dyn) s_cdyn[5 * nd + lt] = s_cdyn[4 * nd + lt];
                     const bool refresh = !last && ++since_refresh >= A.k1_refresh;
                     if (refresh) gsync<TPT>(g);  // the slot buffer below overlays the stage deviations
+                    if (TPT >= 256 && !refresh) {
+                        // first-same-as-last with device-memory stage buffers: batched loads
+                        constexpr int kCh = EPT < 8 ? EPT : 8;
+#pragma unroll
+                        for (int e0 = 0; e0 < EPT; e0 += kCh) {
+                            double k1d[kCh];
+                            float d7[kCh];
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c) {
+                                const int i = lt + (e0 + c) * TPT;
+                                k1d[c] = i < N ? s_k1[i] : 0.0;
+                                d7[c] = i < N ? s_K32[static_cast<size_t>(5) * N + i] : 0.f;
+                            }
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c) {
+                                const int e = e0 + c;
+                                const int i = lt + e * TPT;
+                                y[e] = yn[e];
+                                if (i < N) {
+                                    const double k = k1d[c] + f2d(d7[c]);
+                                    s_k1[i] = k;
+                                    s_k1f[i] = d2f(k);
+                                    s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
+                                }
+                            }
+                        }
+                    } else {
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
@@ -1541,6 +1634,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                                 s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
                             }
                         }
+                    }
                     }
                     if (refresh) {
                         since_refresh = 0;
