@@ -684,6 +684,17 @@ def run_gpu(args) -> None:
     mixed = args.precision != "fp64"
     peak = measure_gemm_peak(torch, dev, torch.float32 if mixed else torch.float64)
     clocks = sampler.summary(local)
+    # the HBM view of the same launch against the measured copy bandwidth (MEASURED_PEAKS.json,
+    # else the machine's fallback figure): how far the kernel is from being memory-bound
+    peaks_file = Path(__file__).resolve().parent / "MEASURED_PEAKS.json"
+    hbm_peak, hbm_src = 6800.0, "fallback"
+    if peaks_file.exists():
+        try:
+            hbm_peak, hbm_src = float(json.loads(peaks_file.read_text())["hbm_gbs"]), "measured"
+        except (ValueError, KeyError):
+            pass
+    traffic_launch = TRAFFIC_BYTES_PER_TRAJECTORY[args.precision] * b
+    hbm_achieved = traffic_launch / kernel_s / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sum(ms) / len(ms), "higher_is_better": True, "scaling": "weak",
@@ -703,7 +714,11 @@ def run_gpu(args) -> None:
                              f"{f_rhs}) / mean launch time; peak = cuBLAS "
                              + ("SGEMM (TF32 off: the FP32 pipe the mixed form's products run on)" if mixed else "DGEMM")
                              + " measured in this run (the driver's peak file has HBM and bf16 only); traffic = ncu DRAM "
-                             "read+write bytes per trajectory of this kernel, scaled to the launch"},
+                             "read+write bytes per trajectory of this kernel, scaled to the launch",
+                     "hbm": {"bound": "hbm", "achieved": hbm_achieved, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": hbm_achieved / hbm_peak, "traffic": traffic_launch,
+                             "peak_source": hbm_src + " copy bandwidth",
+                             "note": "DRAM bytes per launch (ncu) / mean launch time: the kernel is not HBM-bound"}},
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "fp64_gpu": ({"value": b * world * args.steps / total64_s, "unit": "trajectories/s",
                       "ms_per_step": sum(other[0]) / len(other[0]), "attempted_steps_per_launch": other[1],
