@@ -194,6 +194,7 @@ struct obe_plan {
     // device copy (uploaded on first use, per device)
     void* d_blob = nullptr;
     int d_device = -1;
+    uint64_t image_gen = 0;  // incremented with every device image uploaded (recorded graphs check it)
     obe::DevPlan dev{};
     // reusable device scratch of the host-pointer entry points
     void* d_scratch = nullptr;

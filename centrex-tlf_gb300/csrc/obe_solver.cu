@@ -154,6 +154,7 @@ obe_status upload_plan(obe_plan* p) {
     p->dev = P;
     p->d_blob = d;
     p->d_device = dev;
+    ++p->image_gen;
     return OBE_OK;
 }
 
@@ -502,7 +503,7 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
                         double* d_times, obe_traj_stats* d_stats, TrajErr* d_errs, unsigned char* d_blob_area,
                         const CallBlob& cb, const std::vector<double>& save_times, unsigned long long* d_counter,
                         cudaStream_t stream, double* d_tape = nullptr, long long tape_cap = 0, long long tape_stride = 0,
-                        int tape_ckpt = 0) {
+                        int tape_ckpt = 0, unsigned char* d_gscratch = nullptr) {
     CallArgs A;
     fill_call_args(A, o, save_times, cb, d_blob_area);
     A.n_traj = n_traj;
@@ -535,8 +536,10 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
     obe_status st = plan_launch(p->dev, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s, p->shape_gpb);
     if (st != OBE_OK) return st;
     if (s.gstride > 0) {
-        unsigned char* gk = nullptr;
-        if ((st = kscratch(p, s.gstride * static_cast<size_t>(s.blocks) * s.gpb, &gk)) != OBE_OK) return st;
+        // the large systems' per-trajectory stage buffers: the caller's (a recorded graph owns its
+        // own) or the plan's grow-only scratch
+        unsigned char* gk = d_gscratch;
+        if (!gk && (st = kscratch(p, s.gstride * static_cast<size_t>(s.blocks) * s.gpb, &gk)) != OBE_OK) return st;
         A.gscratch = gk;
         A.gstride = s.gstride;
     }
@@ -877,13 +880,14 @@ std::vector<int> job_order(const std::vector<PreparedJob>& pj) {
     return order;
 }
 
-// job q's solve on stream js (its argument block already at q.d)
-obe_status launch_job(PreparedJob& q, cudaStream_t js) {
+// job q's solve on stream js (its argument block already at q.d; d_gscratch: the large systems'
+// stage buffers, or null for the plan's own)
+obe_status launch_job(PreparedJob& q, cudaStream_t js, unsigned char* d_gscratch = nullptr) {
     return solve_device(q.p, q.j->opt, q.j->n_traj, q.j->d_rho0, q.p->N, q.j->n_param_slots, q.j->param_slots,
                         q.j->d_param_values, 0, nullptr, nullptr, q.j->time_count,
                         q.j->time_count * q.j->width * (q.cplx ? 2 : 1), q.j->d_values, nullptr, q.j->d_stats,
                         reinterpret_cast<TrajErr*>(q.d + q.errs_off), q.d, q.cb, q.save_times,
-                        static_cast<unsigned long long*>(q.p->d_counter), js);
+                        static_cast<unsigned long long*>(q.p->d_counter), js, nullptr, 0, 0, 0, d_gscratch);
 }
 }  // namespace
 
@@ -934,6 +938,9 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
 // memory, the queue resets and per-plan kernels captured on forked branches.
 struct obe_multi_graph {
     int device = 0;
+    // each plan and the generation of the device image it had when the launches were recorded (a
+    // plan laid out again gets a new image, which the recorded kernels do not see)
+    std::vector<std::pair<const obe_plan*, uint64_t>> images;
     std::vector<void*> bufs;
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
@@ -975,10 +982,13 @@ obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe
         return code;
     };
     if (!cuda_ok(cudaGetDevice(&G->device), "cudaGetDevice")) return bail(OBE_ERR_CUDA);
-    // argument blocks copied once into memory the graph owns; the large systems' per-trajectory
-    // stage buffers allocated now, so that nothing allocates while the launches are recorded
+    // argument blocks copied once into memory the graph owns, and the large systems' per-trajectory
+    // stage buffers allocated by the graph too (the plan's own grow and move with later calls), so
+    // that nothing allocates while the launches are recorded
+    std::vector<unsigned char*> gks(n_jobs, nullptr);
     for (int k = 0; k < n_jobs; ++k) {
         PreparedJob& q = pj[k];
+        G->images.emplace_back(q.p, q.p->image_gen);
         void* b = nullptr;
         if (!cuda_ok(cudaMalloc(&b, q.need), "cudaMalloc(graph arguments)")) return bail(OBE_ERR_CUDA);
         G->bufs.push_back(b);
@@ -986,9 +996,12 @@ obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe
         if (!cuda_ok(cudaMemcpy(q.d, q.cb.bytes.data(), q.cb.bytes.size(), cudaMemcpyHostToDevice), "cudaMemcpy(graph arguments)"))
             return bail(OBE_ERR_CUDA);
         if (q.shape.gstride > 0 && q.j->n_traj > 0) {
-            unsigned char* gk = nullptr;
-            if ((st = kscratch(q.p, q.shape.gstride * static_cast<size_t>(q.shape.blocks) * q.shape.gpb, &gk)) != OBE_OK)
-                return bail(job_fail(k, st));
+            void* gk = nullptr;
+            if (!cuda_ok(cudaMalloc(&gk, q.shape.gstride * static_cast<size_t>(q.shape.blocks) * q.shape.gpb),
+                         "cudaMalloc(graph stage buffers)"))
+                return bail(OBE_ERR_CUDA);
+            G->bufs.push_back(gk);
+            gks[k] = static_cast<unsigned char*>(gk);
         }
     }
     cudaStream_t cs = nullptr;
@@ -1017,7 +1030,7 @@ obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe
         if (!cuda_ok(cudaStreamWaitEvent(js, start, 0), "cudaStreamWaitEvent")) { rec = OBE_ERR_CUDA; break; }
         if (pj[k].j->n_traj > 0) {
             g_launches = 0;
-            if ((rec = launch_job(pj[k], js)) != OBE_OK) { rec = job_fail(k, rec); break; }
+            if ((rec = launch_job(pj[k], js, gks[k])) != OBE_OK) { rec = job_fail(k, rec); break; }
             launches += g_launches;
         }
         if (!cuda_ok(cudaEventRecord(done, js), "cudaEventRecord") || !cuda_ok(cudaStreamWaitEvent(cs, done, 0), "cudaStreamWaitEvent"))
@@ -1043,6 +1056,15 @@ obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe
 obe_status obe_multi_graph_launch(obe_multi_graph* G, void* stream) {
     g_launches = 0;
     if (!G || !G->exec) { set_error("null argument"); return OBE_ERR_INVALID; }
+    {
+        std::lock_guard<std::mutex> lock(g_plan_mutex);
+        for (const auto& im : G->images)
+            if (!im.first->d_blob || im.first->image_gen != im.second) {
+                set_error("a plan of this graph was laid out again (launch shape changed) since it was recorded: "
+                          "create the graph again");
+                return OBE_ERR_INVALID;
+            }
+    }
     if (!cuda_ok(cudaGraphLaunch(G->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch")) return OBE_ERR_CUDA;
     g_launches = G->launches;
     return OBE_OK;

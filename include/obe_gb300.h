@@ -350,10 +350,12 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
  * obe_multi_graph_launch replays the whole batch as one graph launch on `stream`.  The graph
  * keeps the jobs' device buffers by address: refill d_rho0 / d_param_values between launches and
  * read d_values / d_stats after them (a trajectory's failure is its stats' status).  The jobs'
- * host arrays (options, parameter slots) are read at creation only.  The plans must outlive the
- * graph, and a plan's queue counter and stage buffers serve one solve at a time: no other call
- * may use its plans while a launch is in flight.  obe_last_launch_count() after a launch: the
- * kernels it ran.
+ * host arrays (options, parameter slots) are read at creation only.  The graph owns its argument
+ * blocks and the large systems' stage buffers.  The plans must outlive the graph; a plan's queue
+ * counter serves one solve at a time, so no other call may use its plans while a launch is in
+ * flight; a plan whose launch shape changes (obe_plan_set_shape, obe_plan_autotune) gets a new
+ * device image, and a launch of a graph recorded before that fails with OBE_ERR_INVALID (record
+ * it again).  obe_last_launch_count() after a launch: the kernels it ran.
  */
 typedef struct obe_multi_graph obe_multi_graph;
 obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe_multi_graph** out_graph);
