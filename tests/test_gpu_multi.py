@@ -161,3 +161,63 @@ def test_multi_graph_replays_the_batch(jobs, precision):
                 assert not bool((x["st"].view(-1, 6)[:, 3] >> 32).any())
     finally:
         graph.close()
+
+
+def test_multi_graph_survives_other_calls_and_refuses_a_relaid_plan(jobs):
+    """The graph owns its stage buffers: a larger solve on the same 76-state plan between two
+    launches (which grows the plan's own buffers) leaves the graph's results unchanged.  A plan
+    laid out again (a new launch shape, hence a new device image) makes the graph refuse to
+    launch until it is recorded again."""
+    torch = pytest.importorskip("torch")
+    from centrex_tlf_gb300.native import MultiGraph
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    built = []
+    for _, job, _ in jobs:
+        plan = job["plan"].native
+        opts = plan.options(t0=job["t0"], t1=job["t1"], abstol=job["abstol"], reltol=job["reltol"], dt=job["dt"],
+                            saveat=None, save_start=True, maxiters=100000, solver="tsit5", output="excited_population",
+                            output_indices=None, output_when="final", integral_weights=job["integral_weights"],
+                            stop_event=job["stop_event"], precision="mixed")
+        b = job["packed_rho0_batch"].shape[0]
+        built.append(dict(plan=plan, opts=opts, b=b, slots=job["parameter_slot_indices"], job=job,
+                          rho=torch.from_numpy(job["packed_rho0_batch"]).to(dev),
+                          par=torch.from_numpy(np.ascontiguousarray(job["parameter_batch"]).view(np.float64).reshape(-1)).to(dev),
+                          val=torch.zeros(b, dtype=torch.float64, device=dev), st=torch.zeros(b * 6, dtype=torch.int64, device=dev)))
+    spec = [(x["plan"], x["opts"], x["b"], x["rho"].data_ptr(), x["slots"], x["par"].data_ptr(), 1, x["val"].data_ptr(),
+             x["st"].data_ptr()) for x in built]
+    graph = MultiGraph(spec)
+    try:
+        graph.launch(stream)
+        torch.cuda.synchronize()
+        first = [x["val"].clone() for x in built]
+        # a larger batch on the 76-state plan through the ordinary call
+        big = built[-1]
+        reps = 160 // big["b"] + 1
+        job = dict(big["job"], packed_rho0_batch=np.tile(big["job"]["packed_rho0_batch"], (reps, 1)),
+                   parameter_batch=np.tile(big["job"]["parameter_batch"], (reps, 1)))
+        api.solve_lindblad_batch_ode_py(**job, precision="mixed")
+        graph.launch(stream)
+        torch.cuda.synchronize()
+        for x, v in zip(built, first):
+            assert torch.equal(x["val"], v)
+        # a new launch shape for the 16-state plan: its device image is rebuilt
+        p16 = built[0]["plan"]
+        old = p16.shape()
+        p16.set_shape(64, 0)
+        with pytest.raises(ValueError, match="laid out again"):
+            graph.launch(stream)
+        p16.set_shape(*old)
+        with pytest.raises(ValueError, match="laid out again"):
+            graph.launch(stream)
+    finally:
+        graph.close()
+    graph = MultiGraph(spec)  # recorded again: launches
+    try:
+        assert graph.launch(stream) == len(built)
+        torch.cuda.synchronize()
+        for x, v in zip(built, first):
+            assert torch.equal(x["val"], v)
+    finally:
+        graph.close()
