@@ -392,7 +392,8 @@ def _mixed_fd_check(d, plan, op, p0, slots, t_span, output="excited_population",
         natural = np.abs(base) / np.maximum(np.abs(p0[:, k]), 1e-300)
         tol = rel * np.abs(fd) + floor * natural
         assert np.all(np.abs(grad[:, k] - fd) <= tol), (k, grad[:, k], fd, tol)
-        worst = max(worst, float(np.max(np.abs(grad[:, k] - fd) / np.maximum(np.abs(fd), 1e-300))))
+        worst = max(worst, float(np.max(np.abs(grad[:, k] - fd) / np.maximum(natural, 1e-300))))
+    print(f"mixed adjoint: max |grad - fd| / (|J| / |p|) = {worst:.2e}")
     return grad, worst
 
 
