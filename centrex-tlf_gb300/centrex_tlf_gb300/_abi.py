@@ -286,6 +286,10 @@ def load_library() -> ctypes.CDLL:
     lib.obe_grad_tape_doubles_per_step.restype = ctypes.c_int64
     lib.obe_grad_tape_doubles.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32]
     lib.obe_grad_tape_doubles.restype = ctypes.c_int64
+    lib.obe_grad_tape_doubles_per_step_for.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.obe_grad_tape_doubles_per_step_for.restype = ctypes.c_int64
+    lib.obe_grad_tape_doubles_for.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int32]
+    lib.obe_grad_tape_doubles_for.restype = ctypes.c_int64
     lib.obe_grad_forward.argtypes = [
         ctypes.c_void_p, ctypes.POINTER(ObeSolveOptions), ctypes.c_int64, ctypes.c_void_p, ctypes.c_int32, c_i64p,
         ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,

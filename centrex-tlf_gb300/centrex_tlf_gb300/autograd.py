@@ -31,6 +31,7 @@ from typing import Sequence
 import numpy as np
 import torch
 
+from . import _abi
 from ._options import INTEGRAL_OUTPUTS
 from .native import NativePlan
 
@@ -41,6 +42,11 @@ _ADJ_MESSAGES = {
     2: "the forward trajectory failed or ran past the tape",
     3: "the stop event's function has a zero time derivative at the crossing",
 }
+
+
+def _precision(opts) -> str:
+    """The form an options object solves in ("fp64" or "mixed")."""
+    return "mixed" if int(opts.opts.precision) == _abi.PRECISIONS["mixed"] else "fp64"
 
 
 class ForwardTape:
@@ -56,11 +62,12 @@ class ForwardTape:
         """The accepted steps (t_n, h_n) of every trajectory, as recorded."""
         st = self.stats.view(-1, 6).cpu().numpy()
         b = st.shape[0]
+        prec = _precision(self.opts) if self.opts is not None else "fp64"
         if self.checkpoint_every > 0:
-            per = self.plan.grad_tape_doubles(self.max_steps, self.checkpoint_every)
+            per = self.plan.grad_tape_doubles(self.max_steps, self.checkpoint_every, prec)
             tape = self.tape.view(b, per)[:, : 2 * self.max_steps].reshape(b, self.max_steps, 2).cpu().numpy()
         else:
-            per = self.plan.grad_tape_doubles_per_step()
+            per = self.plan.grad_tape_doubles_per_step(prec)
             tape = self.tape.view(b, self.max_steps, per)[:, :, :2].cpu().numpy()
         return [tape[k, : int(st[k, 0])] for k in range(b)]
 
@@ -70,7 +77,8 @@ class ForwardTape:
         return (st[:, 3] & 0xFFFFFFFF).astype(np.int32)
 
 
-def _checkpoint_every(plan: NativePlan, b: int, max_steps: int, requested: int | None, device=None) -> int:
+def _checkpoint_every(plan: NativePlan, b: int, max_steps: int, requested: int | None, device=None,
+                      precision: str = "fp64") -> int:
     """The full tape while it takes at most a quarter of the device's free memory (at least
     4 GiB), else a start state every 512 steps."""
     if requested is not None:
@@ -78,7 +86,7 @@ def _checkpoint_every(plan: NativePlan, b: int, max_steps: int, requested: int |
     budget = 4 << 30
     if device is not None and device.type == "cuda":
         budget = max(budget, torch.cuda.mem_get_info(device)[0] // 4)
-    return 0 if b * plan.grad_tape_doubles(max_steps, 0) * 8 <= budget else 512
+    return 0 if b * plan.grad_tape_doubles(max_steps, 0, precision) * 8 <= budget else 512
 
 
 def _forward(plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals: torch.Tensor, max_steps: int,
@@ -86,8 +94,9 @@ def _forward(plan: NativePlan, opts, rho0: torch.Tensor, slots: list[int], pvals
     b = rho0.shape[0]
     stream = torch.cuda.current_stream(rho0.device).cuda_stream
     while True:
-        ck = _checkpoint_every(plan, b, max_steps, checkpoint_every, rho0.device)
-        tape = torch.empty(b * plan.grad_tape_doubles(max_steps, ck), dtype=torch.float64, device=rho0.device)
+        prec = _precision(opts)
+        ck = _checkpoint_every(plan, b, max_steps, checkpoint_every, rho0.device, prec)
+        tape = torch.empty(b * plan.grad_tape_doubles(max_steps, ck, prec), dtype=torch.float64, device=rho0.device)
         values = torch.empty(b * opts.width, dtype=torch.float64, device=rho0.device)
         stats = torch.zeros(b * 6, dtype=torch.int64, device=rho0.device)
         plan.grad_forward(opts, b, rho0.data_ptr(), slots, pvals.data_ptr() if slots else None, max_steps,

@@ -246,17 +246,20 @@ class NativePlan:
         return cands
 
     # ---- gradients (obe_grad_forward / obe_grad_backward) -------------------------------
-    def grad_tape_doubles_per_step(self) -> int:
-        return int(self.lib.obe_grad_tape_doubles_per_step(self.handle))
+    def grad_tape_doubles_per_step(self, precision: str = "fp64") -> int:
+        """Doubles of one full-tape record of the form ``precision``."""
+        return int(self.lib.obe_grad_tape_doubles_per_step_for(self.handle, _abi.PRECISIONS[precision]))
 
-    def grad_tape_doubles(self, max_steps: int, checkpoint_every: int = 0) -> int:
-        """Doubles of one trajectory's tape (full records, or checkpoints every C steps)."""
-        return int(self.lib.obe_grad_tape_doubles(self.handle, int(max_steps), int(checkpoint_every)))
+    def grad_tape_doubles(self, max_steps: int, checkpoint_every: int = 0, precision: str = "fp64") -> int:
+        """Doubles of one trajectory's tape (full records, or checkpoints every C steps) of the
+        form ``precision`` (the mixed form's full records are single precision)."""
+        return int(self.lib.obe_grad_tape_doubles_for(self.handle, int(max_steps), int(checkpoint_every),
+                                                      _abi.PRECISIONS[precision]))
 
     def grad_forward(self, opts: SolveOptions, n_traj: int, d_rho0: int, param_slots, d_param_values: int | None,
                      max_steps: int, d_tape: int, d_values: int, d_stats: int, stream: int = 0,
                      checkpoint_every: int = 0) -> None:
-        """The double-precision batch solve that records the gradient tape (device pointers)."""
+        """The batch solve (opts' precision) that records the gradient tape (device pointers)."""
         slots = np.ascontiguousarray(np.asarray(param_slots if param_slots else [0], dtype=np.int64))
         n_param = 0 if d_param_values is None else int(slots.size)
         st = self.lib.obe_grad_forward(

@@ -1271,16 +1271,28 @@ static obe_status grad_check(const obe_plan* p, const obe_solve_options* o, int6
     return OBE_ERR_UNSUPPORTED;
 }
 
-int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan) {
+int64_t obe_grad_tape_doubles_per_step_for(const obe_plan* plan, int32_t precision) {
     if (!plan) return 0;
-    return static_cast<int64_t>(align16((2 + 7 * static_cast<size_t>(plan->N)) * 8) / 8);
+    // a double-precision record: t_n, h_n, y_n and K_1..K_6 in double; the mixed form's: t_n, h_n
+    // in double, then y_n, k_1, d_2..d_7 in single precision
+    const size_t N = static_cast<size_t>(plan->N);
+    const size_t bytes = precision == OBE_PRECISION_MIXED ? 16 + 32 * N : (2 + 7 * N) * 8;
+    return static_cast<int64_t>(align16(bytes) / 8);
+}
+
+int64_t obe_grad_tape_doubles_for(const obe_plan* plan, int64_t max_steps, int32_t checkpoint_every, int32_t precision) {
+    if (!plan || max_steps <= 0 || checkpoint_every < 0) return 0;
+    if (checkpoint_every == 0) return max_steps * obe_grad_tape_doubles_per_step_for(plan, precision);
+    const int64_t n_ck = (max_steps + checkpoint_every - 1) / checkpoint_every;
+    return static_cast<int64_t>(align16((2 * static_cast<size_t>(max_steps) + static_cast<size_t>(n_ck) * plan->N) * 8) / 8);
+}
+
+int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan) {
+    return obe_grad_tape_doubles_per_step_for(plan, OBE_PRECISION_FP64);
 }
 
 int64_t obe_grad_tape_doubles(const obe_plan* plan, int64_t max_steps, int32_t checkpoint_every) {
-    if (!plan || max_steps <= 0 || checkpoint_every < 0) return 0;
-    if (checkpoint_every == 0) return max_steps * obe_grad_tape_doubles_per_step(plan);
-    const int64_t n_ck = (max_steps + checkpoint_every - 1) / checkpoint_every;
-    return static_cast<int64_t>(align16((2 * static_cast<size_t>(max_steps) + static_cast<size_t>(n_ck) * plan->N) * 8) / 8);
+    return obe_grad_tape_doubles_for(plan, max_steps, checkpoint_every, OBE_PRECISION_FP64);
 }
 
 obe_status obe_grad_forward(const obe_plan* plan_c, const obe_solve_options* opt, int64_t n_traj, const double* d_rho0,
@@ -1312,8 +1324,8 @@ obe_status obe_grad_forward(const obe_plan* plan_c, const obe_solve_options* opt
     return solve_device(p, opt, n_traj, d_rho0, p->N, n_param_slots, param_slots, d_param_values, 0, nullptr, nullptr, 1, width,
                         d_values, nullptr, d_stats, reinterpret_cast<TrajErr*>(d + errs_off), d, cb, save_times,
                         static_cast<unsigned long long*>(p->d_counter), s, d_tape, max_steps,
-                        checkpoint_every > 0 ? obe_grad_tape_doubles(p, max_steps, checkpoint_every)
-                                             : obe_grad_tape_doubles_per_step(p),
+                        checkpoint_every > 0 ? obe_grad_tape_doubles_for(p, max_steps, checkpoint_every, opt->precision)
+                                             : obe_grad_tape_doubles_per_step_for(p, opt->precision),
                         checkpoint_every);
 }
 
@@ -1371,8 +1383,9 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     J.tape = d_tape;
     J.tape_cap = max_steps;
     J.ckpt = checkpoint_every;
-    J.rec_stride = obe_grad_tape_doubles_per_step(p);
-    J.tape_stride = checkpoint_every > 0 ? obe_grad_tape_doubles(p, max_steps, checkpoint_every) : J.rec_stride;
+    J.rec_stride = obe_grad_tape_doubles_per_step_for(p, opt->precision);
+    J.tape_stride = checkpoint_every > 0 ? obe_grad_tape_doubles_for(p, max_steps, checkpoint_every, opt->precision)
+                                         : J.rec_stride;
     J.fwd_stats = d_stats;
     J.out_grad = d_out_grad;
     J.param_grad = d_param_grad;

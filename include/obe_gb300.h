@@ -397,6 +397,12 @@ void obe_multi_graph_destroy(obe_multi_graph* graph);
  */
 int64_t obe_grad_tape_doubles_per_step(const obe_plan* plan);
 int64_t obe_grad_tape_doubles(const obe_plan* plan, int64_t max_steps, int32_t checkpoint_every);
+/* The same for the form `precision` (obe_precision): the mixed form's full-tape records are
+ * single precision, 2 + 4N doubles of room instead of 2 + 7N (the two functions above give the
+ * double-precision sizes, enough for either form); obe_grad_forward and obe_grad_backward lay
+ * the tape out with these. */
+int64_t obe_grad_tape_doubles_per_step_for(const obe_plan* plan, int32_t precision);
+int64_t obe_grad_tape_doubles_for(const obe_plan* plan, int64_t max_steps, int32_t checkpoint_every, int32_t precision);
 obe_status obe_grad_forward(const obe_plan* plan, const obe_solve_options* opt, int64_t n_traj,
                             const double* d_rho0, int32_t n_param_slots, const int64_t* param_slots,
                             const double* d_param_values, int64_t max_steps, int32_t checkpoint_every,

@@ -21,12 +21,12 @@ class _FakePlan:
     def __init__(self, N):
         self.N = N
 
-    def grad_tape_doubles_per_step(self):
-        return 2 + 7 * self.N
+    def grad_tape_doubles_per_step(self, precision="fp64"):
+        return 2 + (4 if precision == "mixed" else 7) * self.N
 
-    def grad_tape_doubles(self, max_steps, checkpoint_every=0):
+    def grad_tape_doubles(self, max_steps, checkpoint_every=0, precision="fp64"):
         if checkpoint_every == 0:
-            return max_steps * self.grad_tape_doubles_per_step()
+            return max_steps * self.grad_tape_doubles_per_step(precision)
         return 2 * max_steps + -(-max_steps // checkpoint_every) * self.N
 
 
@@ -87,3 +87,16 @@ def test_unsupported_outputs_are_refused_before_device_work(golden):
     for output in ("selected", "full", "rates"):
         with pytest.raises(NotImplementedError, match="final weighted integrals and final populations"):
             autograd.solve_batch_with_grad(plan, d["rho0_packed"], d["t_span"], p, [names.index("rabi")], output=output)
+
+
+def test_tape_sizes_of_the_two_forms(golden):
+    """The C ABI's tape sizes: the mixed form's full records are single precision (2 + 4N doubles
+    of room, 16-byte aligned), its checkpointed tape is the double-precision one."""
+    d = golden("plan_q1_16")
+    plan = NativePlan(d["payload"])
+    n2 = d["payload"]["n_states"] ** 2
+    assert plan.grad_tape_doubles_per_step() == 2 + 7 * n2
+    assert plan.grad_tape_doubles_per_step("mixed") == 2 + 4 * n2
+    assert plan.grad_tape_doubles(100, 0, "mixed") == 100 * (2 + 4 * n2)
+    assert plan.grad_tape_doubles(100, 16, "mixed") == plan.grad_tape_doubles(100, 16)
+    assert plan.lib.obe_grad_tape_doubles(plan.handle, 100, 0) == 100 * (2 + 7 * n2)
