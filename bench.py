@@ -451,18 +451,61 @@ def measure_hetero_gradient(torch, dev, total: int = 8192, precision: str = "mix
                                     stream.cuda_stream)
 
     per_plan = {}
+    grads = {}
+    ckpts = {}  # the tape length and checkpoint interval the wrapper chose per plan
+
+    def max_steps_of(j):
+        return 8192 if j["name"] == "plan_rc_76" else 2048
 
     def grad():
         for j, plan, opts, b, rho, par, val, st in runs:
             t = time.perf_counter()
             pt = torch.tensor(j["params"].real, dtype=torch.float64, device=dev, requires_grad=True)
-            out = solve_batch_with_grad(plan, rho, (0.0, j["t1"]), pt, j["slots"], dt=1e-3 / j["d"]["gamma"],
-                                        maxiters=1000000, integral_weights=j["weights"], stop_event=j["event"],
-                                        precision=precision, max_steps=8192 if j["name"] == "plan_rc_76" else 2048)
+            out, tape = solve_batch_with_grad(plan, rho, (0.0, j["t1"]), pt, j["slots"], dt=1e-3 / j["d"]["gamma"],
+                                              maxiters=1000000, integral_weights=j["weights"], stop_event=j["event"],
+                                              precision=precision, max_steps=max_steps_of(j), return_tape=True)
+            ckpts[j["name"]] = (tape.max_steps, tape.checkpoint_every)
             out.sum().backward()
             torch.cuda.synchronize()
             assert bool(torch.isfinite(pt.grad).all()), j["name"]
             per_plan[j["name"]] = 1e3 * (time.perf_counter() - t)
+            grads[j["name"]] = pt.grad
+
+    # the three plans' gradients concurrently: each plan's taped forward and reverse sweep on its
+    # own stream through the C ABI (obe_grad_forward / obe_grad_backward), one host synchronisation
+    # between the forwards and the reverse sweeps
+    conc = []
+    for j, plan, opts, b, rho, par, val, st in runs:
+        ms = max_steps_of(j)
+        conc.append(dict(j=j, plan=plan, opts=opts, b=b, rho=rho, ms=ms, stream=torch.cuda.Stream(dev),
+                         stats=torch.zeros(b * 6, dtype=torch.int64, device=dev),
+                         pv=torch.from_numpy(np.ascontiguousarray(j["params"]).view(np.float64).reshape(-1)).to(dev),
+                         out=torch.zeros(b, dtype=torch.float64, device=dev), og=torch.ones(b, dtype=torch.float64, device=dev),
+                         pg=torch.zeros(b, len(j["slots"]), dtype=torch.float64, device=dev),
+                         ast=torch.zeros(b, dtype=torch.int32, device=dev)))
+
+    def grad_concurrent():
+        for c in conc:
+            if "tape" not in c:
+                c["ms"], c["ck"] = ckpts[c["j"]["name"]]
+                c["tape"] = torch.empty(c["b"] * c["plan"].grad_tape_doubles(c["ms"], c["ck"], precision),
+                                        dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        for c in conc:
+            c["plan"].grad_forward(c["opts"], c["b"], c["rho"].data_ptr(), c["j"]["slots"], c["pv"].data_ptr(), c["ms"],
+                                   c["tape"].data_ptr(), c["out"].data_ptr(), c["stats"].data_ptr(), c["stream"].cuda_stream,
+                                   checkpoint_every=c["ck"])
+        torch.cuda.synchronize()
+        for c in conc:
+            stv = c["stats"].view(-1, 6).cpu().numpy()
+            assert not np.any(stv[:, 3] >> 32) and int(stv[:, 0].max()) < c["ms"], c["j"]["name"]
+            c["plan"].grad_backward(c["opts"], c["b"], c["rho"].data_ptr(), c["j"]["slots"], c["pv"].data_ptr(),
+                                    c["j"]["slots"], c["ms"], c["tape"].data_ptr(), c["stats"].data_ptr(), c["og"].data_ptr(),
+                                    c["pg"].data_ptr(), None, c["ast"].data_ptr(), c["stream"].cuda_stream,
+                                    checkpoint_every=c["ck"])
+        torch.cuda.synchronize()
+        for c in conc:
+            assert not bool(c["ast"].any()), c["j"]["name"]
 
     def timed(fn):
         best = float("inf")
@@ -479,15 +522,22 @@ def measure_hetero_gradient(torch, dev, total: int = 8192, precision: str = "mix
     t_fwd = timed(fwd)
     grad()  # untimed: device buffers (tapes, segment buffers) allocated once
     t_grad = timed(grad)
+    grad_concurrent()  # untimed, as above
+    t_conc = timed(grad_concurrent)
+    # the same gradients either way (each trajectory's arithmetic does not depend on the schedule)
+    same = all(torch.equal(c["pg"], grads[c["j"]["name"]]) for c in conc)
     return {"workload": f"{total} instances of the heterogeneous batch (16/39/76-state plans 6:3:1, end times "
                         "U[50, 300]/Γ by a Time() - t_end stop event); d(excited-population integral)/d(Rabi rates, "
                         "detunings, angle, t_end) per instance, Tsit5 discrete adjoint, " + precision,
             "instances": {j["name"]: j["count"] for j in spec}, "fwd_ms": 1e3 * t_fwd, "fwd_plus_grad_ms": 1e3 * t_grad,
             "grad_over_fwd": t_grad / t_fwd, "fwd_plus_grad_ms_per_plan": per_plan,
+            "concurrent_fwd_plus_grad_ms": 1e3 * t_conc, "concurrent_grad_over_fwd": t_conc / t_fwd,
+            "concurrent_gradients_identical": bool(same),
             "note": "forward = the three plans' plain solves one call each (device-resident); gradient = "
                     "solve_batch_with_grad + backward per plan (host-synchronised between the tape check and the "
-                    "reverse sweep), timed after one untimed call; the 76-state trajectories (checkpointed tape) "
-                    "dominate both"}
+                    "reverse sweep), timed after one untimed call; concurrent = the three plans' taped forwards on "
+                    "their own streams, one synchronisation, then their reverse sweeps on their streams; the "
+                    "76-state trajectories (checkpointed tape) dominate both"}
 
 
 def measure_effective(torch, dev, total: int = 4096, cpu_sample: int = 256, reps: int = 2) -> dict:
