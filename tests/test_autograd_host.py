@@ -100,3 +100,35 @@ def test_tape_sizes_of_the_two_forms(golden):
     assert plan.grad_tape_doubles(100, 0, "mixed") == 100 * (2 + 4 * n2)
     assert plan.grad_tape_doubles(100, 16, "mixed") == plan.grad_tape_doubles(100, 16)
     assert plan.lib.obe_grad_tape_doubles(plan.handle, 100, 0) == 100 * (2 + 7 * n2)
+
+
+def test_gradient_entry_points_refuse_unsupported_forms_on_the_host(golden):
+    """obe_grad_forward's checks run before any device work: fixed-step solvers, plans wider than
+    256 threads per trajectory and effective-Hamiltonian plans are refused with their messages.
+    (The tape pointer is a placeholder that the refused calls never reach.)"""
+    d = golden("plan_q1_16")
+    plan = NativePlan(d["payload"])
+    t0, t1 = d["t_span"]
+
+    def opts(pl, **kw):
+        base = dict(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / d["gamma"], saveat=None, save_start=True,
+                    maxiters=1000, solver="tsit5", output="excited_population", output_indices=None, output_when="final",
+                    integral_weights=[(13, 1.0)], stop_event=None)
+        base.update(kw)
+        return pl.options(**base)
+
+    with pytest.raises(NotImplementedError, match="adaptive solvers 'dopri5' and 'tsit5'"):
+        plan.grad_forward(opts(plan, solver="fixed_rk4"), 1, 0, [], None, 10, 16, 0, 0)
+    with pytest.raises(NotImplementedError, match="final weighted integrals"):
+        plan.grad_forward(opts(plan, output="populations", saveat=np.array([t1 / 2]), integral_weights=None), 1, 0, [],
+                          None, 10, 16, 0, 0)
+    big = NativePlan(golden("plan_rc_76")["payload"])
+    big.set_shape(512, 0)
+    with pytest.raises(NotImplementedError, match="256 threads per trajectory or fewer"):
+        big.grad_forward(opts(big, integral_weights=[(70, 1.0)]), 1, 0, [], None, 10, 16, 0, 0)
+    eff = NativePlan.from_effective(golden("plan_eff_r0")["plan"])
+    with pytest.raises(NotImplementedError, match="expanded_sparse plans"):
+        eff.grad_forward(eff.options(t0=0.0, t1=1e-6, abstol=1e-9, reltol=1e-7, dt=1e-10, saveat=None, save_start=True,
+                                     maxiters=1000, solver="tsit5", output="photon_integral", output_indices=None,
+                                     output_when="final", integral_weights=[(0, 1.0)], stop_event=None),
+                         1, 0, [], None, 10, 16, 0, 0)
