@@ -1,6 +1,7 @@
-// obe_adjoint.cuh -- discrete adjoint of the double-precision adaptive solve (gradients of the
-// final populations or of a weighted time integral with respect to base parameters and to the
-// initial state).  No counterpart in the reference, whose Rust crate has no gradient path.
+// obe_adjoint.cuh -- discrete adjoint of the adaptive solve, double precision or the mixed form
+// (gradients of the final populations or of a weighted time integral with respect to base
+// parameters and to the initial state, through stop events).  No counterpart in the reference,
+// whose Rust crate has no gradient path.
 //
 // The forward solve (integrate_kernel with a tape) records, for every accepted step n, its start
 // time t_n, size h_n, start state y_n and the stage derivatives K_1..K_6.  With the step sequence
@@ -16,10 +17,16 @@
 // coefficient programs.  The trapezoid rule of the integral outputs (sum over accepted steps of
 // (t_{n+1} - t_n)(w.y_n + w.y_{n+1}) / 2) adds its weights to ybar at both ends of each segment.
 //
+// A step that a stop event ends maps y_n to the dense output at the event time (a seven-stage map
+// with the interpolant's weights), and the event time's own dependence enters through the event
+// function's derivatives (dense_weights and the event seed below).  The mixed form sweeps its
+// single-precision tape with single-precision products and double-precision accumulation.
+//
 // One group of 32, 64, 128 or 256 threads per trajectory (the plan's width; above 45 states the
-// stage-derivative adjoints, ybar and the class sums move to a per-group slice of device memory
-// and the record streams are read from the plan's device image); the transposed product
-// L^T lambda runs on a second, input-major record stream built by the packer.
+// stage-derivative adjoints and ybar move to a per-group slice of device memory, and the class
+// sums too when shared memory cannot hold them, and the record streams are read from the plan's
+// device image); the transposed product L^T lambda runs on a second, input-major record stream
+// built by the packer.
 #pragma once
 
 #include "obe_kernels.cuh"
