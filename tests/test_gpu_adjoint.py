@@ -435,3 +435,49 @@ def test_mixed_form_gradients_of_the_76_state_system(golden):
     op = oracle.OraclePlan(d["payload"])
     p0 = np.array([[1.2 * g, 2.0 * g, 0.3 * g, -0.2 * g], [2.5 * g, 0.8 * g, -0.4 * g, 0.6 * g]])
     _mixed_fd_check(d, plan, op, p0, _slots(d, ("Ω0", "Ω1", "δ0", "δ1")), (0.0, 6.0 / g), checkpoint_every=16)
+
+
+def test_gradients_of_two_plans_on_concurrent_streams(golden):
+    """The C-ABI gradient entry points on two plans at once, each on its own stream (taped forwards,
+    one synchronisation, reverse sweeps): the same gradients as the autograd wrapper gives one plan
+    at a time (per-trajectory arithmetic does not depend on the schedule)."""
+    dev = torch.device("cuda", 0)
+    runs = []
+    for name, slot_names in (("plan_q1_16_tend", ("rabi", "detuning", "theta", "t_end")),
+                             ("plan_r0_39", ("rabi", "detuning", "theta", "t_end"))):
+        d = golden(name)
+        g = d["gamma"]
+        names = d["payload"]["parameter_graph"]["slot_names"]
+        slots = [names.index(s) for s in slot_names]
+        p0 = np.array([[1.5 * g, 0.5 * g, 0.4, 60.0 / g], [3.0 * g, -1.0 * g, 1.2, 45.0 / g], [0.5 * g, 2.0 * g, 2.2, 80.0 / g]])
+        plan = NativePlan(d["payload"])
+        w = [(i, 1.0) for i in d["excited_indices"]]
+        pt = torch.tensor(p0, dtype=torch.float64, device=dev, requires_grad=True)
+        out, tape = solve_batch_with_grad(plan, d["rho0_packed"], (0.0, 100.0 / g), pt, slots, dt=1e-3 / g,
+                                          integral_weights=w, stop_event=_t_end_event(names), precision="mixed",
+                                          return_tape=True)
+        out.sum().backward()
+        runs.append(dict(plan=plan, opts=tape.opts, b=3, slots=slots, ref=pt.grad, ms=tape.max_steps,
+                         ck=tape.checkpoint_every, rho=tape.rho0, pv=tape.pvals, stream=torch.cuda.Stream(dev)))
+    for r in runs:
+        r["tape"] = torch.empty(r["b"] * r["plan"].grad_tape_doubles(r["ms"], r["ck"], "mixed"), dtype=torch.float64,
+                                device=dev)
+        r["stats"] = torch.zeros(r["b"] * 6, dtype=torch.int64, device=dev)
+        r["out"] = torch.zeros(r["b"], dtype=torch.float64, device=dev)
+        r["pg"] = torch.zeros(r["b"], len(r["slots"]), dtype=torch.float64, device=dev)
+        r["ast"] = torch.zeros(r["b"], dtype=torch.int32, device=dev)
+        r["og"] = torch.ones(r["b"], dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    for r in runs:
+        r["plan"].grad_forward(r["opts"], r["b"], r["rho"].data_ptr(), r["slots"], r["pv"].data_ptr(), r["ms"],
+                               r["tape"].data_ptr(), r["out"].data_ptr(), r["stats"].data_ptr(), r["stream"].cuda_stream,
+                               checkpoint_every=r["ck"])
+    torch.cuda.synchronize()
+    for r in runs:
+        r["plan"].grad_backward(r["opts"], r["b"], r["rho"].data_ptr(), r["slots"], r["pv"].data_ptr(), r["slots"], r["ms"],
+                                r["tape"].data_ptr(), r["stats"].data_ptr(), r["og"].data_ptr(), r["pg"].data_ptr(), None,
+                                r["ast"].data_ptr(), r["stream"].cuda_stream, checkpoint_every=r["ck"])
+    torch.cuda.synchronize()
+    for r in runs:
+        assert not bool(r["ast"].any())
+        assert torch.equal(r["pg"], r["ref"])
