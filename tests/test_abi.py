@@ -176,11 +176,13 @@ def test_no_cpu_fallback_without_gpu(golden):
         api.solve_lindblad_ode_py(plan, d["rho0_packed"], 0.0, 0.5, 1e-10, 1e-8, 1e-3)
 
 
-def test_layout_roundtrip():
-    from centrex_tlf_gb300.lindblad import PackedHermitianLayout
+def test_packed_index_layout():
+    """The packed state ABI (state_layout.py:35-47): diagonal first, then (Re, Im) of the upper
+    triangle row by row; the shim's index function enumerates exactly those slots."""
+    from centrex_tlf_gb300._options import packed_upper_real_index
 
-    layout = PackedHermitianLayout(3)
-    rho = np.array([[0.2, 0.1 + 0.3j, -0.4j], [0.1 - 0.3j, 0.5, 0.2 - 0.1j], [0.4j, 0.2 + 0.1j, 0.3]])
-    packed = layout.pack(rho)
-    assert packed[3] == 0.1 and packed[4] == 0.3 and packed[5] == 0.0 and packed[6] == -0.4
-    np.testing.assert_allclose(layout.unpack(packed), rho)
+    n = 5
+    slots = [packed_upper_real_index(n, i, j) for i in range(n) for j in range(i + 1, n)]
+    assert slots == list(range(n, n * n, 2))
+    assert packed_upper_real_index(3, 0, 1) == 3 and packed_upper_real_index(3, 0, 2) == 5
+    assert packed_upper_real_index(3, 1, 2) == 7
