@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from the reference's own Python code.
 
-Run in a container that has the CeNTREX-TlF reference checkout (default path below, or the
-``CENTREX_REFERENCE`` environment variable):
+Run where a CeNTREX-TlF reference checkout exists, naming it with ``--reference PATH`` or the
+``CENTREX_REFERENCE`` environment variable (there is no default path):
 
-    python tests/golden/make_fixtures.py
+    python tests/golden/make_fixtures.py --reference PATH/TO/CeNTREX-TlF
 
 What it writes (all JSON through ``codec.py``):
 
@@ -49,7 +49,21 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
 import codec  # noqa: E402
 
-REFERENCE = Path(os.environ.get("CENTREX_REFERENCE", "/root/reference"))
+
+def _reference_path() -> Path:
+    """The reference checkout: ``--reference PATH`` or ``CENTREX_REFERENCE``; no default."""
+    if "--reference" in sys.argv:
+        i = sys.argv.index("--reference")
+        if i + 1 >= len(sys.argv):
+            raise SystemExit("--reference needs a path")
+        return Path(sys.argv[i + 1])
+    env = os.environ.get("CENTREX_REFERENCE")
+    if not env:
+        raise SystemExit("name the CeNTREX-TlF checkout with --reference PATH or CENTREX_REFERENCE")
+    return Path(env)
+
+
+REFERENCE = Path()  # set by _import_reference()
 
 # Γ for the benchmark configurations: 2π·1.56 MHz, passed explicitly to the builders.
 GAMMA = 2.0 * np.pi * 1.56e6
@@ -78,6 +92,8 @@ class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
 
 
 def _import_reference():
+    global REFERENCE
+    REFERENCE = _reference_path()
     sys.meta_path.insert(0, _StubFinder())
     sys.path.insert(0, str(REFERENCE))
     import sympy as smp  # noqa: F401
@@ -616,7 +632,7 @@ def fixed_step_kat() -> dict:
     dt 1e-3 as the reference run; the detuning grid is linspace(-2, 2, 201))."""
     import csv
 
-    res = REFERENCE / "benchmarks" / "fixed_step_solver_results"
+    res = _reference_path() / "benchmarks" / "fixed_step_solver_results"
     counts = {}
     runtime_table = (res / "fixed_step_solver_report.md").read_text().split("## Validation")[0]
     for line in runtime_table.splitlines():
@@ -644,7 +660,121 @@ def fixed_step_kat() -> dict:
     }
 
 
+# The coefficient helpers of the expression VM (centrex_tlf/lindblad/helper_functions.py:35-51),
+# each driving the Rabi coupling of a two-level system as a function of time, with the argument
+# sets of the reference's own helper tests (tests/lindblad/test_parameter_helper_wrappers.py)
+# and some arguments as parameter slots (so overrides reach them).
+def _helper_cases():
+    from centrex_tlf.lindblad import parameters as P
+
+    def tup(p, name, v):
+        return p.real(name, v)
+
+    return [
+        (1, "gaussian_2d", lambda p: P.gaussian_2d(p.time(), p.real("y", -0.2), p.real("amp", 1.3), 0.0, 0.1, 0.5, 0.7)),
+        (2, "gaussian_2d_rotated",
+         lambda p: P.gaussian_2d_rotated(p.time(), -0.2, 1.3, p.real("x0", 0.0), 0.1, 0.5, 0.7, p.real("angle", 0.3))),
+        (2, "gaussian_2d_theta", lambda p: P.gaussian_2d(p.time(), -0.1, 1.3, 0.0, 0.1, 0.5, 0.7, theta=0.3)),
+        (3, "phase_modulation", lambda p: P.phase_modulation(p.time(), p.real("beta", 3.8), p.real("omega_m", 1.2))),
+        (4, "square_wave", lambda p: P.square_wave(p.time(), p.real("omega_s", 1.2), 0.3)),
+        (5, "resonant_polarization_modulation",
+         lambda p: P.resonant_polarization_modulation(p.time(), p.real("gamma_m", 0.4), 1.2)),
+        (6, "sawtooth_wave", lambda p: P.sawtooth_wave(p.time(), 1.2, p.real("phase", 0.3))),
+        (7, "variable_on_off", lambda p: P.variable_on_off(p.time(), p.real("ton", 0.1), 0.3, 0.0)),
+        (8, "multipass_2d_intensity",
+         lambda p: P.multipass_2d_intensity(p.time(), -0.2, tup(p, "amps", (1.0, 0.5)), tup(p, "xlocs", (-0.3, 0.4)),
+                                            tup(p, "ylocs", (0.25, -0.1)), 0.7, 0.9)),
+        (9, "rabi_from_intensity", lambda p: 1e-5 * P.rabi_from_intensity(2.0 + p.time() * p.time(), p.real("coupling", 0.4))),
+        (10, "multipass_2d_rabi",
+         lambda p: 1e-5 * P.multipass_2d_rabi(p.time(), -0.2, tup(p, "amps", (1.0, 0.5)), tup(p, "xlocs", (-0.3, 0.4)),
+                                              tup(p, "ylocs", (0.25, -0.1)), 0.7, 0.9, 0.35)),
+        (11, "gaussian_beam_rabi",
+         lambda p: 1e-5 * P.gaussian_beam_rabi(p.time(), -0.2, p.real("intensity", 2.0), -0.3, 0.4, 0.7, 0.9, 0.35)),
+        (12, "variable_on_off_duty", lambda p: P.variable_on_off_duty(p.time(), p.real("duty", 0.25), 2.5, 0.1)),
+        (12, "variable_on_off_duty_invT", lambda p: P.variable_on_off_duty_invT(p.time(), 0.25, 1.3, 0.7)),
+        (13, "alternating_sign", lambda p: P.alternating_sign(p.time(), 0.0, p.real("width", 0.5))),
+        (14, "linear_interp",
+         lambda p: P.linear_interp(p.time(), tup(p, "grid", (0.0, 0.5, 1.0, 2.0)), tup(p, "values", (2.0, 3.0, 4.0, 3.5)))),
+        (15, "gaussian_1d", lambda p: P.gaussian_1d(p.time(), p.real("center", 0.0), 0.5)),
+        # the first two and last two intervals have equal slopes: there SciPy's three-point end
+        # derivative (Python helper) and plan.rs:55-56's end secant (Rust) coincide
+        (16, "pchip_interp",
+         lambda p: P.pchip_interp(p.time(), tup(p, "grid", (0.0, 0.5, 1.0, 1.5, 2.0, 2.5)),
+                                  tup(p, "values", (2.0, 3.0, 4.0, 2.5, 1.0, -0.5)))),
+    ]
+
+
+def save_helpers(centrex_tlf) -> None:
+    """``helpers.json``: one two-level plan per helper case, and packed states, times, overrides and
+    the reference's Python RHS (``structured_rhs``, reference_dense.py:68-77, whose coefficients come
+    from the reference's Python parameter graph and Hamiltonian fill, ir.py:882-1026) at times that
+    span several periods of the periodic helpers and the ends of the interpolation tables.  Times
+    within 1e-7 of a discontinuity (where the last bit decides the side) are left out.
+
+    Beyond the ends of a ``pchip_interp`` table the reference's two evaluators disagree: the Rust
+    VM holds the end values (rust/src/lindblad/plan.rs:90-100, eval.rs:306-311), SciPy's
+    ``PchipInterpolator(extrapolate=True)`` in the Python helper extrapolates the end cubic.  The
+    hot path is the Rust one, so those cases record the Python RHS at the clamped time (the
+    plan depends on time only through the helper) and say so in ``convention``."""
+    import sympy as smp
+    from centrex_tlf.lindblad.parameters import LindbladParameters
+    from centrex_tlf.lindblad.plan_static import prepare_lindblad_problem
+    from centrex_tlf.lindblad.reference_dense import structured_rhs
+    from centrex_tlf.lindblad.utils_setup import OBESystem
+
+    om, de = smp.symbols("Omega delta", real=True)
+    hamiltonian = smp.Matrix([[0, om / 2], [smp.conjugate(om) / 2, -de]])
+    c_array = np.zeros((1, 2, 2), dtype=np.complex128)
+    c_array[0, 0, 1] = np.sqrt(0.3)
+    zeros = np.zeros((2, 2), dtype=np.complex128)
+    times = [-1.93, -1.21, -0.77, -0.31, 0.0, 0.137, 0.41, 0.66, 0.93, 1.37, 1.81, 2.44, 3.1, 5.27]
+    rng = np.random.default_rng(1616)
+    out = []
+    for helper_id, name, build in _helper_cases():
+        system = OBESystem(ground=[], excited=[], QN=[], H_int=zeros, V_ref_int=zeros, couplings=[],
+                           H_symbolic=hamiltonian, C_array=c_array, system=None, coupling_symbols=[om, de],
+                           polarization_symbols=[])
+        params = LindbladParameters()
+        params.bind(om, build(params), finalize=False)
+        params.bind(de, 0.1)
+        prepared = prepare_lindblad_problem(system, params, backend="python", hamiltonian_representation="decomposed")
+        slots = prepared.parameter_graph["slot_names"]
+        scalar_slots = [i for i, v in enumerate(prepared.parameter_graph["base_values"]) if v.get("kind") != "tuple"]
+        overrides = [{}]
+        if scalar_slots:
+            k = scalar_slots[0]
+            base = prepared.parameter_graph["base_values"][k]["re"]
+            overrides.append({k: complex(base * 1.15 + 0.05)})
+        cases = []
+        for over in overrides:
+            view = _with_base_overrides(prepared, over)
+            for t in times:
+                rho = _hermitian(rng, 2, 0.5)
+                packed = prepared.layout.pack(rho)
+                t_eval, convention = float(t), "python"
+                if name == "pchip_interp" and not 0.0 <= t <= 2.5:
+                    t_eval, convention = min(max(float(t), 0.0), 2.5), "rust end clamp"
+                dy = structured_rhs(view, packed, t_eval)
+                jump = max(np.max(np.abs(structured_rhs(view, packed, t_eval + s) - dy)) for s in (-1e-7, 1e-7))
+                if jump > 1e-4 * max(float(np.max(np.abs(dy))), 1e-300):
+                    continue
+                cases.append({
+                    "t": float(t),
+                    "override_slots": np.array(sorted(over), dtype=np.int64),
+                    "override_values": np.array([over[k] for k in sorted(over)], dtype=np.complex128),
+                    "packed": packed,
+                    "structured": dy,
+                    "convention": convention,
+                })
+        out.append({"helper_id": helper_id, "name": name, "slot_names": slots, "payload": prepared.to_payload(),
+                    "cases": cases})
+    codec.save("helpers", {"helpers": out})
+
+
 def main() -> None:
+    if "--helpers" in sys.argv:
+        save_helpers(_import_reference())
+        return
     if "--kat-fixed-step" in sys.argv:
         codec.save("kat_fixed_step", fixed_step_kat())
         return
@@ -750,6 +880,7 @@ def main() -> None:
     save_multi(centrex_tlf)
     save_r2_38(centrex_tlf)
     save_effective(centrex_tlf)
+    save_helpers(centrex_tlf)
 
     # --- the native-boundary call contract of the reference's Python surface ----------------
     codec.save("ffi_calls", record_ffi_calls(centrex_tlf, q1, rho_q))

@@ -1,0 +1,66 @@
+"""The device expression VM's coefficient helpers (IDs 1-16 of
+centrex_tlf/lindblad/helper_functions.py:35-51, rust/src/lindblad/eval.rs) against the reference's
+Python evaluator and the oracle.
+
+Each case of ``tests/golden/helpers.json`` is a two-level plan whose Rabi coupling is one helper
+of time (tuple helpers included: multipass, linear and PCHIP interpolation).  Two routes through
+the device VM are checked:
+
+* the RHS kernel (``obe_rhs_eval``), whose coefficient evaluation is the complex VM: FP64 within
+  1e-10 of the case's largest element of the reference's Python RHS (CUDA's and Python's libm
+  differ in the last bits of exp/sin/cos), and the mixed form within 2e-5 (FP32 products);
+* whole solves (Dopri5, saveat 13 points on [0, 3]), which run the integrator's own coefficient
+  path (static subtrees hoisted into per-trajectory slots, the real-only VM when every slot is
+  real) at every stage: within 1e-9 of the oracle for the smooth helpers and 1e-6 for the
+  discontinuous ones (square wave, sawtooth, on/off gates, alternating sign).  At each jump the
+  controller rejects and retries, and rounding-level differences in h decide where the step past
+  the jump lands, so those solves agree to the solver's tolerance (rtol 1e-8) accumulated over
+  the ~30 jumps in [0, 3] (measured: 2.9e-7 for the 0.4-periodic on/off gate), not to rounding.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from centrex_tlf_gb300 import centrex_tlf_rust as api
+from centrex_tlf_gb300.native import NativePlan
+
+pytestmark = pytest.mark.gpu
+
+DISCONTINUOUS = {4, 6, 7, 12, 13}
+
+
+@pytest.mark.parametrize("index", range(18))
+def test_helper_rhs_matches_python_reference(golden, index):
+    h = golden("helpers")["helpers"][index]
+    plan = NativePlan(h["payload"])
+    for case in h["cases"]:
+        ref = case["structured"]
+        scale = float(np.max(np.abs(ref)))
+        dy = plan.rhs(case["packed"], case["t"], case["override_slots"], case["override_values"])[0]
+        assert np.max(np.abs(dy - ref)) <= 1e-10 * scale, (h["name"], case["t"], "fp64")
+        dm = plan.rhs(case["packed"], case["t"], case["override_slots"], case["override_values"], precision="mixed")[0]
+        assert np.max(np.abs(dm - ref)) <= 2e-5 * scale, (h["name"], case["t"], "mixed")
+
+
+@pytest.mark.parametrize("index", range(18))
+def test_helper_solve_matches_oracle(golden, index):
+    h = golden("helpers")["helpers"][index]
+    plan = api.prepare_lindblad_problem_py(h["payload"])
+    op = oracle.OraclePlan(h["payload"])
+    rho0 = np.array([1.0, 0.0, 0.0, 0.0])
+    saveat = np.linspace(0.0, 3.0, 13)
+    tol = 1e-6 if h["helper_id"] in DISCONTINUOUS else 1e-9
+    times, vals, width, st = api.solve_lindblad_ode_py(plan, rho0, 0.0, 3.0, 1e-10, 1e-8, 1e-3, saveat, True, 100000,
+                                                       "expanded_sparse", "dopri5", "full")
+    o = op.options(t0=0.0, t1=3.0, abstol=1e-10, reltol=1e-8, dt=1e-3, saveat=saveat, save_start=True,
+                   maxiters=100000, solver="dopri5", output="full", output_indices=None, output_when="saveat",
+                   integral_weights=None, stop_event=None)
+    rt, rv, rst = op.solve_single(o, rho0)
+    np.testing.assert_array_equal(times, rt)
+    assert np.all(np.isfinite(vals))
+    err = float(np.max(np.abs(vals.reshape(rv.shape) - rv)))
+    assert err <= tol, f"{h['name']}: max error {err:.3e} > {tol}"
+    assert abs(st["accepted_steps"] - rst["accepted_steps"]) <= 0.05 * rst["accepted_steps"] + 2
