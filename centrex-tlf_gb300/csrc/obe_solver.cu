@@ -1372,7 +1372,7 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
     A.n_traj = n_traj;
     A.rho0 = d_rho0;
     A.rho0_stride = p->N;
-    A.n_param = d_param_values ? n_param_slots : 0;
+    A.n_param = n_param_slots;
     for (int k = 0; k < A.n_param; ++k) A.param_slot[k] = static_cast<int>(param_slots[k]);
     A.param_values = d_param_values;
     A.vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
@@ -1561,6 +1561,10 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
     obe_plan* p = const_cast<obe_plan*>(plan);
     if (!p || !opt || !d_rho0 || !d_values || !d_stats) { set_error("null argument"); return OBE_ERR_INVALID; }
     if (n_traj <= 0) { set_error("n_traj must be positive"); return OBE_ERR_INVALID; }
+    if (n_param_slots < 0 || (n_param_slots > 0 && (!param_slots || !d_param_values))) {
+        set_error("n_param_slots > 0 needs both param_slots and d_param_values");
+        return OBE_ERR_INVALID;
+    }
     if (n_traj > kNoAllocMaxTrajectories) {
         set_error("obe_solve_batch_device_noalloc handles at most " + std::to_string(kNoAllocMaxTrajectories) +
                   " trajectories per call, got " + std::to_string(n_traj));
@@ -1568,7 +1572,10 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
     }
     if (!p->has_expanded && !p->packed.eff) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
     if (obe_device_count() <= 0) { set_error("no CUDA device is available: the GB300 solver has no CPU fallback"); return OBE_ERR_CUDA; }
+    // lock order: the scratch array, then the plan (obe_plan_set_shape / obe_plan_autotune change
+    // the plan's launch shape and layout under g_plan_mutex while this call reads them)
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    std::lock_guard<std::mutex> plan_lock(g_plan_mutex);
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
     if (dev < 0 || dev >= 64) { set_error("device index out of range for the allocation-free entry point"); return OBE_ERR_UNSUPPORTED; }
@@ -1611,7 +1618,7 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
     A.n_traj = n_traj;
     A.rho0 = d_rho0;
     A.rho0_stride = p->N;
-    A.n_param = d_param_values ? n_param_slots : 0;
+    A.n_param = n_param_slots;
     for (int k = 0; k < A.n_param; ++k) A.param_slot[k] = static_cast<int>(param_slots[k]);
     A.param_values = d_param_values;
     A.n_axes = 0;

@@ -419,8 +419,9 @@ obe_status obe_grad_backward(const obe_plan* plan, const obe_solve_options* opt,
 /*
  * Allocation-free form of obe_solve_batch_device (no counterpart in the reference).  Some
  * callers cannot let a library allocate device memory while they solve: a caller that owns all
- * device memory up front through its own arena or a fixed memory budget, or one that records
- * its GPU work into a CUDA graph.  This entry point calls no cudaMalloc/cudaFree (and no
+ * device memory up front through its own arena, or one that runs under a fixed memory budget
+ * in which a cudaMalloc in the middle of a solve would fail or would have to be accounted for
+ * after the fact.  This entry point calls no cudaMalloc/cudaFree (and no
  * allocating library routine); the caller passes every input and output in device memory.  All
  * scratch the integrator needs -- the plan's device image, the per-call argument block, the
  * per-trajectory error records and the work-queue counter -- lives in one fixed file-scope
@@ -433,7 +434,9 @@ obe_status obe_grad_backward(const obe_plan* plan, const obe_solve_options* opt,
  * buffers need device memory of the order of a megabyte per trajectory in flight, far beyond the
  * fixed array; solve those with obe_solve_batch_device.
  * The first call on a device looks up the array's device address (once per device, with that
- * device current); make that first call before any stream capture begins.
+ * device current); make that first call before any stream capture begins.  The address is kept
+ * for the life of the process: a cudaDeviceReset between calls is not supported.
+ * n_param_slots > 0 needs both param_slots and d_param_values (OBE_ERR_INVALID otherwise).
  * Every call shares the one array and leaves its contents behind: calls whose GPU work overlaps
  * (other streams, other host threads) race on it and must be serialised by the caller.
  * Per-trajectory statuses land in d_stats as with obe_solve_batch_device.
