@@ -151,26 +151,29 @@ def cpu_oracle_populations(d, params, slots, sample: int) -> np.ndarray:
 
 
 def run_reference(args) -> None:
+    """The reference arm: the reference's CPU path (its Rust solver restated in C, the oracle) on
+    all host threads, timed on the whole configured scan (`--points`, 4096 by default) every step,
+    warm-up steps included."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     d, params, slots = workload(args.points)
     for _ in range(args.warmup):
-        cpu_oracle_rate(d, params, slots, args.ref_sample)
-    rates, secs = [], []
+        cpu_oracle_rate(d, params, slots, args.points)
+    secs = []
     for _ in range(args.steps):
-        r = cpu_oracle_rate(d, params, slots, args.ref_sample)
-        rates.append(r["value"])
+        r = cpu_oracle_rate(d, params, slots, args.points)
         secs.append(r["seconds"])
-    value = float(args.ref_sample * args.steps / sum(secs))
+    value = float(args.points * args.steps / sum(secs))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)) * args.points / args.ref_sample,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "q1_16state_gaussian_scan_4096pt_tsit5", "points": args.points,
-                   "sample_points_per_step": args.ref_sample, "l2": "n/a (CPU)"},
+                   "points_per_step": args.points, "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "trajectories/s", "cores": r["cores"], "kind": "port",
-                         "sample": r["sample"]},
+                         "sample": f"the whole {args.points}-point scan every step, all {r['cores']} host threads, "
+                                   "C FP64 oracle (-O3)"},
         "e2e": {"value": value, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own path is Rust (PyO3); no Rust toolchain exists here or on the GPU box, so the "
                 "reference arm times its C restatement (oracle/) on all host threads",
@@ -301,6 +304,197 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
                               "that cancels to ~1e-4 of that scale) (tests/test_gpu_adjoint.py)"}}
 
 
+def measure_single(torch, dev, reps: int = 5) -> dict:
+    """One trajectory of the 16-state system at its base parameters (peak Rabi Γ, zero detuning,
+    z polarisation, Gaussian pulse σ = 20/Γ centred at 100/Γ), Dopri5 rtol 1e-8 atol 1e-11 over
+    [0, 200/Γ]: final populations and the excited-population integral through the reference-facing
+    single-solve call (host arrays, one call per output as the reference makes them), FP64 and the
+    mixed form, at the automatic launch width (32 threads) and at 256 threads; against the oracle
+    solving the same trajectory on one host thread."""
+    import codec
+    import oracle
+    from centrex_tlf_gb300 import centrex_tlf_rust as api
+
+    d = codec.load("plan_q1_16")
+    g, (t0, t1) = d["gamma"], d["t_span"]
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    rho0 = d["rho0_packed"]
+
+    def solve(precision):
+        _, pops, _, st = api.solve_lindblad_ode_py(plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / g, None, True, 100000,
+                                                   "expanded_sparse", "dopri5", "populations", None, "final", None,
+                                                   precision=precision)
+        _, integ, _, _ = api.solve_lindblad_ode_py(plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / g, None, True, 100000,
+                                                   "expanded_sparse", "dopri5", "excited_population", None, "final",
+                                                   W_EXCITED, precision=precision)
+        return np.asarray(pops), float(np.asarray(integ).reshape(-1)[-1]), st
+
+    def timed(precision):
+        solve(precision)
+        best = float("inf")
+        for _ in range(reps):
+            start = time.perf_counter()
+            out = solve(precision)
+            best = min(best, time.perf_counter() - start)
+        return best, out
+
+    res = {}
+    for width in (0, 256):
+        plan.native.set_shape(width, 0)
+        for precision in ("fp64", "mixed"):
+            res[(width, precision)] = timed(precision)
+    plan.native.set_shape(0, 0)
+    op = oracle.OraclePlan(d["payload"])
+    common = dict(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=None, save_start=True, maxiters=100000,
+                  solver="dopri5", output_indices=None, output_when="final", stop_event=None)
+    o_pop = op.options(output="populations", integral_weights=None, **{**common, "saveat": np.array([t1]), "save_start": False})
+    o_int = op.options(output="excited_population", integral_weights=W_EXCITED, **common)
+    cpu_best = float("inf")
+    for _ in range(reps):
+        start = time.perf_counter()
+        _, rp, rst = op.solve_single(o_pop, rho0)
+        _, ri, _ = op.solve_single(o_int, rho0)
+        cpu_best = min(cpu_best, time.perf_counter() - start)
+    ref_pops, ref_int = rp.reshape(-1), float(ri.reshape(-1)[-1])
+    out = {"workload": "16-state system at its base parameters, one trajectory, Dopri5 rtol 1e-8 atol 1e-11 over "
+                       "[0, 200/Γ]; final populations + excited-population integral (two reference-facing calls, host "
+                       "arrays)",
+           "oracle_ms": 1e3 * cpu_best, "oracle_cores": 1, "accepted_steps": int(rst["accepted_steps"]),
+           "rejected_steps": int(rst["rejected_steps"])}
+    for (width, precision), (t, (pops, integ, st)) in res.items():
+        key = f"{precision}_{'auto_32_threads' if width == 0 else '256_threads'}"
+        out[key] = {"ms": 1e3 * t, "vs_oracle_speed": cpu_best / t,
+                    "max_population_error_vs_oracle": float(np.max(np.abs(pops - ref_pops))),
+                    "excited_integral_rel_error_vs_oracle": abs(integ - ref_int) / abs(ref_int),
+                    "accepted_steps": int(st["accepted_steps"])}
+    out["note"] = ("one trajectory occupies one thread group: a single solve is latency-bound on the GPU, the batch "
+                   "entry points are the throughput path")
+    return out
+
+
+def ragged76_job(total: int, seed: int = 20241205):
+    """The ragged 76-state scan: `total` trajectories of the X J=0-3 + B J'=1 system (R(0) and
+    P(2) lasers, polarisations switched by 1 MHz square waves), per-laser Rabi U[0.5, 3]Γ and
+    detuning N(0, 0.5Γ), end times U[20, 100] µs through a `Time() - t_end` stop event; Tsit5,
+    rtol 1e-8, atol 1e-11, final populations."""
+    import codec
+
+    d = codec.load("plan_rc_76")
+    g = d["gamma"]
+    names = d["payload"]["parameter_graph"]["slot_names"]
+    rng = np.random.default_rng(seed)
+    t_end = rng.uniform(20e-6, 100e-6, total)
+    params = np.stack([rng.uniform(0.5, 3.0, total) * g, rng.uniform(0.5, 3.0, total) * g,
+                       rng.normal(0.0, 0.5, total) * g, rng.normal(0.0, 0.5, total) * g, t_end], axis=1).astype(np.complex128)
+    ev = {"kind": "runtime_expression",
+          "expression": {"instructions": [{"op": 4}, {"op": 2, "index": names.index("t_end")}, {"op": 6}],
+                         "scalar_only": True, "output_is_tuple": False}}
+    return {"d": d, "params": params, "slots": [names.index(s) for s in ("Ω0", "Ω1", "δ0", "δ1", "t_end")],
+            "event": ev, "t1": 1.01e-4}
+
+
+def measure_ragged76(torch, dev, total: int = 1024, cpu_sample: int = 32) -> dict:
+    """The ragged 76-state scan in one persistent launch per form (device-resident, final
+    populations at each trajectory's own end time), FP64 and mixed, with the launch width the
+    autotuner picks on a probe of the batch; the oracle solves the first `cpu_sample` trajectories
+    on all host threads, for its rate and for the error of both forms."""
+    import oracle
+    from centrex_tlf_gb300.native import NativePlan
+
+    job = ragged76_job(total)
+    d, g = job["d"], job["d"]["gamma"]
+    plan = NativePlan(d["payload"])
+    stream = torch.cuda.current_stream(dev)
+    rho = torch.from_numpy(np.repeat(d["rho0_packed"].reshape(1, -1), total, axis=0)).to(dev)
+    par = torch.from_numpy(np.ascontiguousarray(job["params"]).view(np.float64).reshape(-1)).to(dev)
+    val = torch.zeros(total * 76, dtype=torch.float64, device=dev)
+    st = torch.zeros(total * 6, dtype=torch.int64, device=dev)
+    res = {}
+    for precision in ("fp64", "mixed"):
+        o = plan.options(t0=0.0, t1=job["t1"], abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=np.array([job["t1"]]),
+                         save_start=False, maxiters=1000000, solver="tsit5", output="populations", output_indices=None,
+                         output_when="final", integral_weights=None, stop_event=job["event"], precision=precision)
+        plan.set_shape(0, 0)
+        cands = plan.autotune(o, total, rho.data_ptr(), job["slots"], par.data_ptr(), 1, probe_steps=64,
+                              stream=stream.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.solve_batch_device(o, total, rho.data_ptr(), job["slots"], par.data_ptr(), 1, val.data_ptr(),
+                                st.data_ptr(), stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        stv = st.view(-1, 6).cpu().numpy()
+        if np.any(stv[:, 3] >> 32):
+            raise RuntimeError(f"{int(np.count_nonzero(stv[:, 3] >> 32))} 76-state trajectories failed ({precision})")
+        ms = e0.elapsed_time(e1)
+        res[precision] = {"ms": ms, "value": total / (ms * 1e-3), "unit": "trajectories/s",
+                          "threads_per_trajectory": cands[0]["threads_per_trajectory"],
+                          "accepted_steps": int(stv[:, 0].sum()), "rejected_steps": int(stv[:, 1].sum()),
+                          "pops": val.view(total, 76).cpu().numpy().copy()}
+    plan.set_shape(0, 0)
+    op = oracle.OraclePlan(d["payload"])
+    o = op.options(t0=0.0, t1=job["t1"], abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=np.array([job["t1"]]),
+                   save_start=False, maxiters=1000000, solver="tsit5", output="populations", output_indices=None,
+                   output_when="final", integral_weights=None, stop_event=job["event"])
+    rho0 = np.repeat(d["rho0_packed"].reshape(1, -1), cpu_sample, axis=0)
+    start = time.perf_counter()
+    ref, _, rst = op.solve_batch(o, rho0, job["slots"], job["params"][:cpu_sample])
+    cpu_s = time.perf_counter() - start
+    ref = ref.reshape(cpu_sample, 76)
+    out = {"workload": f"{total} trajectories of the 76-state system, square-wave polarisation switching at 1 MHz, "
+                       "end times U[20, 100] µs by stop event, Tsit5 rtol 1e-8 atol 1e-11, final populations; "
+                       "device-resident, one launch per form",
+           "cpu_oracle": {"value": cpu_sample / cpu_s, "unit": "trajectories/s", "cores": int(oracle.max_threads()),
+                          "sample": f"first {cpu_sample} trajectories", "accepted_steps": int(rst["accepted_steps"].sum())}}
+    for precision, r in res.items():
+        pops = r.pop("pops")
+        r["max_population_error_vs_oracle"] = float(np.max(np.abs(pops[:cpu_sample] - ref)))
+        r["max_trace_drift"] = float(np.max(np.abs(pops.sum(axis=1) - 1.0)))
+        r["speedup_vs_cpu_oracle"] = r["value"] / out["cpu_oracle"]["value"]
+        out[precision] = r
+        res[precision]["_pops"] = pops
+    out["mixed"]["max_population_error_vs_fp64_gpu"] = float(np.max(np.abs(res["mixed"]["_pops"] - res["fp64"]["_pops"])))
+    out["mixed"]["speedup_vs_fp64_gpu"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    for r in res.values():
+        r.pop("_pops", None)
+    out["note"] = ("the square-wave switching makes the RHS discontinuous; solves agree with the oracle to the "
+                   "solver tolerance there (step landings at the jumps), not to rounding")
+    return out
+
+
+def hetero_oracle_sample(spec, prepared, torch, dev, per_plan: int = 6) -> dict:
+    """The oracle on the first `per_plan` instances of each plan of the heterogeneous batch (all
+    host threads): its rate, and the max final-population error of both GPU forms against it."""
+    import oracle
+
+    stream = torch.cuda.current_stream(dev)
+    total_s, total_n, errs = 0.0, 0, {"mixed": 0.0, "fp64": 0.0}
+    for j, (plan, _, b, rho, slots, par, _, st) in zip(spec, prepared):
+        k = min(per_plan, b)
+        if k == 0:
+            continue
+        d, g = j["d"], j["d"]["gamma"]
+        n = d["payload"]["n_states"]
+        o_kw = dict(t0=0.0, t1=j["t1"], abstol=1e-11, reltol=1e-8, dt=1e-3 / g, saveat=np.array([j["t1"]]),
+                    save_start=False, maxiters=1000000, solver="tsit5", output="populations", output_indices=None,
+                    output_when="final", integral_weights=None, stop_event=j["event"])
+        op = oracle.OraclePlan(d["payload"])
+        rho0 = np.repeat(d["rho0_packed"].reshape(1, -1), k, axis=0)
+        start = time.perf_counter()
+        ref, _, _ = op.solve_batch(op.options(**o_kw), rho0, j["slots"], j["params"][:k])
+        total_s += time.perf_counter() - start
+        total_n += k
+        pv = torch.zeros(k * n, dtype=torch.float64, device=dev)
+        for prec in errs:
+            plan.solve_batch_device(plan.options(precision=prec, **o_kw), k, rho.data_ptr(), slots, par.data_ptr(), 1,
+                                    pv.data_ptr(), st.data_ptr(), stream.cuda_stream)
+            torch.cuda.synchronize()
+            errs[prec] = max(errs[prec], float(np.max(np.abs(pv.view(k, n).cpu().numpy() - ref.reshape(k, n)))))
+    return {"cpu_oracle": {"value": total_n / total_s, "unit": "trajectories/s", "cores": int(oracle.max_threads()),
+                           "sample": f"first {per_plan} instances of each plan ({total_n} in all)"},
+            "max_population_error_vs_oracle": errs}
+
+
 HETERO_PLANS = (("plan_q1_16_tend", 6), ("plan_r0_39", 3), ("plan_rc_76", 1))
 
 
@@ -399,6 +593,7 @@ def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
     t_graph, _ = timed(lambda prec: graph.launch(stream.cuda_stream), "mixed")
     graph.close()
     t_64, _ = timed(multi, "fp64", warm=False)
+    sample = hetero_oracle_sample(spec, prepared, torch, dev)
     err = 0.0
     for j, (*_, val, _) in zip(spec, prepared):
         t_end = j["params"][:, -1].real
@@ -415,7 +610,12 @@ def measure_heterogeneous(torch, dev, total: int = 8192, reps: int = 1) -> dict:
         "cuda_graph_ms": 1e3 * t_graph,
         "fp64_ms": 1e3 * t_64, "speedup_of_mixed": t_64 / t_multi,
         "max_time_averaged_population_error_vs_fp64": err,
-        "note": "fp64 timed on its first call (plans already on the device); the error is |integral difference| / t_end",
+        "cpu_oracle": sample["cpu_oracle"],
+        "speedup_vs_cpu_oracle": (total / t_multi) / sample["cpu_oracle"]["value"],
+        "max_population_error_vs_oracle": sample["max_population_error_vs_oracle"],
+        "note": "fp64 timed on its first call (plans already on the device); the time-averaged error is |integral "
+                "difference| / t_end; the population errors are final populations at each instance's end time on "
+                "the oracle's sample",
     }
 
 
@@ -721,6 +921,8 @@ def run_gpu(args) -> None:
     gradient = measure_gradient(torch, d, params, dev) if not args.no_gradient else None
     hetero = measure_heterogeneous(torch, dev, total=args.hetero_instances) if args.hetero_instances > 0 else None
     effective = measure_effective(torch, dev) if not args.no_effective else None
+    single = measure_single(torch, dev) if not args.no_single else None
+    ragged = measure_ragged76(torch, dev, total=args.ragged_instances) if args.ragged_instances > 0 else None
     hetero_grad = (measure_hetero_gradient(torch, dev, total=args.hetero_grad_instances)
                    if args.hetero_grad_instances > 0 else None)
     gpu_obs = np.asarray(out[1])[: args.cpu_sample]
@@ -780,6 +982,8 @@ def run_gpu(args) -> None:
         "heterogeneous": hetero,
         "heterogeneous_gradient": hetero_grad,
         "effective": effective,
+        "single_solve": single,
+        "ragged_76": ragged,
     }
     print(json.dumps(line))
     if world > 1:
@@ -869,6 +1073,9 @@ def main() -> None:
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 path beside mixed")
     ap.add_argument("--no-gradient", action="store_true", help="skip timing the adjoint beside the forward solve")
     ap.add_argument("--no-effective", action="store_true", help="skip timing the effective-Hamiltonian path")
+    ap.add_argument("--no-single", action="store_true", help="skip timing the single 16-state solve")
+    ap.add_argument("--ragged-instances", type=int, default=1024,
+                    help="trajectories of the ragged 76-state scan timed beside the scan (0 skips it)")
     ap.add_argument("--hetero-instances", type=int, default=8192,
                     help="instances of the heterogeneous 16/39/76-state batch timed beside the scan (0 skips it)")
     ap.add_argument("--hetero-grad-instances", type=int, default=512,
@@ -878,7 +1085,6 @@ def main() -> None:
     ap.add_argument("--checkpoint-every", type=int, default=None,
                     help="--case gradient: the tape's checkpoint interval (default: full tape while it fits)")
     ap.add_argument("--cpu-sample", type=int, default=128)
-    ap.add_argument("--ref-sample", type=int, default=256)
     ap.add_argument("--case", choices=["scan", "gradient", "heterogeneous", "hetero-gradient", "large"], default="scan",
                     help="scan: the benchmark line; the others run one workload alone (profiling)")
     ap.add_argument("--threads-per-trajectory", type=int, default=0,
