@@ -321,9 +321,10 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
     rho0 = d["rho0_packed"]
 
     def solve(precision):
-        _, pops, _, st = api.solve_lindblad_ode_py(plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / g, None, True, 100000,
-                                                   "expanded_sparse", "dopri5", "populations", None, "final", None,
-                                                   precision=precision)
+        # final populations as the reference's solve_lindblad passes them: saveat [t1], no start point
+        _, pops, _, st = api.solve_lindblad_ode_py(plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / g, np.array([t1]), False,
+                                                   100000, "expanded_sparse", "dopri5", "populations", None, "final",
+                                                   None, precision=precision)
         _, integ, _, _ = api.solve_lindblad_ode_py(plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / g, None, True, 100000,
                                                    "expanded_sparse", "dopri5", "excited_population", None, "final",
                                                    W_EXCITED, precision=precision)
@@ -864,6 +865,14 @@ def run_gpu(args) -> None:
                              output_when="final", integral_weights=W_EXCITED, stop_event=None, precision="fp64")
         ms64, att64 = timed(o64, args.steps)
         other = (ms64, att64)
+    # the opt-in variant with single-precision stage inputs, error norm and controller
+    fast = None
+    if args.precision == "mixed" and not args.no_fp64_compare:
+        o32 = native.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=None, save_start=True,
+                             maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
+                             output_when="final", integral_weights=W_EXCITED, stop_event=None,
+                             precision="mixed_fp32_control")
+        fast = timed(o32, args.steps)
     total_s = sum(ms) * 1e-3
     total64_s = sum(other[0]) * 1e-3 if other else 0.0
     total_s, total64_s = max_over_ranks([total_s, total64_s], device=dev)
@@ -901,6 +910,7 @@ def run_gpu(args) -> None:
     p64 = pops("fp64")
     pm = p64 if args.precision == "fp64" else pops(args.precision)
     max_pop_err = float(np.max(np.abs(pm - p64)))
+    p32c = pops("mixed_fp32_control") if fast is not None else None
     # per-result diagnostics the solve reports beside its error: trace drift of the final state
     # (|sum of populations - 1|; rho0 has unit trace) for both forms, and the error of both forms
     # against the FP64 oracle on the CPU-baseline sample
@@ -928,6 +938,17 @@ def run_gpu(args) -> None:
     gpu_obs = np.asarray(out[1])[: args.cpu_sample]
     obs_rel = float(np.max(np.abs(gpu_obs - cpu["values"]) / np.maximum(np.abs(cpu["values"]), 1e-300)))
     accuracy["observable_max_rel_err_vs_cpu_oracle"] = obs_rel
+    fast_line = None
+    if fast is not None:
+        fast_value = b * world * args.steps / (sum(fast[0]) * 1e-3)
+        fast_line = {"value": fast_value, "unit": "trajectories/s", "ms_per_step": sum(fast[0]) / len(fast[0]),
+                     "attempted_steps_per_launch": fast[1],
+                     "speedup_vs_fp64_gpu": fast_value / (b * world * args.steps / total64_s) if other else None,
+                     "max_population_error_vs_fp64_gpu": float(np.max(np.abs(p32c - p64))),
+                     "max_population_error_vs_fp64_oracle": float(np.max(np.abs(p32c[: args.cpu_sample] - p_orc))),
+                     "max_trace_drift": float(np.max(np.abs(p32c.sum(axis=1) - 1.0))),
+                     "note": "opt-in variant (precision='mixed_fp32_control'): stage inputs, error norm and step-size "
+                             "controller in single precision, no trace renormalisation"}
 
     f_rhs, per_step = flops_per_step_unit(d["payload"])
     flops_per_launch = attempted * per_step
@@ -945,7 +966,7 @@ def run_gpu(args) -> None:
             hbm_peak, hbm_src = float(json.loads(peaks_file.read_text())["hbm_gbs"]), "measured"
         except (ValueError, KeyError):
             pass
-    traffic_launch = TRAFFIC_BYTES_PER_TRAJECTORY[args.precision] * b
+    traffic_launch = TRAFFIC_BYTES_PER_TRAJECTORY["fp64" if args.precision == "fp64" else "mixed"] * b
     hbm_achieved = traffic_launch / kernel_s / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
@@ -961,7 +982,7 @@ def run_gpu(args) -> None:
         "gpu_launches": launches,
         "roofline": {"bound": "fp32" if mixed else "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak,
-                     "traffic": TRAFFIC_BYTES_PER_TRAJECTORY[args.precision] * b,
+                     "traffic": TRAFFIC_BYTES_PER_TRAJECTORY["fp64" if args.precision == "fp64" else "mixed"] * b,
                      "note": "algorithmic FLOPs (6*F_rhs + 60*N per attempted step, F_rhs = "
                              f"{f_rhs}) / mean launch time; peak = cuBLAS "
                              + ("SGEMM (TF32 off: the FP32 pipe the mixed form's products run on)" if mixed else "DGEMM")
@@ -977,6 +998,7 @@ def run_gpu(args) -> None:
                       "speedup_of_this_precision": (b * world * args.steps / total_s) / (b * world * args.steps / total64_s)}
                      if other else None),
         "accuracy": accuracy,
+        "mixed_fp32_control": fast_line,
         "clocks": clocks,
         "gradient": gradient,
         "heterogeneous": hetero,
@@ -1069,7 +1091,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp32_control"], default="mixed")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 path beside mixed")
     ap.add_argument("--no-gradient", action="store_true", help="skip timing the adjoint beside the forward solve")
     ap.add_argument("--no-effective", action="store_true", help="skip timing the effective-Hamiltonian path")

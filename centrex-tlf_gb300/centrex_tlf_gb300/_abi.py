@@ -32,7 +32,7 @@ OUTPUT_WEIGHTED_RATE = 4
 EVENT_NONE = 0
 EVENT_POPULATION = 1
 EVENT_EXPRESSION = 2
-PRECISIONS = {"fp64": 0, "mixed": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1, "mixed_fp32_control": 2}
 
 _p = ctypes.POINTER
 c_i32p = _p(ctypes.c_int32)
@@ -224,6 +224,8 @@ def load_library() -> ctypes.CDLL:
     lib.obe_plan_packed_len.restype = ctypes.c_int64
     lib.obe_plan_n_states.argtypes = [ctypes.c_void_p]
     lib.obe_plan_n_states.restype = ctypes.c_int32
+    lib.obe_plan_trace_preserving.argtypes = [ctypes.c_void_p]
+    lib.obe_plan_trace_preserving.restype = ctypes.c_int32
     lib.obe_rhs_eval.argtypes = [
         ctypes.c_void_p, ctypes.c_int64, c_f64p, c_f64p, ctypes.c_int32, c_i64p, c_f64p,
         ctypes.c_int32, c_f64p,

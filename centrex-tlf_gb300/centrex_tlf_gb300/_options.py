@@ -62,7 +62,7 @@ class SolveOptions:
                 f"got {solver!r}"
             )
         if precision not in _abi.PRECISIONS:
-            raise ValueError(f"precision must be 'fp64' or 'mixed', got {precision!r}")
+            raise ValueError(f"precision must be 'fp64', 'mixed' or 'mixed_fp32_control', got {precision!r}")
         o = ObeSolveOptions()
         o.t0, o.t1 = float(t0), float(t1)
         o.abstol, o.reltol, o.dt = float(abstol), float(reltol), float(dt)

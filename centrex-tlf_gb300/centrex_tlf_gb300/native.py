@@ -59,6 +59,11 @@ class NativePlan:
             self.lib.obe_plan_destroy(h)
             self.handle = None
 
+    @property
+    def trace_preserving(self) -> bool:
+        """The plan's RHS keeps the trace (the mixed form then renormalises it every step)."""
+        return bool(self.lib.obe_plan_trace_preserving(self.handle))
+
     @classmethod
     def from_effective(cls, plan_dict: dict) -> "NativePlan":
         """An interpolated effective-Hamiltonian plan (obe_effective_plan_create) from the plan

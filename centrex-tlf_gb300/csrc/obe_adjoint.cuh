@@ -515,8 +515,9 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
         const long long s0 = sg * seg_len, s1 = s0 + seg_len < n_acc ? s0 + seg_len : n_acc;
         if (J.ckpt > 0 && MIXED) {
             // replay the segment's steps from its checkpointed start state as the mixed forward took
-            // them: single-precision stage deviations d_2..d_7 (the same deviation-form gather), the
-            // solution and k_1 (first same as last, refreshed in double precision at the segment start
+            // them: single-precision stage deviations d_2..d_7 (the same deviation-form gather) from
+            // stage inputs summed in double, the solution, the trace renormalisation (trace-preserving
+            // plans) and k_1 (first same as last, refreshed in double precision at the segment start
             // and every k1_refresh steps) in double; each step stored as a single-precision record
             // [y_n, k_1, d_2..d_7].  Scratch after the segment's records: y, k_1 (double), k_1 (single).
             double* yx = segbuf + static_cast<size_t>(J.ckpt + 1) * J.rec_stride;
@@ -529,6 +530,17 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
             float4* cv = reinterpret_cast<float4*>(gb + Lay.cv);
             const double* ck = tbase + 2 * J.tape_cap + static_cast<size_t>(sg) * N;
             for (int i = lt; i < N; i += TPT) yx[i] = ck[i];
+            // the trajectory's initial trace, which the forward restores after every accepted step
+            const bool renorm = P.trace_preserving != 0;
+            double tr0 = 1.0;
+            bool renorm_t = false;
+            if (renorm) {
+                const double* r0 = A.rho0 + traj * A.rho0_stride;
+                double tr = 0.0;
+                for (int i = lt; i < n; i += TPT) tr += r0[i];
+                tr0 = group_sum<TPT>(tr, s_red, lt, g);
+                renorm_t = isfinite(tr0) && tr0 != 0.0;
+            }
             // the table's fixed part: the records' zero coefficient and the time-independent formulas
             // (no change within a step); the formula stream refreshes the time-dependent ones per stage
             if (lt == 0) T4[0] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -565,12 +577,11 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     since = 0;
                 }
                 stage_classes<TPT>(P, s_cstat, s_cdyn, nd, cv, lt);
-                const float hf = d2f(h);
                 for (int s = 0; s < 6; ++s) {
                     for (int i = lt; i < N; i += TPT) {
-                        float acc = 0.f;
-                        for (int j = 1; j <= s; ++j) acc = fmaf(kTabF.a[M][s][j], K32[static_cast<size_t>(j - 1) * N + i], acc);
-                        const float dv = hf * fmaf(kTabF.csum[M][s], k1fx[i], acc);
+                        double acc = kCsum.c[M][s] * k1x[i];
+                        for (int j = 1; j <= s; ++j) acc = fma(kTab.a[M][s][j], f2d(K32[static_cast<size_t>(j - 1) * N + i]), acc);
+                        const float dv = d2f(h * acc);
                         const float yv32 = d2f(yx[i]);
                         if (i < n) {
                             G4[i] = make_float4(dv, 0.f, yv32, 0.f);
@@ -590,14 +601,27 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 double* out = segbuf + static_cast<size_t>(st - s0) * J.rec_stride;
                 if (lt == 0) { out[0] = tn; out[1] = h; }
                 float* fo = reinterpret_cast<float*>(out + 2);
+                double tr = 0.0;
                 for (int i = lt; i < N; i += TPT) {
                     fo[i] = d2f(yx[i]);
                     fo[N + i] = k1fx[i];
                     for (int r = 0; r < 6; ++r) fo[static_cast<size_t>(2 + r) * N + i] = K32[static_cast<size_t>(r) * N + i];
-                    float acc = 0.f;
-                    for (int j = 1; j < 6; ++j) acc = fmaf(kTabF.a[M][5][j], K32[static_cast<size_t>(j - 1) * N + i], acc);
-                    yx[i] = yx[i] + h * (k1x[i] + f2d(acc));
-                    const double k = k1x[i] + f2d(K32[static_cast<size_t>(5) * N + i]);
+                    double acc = kCsum.c[M][5] * k1x[i];
+                    for (int j = 1; j < 6; ++j) acc = fma(kTab.a[M][5][j], f2d(K32[static_cast<size_t>(j - 1) * N + i]), acc);
+                    yx[i] = yx[i] + h * acc;
+                    if (i < n) tr += yx[i];
+                }
+                double rf = 1.0;
+                if (renorm_t) {
+                    tr = group_sum<TPT>(tr, s_red, lt, g);
+                    if (tr != 0.0 && isfinite(tr)) rf = tr0 / tr;
+                }
+                for (int i = lt; i < N; i += TPT) {
+                    double k = k1x[i] + f2d(K32[static_cast<size_t>(5) * N + i]);
+                    if (renorm_t) {
+                        yx[i] *= rf;
+                        k *= rf;
+                    }
                     k1x[i] = k;
                     k1fx[i] = d2f(k);
                 }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -121,6 +122,9 @@ struct DevPlan {
     const uint32_t* bil;         // [n_biter * tpt]
     // populations are y[i * pop_stride] (1 packed; n + 1 for the split-real effective state)
     int32_t pop_stride;
+    // the RHS keeps the trace for every coefficient value (sum over the diagonal outputs of every
+    // input's and coefficient's products is zero): the mixed form renormalises the trace
+    int32_t trace_preserving;
     // interpolated effective-Hamiltonian plans (eff != 0; N = real_dim): the RHS is
     // L_c(x) y + (Omega / 2) L_o(x) y + delta L_d(x) y with x, Omega, delta = coefficients 0, 1, 2
     int32_t eff;
@@ -178,6 +182,7 @@ struct HostPacked {
     int32_t max_stack = 0;
     int32_t n_vm_slots = 0;     // parameter slots plus the hoisted static subexpressions
     int32_t dyn_real_closed = 0;  // every time-dependent compound is real_ok
+    int32_t trace_preserving = 0;
 };
 
 }  // namespace obe
@@ -205,6 +210,9 @@ struct obe_plan {
     size_t gk_bytes = 0;
     // launch shape fixed by obe_plan_set_shape / obe_plan_autotune (0: the automatic choice)
     int32_t shape_tpt = 0, shape_gpb = 0;
+    // serialises the entry points that use this plan's layout, device image and scratch; calls on
+    // different plans (e.g. one per device) run concurrently
+    std::mutex mu;
 };
 
 namespace obe {

@@ -92,9 +92,26 @@ constexpr TableausF make_tableaus_f() {
     return t;
 }
 
+// row sums of a in double (the k_1 weight of a stage input in the deviation form), summed left
+// to right
+struct RowSums {
+    double c[2][6];
+};
+constexpr RowSums make_row_sums() {
+    RowSums t{};
+    for (int m = 0; m < 2; ++m)
+        for (int r = 0; r < 6; ++r) {
+            double sum = 0.0;
+            for (int j = 0; j < 6; ++j) sum += kTabHost.a[m][r][j];
+            t.c[m][r] = sum;
+        }
+    return t;
+}
+
 // compile-time tables, one copy per translation unit (no runtime initialisation)
 static __constant__ Tableaus kTab = kTabHost;
 static __constant__ TableausF kTabF = make_tableaus_f();
+static __constant__ RowSums kCsum = make_row_sums();
 
 constexpr int kMaxWeights = 64;
 constexpr int kMaxSelected = 64;
@@ -173,6 +190,7 @@ struct CallArgs {
     int tape_ckpt;
     int vm_depth;    // VM stack depth of the plan's and the event's programs
     int fixed;       // 0: adaptive; else the fixed-step obe_solver value (double-precision form only)
+    int ctrl32;      // mixed form: stage inputs, error norm and controller in single precision, no renormalisation
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -683,6 +701,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
     long long* s_traj = reinterpret_cast<long long*>(gb + Lay.traj);
     const int nd = P.n_dyn > 0 ? P.n_dyn : 1;
     const int S = P.n_static_formula, F = P.n_formula;
+    // mixed form: single-precision stage inputs, error norm and controller (opt-in variant), and
+    // the trace renormalisation of the double-precision-control form on trace-preserving plans
+    const bool ctrl32 = MIXED && A.ctrl32 != 0;
+    const bool renorm = MIXED && !ctrl32 && P.trace_preserving != 0;
 
     // this thread's VM lane (lanes 0..5 only)
     VMLane L;
@@ -741,6 +763,18 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             y[e] = i < N ? r0[i] : 0.0;
             yn[e] = 0.0;
             if (i < N) s_G64[gsl(i)] = y[e];
+        }
+
+        // the initial trace, restored after every accepted step when renormalising
+        double tr0 = 1.0;
+        bool renorm_t = false;
+        if (renorm) {
+            double tr = 0.0;
+#pragma unroll
+            for (int e = 0; e < EPT; ++e)
+                if (lt + e * TPT < n) tr += y[e];
+            tr0 = group_sum<TPT>(tr, s_red, lt, g);
+            renorm_t = isfinite(tr0) && tr0 != 0.0;
         }
 
         long long accepted = 0, rejected = 0, rhs_calls = 0, count = 0;
@@ -1228,10 +1262,60 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 const float hf = d2f(h);
 #pragma unroll 1
                 for (int s = 0; s < 6; ++s) {
-                    // stage input deviation y_s - y_n = h (c_s k_1 + sum_j a_sj d_j), in single
-                    // precision (small next to y_n); the solution y_{n+1} itself in double
+                    // stage input deviation y_s - y_n = h (c_s k_1 + sum_j a_sj d_j) and the solution
+                    // y_{n+1} = y_n + h (k_1 + sum_j b_j d_j): summed in double from the double k_1 and
+                    // the single-precision d_j (exact conversions), the deviation then rounded once
+                    // to single precision for the stage's products.  The single-precision-control
+                    // variant (A.ctrl32) sums the deviation in single precision.
                     const float csum = kTabF.csum[M][s];
-                    if constexpr (TPT >= 256) {
+                    if (!ctrl32) {
+                        const double cs = kCsum.c[M][s];
+                        if constexpr (TPT >= 256) {
+                            constexpr int kCh = EPT < 8 ? EPT : 8;
+#pragma unroll
+                            for (int e0 = 0; e0 < EPT; e0 += kCh) {
+                                float kv[kCh][5];
+                                double k1d[kCh];
+#pragma unroll
+                                for (int c = 0; c < kCh; ++c) {
+                                    const int i = lt + (e0 + c) * TPT;
+                                    const bool in = i < N;
+#pragma unroll
+                                    for (int j = 1; j < 6; ++j)
+                                        kv[c][j - 1] = (in && j <= s) ? s_K32[static_cast<size_t>(j - 1) * N + i] : 0.f;
+                                    k1d[c] = in ? s_k1[i] : 0.0;
+                                }
+#pragma unroll
+                                for (int c = 0; c < kCh; ++c) {
+                                    const int e = e0 + c;
+                                    const int i = lt + e * TPT;
+                                    if (i < N) {
+                                        double acc = cs * k1d[c];
+#pragma unroll
+                                        for (int j = 1; j < 6; ++j)
+                                            if (j <= s) acc = fma(kTab.a[M][s][j], f2d(kv[c][j - 1]), acc);
+                                        const double dv = h * acc;
+                                        if (s == 5) yn[e] = y[e] + dv;
+                                        s_G4f[gslot32(i, n)] = d2f(dv);
+                                    }
+                                }
+                            }
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < EPT; ++e) {
+                                const int i = lt + e * TPT;
+                                if (i < N) {
+                                    double acc = cs * s_k1[i];
+#pragma unroll
+                                    for (int j = 1; j < 6; ++j)
+                                        if (j <= s) acc = fma(kTab.a[M][s][j], f2d(s_K32[static_cast<size_t>(j - 1) * N + i]), acc);
+                                    const double dv = h * acc;
+                                    if (s == 5) yn[e] = y[e] + dv;
+                                    s_G4f[gslot32(i, n)] = d2f(dv);
+                                }
+                            }
+                        }
+                    } else if constexpr (TPT >= 256) {
                         // the stage buffers live in device memory here: each batch of kCh elements
                         // issues all its loads before the first use, so the L2 round trips overlap
                         // (the same arithmetic as below)
@@ -1288,8 +1372,52 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                     gather_dev<TPT>(P, s_rec, s_out, s_T4, s_G4, s_K32 + static_cast<size_t>(s) * N, lt);
                     gsync<TPT>(g);
                 }
-                // error estimate from the deviations alone (the error weights sum to zero); the
-                // per-element ratios in single precision, their sum and the controller in double
+                // error estimate from the deviations alone (the error weights sum to zero): the
+                // weighted sums, the per-element ratios, their sum and the norm in double (the
+                // single-precision-control variant: in single precision)
+                if (!ctrl32) {
+                    if constexpr (TPT >= 256) {
+                        constexpr int kCh = EPT < 8 ? EPT : 8;
+#pragma unroll
+                        for (int e0 = 0; e0 < EPT; e0 += kCh) {
+                            float kv[kCh][6];
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c) {
+                                const int i = lt + (e0 + c) * TPT;
+#pragma unroll
+                                for (int j = 1; j < 7; ++j) kv[c][j - 1] = i < N ? s_K32[static_cast<size_t>(j - 1) * N + i] : 0.f;
+                            }
+#pragma unroll
+                            for (int c = 0; c < kCh; ++c) {
+                                const int e = e0 + c;
+                                if (lt + e * TPT < N) {
+                                    double acc = 0.0;
+#pragma unroll
+                                    for (int j = 1; j < 7; ++j)
+                                        if (M == 1 || j != 1) acc = fma(kTab.e[M][j], f2d(kv[c][j - 1]), acc);
+                                    const double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
+                                    const double q = (h * acc) / sc;
+                                    err = fma(q, q, err);
+                                }
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < EPT; ++e) {
+                            const int i = lt + e * TPT;
+                            if (i < N) {
+                                double acc = 0.0;
+#pragma unroll
+                                for (int j = 1; j < 7; ++j)
+                                    if (M == 1 || j != 1) acc = fma(kTab.e[M][j], f2d(s_K32[static_cast<size_t>(j - 1) * N + i]), acc);
+                                const double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
+                                const double q = (h * acc) / sc;
+                                err = fma(q, q, err);
+                            }
+                        }
+                    }
+                    err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
+                } else {
                 float errf = 0.f;
                 if constexpr (TPT >= 256) {
                     // device-memory stage buffers: batched loads, as in the stage inputs
@@ -1353,6 +1481,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                     gsync<TPT>(g);
                 }
                 err32 = sqrtf(errf / static_cast<float>(N));
+                }
             }
             rhs_calls += 6;
             if constexpr (!MIXED) err = sqrt(group_sum<TPT>(err, s_red, lt, g) / static_cast<double>(N));
@@ -1361,7 +1490,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             // differ from a double-precision controller's by ~1e-7 relative.
             double fac11 = 0.0, hn;
             bool accept_step;
-            if constexpr (MIXED) {
+            if (MIXED && ctrl32) {
                 const float f11 = exp2f(static_cast<float>(alpha) * log2f(err32));
                 float facf = f11 * exp2f(static_cast<float>(-beta) * log2f(fac_old32));
                 facf = fmaxf(static_cast<float>(facc2), fminf(static_cast<float>(facc1), facf / static_cast<float>(safety)));
@@ -1590,6 +1719,17 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 } else {
                     // the coefficients at t_{n+1} = x + h are row 4; they become the step-start row
                     if (lt < P.n_dyn) s_cdyn[5 * nd + lt] = s_cdyn[4 * nd + lt];
+                    // trace renormalisation in double: the next step starts from y_{n+1} tr_0 / tr(y_{n+1})
+                    // and, the RHS being linear, from k_1 scaled alike
+                    double rf = 1.0;
+                    if (renorm_t) {
+                        double tr = 0.0;
+#pragma unroll
+                        for (int e = 0; e < EPT; ++e)
+                            if (lt + e * TPT < n) tr += yn[e];
+                        tr = group_sum<TPT>(tr, s_red, lt, g);
+                        if (tr != 0.0 && isfinite(tr)) rf = tr0 / tr;
+                    }
                     const bool refresh = !last && ++since_refresh >= A.k1_refresh;
                     if (refresh) gsync<TPT>(g);  // the slot buffer below overlays the stage deviations
                     if (TPT >= 256 && !refresh) {
@@ -1609,9 +1749,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             for (int c = 0; c < kCh; ++c) {
                                 const int e = e0 + c;
                                 const int i = lt + e * TPT;
-                                y[e] = yn[e];
+                                y[e] = renorm_t ? yn[e] * rf : yn[e];
                                 if (i < N) {
-                                    const double k = k1d[c] + f2d(d7[c]);
+                                    double k = k1d[c] + f2d(d7[c]);
+                                    if (renorm_t) k *= rf;
                                     s_k1[i] = k;
                                     s_k1f[i] = d2f(k);
                                     s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
@@ -1622,13 +1763,14 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 #pragma unroll
                     for (int e = 0; e < EPT; ++e) {
                         int i = lt + e * TPT;
-                        y[e] = yn[e];
+                        y[e] = renorm_t ? yn[e] * rf : yn[e];
                         if (i < N) {
                             if (refresh) {
                                 s_G64[gsl(i)] = y[e];
                             } else {
                                 // first-same-as-last: k_1 of the next step is k_7 = k_1 + d_7
                                 double k = s_k1[i] + f2d(s_K32[static_cast<size_t>(5) * N + i]);
+                                if (renorm_t) k *= rf;
                                 s_k1[i] = k;
                                 s_k1f[i] = d2f(k);
                                 s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
@@ -1646,7 +1788,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 h = hn;
                 if (last) break;
             } else {
-                if constexpr (!MIXED) hn = h / fmin(facc1, fac11 / safety);
+                if (!MIXED || !ctrl32) hn = h / fmin(facc1, fac11 / safety);
                 reject = true;
                 last = false;
                 if (accepted >= 1) ++rejected;

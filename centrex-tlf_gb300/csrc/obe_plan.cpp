@@ -9,6 +9,7 @@
 // thread-interleaved so that each step of the gather loop is one conflict-free shared-memory
 // word per thread.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -727,6 +728,43 @@ obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
                 cursor += 2;
             }
 
+        // ---- trace preservation ------------------------------------------------------------
+        // The trace is the sum of the diagonal outputs, each Re(f c^(*) v^(*)) summed over its
+        // terms.  With c = a + ib (conjugated: a - ib) and v = x + iy (conjugated: x - iy), a term
+        // contributes f_re a x - f_im s_c b x - f_im s_v a y - f_re s_c s_v b y (s = -1 when
+        // conjugated; a static term has a = 1, b = 0).  The RHS keeps the trace for every state and
+        // every coefficient value exactly when, per (input, coefficient), the four sums over the
+        // diagonal outputs vanish -- up to rounding against the largest factor.
+        {
+            std::map<std::pair<int64_t, int64_t>, std::array<double, 4>> sums;
+            double scale = 0.0;
+            for (int32_t i = 0; i < n; ++i) {
+                const int64_t u = upper_index(n, i, i);
+                for (int64_t t = d->output_ptrs[u]; t < d->output_ptrs[u + 1]; ++t) {
+                    const double fr = d->factors_re[t], fi = d->factors_im[t];
+                    scale = std::max(scale, std::max(std::fabs(fr), std::fabs(fi)));
+                    const double sc = d->coeff_indices[t] >= 0 && d->coeff_conj[t] ? -1.0 : 1.0;
+                    const double sv = d->input_conj[t] ? -1.0 : 1.0;
+                    auto& acc = sums[{d->input_indices[t], d->coeff_indices[t]}];
+                    acc[0] += fr;
+                    acc[1] += -fi * sc;
+                    acc[2] += -fi * sv;
+                    acc[3] += -fr * sc * sv;
+                }
+            }
+            bool keeps = true;
+            for (const auto& kv : sums) {
+                const bool is_static = kv.first.second < 0;
+                const bool diag_in = u_im[kv.first.first] < 0;
+                const auto& a = kv.second;
+                // a static term has no b; a diagonal input has no y
+                const double resid = std::max(std::max(std::fabs(a[0]), is_static ? 0.0 : std::fabs(a[1])),
+                                              std::max(diag_in ? 0.0 : std::fabs(a[2]), is_static || diag_in ? 0.0 : std::fabs(a[3])));
+                if (resid > 1e-12 * scale) { keeps = false; break; }
+            }
+            hp.trace_preserving = keeps ? 1 : 0;
+        }
+
         // ---- records and formulas -----------------------------------------------------------
         // A formula is the exact list of (factor, class) products of the terms merged into one
         // record; identical lists share one table entry.
@@ -865,6 +903,8 @@ obe_status obe_plan_create(const obe_plan_desc* desc, obe_plan** out_plan) {
 
 int64_t obe_plan_packed_len(const obe_plan* plan) { return plan ? plan->N : 0; }
 int32_t obe_plan_n_states(const obe_plan* plan) { return plan ? plan->n : 0; }
+
+int32_t obe_plan_trace_preserving(const obe_plan* plan) { return plan ? plan->packed.trace_preserving : 0; }
 
 int32_t obe_abi_version(void) { return OBE_ABI_VERSION; }
 

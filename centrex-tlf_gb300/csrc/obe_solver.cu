@@ -42,13 +42,12 @@ size_t put(std::vector<unsigned char>& blob, const std::vector<T>& v) {
 }
 
 int k1_refresh_interval() {
-    static int v = 0;
-    if (!v) {
+    // every 32 accepted steps: measured on the 4096-point 16-state scan, 8 -> 32 is 5 % faster
+    // at a population error against FP64 of 4.3e-9 (8.7e-10 at 8; 9.7e-8 with no refresh)
+    static const int v = [] {
         const char* env = std::getenv("OBE_K1_REFRESH");
-        // every 32 accepted steps: measured on the 4096-point 16-state scan, 8 -> 32 is 5 % faster
-        // at a population error against FP64 of 4.3e-9 (8.7e-10 at 8; 9.7e-8 with no refresh)
-        v = env ? std::max(1, std::atoi(env)) : 32;
-    }
+        return env ? std::max(1, std::atoi(env)) : 32;
+    }();
     return v;
 }
 
@@ -76,6 +75,7 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     P.n_slots = std::max(p->n_slots, h.n_vm_slots);
     P.n_base = p->n_base;
     P.dyn_real_closed = h.dyn_real_closed;
+    P.trace_preserving = h.trace_preserving;
     P.base_val = reinterpret_cast<const double*>(base + o_bv);
     P.base_tuple = reinterpret_cast<const int32_t*>(base + o_bt);
     P.tuple_ptr = reinterpret_cast<const int32_t*>(base + o_tp);
@@ -209,13 +209,12 @@ cudaError_t dispatch_shape(const DevPlan& P, const CallArgs& A, const LaunchShap
 }
 
 int sm_count() {
-    static int count = 0;
-    if (!count) {
-        int dev = 0;
+    static const int count = [] {
+        int dev = 0, c = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
-        if (count <= 0) count = 1;
-    }
+        cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev);
+        return c > 0 ? c : 1;
+    }();
     return count;
 }
 
@@ -323,6 +322,11 @@ std::string traj_message(int code, const TrajErr& e) {
     }
 }
 
+// the mixed integrator (either control precision) runs the solve
+inline bool is_mixed(int32_t precision) {
+    return precision == OBE_PRECISION_MIXED || precision == OBE_PRECISION_MIXED_FP32_CONTROL;
+}
+
 // Everything a solve needs on the device besides the plan: the per-call blob of small arrays.
 struct CallBlob {
     std::vector<unsigned char> bytes;
@@ -333,7 +337,11 @@ struct CallBlob {
 obe_status validate_options(const obe_plan* p, const obe_solve_options* o, std::vector<double>& save_times, CallBlob& cb,
                             int64_t* width_out, int* is_complex) {
     const bool eff = p->packed.eff != 0;
-    if (eff && o->precision == OBE_PRECISION_MIXED) {
+    if (o->precision != OBE_PRECISION_FP64 && !is_mixed(o->precision)) {
+        set_error("precision must be 'fp64', 'mixed' or 'mixed_fp32_control'");
+        return OBE_ERR_INVALID;
+    }
+    if (eff && is_mixed(o->precision)) {
         set_error("effective-Hamiltonian plans solve in double precision");
         return OBE_ERR_UNSUPPORTED;
     }
@@ -349,7 +357,7 @@ obe_status validate_options(const obe_plan* p, const obe_solve_options* o, std::
         set_error("solver must be 'dopri5', 'tsit5', 'fixed_dopri5', 'fixed_rk2', or 'fixed_rk4'");
         return OBE_ERR_INVALID;
     }
-    if (o->solver >= OBE_SOLVER_FIXED_DOPRI5 && o->precision == OBE_PRECISION_MIXED) {
+    if (o->solver >= OBE_SOLVER_FIXED_DOPRI5 && is_mixed(o->precision)) {
         set_error("precision='mixed' is implemented for the adaptive solvers 'dopri5' and 'tsit5'");
         return OBE_ERR_UNSUPPORTED;
     }
@@ -470,6 +478,7 @@ void fill_call_args(CallArgs& A, const obe_solve_options* o, const std::vector<d
     A.ev_fn = reinterpret_cast<const int32_t*>(d_blob + cb.o_evfn);
     A.ev_val = reinterpret_cast<const double*>(d_blob + cb.o_evval);
     A.fixed = o->solver >= OBE_SOLVER_FIXED_DOPRI5 ? o->solver : 0;
+    A.ctrl32 = o->precision == OBE_PRECISION_MIXED_FP32_CONTROL ? 1 : 0;
 }
 
 cudaError_t launch_integrate(const obe_plan* p, const CallArgs& A, bool mixed, int solver, const LaunchShape& s, cudaStream_t st) {
@@ -533,7 +542,7 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
     A.tape_stride = tape_stride;
     A.tape_ckpt = tape_ckpt;
     LaunchShape s;
-    obe_status st = plan_launch(p->dev, o->precision == OBE_PRECISION_MIXED, n_traj, A.vm_depth, &s, p->shape_gpb);
+    obe_status st = plan_launch(p->dev, is_mixed(o->precision), n_traj, A.vm_depth, &s, p->shape_gpb);
     if (st != OBE_OK) return st;
     if (s.gstride > 0) {
         // the large systems' per-trajectory stage buffers: the caller's (a recorded graph owns its
@@ -544,12 +553,30 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
         A.gstride = s.gstride;
     }
     if (!cuda_ok(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync")) return OBE_ERR_CUDA;
-    if (!cuda_ok(launch_integrate(p, A, o->precision == OBE_PRECISION_MIXED, o->solver, s, stream), "kernel launch")) return OBE_ERR_CUDA;
+    if (!cuda_ok(launch_integrate(p, A, is_mixed(o->precision), o->solver, s, stream), "kernel launch")) return OBE_ERR_CUDA;
     g_launches += 1;
     return OBE_OK;
 }
 
-std::mutex g_plan_mutex;  // a plan's scratch is shared by the host-pointer entry points
+// Holds the mutexes of several plans, taken in address order (every caller uses that order,
+// so two multi-plan calls cannot deadlock); duplicates are taken once.
+class PlanLocks {
+  public:
+    template <typename It>
+    PlanLocks(It first, It last) : plans_(first, last) {
+        std::sort(plans_.begin(), plans_.end());
+        plans_.erase(std::unique(plans_.begin(), plans_.end()), plans_.end());
+        for (obe_plan* p : plans_) p->mu.lock();
+    }
+    ~PlanLocks() {
+        for (auto it = plans_.rbegin(); it != plans_.rend(); ++it) (*it)->mu.unlock();
+    }
+    PlanLocks(const PlanLocks&) = delete;
+    PlanLocks& operator=(const PlanLocks&) = delete;
+
+  private:
+    std::vector<obe_plan*> plans_;
+};
 
 }  // namespace
 }  // namespace obe
@@ -607,7 +634,7 @@ obe_status obe_solve_batch_device(const obe_plan* plan_c, const obe_solve_option
     g_launches = 0;
     obe_plan* p = const_cast<obe_plan*>(plan_c);
     if (!p || !opt) { set_error("null argument"); return OBE_ERR_INVALID; }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> lock(p->mu);
     return solve_batch_device_locked(p, opt, n_traj, d_rho0, n_param_slots, param_slots, d_param_values, time_count, width,
                                      d_values, d_stats, stream);
 }
@@ -668,7 +695,7 @@ obe_status obe_plan_set_shape(obe_plan* p, int32_t tpt, int32_t gpb) {
         return OBE_ERR_INVALID;
     }
     if (gpb < 0) { set_error("trajectories per CTA must be non-negative"); return OBE_ERR_INVALID; }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> lock(p->mu);
     relayout(p, tpt > 0 ? tpt : default_width(p));
     p->shape_tpt = tpt;
     p->shape_gpb = gpb;
@@ -688,7 +715,7 @@ obe_status obe_plan_autotune(obe_plan* p, const obe_solve_options* opt, int64_t 
     if (!p || !opt) { set_error("null argument"); return OBE_ERR_INVALID; }
     if (n_traj <= 0) { set_error("autotuning needs a non-empty batch"); return OBE_ERR_INVALID; }
     if (probe_steps < 1) { set_error("probe_steps must be positive"); return OBE_ERR_INVALID; }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> lock(p->mu);
     const int gpb_before = p->shape_gpb;
     obe_status st = ensure_ready(p);
     if (st != OBE_OK) return st;
@@ -699,7 +726,7 @@ obe_status obe_plan_autotune(obe_plan* p, const obe_solve_options* opt, int64_t 
     int cplx = 0;
     if ((st = validate_options(p, opt, save_times, cb, &w, &cplx)) != OBE_OK) return st;
     if (w != width) { set_error("output width mismatch"); return OBE_ERR_INVALID; }
-    const bool mixed = opt->precision == OBE_PRECISION_MIXED;
+    const bool mixed = is_mixed(opt->precision);
     const int vm_depth = std::max(p->dev.max_stack, std::max(cb.ev_len, 1));
     // candidates: the automatic width and the wider compiled ones up to 4x it, in the same
     // memory layout; each with as many trajectories per CTA as fit, half of that, and one
@@ -790,6 +817,7 @@ struct JobStreams {
     cudaEvent_t start = nullptr;
 };
 JobStreams g_job_streams;
+std::mutex g_multi_mutex;  // the job streams above: one heterogeneous batch at a time, taken before any plan's mutex
 
 obe_status job_streams(int dev, JobStreams** out) {
     JobStreams& J = g_job_streams;
@@ -862,7 +890,7 @@ obe_status prepare_jobs(int32_t n_jobs, const obe_batch_job* jobs, std::vector<P
         if ((st = validate_options(q.p, q.j->opt, q.save_times, q.cb, &w, &q.cplx)) != OBE_OK) return job_fail(k, st);
         if (w != q.j->width) { set_error("output width mismatch"); return job_fail(k, OBE_ERR_INVALID); }
         const int vm_depth = std::max(q.p->dev.max_stack, std::max(q.cb.ev_len, 1));
-        if ((st = plan_launch(q.p->dev, q.j->opt->precision == OBE_PRECISION_MIXED, std::max<int64_t>(q.j->n_traj, 1), vm_depth,
+        if ((st = plan_launch(q.p->dev, is_mixed(q.j->opt->precision), std::max<int64_t>(q.j->n_traj, 1), vm_depth,
                               &q.shape, q.p->shape_gpb)) != OBE_OK)
             return job_fail(k, st);
         q.errs_off = align16(q.cb.bytes.size());
@@ -899,7 +927,11 @@ obe_status obe_solve_multi_device(int32_t n_jobs, const obe_batch_job* jobs, voi
     }
     if (n_jobs == 0) return OBE_OK;
     if (!jobs) { set_error("null argument"); return OBE_ERR_INVALID; }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> multi_lock(g_multi_mutex);
+    std::vector<obe_plan*> job_plans;
+    for (int k = 0; k < n_jobs; ++k)
+        if (jobs[k].plan) job_plans.push_back(const_cast<obe_plan*>(jobs[k].plan));
+    PlanLocks plan_locks(job_plans.begin(), job_plans.end());
     std::vector<PreparedJob> pj;
     obe_status pst = prepare_jobs(n_jobs, jobs, pj);
     if (pst != OBE_OK) return pst;
@@ -972,7 +1004,11 @@ obe_status obe_multi_graph_create(int32_t n_jobs, const obe_batch_job* jobs, obe
         return OBE_ERR_INVALID;
     }
     if (!jobs) { set_error("null argument"); return OBE_ERR_INVALID; }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> multi_lock(g_multi_mutex);
+    std::vector<obe_plan*> job_plans;
+    for (int k = 0; k < n_jobs; ++k)
+        if (jobs[k].plan) job_plans.push_back(const_cast<obe_plan*>(jobs[k].plan));
+    PlanLocks plan_locks(job_plans.begin(), job_plans.end());
     std::vector<PreparedJob> pj;
     obe_status st = prepare_jobs(n_jobs, jobs, pj);
     if (st != OBE_OK) return st;
@@ -1057,7 +1093,9 @@ obe_status obe_multi_graph_launch(obe_multi_graph* G, void* stream) {
     g_launches = 0;
     if (!G || !G->exec) { set_error("null argument"); return OBE_ERR_INVALID; }
     {
-        std::lock_guard<std::mutex> lock(g_plan_mutex);
+        std::vector<obe_plan*> gp;
+        for (const auto& im : G->images) gp.push_back(const_cast<obe_plan*>(im.first));
+        PlanLocks plan_locks(gp.begin(), gp.end());
         for (const auto& im : G->images)
             if (!im.first->d_blob || im.first->image_gen != im.second) {
                 set_error("a plan of this graph was laid out again (launch shape changed) since it was recorded: "
@@ -1077,7 +1115,7 @@ static obe_status solve_host(obe_plan* p, const obe_solve_options* o, long long 
                              int64_t width, double* values, obe_traj_stats* stats_out, double* times_out, bool single,
                              std::vector<obe_traj_stats>* stats_vec) {
     g_launches = 0;
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> lock(p->mu);
     obe_status st = ensure_ready(p);
     if (st != OBE_OK) return st;
     if (n_axes > 0) {
@@ -1307,7 +1345,7 @@ obe_status obe_grad_forward(const obe_plan* plan_c, const obe_solve_options* opt
     obe_status st = grad_check(p, opt, &gw);
     if (st != OBE_OK) return st;
     if (gw != width) { set_error("output width mismatch"); return OBE_ERR_INVALID; }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> lock(p->mu);
     if ((st = ensure_ready(p)) != OBE_OK) return st;
     if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
     std::vector<double> save_times;
@@ -1355,7 +1393,7 @@ obe_status obe_grad_backward(const obe_plan* plan_c, const obe_solve_options* op
             return OBE_ERR_INVALID;
         }
     }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    std::lock_guard<std::mutex> lock(p->mu);
     if ((st = ensure_ready(p)) != OBE_OK) return st;
     if ((st = check_params(p, n_param_slots, param_slots)) != OBE_OK) return st;
     std::vector<double> save_times;
@@ -1463,12 +1501,12 @@ static obe_status rhs_eval(const obe_plan* plan, int64_t count, const double* t,
     obe_plan* p = const_cast<obe_plan*>(plan);
     if (!p || !t || !y || !dy || count <= 0) { set_error("invalid RHS arguments"); return OBE_ERR_INVALID; }
     if (!p->has_expanded && !p->packed.eff) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
-    if (p->packed.eff && precision == OBE_PRECISION_MIXED) { set_error("effective-Hamiltonian plans solve in double precision"); return OBE_ERR_UNSUPPORTED; }
-    std::lock_guard<std::mutex> lock(g_plan_mutex);
+    if (p->packed.eff && is_mixed(precision)) { set_error("effective-Hamiltonian plans solve in double precision"); return OBE_ERR_UNSUPPORTED; }
+    std::lock_guard<std::mutex> lock(p->mu);
     obe_status st = ensure_ready(p);
     if (st != OBE_OK) return st;
     if ((st = check_params(p, n_override_slots, override_slots)) != OBE_OK) return st;
-    const bool mixed = precision == OBE_PRECISION_MIXED;
+    const bool mixed = is_mixed(precision);
     LaunchShape s;
     const int vm_depth = std::max(p->dev.max_stack, 1);
     // the RHS kernel keeps both forms in the double-precision group layout
@@ -1573,9 +1611,9 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
     if (!p->has_expanded && !p->packed.eff) { set_error("execution_mode='expanded_sparse' requires a decomposed Hamiltonian plan"); return OBE_ERR_INVALID; }
     if (obe_device_count() <= 0) { set_error("no CUDA device is available: the GB300 solver has no CPU fallback"); return OBE_ERR_CUDA; }
     // lock order: the scratch array, then the plan (obe_plan_set_shape / obe_plan_autotune change
-    // the plan's launch shape and layout under g_plan_mutex while this call reads them)
+    // the plan's launch shape and layout under the plan's mutex while this call reads them)
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    std::lock_guard<std::mutex> plan_lock(g_plan_mutex);
+    std::lock_guard<std::mutex> plan_lock(p->mu);
     int dev = 0;
     if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return OBE_ERR_CUDA;
     if (dev < 0 || dev >= 64) { set_error("device index out of range for the allocation-free entry point"); return OBE_ERR_UNSUPPORTED; }
@@ -1633,7 +1671,7 @@ extern "C" obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const
     A.k1_refresh = k1_refresh_interval();
     A.vm_depth = std::max(P.max_stack, std::max(cb.ev_len, 1));
 
-    const bool mixed = opt->precision == OBE_PRECISION_MIXED;
+    const bool mixed = is_mixed(opt->precision);
     LaunchShape shape;
     if ((st = plan_launch(P, mixed, n_traj, A.vm_depth, &shape, p->shape_gpb)) != OBE_OK) return st;
     if (shape.gstride > 0) {

@@ -4,7 +4,7 @@
  * This is the native boundary that replaces the reference's PyO3 extension for the Lindblad
  * hot path (crate `centrex_tlf_rust`, rust/src/lindblad/python_api.rs).  Every entry point
  * takes plain pointers and sizes; nothing here names a Python, Rust or torch type.  All
- * arithmetic on the device is FP64 unless a solve asks for OBE_PRECISION_MIXED.
+ * arithmetic on the device is FP64 unless a solve asks for a mixed precision (obe_precision).
  *
  * Error convention: every function returns an obe_status.  On failure the message of the
  * matching reference error (a Python ValueError there) is available from obe_last_error()
@@ -52,7 +52,22 @@ typedef enum {
 
 typedef enum { OBE_EVENT_NONE = 0, OBE_EVENT_POPULATION = 1, OBE_EVENT_EXPRESSION = 2 } obe_event_kind;
 
-typedef enum { OBE_PRECISION_FP64 = 0, OBE_PRECISION_MIXED = 1 } obe_precision;
+/*
+ * Precision of an adaptive solve (no counterpart in the reference, which is FP64 throughout).
+ *   OBE_PRECISION_FP64: every operation in double precision (the drop-in form).
+ *   OBE_PRECISION_MIXED: the RHS coefficient products in single precision (as stage deviations
+ *     d_s = K_s - K_1, see obe_kernels.cuh); the stage combinations, the state accumulation, the
+ *     error norm and the step-size controller in double precision, and, for a trace-preserving
+ *     plan, the trace renormalised in double precision after every accepted step.
+ *   OBE_PRECISION_MIXED_FP32_CONTROL: as OBE_PRECISION_MIXED, but the stage inputs, the error
+ *     norm and the controller in single precision and no renormalisation (faster, step sizes
+ *     ~1e-7 relative from a double-precision controller's).  Forward solves only.
+ */
+typedef enum {
+    OBE_PRECISION_FP64 = 0,
+    OBE_PRECISION_MIXED = 1,
+    OBE_PRECISION_MIXED_FP32_CONTROL = 2
+} obe_precision;
 
 /*
  * A compiled expression program: the reference's bytecode (centrex_tlf/lindblad/ir.py:28-47,
@@ -176,6 +191,10 @@ void obe_plan_destroy(obe_plan* plan);
 /* Packed length n*n and state count of a plan. */
 int64_t obe_plan_packed_len(const obe_plan* plan);
 int32_t obe_plan_n_states(const obe_plan* plan);
+/* 1 when the plan's RHS keeps the trace of every state for every coefficient value (no
+ * population leaves the system), as found by the packer; OBE_PRECISION_MIXED then renormalises the
+ * trace after every accepted step.  No counterpart in the reference. */
+int32_t obe_plan_trace_preserving(const obe_plan* plan);
 
 /*
  * One RHS evaluation per state on the device: lindblad_rhs_py(plan, packed_state, t,

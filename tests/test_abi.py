@@ -186,3 +186,26 @@ def test_packed_index_layout():
     assert slots == list(range(n, n * n, 2))
     assert packed_upper_real_index(3, 0, 1) == 3 and packed_upper_real_index(3, 0, 2) == 5
     assert packed_upper_real_index(3, 1, 2) == 7
+
+
+def test_trace_preservation_found_on_host(golden):
+    """The packer finds which plans keep the trace (the mixed form renormalises those): every
+    reference-built system here does; dropping the transfer of one decay channel breaks it."""
+    import copy
+
+    from centrex_tlf_gb300.native import NativePlan
+
+    for name in ("two_level", "two_level_td", "chain3", "q1_16", "r0_39", "rc_76"):
+        assert NativePlan(golden(f"plan_{name}")["payload"]).trace_preserving, name
+    payload = copy.deepcopy(golden("plan_two_level")["payload"])
+    e = payload["expanded_rhs_plan"]
+    n = payload["n_states"]
+    # the +rate rho_11 transfer into rho_00: the term of output (0, 0) whose input is (1, 1)
+    diag1 = n  # upper index of (1, 1)
+    terms = [t for t in range(int(e["output_ptrs"][0]), int(e["output_ptrs"][1]))
+             if int(e["input_indices"][t]) == diag1 and int(e["coeff_indices"][t]) < 0]
+    assert terms
+    fr = np.array(e["factors_re"], dtype=float)
+    fr[terms[0]] *= 0.5
+    e["factors_re"] = fr
+    assert not NativePlan(payload).trace_preserving

@@ -15,7 +15,9 @@ the device VM are checked:
   discontinuous ones (square wave, sawtooth, on/off gates, alternating sign).  At each jump the
   controller rejects and retries, and rounding-level differences in h decide where the step past
   the jump lands, so those solves agree to the solver's tolerance (rtol 1e-8) accumulated over
-  the ~30 jumps in [0, 3] (measured: 2.9e-7 for the 0.4-periodic on/off gate), not to rounding.
+  the ~30 jumps in [0, 3] (measured: 2.9e-7 for the 0.4-periodic on/off gate), not to rounding;
+  the interpolation tables have kinks at their knots (linear: C0, PCHIP: C1), where the error
+  estimate jumps and the step sequences part at rounding level: 1e-7 (measured 5.7e-9 for PCHIP).
 """
 
 from __future__ import annotations
@@ -30,6 +32,7 @@ from centrex_tlf_gb300.native import NativePlan
 pytestmark = pytest.mark.gpu
 
 DISCONTINUOUS = {4, 6, 7, 12, 13}
+KINKED = {14, 16}  # interpolation tables: C0 (linear) and C1 (PCHIP) at the knots and table ends
 
 
 @pytest.mark.parametrize("index", range(18))
@@ -52,7 +55,7 @@ def test_helper_solve_matches_oracle(golden, index):
     op = oracle.OraclePlan(h["payload"])
     rho0 = np.array([1.0, 0.0, 0.0, 0.0])
     saveat = np.linspace(0.0, 3.0, 13)
-    tol = 1e-6 if h["helper_id"] in DISCONTINUOUS else 1e-9
+    tol = 1e-6 if h["helper_id"] in DISCONTINUOUS else (1e-7 if h["helper_id"] in KINKED else 1e-9)
     times, vals, width, st = api.solve_lindblad_ode_py(plan, rho0, 0.0, 3.0, 1e-10, 1e-8, 1e-3, saveat, True, 100000,
                                                        "expanded_sparse", "dopri5", "full")
     o = op.options(t0=0.0, t1=3.0, abstol=1e-10, reltol=1e-8, dt=1e-3, saveat=saveat, save_start=True,

@@ -157,10 +157,10 @@ def test_q1_integral_trace_final_and_rate(q1):
     np.testing.assert_allclose(v, rv.reshape(-1), atol=1e-10)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6), ("mixed_fp32_control", 1e-6)])
 def test_q1_parameter_scan_matches_oracle(q1, precision, tol):
     """The benchmark scan (Tsit5, excited-population integral and final populations) on 96
-    seeded points of its distribution; the mixed form holds the 1e-6 population bar."""
+    seeded points of its distribution; both mixed forms hold the 1e-6 population bar."""
     d, plan, op = q1
     gamma, (t0, t1) = d["gamma"], d["t_span"]
     params = _scan_params(d, 96, seed=3)
@@ -279,3 +279,22 @@ def test_device_resident_batch_matches_host_batch(q1):
     np.testing.assert_array_equal(d_val.cpu().numpy(), np.asarray(host_vals))
     status = d_st.view(params.shape[0], 6)[:, 3].cpu().numpy() >> 32
     assert np.all(status == 0)
+
+
+def test_mixed_form_keeps_the_trace(q1):
+    """The mixed form renormalises the trace in double precision after every accepted step on a
+    trace-preserving plan: the final populations sum to the initial trace to rounding (the
+    single-precision-control variant, which does not renormalise, drifts by its rounding)."""
+    d, plan, op = q1
+    assert plan.native.trace_preserving
+    gamma, (t0, t1) = d["gamma"], d["t_span"]
+    params = _scan_params(d, 64, seed=21)
+    rho0 = np.repeat(d["rho0_packed"].reshape(1, -1), params.shape[0], axis=0)
+    drift = {}
+    for precision in ("mixed", "mixed_fp32_control"):
+        _, pops, _, _, _ = api.solve_lindblad_batch_ode_py(
+            plan, rho0, t0, t1, 1e-11, 1e-8, 1e-3 / gamma, solver="tsit5", output="populations",
+            parameter_slot_indices=_slots(d), parameter_batch=params, precision=precision)
+        drift[precision] = float(np.max(np.abs(np.asarray(pops).reshape(-1, 16).sum(axis=1) - 1.0)))
+    assert drift["mixed"] <= 1e-13, drift
+    assert drift["mixed_fp32_control"] <= 1e-6, drift
