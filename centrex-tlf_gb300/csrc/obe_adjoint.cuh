@@ -578,10 +578,11 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 }
                 stage_classes<TPT>(P, s_cstat, s_cdyn, nd, cv, lt);
                 for (int s = 0; s < 6; ++s) {
+                    const double hcs = h * kCsum.c[M][s];
                     for (int i = lt; i < N; i += TPT) {
-                        double acc = kCsum.c[M][s] * k1x[i];
-                        for (int j = 1; j <= s; ++j) acc = fma(kTab.a[M][s][j], f2d(K32[static_cast<size_t>(j - 1) * N + i]), acc);
-                        const float dv = d2f(h * acc);
+                        double acc = hcs * k1x[i];
+                        for (int j = 1; j <= s; ++j) acc = fma(h * kTab.a[M][s][j], f2d(K32[static_cast<size_t>(j - 1) * N + i]), acc);
+                        const float dv = d2f(acc);
                         const float yv32 = d2f(yx[i]);
                         if (i < n) {
                             G4[i] = make_float4(dv, 0.f, yv32, 0.f);
@@ -606,9 +607,9 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     fo[i] = d2f(yx[i]);
                     fo[N + i] = k1fx[i];
                     for (int r = 0; r < 6; ++r) fo[static_cast<size_t>(2 + r) * N + i] = K32[static_cast<size_t>(r) * N + i];
-                    double acc = kCsum.c[M][5] * k1x[i];
-                    for (int j = 1; j < 6; ++j) acc = fma(kTab.a[M][5][j], f2d(K32[static_cast<size_t>(j - 1) * N + i]), acc);
-                    yx[i] = yx[i] + h * acc;
+                    double acc = (h * kCsum.c[M][5]) * k1x[i];
+                    for (int j = 1; j < 6; ++j) acc = fma(h * kTab.a[M][5][j], f2d(K32[static_cast<size_t>(j - 1) * N + i]), acc);
+                    yx[i] = yx[i] + acc;
                     if (i < n) tr += yx[i];
                 }
                 double rf = 1.0;

@@ -337,6 +337,24 @@ __device__ __forceinline__ float d2f(double d) {
     return __uint_as_float(sign | r);
 }
 
+// max(|a|, |b|) of two doubles by their bit patterns (integer pipe; for non-negative doubles the
+// integer order of the bits is the numeric order)
+__device__ __forceinline__ double max_abs(double a, double b) {
+    const long long ia = __double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFLL;
+    const long long ib = __double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFLL;
+    return __longlong_as_double(ia > ib ? ia : ib);
+}
+
+// 1 / x for x > 0: a single-precision reciprocal refined by one Newton-Raphson step in double
+// (r1 = r0 + r0 (1 - x r0)), relative error ~(2^-23)^2; x outside the single-precision normal
+// range takes the double division
+__device__ __forceinline__ double recip_nr(double x) {
+    const uint32_t e = (static_cast<uint32_t>(__double2hiint(x)) >> 20) & 0x7FFu;
+    if (e < 898u || e > 1149u) return 1.0 / x;
+    const double r0 = f2d(__frcp_rn(d2f(x)));
+    return fma(r0, fma(-x, r0, 1.0), r0);
+}
+
 __device__ __forceinline__ int gslot64(int i, int n) { return i < n ? 2 * i : n + i; }
 // float index of packed element i's deviation inside G4 (float4[U]); + 2 for y_n
 __device__ __forceinline__ int gslot32(int i, int n) { return i < n ? 4 * i : 4 * (n + ((i - n) >> 1)) + ((i - n) & 1); }
@@ -381,6 +399,15 @@ __device__ __forceinline__ double2 eval_expr(const DevPlan& P, DevExpr e, const 
 static __device__ __noinline__ void eval_compounds(const DevPlan& P, VMLane L, double t, bool only_dynamic) {
     for (int c = 0; c < P.n_comp; ++c)
         if (!only_dynamic || P.comp_dynamic[c]) L.slots[P.comp_slot[c]] = eval_expr(P, P.comp_expr[c], L, t);
+}
+
+// The time-dependent compounds and coefficients at time t into one coefficient row: one call
+// site per lane and step in the integrator (the registers live across a call are saved around
+// it, so the VM's work sits behind a single call).
+static __device__ __noinline__ void dyn_row(const DevPlan& P, VMLane L, double t, double2* row) {
+    for (int c = 0; c < P.n_comp; ++c)
+        if (P.comp_dynamic[c]) L.slots[P.comp_slot[c]] = eval_expr(P, P.comp_expr[c], L, t);
+    for (int j = 0; j < P.n_dyn; ++j) row[j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t);
 }
 
 __device__ __forceinline__ double2 coeff_value(const DevPlan& P, int cls, const double2* cstat, const double2* crow) {
@@ -599,14 +626,11 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
         const float4 cn = T4[w1 >> kRecCoefShift];
         const float4 vn = G4[w1 & kRecIndexMask];
         if (w & kRecConj) { v.y = -v.y; v.w = -v.w; }
-        ar = fmaf(c.x, v.x, ar);
-        ar = fmaf(-c.y, v.y, ar);
-        ar = fmaf(c.z, v.z, ar);
-        ar = fmaf(-c.w, v.w, ar);
-        ai = fmaf(c.x, v.y, ai);
-        ai = fmaf(c.y, v.x, ai);
-        ai = fmaf(c.z, v.w, ai);
-        ai = fmaf(c.w, v.z, ai);
+        // the record's product off the accumulator's chain: one add per record on ar / ai, so the
+        // products of consecutive records overlap (one warp per trajectory leaves little else to
+        // hide the FMA latency behind)
+        ar += fmaf(c.x, v.x, fmaf(-c.y, v.y, fmaf(c.z, v.z, -c.w * v.w)));
+        ai += fmaf(c.x, v.y, fmaf(c.y, v.x, fmaf(c.z, v.w, c.w * v.z)));
         if (w & kRecFlush) {
             uint32_t d = s_out[o * TPT + lt];
             K[d & 0xFFFFu] = ar;
@@ -889,8 +913,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
         // evaluate the time-dependent coefficients at t into row `row` of s_cdyn (lane 0)
         auto dyn_coeffs_at = [&](double t, int row) {
             if (P.n_dyn > 0 && lt == 0) {
-                eval_compounds(P, L, t, true);
-                for (int j = 0; j < P.n_dyn; ++j) s_cdyn[row * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t);
+                dyn_row(P, L, t, s_cdyn + row * nd);
             }
         };
         // one double-precision RHS from the slot buffer: formulas for coefficient row `row`, gather into out
@@ -981,8 +1004,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                         if (lt == 5 || lt == 0 || lt == 4 || dp) {
                             double ts = x;
                             if (lt < 5) ts = dp ? x + h * (lt < 4 ? kTab.c[0][lt] : 1.0) : (lt == 0 ? x + 0.5 * h : x + h);
-                            eval_compounds(P, L, ts, true);
-                            for (int j = 0; j < P.n_dyn; ++j) s_cdyn[lt * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, ts);
+                            dyn_row(P, L, ts, s_cdyn + lt * nd);
                         }
                     }
                     // k_1 = f(x, y)
@@ -1152,6 +1174,9 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
         // controller state (common.rs:20-46)
         const double beta = 0.04, alpha = 0.2 - beta * 0.75, facc1 = 1.0 / 0.2, facc2 = 1.0 / 10.0, safety = 0.9;
         double fac_old = 1.0e-4;
+        // log2(1e-4): the mixed form's controller keeps log2(fac_old)
+        constexpr double kLog2Fac0 = -13.287712379549449;
+        double lfac_old = kLog2Fac0;
         float fac_old32 = 1.0e-4f;
         const float atolf = static_cast<float>(A.atol), rtolf = static_cast<float>(A.rtol);  // mixed error norm
         const double h_maxc = fabs(t1 - t0);
@@ -1215,8 +1240,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             if (P.n_dyn > 0 && lt < 5) {
                 double c = lt < 4 ? kTab.c[M][lt] : 1.0;
                 double ts = x + h * c;
-                eval_compounds(P, L, ts, true);
-                for (int j = 0; j < P.n_dyn; ++j) s_cdyn[lt * nd + j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, ts);
+                dyn_row(P, L, ts, s_cdyn + lt * nd);
             }
             if constexpr (MIXED) {
                 gsync<TPT>(g);
@@ -1269,7 +1293,11 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                     // variant (A.ctrl32) sums the deviation in single precision.
                     const float csum = kTabF.csum[M][s];
                     if (!ctrl32) {
-                        const double cs = kCsum.c[M][s];
+                        // the step size folded into the stage's weights once per stage
+                        const double hcs = h * kCsum.c[M][s];
+                        double ha[5];
+#pragma unroll
+                        for (int j = 1; j < 6; ++j) ha[j - 1] = j <= s ? h * kTab.a[M][s][j] : 0.0;
                         if constexpr (TPT >= 256) {
                             constexpr int kCh = EPT < 8 ? EPT : 8;
 #pragma unroll
@@ -1290,11 +1318,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                                     const int e = e0 + c;
                                     const int i = lt + e * TPT;
                                     if (i < N) {
-                                        double acc = cs * k1d[c];
+                                        double dv = hcs * k1d[c];
 #pragma unroll
                                         for (int j = 1; j < 6; ++j)
-                                            if (j <= s) acc = fma(kTab.a[M][s][j], f2d(kv[c][j - 1]), acc);
-                                        const double dv = h * acc;
+                                            if (j <= s) dv = fma(ha[j - 1], f2d(kv[c][j - 1]), dv);
                                         if (s == 5) yn[e] = y[e] + dv;
                                         s_G4f[gslot32(i, n)] = d2f(dv);
                                     }
@@ -1305,11 +1332,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             for (int e = 0; e < EPT; ++e) {
                                 const int i = lt + e * TPT;
                                 if (i < N) {
-                                    double acc = cs * s_k1[i];
+                                    double dv = hcs * s_k1[i];
 #pragma unroll
                                     for (int j = 1; j < 6; ++j)
-                                        if (j <= s) acc = fma(kTab.a[M][s][j], f2d(s_K32[static_cast<size_t>(j - 1) * N + i]), acc);
-                                    const double dv = h * acc;
+                                        if (j <= s) dv = fma(ha[j - 1], f2d(s_K32[static_cast<size_t>(j - 1) * N + i]), dv);
                                     if (s == 5) yn[e] = y[e] + dv;
                                     s_G4f[gslot32(i, n)] = d2f(dv);
                                 }
@@ -1372,9 +1398,11 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                     gather_dev<TPT>(P, s_rec, s_out, s_T4, s_G4, s_K32 + static_cast<size_t>(s) * N, lt);
                     gsync<TPT>(g);
                 }
-                // error estimate from the deviations alone (the error weights sum to zero): the
-                // weighted sums, the per-element ratios, their sum and the norm in double (the
-                // single-precision-control variant: in single precision)
+                // error estimate from the deviations alone (the error weights sum to zero): each
+                // element's estimate h sum_j e_j d_j is a combination of the single-precision d_j,
+                // summed in single precision and converted exactly; its scale from the double state,
+                // the ratio, the sum of squares and the norm in double (the single-precision-control
+                // variant: all in single precision)
                 if (!ctrl32) {
                     if constexpr (TPT >= 256) {
                         constexpr int kCh = EPT < 8 ? EPT : 8;
@@ -1391,12 +1419,12 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             for (int c = 0; c < kCh; ++c) {
                                 const int e = e0 + c;
                                 if (lt + e * TPT < N) {
-                                    double acc = 0.0;
+                                    float acc = 0.f;
 #pragma unroll
                                     for (int j = 1; j < 7; ++j)
-                                        if (M == 1 || j != 1) acc = fma(kTab.e[M][j], f2d(kv[c][j - 1]), acc);
-                                    const double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
-                                    const double q = (h * acc) / sc;
+                                        if (M == 1 || j != 1) acc = fmaf(kTabF.e[M][j], kv[c][j - 1], acc);
+                                    const double sc = fma(max_abs(y[e], yn[e]), A.rtol, A.atol);
+                                    const double q = h * f2d(acc) * recip_nr(sc);
                                     err = fma(q, q, err);
                                 }
                             }
@@ -1406,12 +1434,12 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                         for (int e = 0; e < EPT; ++e) {
                             const int i = lt + e * TPT;
                             if (i < N) {
-                                double acc = 0.0;
+                                float acc = 0.f;
 #pragma unroll
                                 for (int j = 1; j < 7; ++j)
-                                    if (M == 1 || j != 1) acc = fma(kTab.e[M][j], f2d(s_K32[static_cast<size_t>(j - 1) * N + i]), acc);
-                                const double sc = A.atol + fmax(fabs(y[e]), fabs(yn[e])) * A.rtol;
-                                const double q = (h * acc) / sc;
+                                    if (M == 1 || j != 1) acc = fmaf(kTabF.e[M][j], s_K32[static_cast<size_t>(j - 1) * N + i], acc);
+                                const double sc = fma(max_abs(y[e], yn[e]), A.rtol, A.atol);
+                                const double q = h * f2d(acc) * recip_nr(sc);
                                 err = fma(q, q, err);
                             }
                         }
@@ -1498,6 +1526,16 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 accept_step = err32 <= 1.0f;
                 if (accept_step) fac_old32 = fmaxf(err32, 1.0e-4f);
                 else hn = h * f2d(1.0f / fminf(static_cast<float>(facc1), f11 / static_cast<float>(safety)));
+            } else if (MIXED) {
+                // the same controller in double as exp2 of logarithms, the old factor's logarithm
+                // kept from the step that set it: err^alpha fac_old^-beta = 2^(alpha log2 err - beta log2 fac_old)
+                const double lerr = log2(err);
+                fac11 = exp2(alpha * lerr);
+                double fac = exp2(alpha * lerr - beta * lfac_old);
+                fac = fmax(facc2, fmin(facc1, fac / safety));
+                hn = h / fac;
+                accept_step = err <= 1.0;
+                if (accept_step) lfac_old = fmax(lerr, kLog2Fac0);
             } else {
                 fac11 = pow(err, alpha);
                 double fac = fac11 * pow(fac_old, -beta);
