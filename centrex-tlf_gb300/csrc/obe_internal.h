@@ -125,6 +125,9 @@ struct DevPlan {
     // the RHS keeps the trace for every coefficient value (sum over the diagonal outputs of every
     // input's and coefficient's products is zero): the mixed form renormalises the trace
     int32_t trace_preserving;
+    // per Hamiltonian coefficient: the largest |factor| of the RHS terms it multiplies (the weight
+    // of that coefficient's magnitude in the launch's cost estimate per trajectory)
+    const double* coeff_scale;   // [n_coeff]
     // interpolated effective-Hamiltonian plans (eff != 0; N = real_dim): the RHS is
     // L_c(x) y + (Omega / 2) L_o(x) y + delta L_d(x) y with x, Omega, delta = coefficients 0, 1, 2
     int32_t eff;
@@ -183,6 +186,7 @@ struct HostPacked {
     int32_t n_vm_slots = 0;     // parameter slots plus the hoisted static subexpressions
     int32_t dyn_real_closed = 0;  // every time-dependent compound is real_ok
     int32_t trace_preserving = 0;
+    std::vector<double> coeff_scale;
 };
 
 }  // namespace obe
@@ -208,6 +212,9 @@ struct obe_plan {
     // global stage buffers of large systems (grow-only)
     void* d_gk = nullptr;
     size_t gk_bytes = 0;
+    // the cost-ordered queue of a launch: per trajectory its cost estimate and the order (grow-only)
+    void* d_ord = nullptr;
+    size_t ord_bytes = 0;
     // launch shape fixed by obe_plan_set_shape / obe_plan_autotune (0: the automatic choice)
     int32_t shape_tpt = 0, shape_gpb = 0;
     // serialises the entry points that use this plan's layout, device image and scratch; calls on

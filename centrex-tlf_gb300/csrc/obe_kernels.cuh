@@ -179,6 +179,7 @@ struct CallArgs {
     TrajErr* errs;
     unsigned long long* counter;
     int k1_refresh;  // mixed form: recompute k_1 in double every this many accepted steps
+    const long long* order;   // queue position -> trajectory (cost-ordered launches), or null: identity
     unsigned char* gscratch;  // large systems: per-group global slices of the stage buffers
     size_t gstride;           // bytes per slice
     // gradient tape (double-precision adaptive solves), null when off.  tape_ckpt == 0: per
@@ -741,7 +742,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
     }
 
     while (true) {
-        if (lt == 0) *s_traj = static_cast<long long>(atomicAdd(A.counter, 1ull));
+        if (lt == 0) {
+            const long long q = static_cast<long long>(atomicAdd(A.counter, 1ull));
+            *s_traj = q < A.n_traj && A.order ? A.order[q] : q;
+        }
         gsync<TPT>(g);
         const long long traj = *s_traj;
         gsync<TPT>(g);

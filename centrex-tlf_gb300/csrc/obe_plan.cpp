@@ -764,6 +764,13 @@ obe_status pack_plan(const obe_plan_desc* d, obe_plan* p) {
             }
             hp.trace_preserving = keeps ? 1 : 0;
         }
+        // the cost estimate's weights: per coefficient, its largest term factor
+        hp.coeff_scale.assign(static_cast<size_t>(std::max<int64_t>(d->n_coefficients, 1)), 0.0);
+        for (int64_t t = 0; t < T; ++t) {
+            const int64_t k = d->coeff_indices[t];
+            if (k >= 0)
+                hp.coeff_scale[k] = std::max(hp.coeff_scale[k], std::max(std::fabs(d->factors_re[t]), std::fabs(d->factors_im[t])));
+        }
 
         // ---- records and formulas -----------------------------------------------------------
         // A formula is the exact list of (factor, class) products of the terms merged into one

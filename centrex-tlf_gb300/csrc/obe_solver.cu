@@ -64,6 +64,7 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     size_t o_rec = put(blob, h.rec), o_lo = put(blob, h.lane_out), o_fs = put(blob, h.fstream);
     size_t o_tr = put(blob, h.trec), o_li = put(blob, h.lane_in), o_bil = put(blob, h.bil);
     size_t o_eg = put(blob, h.eff_grid), o_er = put(blob, h.eff_rows), o_ec = put(blob, h.eff_cols), o_ef = put(blob, h.eff_coef);
+    size_t o_ks = put(blob, h.coeff_scale);
     P = DevPlan{};
     P.n = p->n;
     P.N = static_cast<int32_t>(p->N);
@@ -76,6 +77,7 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     P.n_base = p->n_base;
     P.dyn_real_closed = h.dyn_real_closed;
     P.trace_preserving = h.trace_preserving;
+    P.coeff_scale = reinterpret_cast<const double*>(base + o_ks);
     P.base_val = reinterpret_cast<const double*>(base + o_bv);
     P.base_tuple = reinterpret_cast<const int32_t*>(base + o_bt);
     P.tuple_ptr = reinterpret_cast<const int32_t*>(base + o_tp);
@@ -196,6 +198,140 @@ obe_status kscratch(obe_plan* p, size_t bytes, unsigned char** out) {
         p->gk_bytes = bytes;
     }
     *out = static_cast<unsigned char*>(p->d_gk);
+    return OBE_OK;
+}
+
+// ---- cost-ordered launches ---------------------------------------------------------------
+// A persistent launch pulls trajectories from a queue; in index order the launch lasts until its
+// slowest warp has worked through whichever trajectories it happened to pull, and the long ones
+// pulled last set that time (on the 16-state scan's 4096 points the makespan is 1.56x the
+// evenly shared work).  The queue is therefore ordered longest-first by a cost estimate made from
+// the inputs alone (no solve): the integral over the solve's time span of the Hamiltonian's
+// coefficient magnitude, sqrt(sum_k (|c_k(t)| s_k)^2) with s_k the largest factor of the terms
+// coefficient k multiplies (the generalised Rabi frequency of a driven transition), sampled at
+// kCostSamples times and cut at a runtime-expression stop event's first sign change (the ragged
+// end times).  Steps of an explicit adaptive solver scale with that phase; the order is a counting
+// sort into kOrderBuckets logarithmic buckets (longest first; within a bucket in any order).  The
+// results do not depend on the order: every trajectory's arithmetic is its own.
+constexpr int kCostSamples = 32;
+constexpr int kOrderBuckets = 1024;
+
+__global__ void __launch_bounds__(128) cost_kernel(const DevPlan P, const CallArgs A, float* cost, unsigned int* range) {
+    const long long traj = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (traj >= A.n_traj) return;
+    double2 slots[kMaxSlots], stk[kMaxStack];
+    int32_t tup[kMaxStack];
+    VMLane L;
+    L.slots = slots;
+    L.stack.v = stk;
+    L.stack.tup = tup;
+    L.real = false;
+    init_slots(P, A, traj, slots);
+    eval_compounds(P, L, A.t0, false);
+    bool real = P.dyn_real_closed != 0;
+    for (int i = 0; i < P.n_slots && real; ++i) real = slots[i].y == 0.0;
+    L.real = real;
+    double w0 = 0.0;
+    for (int k = 0; k < P.n_coeff; ++k) {
+        if (P.coeff_dynamic[k]) continue;
+        const double2 c = eval_expr(P, P.coeff_expr[k], L, A.t0);
+        const double a = hypot(c.x, c.y) * P.coeff_scale[k];
+        w0 += a * a;
+    }
+    const bool ev = A.ev_kind == OBE_EVENT_EXPRESSION && A.ev_len > 0;
+    double g0 = 0.0;
+    if (ev) g0 = vm_eval(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, L.slots, A.t0, L.stack).x;
+    const double dt = (A.t1 - A.t0) / kCostSamples;
+    double c = 0.0, span = 0.0;
+    for (int q = 0; q < kCostSamples; ++q) {
+        const double t = A.t0 + (q + 0.5) * dt;
+        if (P.n_dyn > 0 || ev) eval_compounds(P, L, t, true);
+        if (ev) {
+            const double gq = vm_eval(P, A.ev_op, A.ev_arg, A.ev_fn, A.ev_val, 0, A.ev_len, L.slots, t, L.stack).x;
+            if ((g0 < 0.0 && gq >= 0.0) || (g0 > 0.0 && gq <= 0.0)) break;
+        }
+        double w = w0;
+        for (int j = 0; j < P.n_dyn; ++j) {
+            const double2 cv = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t);
+            const double a = hypot(cv.x, cv.y) * P.coeff_scale[P.dyn_ids[j]];
+            w += a * a;
+        }
+        c += sqrt(w) * dt;
+        span += dt;
+    }
+    // a trajectory without a drive still orders by the length of its span
+    c += 1e-9 * span / (A.t1 - A.t0);
+    const float cf = isfinite(c) && c > 1e-30 ? static_cast<float>(c) : 1e-30f;
+    cost[traj] = cf;
+    atomicMin(&range[0], __float_as_uint(cf));  // positive floats order like their bit patterns
+    atomicMax(&range[1], __float_as_uint(cf));
+}
+
+__device__ __forceinline__ int cost_bucket(float c, const unsigned int* range) {
+    const float lo = logf(__uint_as_float(range[0])), hi = logf(__uint_as_float(range[1]));
+    if (!(hi > lo)) return 0;
+    const int b = static_cast<int>((hi - logf(c)) / (hi - lo) * (kOrderBuckets - 1) + 0.5f);
+    return b < 0 ? 0 : (b >= kOrderBuckets ? kOrderBuckets - 1 : b);
+}
+
+__global__ void order_histogram_kernel(long long n, const float* cost, const unsigned int* range, unsigned int* hist) {
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&hist[cost_bucket(cost[i], range)], 1u);
+}
+
+// exclusive scan of the bucket counts into bucket offsets, one thread (kOrderBuckets adds)
+__global__ void order_scan_kernel(unsigned int* hist) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned int run = 0;
+    for (int b = 0; b < kOrderBuckets; ++b) {
+        const unsigned int c = hist[b];
+        hist[b] = run;
+        run += c;
+    }
+}
+
+__global__ void order_scatter_kernel(long long n, const float* cost, const unsigned int* range, unsigned int* off,
+                                     long long* order) {
+    const long long i = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < n) order[atomicAdd(&off[cost_bucket(cost[i], range)], 1u)] = i;
+}
+
+bool ordering_enabled() {
+    static const bool on = [] {
+        const char* env = std::getenv("OBE_ORDER");
+        return !(env && env[0] == '0');
+    }();
+    return on;
+}
+
+// Fills A.order with the longest-first queue of this launch on `stream` (4 small kernels), from a
+// grow-only per-plan buffer; returns the number of launches issued.
+obe_status order_queue(obe_plan* p, CallArgs& A, cudaStream_t stream, int* launches) {
+    const long long n = A.n_traj;
+    const size_t o_ord = 0, o_cost = align16(static_cast<size_t>(n) * 8), o_hist = align16(o_cost + static_cast<size_t>(n) * 4);
+    const size_t o_rng = o_hist + kOrderBuckets * 4, bytes = align16(o_rng + 8);
+    if (p->ord_bytes < bytes) {
+        if (p->d_ord) cudaFree(p->d_ord);
+        p->d_ord = nullptr;
+        p->ord_bytes = 0;
+        if (!cuda_ok(cudaMalloc(&p->d_ord, bytes), "cudaMalloc(queue order)")) return OBE_ERR_CUDA;
+        p->ord_bytes = bytes;
+    }
+    unsigned char* b = static_cast<unsigned char*>(p->d_ord);
+    long long* order = reinterpret_cast<long long*>(b + o_ord);
+    float* cost = reinterpret_cast<float*>(b + o_cost);
+    unsigned int* hist = reinterpret_cast<unsigned int*>(b + o_hist);
+    unsigned int* range = reinterpret_cast<unsigned int*>(b + o_rng);
+    if (!cuda_ok(cudaMemsetAsync(hist, 0, kOrderBuckets * 4 + 8, stream), "cudaMemsetAsync(order)")) return OBE_ERR_CUDA;
+    if (!cuda_ok(cudaMemsetAsync(range, 0xFF, 4, stream), "cudaMemsetAsync(order)")) return OBE_ERR_CUDA;
+    const unsigned int blocks = static_cast<unsigned int>((n + 127) / 128);
+    cost_kernel<<<blocks, 128, 0, stream>>>(p->dev, A, cost, range);
+    order_histogram_kernel<<<blocks, 128, 0, stream>>>(n, cost, range, hist);
+    order_scan_kernel<<<1, 32, 0, stream>>>(hist);
+    order_scatter_kernel<<<blocks, 128, 0, stream>>>(n, cost, range, hist, order);
+    if (!cuda_ok(cudaGetLastError(), "order kernels")) return OBE_ERR_CUDA;
+    A.order = order;
+    *launches = 4;
     return OBE_OK;
 }
 
@@ -553,6 +689,16 @@ obe_status solve_device(obe_plan* p, const obe_solve_options* o, long long n_tra
         A.gstride = s.gstride;
     }
     if (!cuda_ok(cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync")) return OBE_ERR_CUDA;
+    // longest-first queue when the batch runs in more than one wave (not while a graph records:
+    // the order's buffer may have to grow)
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    if (!cuda_ok(cudaStreamIsCapturing(stream, &cap_status), "cudaStreamIsCapturing")) return OBE_ERR_CUDA;
+    if (ordering_enabled() && !p->packed.eff && cap_status == cudaStreamCaptureStatusNone &&
+        n_traj > static_cast<long long>(s.blocks) * s.gpb) {
+        int n_order = 0;
+        if ((st = order_queue(p, A, stream, &n_order)) != OBE_OK) return st;
+        g_launches += n_order;
+    }
     if (!cuda_ok(launch_integrate(p, A, is_mixed(o->precision), o->solver, s, stream), "kernel launch")) return OBE_ERR_CUDA;
     g_launches += 1;
     return OBE_OK;
@@ -608,6 +754,7 @@ void obe_plan_destroy(obe_plan* plan) {
     if (plan->d_blob) cudaFree(plan->d_blob);
     if (plan->d_scratch) cudaFree(plan->d_scratch);
     if (plan->d_gk) cudaFree(plan->d_gk);
+    if (plan->d_ord) cudaFree(plan->d_ord);
     if (plan->d_counter) cudaFree(plan->d_counter);
     delete plan;
 }
