@@ -309,7 +309,7 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
     z polarisation, Gaussian pulse σ = 20/Γ centred at 100/Γ), Dopri5 rtol 1e-8 atol 1e-11 over
     [0, 200/Γ]: final populations and the excited-population integral through the reference-facing
     single-solve call (host arrays, one call per output as the reference makes them), FP64 and the
-    mixed form, at the automatic launch width (32 threads) and at 256 threads; against the oracle
+    mixed form, at the automatic launch width (32 threads) and at 64 and 128 threads; against the oracle
     solving the same trajectory on one host thread."""
     import codec
     import oracle
@@ -340,7 +340,7 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
         return best, out
 
     res = {}
-    for width in (0, 256):
+    for width in (0, 64, 128):
         plan.native.set_shape(width, 0)
         for precision in ("fp64", "mixed"):
             res[(width, precision)] = timed(precision)
@@ -363,7 +363,7 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
            "oracle_ms": 1e3 * cpu_best, "oracle_cores": 1, "accepted_steps": int(rst["accepted_steps"]),
            "rejected_steps": int(rst["rejected_steps"])}
     for (width, precision), (t, (pops, integ, st)) in res.items():
-        key = f"{precision}_{'auto_32_threads' if width == 0 else '256_threads'}"
+        key = f"{precision}_{'auto_32_threads' if width == 0 else f'{width}_threads'}"
         out[key] = {"ms": 1e3 * t, "vs_oracle_speed": cpu_best / t,
                     "max_population_error_vs_oracle": float(np.max(np.abs(pops - ref_pops))),
                     "excited_integral_rel_error_vs_oracle": abs(integ - ref_int) / abs(ref_int),
@@ -1020,6 +1020,97 @@ def run_gpu(args) -> None:
         torch.distributed.destroy_process_group()
 
 
+def measure_dense76(torch, dev, total: int = 1024, reps: int = 5) -> dict:
+    """The tensor-core question for the 76-state system: the dense commutator -i[H, rho] of a batch of
+    states, H = static + sum_k c_k B_k assembled per state, as batched complex GEMMs on cuBLAS
+    (complex64 with TF32 tensor cores, complex64 on the FP32 pipe, and the real/imaginary split in
+    bf16 on the tensor cores, the fastest and least precise stand-in), against this package's
+    sparse gather RHS (obe_rhs_eval, FP64 and the mixed form's single-precision products) on the
+    same states.  Device times of every kernel come from an ncu launch list of this case."""
+    import codec
+    from centrex_tlf_gb300.native import NativePlan
+
+    d = codec.load("plan_rc_76")
+    hp = d["payload"]["hamiltonian_plan"]
+    n = int(d["payload"]["n_states"])
+    basis = []
+    for c in hp["coefficients"]:
+        m = np.zeros((n, n), dtype=np.complex128)
+        for t in c["basis_terms"]:
+            m[t["i"], t["j"]] += t["re"] + 1j * t["im"]
+        basis.append(m)
+    k = len(basis)
+    rng = np.random.default_rng(76)
+    g = d["gamma"]
+    coeffs = (rng.normal(size=(total, k)) + 1j * rng.normal(size=(total, k))) * g
+    rho = rng.normal(size=(total, n, n)) + 1j * rng.normal(size=(total, n, n))
+    rho = (rho + rho.conj().transpose(0, 2, 1)) / (2 * n)
+    S = torch.tensor(np.asarray(hp["static_matrix"]), dtype=torch.complex64, device=dev)
+    Bk = torch.tensor(np.stack(basis).reshape(k, n * n), dtype=torch.complex64, device=dev)
+    C = torch.tensor(coeffs, dtype=torch.complex64, device=dev)
+    R = torch.tensor(rho, dtype=torch.complex64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def commutator():
+        H = (C @ Bk).view(total, n, n) + S
+        return -1j * (torch.bmm(H, R) - torch.bmm(R, H))
+
+    def commutator_bf16():
+        H = (C @ Bk).view(total, n, n) + S
+        hr, hi = H.real.to(torch.bfloat16), H.imag.to(torch.bfloat16)
+        rr, ri = R.real.to(torch.bfloat16), R.imag.to(torch.bfloat16)
+        a_re = torch.bmm(hr, rr) - torch.bmm(hi, ri)
+        a_im = torch.bmm(hr, ri) + torch.bmm(hi, rr)
+        b_re = torch.bmm(rr, hr) - torch.bmm(ri, hi)
+        b_im = torch.bmm(rr, hi) + torch.bmm(ri, hr)
+        return (a_im - b_im), -(a_re - b_re)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    tf32 = torch.backends.cuda.matmul.allow_tf32
+    try:
+        torch.backends.cuda.matmul.allow_tf32 = True
+        t_tf32 = timed(commutator)
+        torch.backends.cuda.matmul.allow_tf32 = False
+        t_fp32 = timed(commutator)
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = tf32
+    t_bf16 = timed(commutator_bf16)
+    # the sparse RHS on the same states (host arrays; the ncu launch list has the kernel alone)
+    plan = NativePlan(d["payload"])
+    idx = np.triu_indices(n, 1)
+    packed = np.concatenate([rho.diagonal(axis1=1, axis2=2).real,
+                             np.stack([rho[:, idx[0], idx[1]].real, rho[:, idx[0], idx[1]].imag], axis=-1).reshape(total, -1)],
+                            axis=1)
+    walls = {}
+    for prec in ("fp64", "mixed"):
+        plan.rhs(packed[:4], 0.0, precision=prec)
+        best = float("inf")
+        for _ in range(reps):
+            start = time.perf_counter()
+            plan.rhs(packed, 0.0, precision=prec)
+            best = min(best, time.perf_counter() - start)
+        walls[prec] = 1e3 * best
+    f_rhs, _ = flops_per_step_unit(d["payload"])
+    dense_flop = 16 * n ** 3
+    return {"workload": f"{total} states of the 76-state system: one RHS each", "states": total,
+            "dense_flop_per_state": dense_flop, "sparse_flop_per_state": f_rhs, "flop_ratio": dense_flop / f_rhs,
+            "dense_ms": {"complex64_tf32_tensor": t_tf32, "complex64_fp32": t_fp32, "bf16_split_tensor": t_bf16},
+            "sparse_obe_rhs_eval_wall_ms_with_copies": walls,
+            "note": "device times per kernel: ncu launch list of `bench.py --case dense76`"}
+
+
 def run_case(args) -> None:
     """One workload on its own, for profiling: `gradient` (the adjoint workload at a fixed launch
     width), `heterogeneous` (the 16/39/76-state batch) or `large` (one wave of 76-state
@@ -1029,6 +1120,9 @@ def run_case(args) -> None:
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     times = []
+    if args.case == "dense76":
+        print(json.dumps({"case": args.case, **measure_dense76(torch, dev, total=args.points, reps=max(1, args.steps))}))
+        return
     if args.case == "heterogeneous":
         r = measure_heterogeneous(torch, dev, total=args.points, reps=max(1, args.steps))
         print(json.dumps({"case": args.case, **r}))
@@ -1099,7 +1193,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp32_control"], default="mixed")
+    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed_fp32_control"], default="mixed_fp32_control",
+                    help="the headline form (every form is timed beside it; all hold the 1e-6 population bar)")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip timing the plain FP64 path beside mixed")
     ap.add_argument("--no-gradient", action="store_true", help="skip timing the adjoint beside the forward solve")
     ap.add_argument("--no-effective", action="store_true", help="skip timing the effective-Hamiltonian path")
@@ -1115,7 +1210,7 @@ def main() -> None:
     ap.add_argument("--checkpoint-every", type=int, default=None,
                     help="--case gradient: the tape's checkpoint interval (default: full tape while it fits)")
     ap.add_argument("--cpu-sample", type=int, default=128)
-    ap.add_argument("--case", choices=["scan", "gradient", "heterogeneous", "hetero-gradient", "large"], default="scan",
+    ap.add_argument("--case", choices=["scan", "gradient", "heterogeneous", "hetero-gradient", "large", "dense76"], default="scan",
                     help="scan: the benchmark line; the others run one workload alone (profiling)")
     ap.add_argument("--threads-per-trajectory", type=int, default=0,
                     help="launch width of the gradient and large cases (0: automatic)")
