@@ -337,14 +337,16 @@ def test_gradients_through_a_population_event(golden, output, ck):
 
 
 def _mixed_fd_check(d, plan, op, p0, slots, t_span, output="excited_population", checkpoint_every=0, stop_event=None,
-                    hits_expected=None, rel=1e-5, floor=1e-6):
+                    hits_expected=None, rel=1e-5, floor=2e-6):
     """The mixed form (single-precision RHS and reverse-sweep products, double-precision state and
     accumulation) against central differences of the double-precision replay of the mixed
-    forward's own frozen steps: 1e-5 relative, with a floor of 1e-6 of the natural scale |J|/|p|
-    for the single-precision products' rounding.  The costate is integrated with single-precision
-    transposed products, so a derivative that cancels to ~1e-4 of its natural scale (the pulse
-    centre's) carries relative errors up to ~1e-2 (measured 4e-7 of |J|/|p|); the Rabi rate,
-    detuning and angle derivatives agree to ~3e-6 relative."""
+    forward's own frozen steps: 1e-5 relative, with a floor of 2e-6 of the natural scale |J|/|p|.
+    The sweep linearises around the mixed forward's states (within ~1e-8 relative of the double
+    replay's) rounded to single precision for its products, so a derivative that cancels to ~1e-4
+    of its natural scale (the pulse centre's) carries errors of a few 1e-7 of |J|/|p| (measured
+    3.4e-7 to 9.6e-7; 0.5e-7 to 6.4e-7 with k_1 refreshed in double every step, which shows the
+    forward states' share); the Rabi rate, detuning and angle derivatives agree to ~3e-6
+    relative."""
     g = d["gamma"]
     integral = output != "populations"
     w = [(i, 1.0) for i in d["excited_indices"]]
