@@ -203,8 +203,8 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 //               (d_2..d_7), k1f float[N], k1 double[N]; the double-precision tab double2[1+F]
 //               and G double2[U] serve only the k_1 refreshes, when K32 and k1f are dead, and
 //               share their storage
-//   both: ybuf double[N] (outputs, events), VM slot and stack storage for the six VM lanes,
-//   coefficient rows, reduction scratch.
+//   both: ybuf double[N] (outputs, events; the mixed form's aliases G4), VM slot and stack
+//   storage for the six VM lanes, coefficient rows, reduction scratch.
 //   large systems (256 or 512 threads per trajectory, n > 45): the stage buffers K (k1, k1f) and ybuf --
 //   and in the mixed form also the refresh buffers tab and G -- live in a per-group slice of
 //   global memory (L2-resident: one trajectory per SM); `gbytes` is the slice's size.
@@ -243,7 +243,14 @@ __host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula,
         L.G = o; o = align16(o + U * 16);
         L.K = ok; ok = align16(ok + 7 * 8 * static_cast<size_t>(N));
     }
-    L.ybuf = ok; ok = align16(ok + static_cast<size_t>(N) * 8);
+    if (mixed && !big) {
+        // the output / event buffer shares the deviation slot buffer G4 (U float4 >= N doubles):
+        // the two are never live together, and G4's y_n halves and the diagonal slots' zero
+        // imaginary halves are written again after every use of the buffer (restore_g4)
+        L.ybuf = L.G4;
+    } else {
+        L.ybuf = ok; ok = align16(ok + static_cast<size_t>(N) * 8);
+    }
     L.gbytes = og;
     L.vm_slots = o; o = align16(o + 6 * static_cast<size_t>(n_slots > 0 ? n_slots : 1) * 16);
     L.vm_stack = o; o = align16(o + 6 * static_cast<size_t>(vm_depth) * 16);
@@ -661,7 +668,7 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
 // Threads per CTA of the integrator: the mixed form's smaller per-trajectory footprint fits
 // more trajectory groups per SM (shared memory), at a register budget of 65536 / threads.
 constexpr int kThreadsFp64 = 256;
-constexpr int kThreadsMixed = 352;
+constexpr int kThreadsMixed = 384;
 
 template <int TPT, int EPT, bool MIXED>
 __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThreadsMixed : kThreadsFp64, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
@@ -1191,15 +1198,36 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
         int si = 0;
 
         // K_1 = f(t, y) in double from the slot buffer (which holds y)
+        // the mixed form's G4 after the output buffer (its alias) was used: y_n's single-precision
+        // halves and the diagonal slots' zero imaginary halves (deviation and y_n); the deviation
+        // halves are written afresh by every stage
+        auto restore_g4 = [&]() {
+            if constexpr (MIXED && TPT < 256) {
+#pragma unroll
+                for (int e = 0; e < EPT; ++e) {
+                    const int i = lt + e * TPT;
+                    if (i < N) s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
+                    if (i < n) {
+                        s_G4f[4 * i + 1] = 0.f;
+                        s_G4f[4 * i + 3] = 0.f;
+                    }
+                }
+            }
+        };
         auto refresh_k1 = [&](int row) {
             rhs64(row, k1_out);
             if constexpr (MIXED) {
 #pragma unroll
                 for (int e = 0; e < EPT; ++e) {
                     int i = lt + e * TPT;
-                    if (i < N) {
-                        s_k1f[i] = d2f(s_k1[i]);
-                        s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
+                    if (i < N) s_k1f[i] = d2f(s_k1[i]);
+                }
+                restore_g4();
+                if constexpr (TPT >= 256) {
+#pragma unroll
+                    for (int e = 0; e < EPT; ++e) {
+                        int i = lt + e * TPT;
+                        if (i < N) s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
                     }
                 }
             }
@@ -1228,6 +1256,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             }
         }
 
+        if (!done) {
+            gsync<TPT>(g);  // the start's event and output reads of the buffer are complete
+            restore_g4();
+        }
         long long ns = 0, nst = 0, ia = 0;
         int since_refresh = 0;
         bool last = false;
@@ -1816,6 +1848,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                                 s_k1[i] = k;
                                 s_k1f[i] = d2f(k);
                                 s_G4f[gslot32(i, n) + 2] = d2f(y[e]);
+                                if (TPT < 256 && i < n) {  // the output buffer's alias (restore_g4)
+                                    s_G4f[4 * i + 1] = 0.f;
+                                    s_G4f[4 * i + 3] = 0.f;
+                                }
                             }
                         }
                     }
