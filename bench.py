@@ -339,6 +339,15 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
             best = min(best, time.perf_counter() - start)
         return best, out
 
+    # the fixed cost of one reference-facing call: a solve over one initial step
+    _, _, _, st1 = api.solve_lindblad_ode_py(plan, rho0, t0, t0 + 1e-3 / g, 1e-11, 1e-8, 1e-3 / g, None, True, 100000,
+                                             "expanded_sparse", "dopri5", "excited_population", None, "final", W_EXCITED)
+    call_ms = float("inf")
+    for _ in range(reps):
+        start = time.perf_counter()
+        api.solve_lindblad_ode_py(plan, rho0, t0, t0 + 1e-3 / g, 1e-11, 1e-8, 1e-3 / g, None, True, 100000,
+                                  "expanded_sparse", "dopri5", "excited_population", None, "final", W_EXCITED)
+        call_ms = min(call_ms, 1e3 * (time.perf_counter() - start))
     res = {}
     for width in (0, 64, 128):
         plan.native.set_shape(width, 0)
@@ -361,6 +370,7 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
                        "[0, 200/Γ]; final populations + excited-population integral (two reference-facing calls, host "
                        "arrays)",
            "oracle_ms": 1e3 * cpu_best, "oracle_cores": 1, "accepted_steps": int(rst["accepted_steps"]),
+           "one_step_call_ms": call_ms, "one_step_call_steps": int(st1["accepted_steps"]),
            "rejected_steps": int(rst["rejected_steps"])}
     for (width, precision), (t, (pops, integ, st)) in res.items():
         key = f"{precision}_{'auto_32_threads' if width == 0 else f'{width}_threads'}"
@@ -1087,6 +1097,29 @@ def measure_dense76(torch, dev, total: int = 1024, reps: int = 5) -> dict:
     finally:
         torch.backends.cuda.matmul.allow_tf32 = tf32
     t_bf16 = timed(commutator_bf16)
+    # this package's tcgen05 kernel on the same states (H assembled by the same GEMM)
+    import ctypes
+
+    from centrex_tlf_gb300 import _abi
+
+    lib = _abi.load_library()
+    H_all = ((C @ Bk).view(total, n, n) + S).contiguous()
+    out_tc = torch.empty_like(R)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def commutator_tcgen05():
+        H = ((C @ Bk).view(total, n, n) + S).contiguous()
+        rc = lib.obe_dense_commutator_tf32(total, n, H.data_ptr(), R.data_ptr(), out_tc.data_ptr(), status.data_ptr(),
+                                           ctypes.c_void_p(stream.cuda_stream))
+        if rc != _abi.OBE_OK:
+            raise RuntimeError("obe_dense_commutator_tf32 failed")
+
+    t_tc = timed(commutator_tcgen05)
+    if int(status.item()) != 0:
+        raise RuntimeError("the tensor-core commutator's wait gave up")
+    ref = -1j * (torch.bmm(H_all.to(torch.complex128), R.to(torch.complex128))
+                 - torch.bmm(R.to(torch.complex128), H_all.to(torch.complex128)))
+    tc_err = float((out_tc.to(torch.complex128) - ref).abs().max() / ref.abs().max())
     # the sparse RHS on the same states (host arrays; the ncu launch list has the kernel alone)
     plan = NativePlan(d["payload"])
     idx = np.triu_indices(n, 1)
@@ -1106,7 +1139,9 @@ def measure_dense76(torch, dev, total: int = 1024, reps: int = 5) -> dict:
     dense_flop = 16 * n ** 3
     return {"workload": f"{total} states of the 76-state system: one RHS each", "states": total,
             "dense_flop_per_state": dense_flop, "sparse_flop_per_state": f_rhs, "flop_ratio": dense_flop / f_rhs,
-            "dense_ms": {"complex64_tf32_tensor": t_tf32, "complex64_fp32": t_fp32, "bf16_split_tensor": t_bf16},
+            "dense_ms": {"complex64_tf32_tensor": t_tf32, "complex64_fp32": t_fp32, "bf16_split_tensor": t_bf16,
+                         "tcgen05_tf32_this_package": t_tc},
+            "tcgen05_max_error_of_largest_element": tc_err,
             "sparse_obe_rhs_eval_wall_ms_with_copies": walls,
             "note": "device times per kernel: ncu launch list of `bench.py --case dense76`"}
 

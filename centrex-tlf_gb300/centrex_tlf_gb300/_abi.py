@@ -226,6 +226,9 @@ def load_library() -> ctypes.CDLL:
     lib.obe_plan_n_states.restype = ctypes.c_int32
     lib.obe_plan_trace_preserving.argtypes = [ctypes.c_void_p]
     lib.obe_plan_trace_preserving.restype = ctypes.c_int32
+    lib.obe_dense_commutator_tf32.argtypes = [ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.obe_dense_commutator_tf32.restype = ctypes.c_int
     lib.obe_rhs_eval.argtypes = [
         ctypes.c_void_p, ctypes.c_int64, c_f64p, c_f64p, ctypes.c_int32, c_i64p, c_f64p,
         ctypes.c_int32, c_f64p,

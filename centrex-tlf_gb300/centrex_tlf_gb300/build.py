@@ -68,9 +68,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with tempfile.TemporaryDirectory(prefix="obe_build_") as tmp:
         tmp = Path(tmp)
         common = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INCLUDE}"]
-        objs = [tmp / "obe_solver.o", tmp / "obe_plan.o"]
+        objs = [tmp / "obe_solver.o", tmp / "obe_plan.o", tmp / "obe_dense.o"]
         cmds = [
             common + ["-c", str(CSRC / "obe_solver.cu"), "-o", str(objs[0])],
+            common + ["-c", str(CSRC / "obe_dense.cu"), "-o", str(objs[2])],
             ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{INCLUDE}", "-c", str(CSRC / "obe_plan.cpp"), "-o", str(objs[1])],
         ]
         # one object per kernel shape (threads per trajectory, elements per thread), compiled in parallel

@@ -466,6 +466,16 @@ obe_status obe_solve_batch_device_noalloc(const obe_plan* plan, const obe_solve_
                                           int64_t time_count, int64_t width, double* d_values,
                                           obe_traj_stats* d_stats, void* stream);
 
+/*
+ * The dense batched commutator out = -i [H, rho] of `count` states on the tensor cores (no
+ * counterpart in the reference; the measurement behind keeping the sparse gather at >= 64
+ * states): H and rho Hermitian, n <= 80, [count][n][n] complex64 (re, im interleaved) in device
+ * memory; tcgen05.mma kind::tf32 (products at TF32 precision, FP32 accumulation).  d_status[0]
+ * counts states whose tensor-core wait gave up (0 on success); asynchronous on `stream`.
+ */
+obe_status obe_dense_commutator_tf32(int64_t count, int32_t n, const float* d_h, const float* d_rho, float* d_out,
+                                     uint32_t* d_status, void* stream);
+
 /* Number of kernel launches issued by the last solve in this thread (for accounting). */
 int64_t obe_last_launch_count(void);
 
