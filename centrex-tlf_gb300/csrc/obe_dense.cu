@@ -36,6 +36,7 @@ constexpr int kTiles = 4;            // Hr, Hi, Rr, Ri
 // room beyond the four tiles: the mbarrier and the tensor-memory address sit at the end, past any
 // address a descriptor of these tiles can reach
 constexpr int kSmemBytes = 200 * 1024;
+static_assert(kTiles * kTileBytes + 128 <= kSmemBytes, "the tiles and the barrier words must fit");
 constexpr int kWaitLimit = 1 << 22;  // mbarrier polls before the CTA gives up
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -125,9 +126,11 @@ __global__ void __launch_bounds__(128, 1) dense_commutator_kernel(long long coun
     for (long long b = blockIdx.x; b < count && ok; b += gridDim.x) {
         const float2* hb = h + static_cast<size_t>(b) * n * n;
         const float2* rb = rho + static_cast<size_t>(b) * n * n;
-        // the four tiles, zero outside the n x n block
+        // the four tiles, zero outside the n x n block; a warp fills one core matrix at a time
+        // (8 rows x 4 columns, 128 contiguous bytes), so its stores meet no bank conflict
         for (int q = tid; q < kRows * kMaxN; q += 128) {
-            const int r = q / kMaxN, k = q - r * kMaxN;
+            const int t = q & 31, cm = q >> 5;  // core matrix cm = K-chunk * 16 + row group
+            const int r = (cm & 15) * 8 + (t >> 2), k = (cm >> 4) * 4 + (t & 3);
             float2 hv = make_float2(0.f, 0.f), rv = make_float2(0.f, 0.f);
             if (r < n && k < n) {
                 hv = hb[r * n + k];
