@@ -112,6 +112,19 @@ def test_argument_validation_before_any_device_work(golden):
                                         saveat=np.array([0.5, 2.0]), output_when="saveat")
 
 
+def test_empty_batch_returns_empty_result_without_device(golden):
+    """Zero trajectories: the reference's batch loop runs no trajectory and returns width 0,
+    time_count 0 and no times (ode_batch.rs:297-306); no device work is needed for that, so this
+    runs without a GPU.  The argument checks still apply to an empty batch."""
+    d = golden("plan_two_level")
+    plan = api.prepare_lindblad_problem_py(d["payload"])
+    times, values, width, tc, stats = api.solve_lindblad_batch_ode_py(plan, np.zeros((0, 4)), 0.0, 1.0, 1e-8, 1e-6, 1e-3)
+    assert times.size == 0 and values.size == 0 and width == 0 and tc == 0
+    assert stats["accepted_steps"] == 0 and stats["event_triggered_by_trajectory"] == []
+    with pytest.raises(ValueError, match="rho0 dim mismatch: 3 vs 4"):
+        api.solve_lindblad_batch_ode_py(plan, np.zeros((0, 3)), 0.0, 1.0, 1e-8, 1e-6, 1e-3)
+
+
 def test_multi_batch_validation_before_device_work(golden):
     """The heterogeneous batch checks every job before it touches the device, and names the job."""
     d = golden("plan_two_level")
