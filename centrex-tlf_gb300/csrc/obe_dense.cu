@@ -127,20 +127,34 @@ __global__ void __launch_bounds__(128, 1) dense_commutator_kernel(long long coun
         const float2* hb = h + static_cast<size_t>(b) * n * n;
         const float2* rb = rho + static_cast<size_t>(b) * n * n;
         // the four tiles, zero outside the n x n block; a warp fills one core matrix at a time
-        // (8 rows x 4 columns, 128 contiguous bytes), so its stores meet no bank conflict
-        for (int q = tid; q < kRows * kMaxN; q += 128) {
-            const int t = q & 31, cm = q >> 5;  // core matrix cm = K-chunk * 16 + row group
-            const int r = (cm & 15) * 8 + (t >> 2), k = (cm >> 4) * 4 + (t & 3);
-            float2 hv = make_float2(0.f, 0.f), rv = make_float2(0.f, 0.f);
-            if (r < n && k < n) {
-                hv = hb[r * n + k];
-                rv = rb[r * n + k];
+        // (8 rows x 4 columns, 128 contiguous bytes), so its stores meet no bank conflict.  Each
+        // thread covers kRows * kMaxN / 128 = 80 elements, in batches of kBatch whose loads are all
+        // issued before the first store (four warps per SM leave little else to hide them behind).
+        constexpr int kPerThread = kRows * kMaxN / 128, kBatch = 8;
+        static_assert(kPerThread % kBatch == 0, "whole batches per thread");
+        for (int q0 = 0; q0 < kPerThread; q0 += kBatch) {
+            float2 hv[kBatch], rv[kBatch];
+            int off[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int q = (q0 + u) * 128 + tid;
+                const int t = q & 31, cm = q >> 5;  // core matrix cm = K-chunk * 16 + row group
+                const int r = (cm & 15) * 8 + (t >> 2), k = (cm >> 4) * 4 + (t & 3);
+                hv[u] = make_float2(0.f, 0.f);
+                rv[u] = make_float2(0.f, 0.f);
+                if (r < n && k < n) {
+                    hv[u] = hb[r * n + k];
+                    rv[u] = rb[r * n + k];
+                }
+                off[u] = tile_off(r, k);
             }
-            const int o = tile_off(r, k);
-            *reinterpret_cast<float*>(tiles + 0 * kTileBytes + o) = hv.x;
-            *reinterpret_cast<float*>(tiles + 1 * kTileBytes + o) = hv.y;
-            *reinterpret_cast<float*>(tiles + 2 * kTileBytes + o) = rv.x;
-            *reinterpret_cast<float*>(tiles + 3 * kTileBytes + o) = rv.y;
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                *reinterpret_cast<float*>(tiles + 0 * kTileBytes + off[u]) = hv[u].x;
+                *reinterpret_cast<float*>(tiles + 1 * kTileBytes + off[u]) = hv[u].y;
+                *reinterpret_cast<float*>(tiles + 2 * kTileBytes + off[u]) = rv[u].x;
+                *reinterpret_cast<float*>(tiles + 3 * kTileBytes + off[u]) = rv[u].y;
+            }
         }
         // generic-proxy writes -> visible to the tensor core's async proxy
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
