@@ -670,7 +670,9 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
 constexpr int kThreadsFp64 = 256;
 constexpr int kThreadsMixed = 384;
 
-template <int TPT, int EPT, bool MIXED>
+// C32: the mixed form's single-precision-control variant, compiled as a kernel of its own so that
+// neither variant carries the other's registers and branches
+template <int TPT, int EPT, bool MIXED, bool C32>
 __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThreadsMixed : kThreadsFp64, 1) integrate_kernel(const DevPlan P, const CallArgs A, int gpb, size_t group_bytes, int M) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int g = static_cast<int>(threadIdx.x) / TPT;
@@ -735,7 +737,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
     const int S = P.n_static_formula, F = P.n_formula;
     // mixed form: single-precision stage inputs, error norm and controller (opt-in variant), and
     // the trace renormalisation of the double-precision-control form on trace-preserving plans
-    const bool ctrl32 = MIXED && A.ctrl32 != 0;
+    constexpr bool ctrl32 = MIXED && C32;
     const bool renorm = MIXED && !ctrl32 && P.trace_preserving != 0;
 
     // this thread's VM lane (lanes 0..5 only)
@@ -2007,7 +2009,10 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : 256) rhs_kernel(const DevPla
 template <int TPT, int EPT, bool MIXED>
 cudaError_t launch_integrate_shape(const DevPlan& P, const CallArgs& A, int blocks, int gpb, size_t smem, size_t group_bytes,
                                    int method, cudaStream_t stream) {
-    auto k = integrate_kernel<TPT, EPT, MIXED>;
+    auto k = integrate_kernel<TPT, EPT, MIXED, false>;
+    if constexpr (MIXED) {
+        if (A.ctrl32) k = integrate_kernel<TPT, EPT, true, true>;
+    }
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     k<<<blocks, gpb * TPT, smem, stream>>>(P, A, gpb, group_bytes, method);
