@@ -415,6 +415,7 @@ def measure_ragged76(torch, dev, total: int = 1024, cpu_sample: int = 32, fp64_s
 
     job = ragged76_job(total)
     d, g = job["d"], job["d"]["gamma"]
+    f_rhs, per_step = flops_per_step_unit(d["payload"])
     plan = NativePlan(d["payload"])
     stream = torch.cuda.current_stream(dev)
     rho = torch.from_numpy(np.repeat(d["rho0_packed"].reshape(1, -1), total, axis=0)).to(dev)
@@ -440,9 +441,12 @@ def measure_ragged76(torch, dev, total: int = 1024, cpu_sample: int = 32, fp64_s
         if np.any(stv[:, 3] >> 32):
             raise RuntimeError(f"{int(np.count_nonzero(stv[:, 3] >> 32))} 76-state trajectories failed ({precision})")
         ms = e0.elapsed_time(e1)
+        attempted = int(stv[:, 0].sum()) + int(stv[:, 1].sum())
         res[precision] = {"ms": ms, "trajectories": count, "value": count / (ms * 1e-3), "unit": "trajectories/s",
                           "threads_per_trajectory": cands[0]["threads_per_trajectory"],
                           "accepted_steps": int(stv[:, 0].sum()), "rejected_steps": int(stv[:, 1].sum()),
+                          # algorithmic work (6 F_rhs + 60 N per attempted step) over the launch
+                          "achieved_tflops": attempted * per_step / (ms * 1e-3) / 1e12,
                           "pops": val.view(total, 76)[:count].cpu().numpy().copy()}
     plan.set_shape(0, 0)
     op = oracle.OraclePlan(d["payload"])
@@ -473,7 +477,8 @@ def measure_ragged76(torch, dev, total: int = 1024, cpu_sample: int = 32, fp64_s
     for r in res.values():
         r.pop("_pops", None)
     out["note"] = ("the square-wave switching makes the RHS discontinuous; solves agree with the oracle to the "
-                   "solver tolerance there (step landings at the jumps), not to rounding")
+                   "solver tolerance there (step landings at the jumps), not to rounding; achieved_tflops counts "
+                   f"6*F_rhs + 60*N flop per attempted step (F_rhs = {f_rhs}, N = {76 * 76})")
     return out
 
 
