@@ -616,8 +616,9 @@ __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __r
 }
 
 // Stage deviation d_s = L(t_s) (y_s - y_n) + (L(t_s) - L(t_n)) y_n, all in single precision.
-// Software-pipelined: the record two iterations ahead and the operands of the next one are in
-// flight while the current record is summed (the loop is latency-bound otherwise).
+// Software-pipelined: the operands of the next record and the record word two ahead are in flight
+// while the current record is summed (the loop is latency-bound otherwise).  Two records per
+// iteration, so that the pipeline's operand registers alternate instead of being copied.
 template <int TPT>
 __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __restrict__ s_rec, const uint32_t* __restrict__ s_out,
                                            const float4* __restrict__ T4, const float4* __restrict__ G4, float* __restrict__ K,
@@ -625,18 +626,10 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
     float ar = 0.f, ai = 0.f;
     int o = 0;
     const int n_iter = P.n_iter;
-    uint32_t w = s_rec[lt];
-    uint32_t w1 = n_iter > 1 ? s_rec[TPT + lt] : 0u;
-    float4 c = T4[w >> kRecCoefShift];
-    float4 v = G4[w & kRecIndexMask];
-    for (int it = 0; it < n_iter; ++it) {
-        const uint32_t w2 = it + 2 < n_iter ? s_rec[(it + 2) * TPT + lt] : 0u;
-        const float4 cn = T4[w1 >> kRecCoefShift];
-        const float4 vn = G4[w1 & kRecIndexMask];
+    // one record: its product off the accumulator's chain (one add per record on ar / ai, so the
+    // products of consecutive records overlap), then the output's store when it is the last
+    auto sum = [&](uint32_t w, float4 c, float4 v) {
         if (w & kRecConj) { v.y = -v.y; v.w = -v.w; }
-        // the record's product off the accumulator's chain: one add per record on ar / ai, so the
-        // products of consecutive records overlap (one warp per trajectory leaves little else to
-        // hide the FMA latency behind)
         ar += fmaf(c.x, v.x, fmaf(-c.y, v.y, fmaf(c.z, v.z, -c.w * v.w)));
         ai += fmaf(c.x, v.y, fmaf(c.y, v.x, fmaf(c.z, v.w, c.w * v.z)));
         if (w & kRecFlush) {
@@ -648,11 +641,25 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
             ai = 0.f;
             ++o;
         }
-        w = w1;
-        w1 = w2;
-        c = cn;
-        v = vn;
+    };
+    uint32_t w0 = s_rec[lt];
+    uint32_t w1 = n_iter > 1 ? s_rec[TPT + lt] : 0u;
+    float4 c0 = T4[w0 >> kRecCoefShift];
+    float4 v0 = G4[w0 & kRecIndexMask];
+    int it = 0;
+    for (; it + 1 < n_iter; it += 2) {
+        const uint32_t w2 = it + 2 < n_iter ? s_rec[(it + 2) * TPT + lt] : 0u;
+        const float4 c1 = T4[w1 >> kRecCoefShift];
+        const float4 v1 = G4[w1 & kRecIndexMask];
+        sum(w0, c0, v0);
+        const uint32_t w3 = it + 3 < n_iter ? s_rec[(it + 3) * TPT + lt] : 0u;
+        c0 = T4[w2 >> kRecCoefShift];
+        v0 = G4[w2 & kRecIndexMask];
+        sum(w1, c1, v1);
+        w0 = w2;
+        w1 = w3;
     }
+    if (it < n_iter) sum(w0, c0, v0);
 }
 
 // ------------------------------------------------------------------------------------------
