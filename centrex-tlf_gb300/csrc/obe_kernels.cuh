@@ -479,13 +479,10 @@ template <int TPT>
 __device__ __forceinline__ void fill_formulas_dev(int n_fiter, const float4* __restrict__ fs, const float4* __restrict__ cv,
                                                   float4* __restrict__ T4, int lt) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 2
-    for (int it = 0; it < n_fiter; ++it) {
-        const float4 r = fs[it * TPT + lt];
+    // one product: factor (r.x, r.y) times the class value and change (c), or a static factor
+    auto sum = [&](float4 r, float4 c) {
         const uint32_t meta = __float_as_uint(r.z);
-        const int cls = static_cast<int>(meta & kFStreamClassMask) - 1;
-        if (cls >= 0) {
-            const float4 c = cv[cls];
+        if ((meta & kFStreamClassMask) != 0u) {
             acc.x = fmaf(r.x, c.x, fmaf(-r.y, c.y, acc.x));
             acc.y = fmaf(r.x, c.y, fmaf(r.y, c.x, acc.y));
             acc.z = fmaf(r.x, c.z, fmaf(-r.y, c.w, acc.z));
@@ -498,7 +495,30 @@ __device__ __forceinline__ void fill_formulas_dev(int n_fiter, const float4* __r
             T4[meta >> kFStreamFormulaShift] = acc;
             acc = make_float4(0.f, 0.f, 0.f, 0.f);
         }
+    };
+    // the class value of a product (any value for a static factor, which does not read it)
+    auto cls_of = [&](float4 r) {
+        const uint32_t k = __float_as_uint(r.z) & kFStreamClassMask;
+        return cv[k != 0u ? k - 1 : 0];
+    };
+    if (n_fiter <= 0) return;
+    // software-pipelined like the gather: the product two ahead and the class value of the next
+    // one are in flight while the current product is summed, two products per iteration
+    float4 r0 = fs[lt];
+    float4 r1 = n_fiter > 1 ? fs[TPT + lt] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 c0 = cls_of(r0);
+    int it = 0;
+    for (; it + 1 < n_fiter; it += 2) {
+        const float4 r2 = it + 2 < n_fiter ? fs[(it + 2) * TPT + lt] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 c1 = cls_of(r1);
+        sum(r0, c0);
+        const float4 r3 = it + 3 < n_fiter ? fs[(it + 3) * TPT + lt] : make_float4(0.f, 0.f, 0.f, 0.f);
+        c0 = cls_of(r2);
+        sum(r1, c1);
+        r0 = r2;
+        r1 = r3;
     }
+    if (it < n_fiter) sum(r0, c0);
 }
 
 // Per-class single-precision values and changes since the step start for the five stage rows
