@@ -84,6 +84,15 @@ struct DevPlan {
     int32_t time_dependent;
     int32_t max_stack;           // deepest VM stack of the plan's programs
     int32_t dyn_real_closed;     // every time-dependent compound maps real slots to real values
+    // the time-dependent programs in evaluation order, compacted for the per-step coefficient rows:
+    // n_vcomp compounds (pad = the compound's slot), then the n_dyn coefficients (pad = row
+    // position); starts index the compact instruction arrays vop/varg/vfn/vval (n_vins entries)
+    int32_t n_vcomp, n_vprog, n_vins;
+    const DevExpr* vprog;
+    const int32_t* vop;
+    const int32_t* varg;
+    const int32_t* vfn;
+    const double* vval;          // [2 * n_vins]
     // PCHIP tables (plan.rs:27-116)
     int32_t n_pchip;
     const int32_t* pchip_ptr;

@@ -192,6 +192,7 @@ struct CallArgs {
     int vm_depth;    // VM stack depth of the plan's and the event's programs
     int fixed;       // 0: adaptive; else the fixed-step obe_solver value (double-precision form only)
     int ctrl32;      // mixed form: stage inputs, error norm and controller in single precision, no renormalisation
+    int vm_smem;     // the compact time-dependent programs are staged in shared memory (PlanSmem::vprog..)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -267,12 +268,23 @@ __host__ __device__ inline GroupLayout group_layout(int n, int N, int n_formula,
 // time-dependent formulas, their product lists (offsets, coefficient classes, factors in the
 // precision of the form).
 struct PlanSmem {
-    size_t rec, out, fstream, fptr, fcls, ffac, bytes;
+    size_t rec, out, fstream, fptr, fcls, ffac, vprog, vval, vop, varg, vfn, bytes;
 };
 
-__host__ __device__ inline PlanSmem plan_smem(const DevPlan& P, int tpt, bool mixed) {
+// with_vm: also the compact time-dependent programs (the per-step coefficient rows read their
+// instructions from shared memory instead of through L1, which the local-memory traffic and the
+// stage buffers keep busy)
+__host__ __device__ inline PlanSmem plan_smem(const DevPlan& P, int tpt, bool mixed, bool with_vm = false) {
     PlanSmem L{};
     size_t o = 0;
+    if (with_vm) {
+        // at the start of the shared memory, where dyn_row finds it
+        L.vprog = o; o = align16(o + static_cast<size_t>(P.n_vprog) * sizeof(DevExpr));
+        L.vval = o; o = align16(o + static_cast<size_t>(P.n_vins) * 16);
+        L.vop = o; o = align16(o + static_cast<size_t>(P.n_vins) * 4);
+        L.varg = o; o = align16(o + static_cast<size_t>(P.n_vins) * 4);
+        L.vfn = o; o = align16(o + static_cast<size_t>(P.n_vins) * 4);
+    }
     L.rec = o; o += static_cast<size_t>(P.n_iter) * tpt * 4;
     L.out = o; o = align16(o + static_cast<size_t>(P.n_out) * tpt * 4);
     if (mixed) {
@@ -409,13 +421,41 @@ static __device__ __noinline__ void eval_compounds(const DevPlan& P, VMLane L, d
         if (!only_dynamic || P.comp_dynamic[c]) L.slots[P.comp_slot[c]] = eval_expr(P, P.comp_expr[c], L, t);
 }
 
+// The compact time-dependent programs (DevPlan::vprog..), in shared or device memory.
+struct VMProg {
+    const DevExpr* prog;
+    const int32_t* op;
+    const int32_t* arg;
+    const int32_t* fn;
+    const double* val;
+};
+
 // The time-dependent compounds and coefficients at time t into one coefficient row: one call
 // site per lane and step in the integrator (the registers live across a call are saved around
-// it, so the VM's work sits behind a single call).
-static __device__ __noinline__ void dyn_row(const DevPlan& P, VMLane L, double t, double2* row) {
-    for (int c = 0; c < P.n_comp; ++c)
-        if (P.comp_dynamic[c]) L.slots[P.comp_slot[c]] = eval_expr(P, P.comp_expr[c], L, t);
-    for (int j = 0; j < P.n_dyn; ++j) row[j] = eval_expr(P, P.coeff_expr[P.dyn_ids[j]], L, t);
+// it, so the VM's work sits behind a single call).  The programs come compacted in evaluation
+// order: the compounds (into their slots) and then the coefficients (into the row).
+static __device__ __noinline__ void dyn_row(const DevPlan& P, int vm_smem, VMLane L, double t, double2* row) {
+    VMProg V{P.vprog, P.vop, P.varg, P.vfn, P.vval};
+    if (vm_smem) {
+        // the copy the integrator staged at the start of its shared memory (plan_smem, with_vm)
+        extern __shared__ __align__(16) unsigned char smem[];
+        const PlanSmem PS = plan_smem(P, 0, false, true);
+        V = VMProg{reinterpret_cast<const DevExpr*>(smem + PS.vprog), reinterpret_cast<const int32_t*>(smem + PS.vop),
+                   reinterpret_cast<const int32_t*>(smem + PS.varg), reinterpret_cast<const int32_t*>(smem + PS.vfn),
+                   reinterpret_cast<const double*>(smem + PS.vval)};
+    }
+    for (int q = 0; q < P.n_vprog; ++q) {
+        const DevExpr e = V.prog[q];
+        double2 v;
+        if (L.real && e.real_ok)
+            v = make_double2(vm_eval_real(P, V.op, V.arg, V.fn, V.val, e.start, e.len, L.slots, t,
+                                          reinterpret_cast<double*>(L.stack.v)),
+                             0.0);
+        else
+            v = vm_eval(P, V.op, V.arg, V.fn, V.val, e.start, e.len, L.slots, t, L.stack);
+        if (q < P.n_vcomp) L.slots[e.pad] = v;
+        else row[e.pad] = v;
+    }
 }
 
 __device__ __forceinline__ double2 coeff_value(const DevPlan& P, int cls, const double2* cstat, const double2* crow) {
@@ -707,7 +747,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
     const int n = P.n, N = P.N, U = P.U;
 
     // stage the plan's gather stream and time-dependent formula products once per CTA
-    const PlanSmem PS = plan_smem(P, TPT, MIXED);
+    const PlanSmem PS = plan_smem(P, TPT, MIXED, A.vm_smem != 0);
     // packed index -> double index in the slot buffer (identity for the split-real effective state)
     auto gsl = [&](int i) -> int {
         if constexpr (MIXED) return gslot64(i, P.n);
@@ -719,6 +759,23 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
     int32_t* s_fcls = reinterpret_cast<int32_t*>(smem + PS.fcls);
     double2* s_ffac64 = reinterpret_cast<double2*>(smem + PS.ffac);
     uint32_t* s_fstream = reinterpret_cast<uint32_t*>(smem + PS.fstream);
+    // the per-step coefficient rows' programs: staged in shared memory when the host found room
+    if (A.vm_smem) {
+        DevExpr* s_vprog = reinterpret_cast<DevExpr*>(smem + PS.vprog);
+        double* s_vval = reinterpret_cast<double*>(smem + PS.vval);
+        int32_t* s_vop = reinterpret_cast<int32_t*>(smem + PS.vop);
+        int32_t* s_varg = reinterpret_cast<int32_t*>(smem + PS.varg);
+        int32_t* s_vfn = reinterpret_cast<int32_t*>(smem + PS.vfn);
+        for (int i = threadIdx.x; i < P.n_vprog; i += blockDim.x) s_vprog[i] = P.vprog[i];
+        for (int i = threadIdx.x; i < P.n_vins; i += blockDim.x) {
+            s_vop[i] = P.vop[i];
+            s_varg[i] = P.varg[i];
+            s_vfn[i] = P.vfn[i];
+            s_vval[2 * i] = P.vval[2 * i];
+            s_vval[2 * i + 1] = P.vval[2 * i + 1];
+        }
+    }
+    const int vm_smem = A.vm_smem;
     {
         for (int i = threadIdx.x; i < P.n_iter * TPT; i += blockDim.x) s_rec[i] = P.rec[i];
         for (int i = threadIdx.x; i < P.n_out * TPT; i += blockDim.x) s_out[i] = P.lane_out[i];
@@ -953,7 +1010,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
         // evaluate the time-dependent coefficients at t into row `row` of s_cdyn (lane 0)
         auto dyn_coeffs_at = [&](double t, int row) {
             if (P.n_dyn > 0 && lt == 0) {
-                dyn_row(P, L, t, s_cdyn + row * nd);
+                dyn_row(P, vm_smem, L, t, s_cdyn + row * nd);
             }
         };
         // one double-precision RHS from the slot buffer: formulas for coefficient row `row`, gather into out
@@ -1044,7 +1101,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                         if (lt == 5 || lt == 0 || lt == 4 || dp) {
                             double ts = x;
                             if (lt < 5) ts = dp ? x + h * (lt < 4 ? kTab.c[0][lt] : 1.0) : (lt == 0 ? x + 0.5 * h : x + h);
-                            dyn_row(P, L, ts, s_cdyn + lt * nd);
+                            dyn_row(P, vm_smem, L, ts, s_cdyn + lt * nd);
                         }
                     }
                     // k_1 = f(x, y)
@@ -1305,7 +1362,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             if (P.n_dyn > 0 && lt < 5) {
                 double c = lt < 4 ? kTab.c[M][lt] : 1.0;
                 double ts = x + h * c;
-                dyn_row(P, L, ts, s_cdyn + lt * nd);
+                dyn_row(P, vm_smem, L, ts, s_cdyn + lt * nd);
             }
             if constexpr (MIXED) {
                 gsync<TPT>(g);

@@ -65,7 +65,35 @@ void build_plan_image(const obe_plan* p, std::vector<unsigned char>& blob, uintp
     size_t o_tr = put(blob, h.trec), o_li = put(blob, h.lane_in), o_bil = put(blob, h.bil);
     size_t o_eg = put(blob, h.eff_grid), o_er = put(blob, h.eff_rows), o_ec = put(blob, h.eff_cols), o_ef = put(blob, h.eff_coef);
     size_t o_ks = put(blob, h.coeff_scale);
+    // the time-dependent compounds and coefficients, their instructions copied contiguously
+    std::vector<DevExpr> vprog;
+    std::vector<int32_t> vop, varg, vfn;
+    std::vector<double> vval;
+    auto add_prog = [&](const DevExpr& e, int32_t target) {
+        DevExpr c{static_cast<int32_t>(vop.size()), e.len, e.real_ok, target};
+        for (int32_t k = e.start; k < e.start + e.len; ++k) {
+            vop.push_back(h.ins_op[k]);
+            varg.push_back(h.ins_arg[k]);
+            vfn.push_back(h.ins_fn[k]);
+            vval.push_back(h.ins_val[2 * k]);
+            vval.push_back(h.ins_val[2 * k + 1]);
+        }
+        vprog.push_back(c);
+    };
+    for (size_t c = 0; c < h.comp_slot.size(); ++c)
+        if (h.comp_dynamic[c]) add_prog(h.comp_expr[c], h.comp_slot[c]);
+    const int32_t n_vcomp = static_cast<int32_t>(vprog.size());
+    for (size_t j = 0; j < h.dyn_ids.size(); ++j) add_prog(h.coeff_expr[h.dyn_ids[j]], static_cast<int32_t>(j));
+    size_t o_vp = put(blob, vprog), o_vo = put(blob, vop), o_va = put(blob, varg), o_vf = put(blob, vfn), o_vv = put(blob, vval);
     P = DevPlan{};
+    P.n_vcomp = n_vcomp;
+    P.n_vprog = static_cast<int32_t>(vprog.size());
+    P.n_vins = static_cast<int32_t>(vop.size());
+    P.vprog = reinterpret_cast<const DevExpr*>(base + o_vp);
+    P.vop = reinterpret_cast<const int32_t*>(base + o_vo);
+    P.varg = reinterpret_cast<const int32_t*>(base + o_va);
+    P.vfn = reinterpret_cast<const int32_t*>(base + o_vf);
+    P.vval = reinterpret_cast<const double*>(base + o_vv);
     P.n = p->n;
     P.N = static_cast<int32_t>(p->N);
     P.U = static_cast<int32_t>(p->U);
@@ -186,6 +214,7 @@ struct LaunchShape {
     int tpt, ept, gpb, blocks;
     size_t group_bytes, smem;
     size_t gstride;  // large systems: global stage-buffer bytes per group (0 otherwise)
+    int vm_smem = 0; // the time-dependent programs staged in shared memory (CallArgs::vm_smem)
 };
 
 // grow-only global stage-buffer scratch of a plan (large systems)
@@ -336,7 +365,9 @@ obe_status order_queue(obe_plan* p, CallArgs& A, cudaStream_t stream, int* launc
 }
 
 template <bool MIXED>
-cudaError_t dispatch_shape(const DevPlan& P, const CallArgs& A, const LaunchShape& s, int method, cudaStream_t st) {
+cudaError_t dispatch_shape(const DevPlan& P, const CallArgs& A0, const LaunchShape& s, int method, cudaStream_t st) {
+    CallArgs A = A0;
+    A.vm_smem = s.vm_smem;
 #define OBE_DISPATCH(T, E) \
     if (s.tpt == T && s.ept == E) return launch_integrate_shape<T, E, MIXED>(P, A, s.blocks, s.gpb, s.smem, s.group_bytes, method, st);
     OBE_FOR_EACH_SHAPE(OBE_DISPATCH)
@@ -384,6 +415,12 @@ obe_status plan_launch(const DevPlan& P, bool mixed, long long n_traj, int vm_de
     }
     s->gpb = gpb;
     s->smem = plan_bytes + gpb * L.bytes;
+    // the time-dependent programs in shared memory too, when that costs no trajectory group
+    const size_t plan_vm = plan_smem(P, s->tpt, mixed, true).bytes;
+    if (P.n_vprog > 0 && plan_vm + gpb * L.bytes <= limit) {
+        s->vm_smem = 1;
+        s->smem = plan_vm + gpb * L.bytes;
+    }
     int blocks_per_sm = std::max<int>(1, static_cast<int>(limit / s->smem));
     long long want = (n_traj + gpb - 1) / gpb;
     long long cap = static_cast<long long>(sm_count()) * blocks_per_sm;
@@ -615,6 +652,7 @@ void fill_call_args(CallArgs& A, const obe_solve_options* o, const std::vector<d
     A.ev_val = reinterpret_cast<const double*>(d_blob + cb.o_evval);
     A.fixed = o->solver >= OBE_SOLVER_FIXED_DOPRI5 ? o->solver : 0;
     A.ctrl32 = o->precision == OBE_PRECISION_MIXED_FP32_CONTROL ? 1 : 0;
+    A.vm_smem = 0;  // set per launch shape (dispatch_shape)
 }
 
 cudaError_t launch_integrate(const obe_plan* p, const CallArgs& A, bool mixed, int solver, const LaunchShape& s, cudaStream_t st) {
