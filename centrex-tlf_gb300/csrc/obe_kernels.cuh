@@ -823,6 +823,9 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
     // the trace renormalisation of the double-precision-control form on trace-preserving plans
     constexpr bool ctrl32 = MIXED && C32;
     const bool renorm = MIXED && !ctrl32 && P.trace_preserving != 0;
+    // weighted outputs of one-warp trajectories take each accepted step's value from the registers
+    const bool weighted_regs = TPT == 32 && A.n_weights <= 16 &&
+                               (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL || A.output == OBE_OUTPUT_WEIGHTED_RATE);
 
     // this thread's VM lane (lanes 0..5 only)
     VMLane L;
@@ -920,6 +923,17 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
         double* out_times = A.times ? A.times + traj * A.cap : nullptr;
 
         // push the group's state in s_ybuf (already written and synced) as one output point
+        // lane 0: a weighted output's value at t (output.rs:314-330: the trapezoid of the integral)
+        auto weighted_value = [&](double t, long long pt, bool store, double value) {
+            if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL) {
+                if (isfinite(last_t)) integral += 0.5 * (last_value + value) * (t - last_t);
+                last_t = t;
+                last_value = value;
+                if (A.store_trace && store) out_vals[pt] = integral;
+            } else if (store) {
+                out_vals[pt] = value;
+            }
+        };
         auto push = [&](double t) {
             last_time = t;
             has_last_time = true;
@@ -947,14 +961,7 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 if (lt == 0) {
                     double value = 0.0;
                     for (int k = 0; k < A.n_weights; ++k) value += A.w_val[k] * s_ybuf[A.w_idx[k]];
-                    if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL) {
-                        if (isfinite(last_t)) integral += 0.5 * (last_value + value) * (t - last_t);
-                        last_t = t;
-                        last_value = value;
-                        if (A.store_trace && store) out_vals[pt] = integral;
-                    } else if (store) {
-                        out_vals[pt] = value;
-                    }
+                    weighted_value(t, pt, store, value);
                 }
                 break;
             }
@@ -963,6 +970,18 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
             if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace) count = 1;
             else ++count;
             gsync<TPT>(g);
+        };
+        // push for a weighted output whose value lane 0 already holds (one-warp trajectories)
+        auto push_weighted = [&](double t, double value) {
+            last_time = t;
+            has_last_time = true;
+            const long long pt = count;
+            const bool store = pt < A.cap;
+            if (lt == 0) weighted_value(t, pt, store, value);
+            if (lt == 0 && out_times && store && !(A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace)) out_times[pt] = t;
+            if (A.output == OBE_OUTPUT_WEIGHTED_INTEGRAL && !A.store_trace) count = 1;
+            else ++count;
+            __syncwarp();
         };
         auto stage_registers_to_buf = [&](const double* v) {
 #pragma unroll
@@ -1790,8 +1809,26 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                         ++si;
                     }
                 } else if (!hit) {
-                    stage_registers_to_buf(yn);
-                    push(x);
+                    if (TPT == 32 && weighted_regs) {
+                        // the weighted value from the registers: each weight's element shuffled to
+                        // lane 0 from the lane that holds it, summed in the weights' order as push
+                        // sums them (the same value, without staging y_{n+1} in shared memory)
+                        double value = 0.0;
+                        for (int k = 0; k < A.n_weights; ++k) {
+                            const int idx = A.w_idx[k];
+                            const int e = idx / TPT;
+                            double sel = 0.0;
+#pragma unroll
+                            for (int q = 0; q < EPT; ++q)
+                                if (q == e) sel = yn[q];
+                            const double yv = __shfl_sync(0xffffffffu, sel, idx % TPT);
+                            value += A.w_val[k] * yv;
+                        }
+                        push_weighted(x, value);
+                    } else {
+                        stage_registers_to_buf(yn);
+                        push(x);
+                    }
                 }
                 // the step for the adjoint: start time, size, start state and stages 1-6 (or,
                 // checkpointed, the step and every tape_ckpt-th start state).  The step that ends on
