@@ -434,7 +434,7 @@ struct VMProg {
 // site per lane and step in the integrator (the registers live across a call are saved around
 // it, so the VM's work sits behind a single call).  The programs come compacted in evaluation
 // order: the compounds (into their slots) and then the coefficients (into the row).
-static __device__ __noinline__ void dyn_row(const DevPlan& P, int vm_smem, VMLane L, double t, double2* row) {
+static __device__ __forceinline__ void dyn_row(const DevPlan& P, int vm_smem, VMLane L, double t, double2* row) {
     VMProg V{P.vprog, P.vop, P.varg, P.vfn, P.vval};
     if (vm_smem) {
         // the copy the integrator staged at the start of its shared memory (plan_smem, with_vm)
@@ -448,8 +448,8 @@ static __device__ __noinline__ void dyn_row(const DevPlan& P, int vm_smem, VMLan
         const DevExpr e = V.prog[q];
         double2 v;
         if (L.real && e.real_ok)
-            v = make_double2(vm_eval_real(P, V.op, V.arg, V.fn, V.val, e.start, e.len, L.slots, t,
-                                          reinterpret_cast<double*>(L.stack.v)),
+            v = make_double2(vm_eval_real_inl(P, V.op, V.arg, V.fn, V.val, e.start, e.len, L.slots, t,
+                                              reinterpret_cast<double*>(L.stack.v)),
                              0.0);
         else
             v = vm_eval(P, V.op, V.arg, V.fn, V.val, e.start, e.len, L.slots, t, L.stack);

@@ -328,9 +328,9 @@ static __device__ __noinline__ double2 vm_eval(const DevPlan& P, const int32_t* 
 // (a b) / (b b), tan(z) as sin(2z) / (cos(2z) + 1), integer powers by the same repeated
 // multiplication -- so the two paths agree bit for bit while the real one issues a fraction of
 // the double-precision instructions.  The stack is the caller's VM stack storage.
-static __device__ __noinline__ double vm_eval_real(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
-                                            const double* val, int32_t start, int32_t len, const double2* slots, double t,
-                                            double* st) {
+static __device__ __forceinline__ double vm_eval_real_inl(const DevPlan& P, const int32_t* op, const int32_t* arg,
+                                                          const int32_t* fn, const double* val, int32_t start, int32_t len,
+                                                          const double2* slots, double t, double* st) {
     int sp = 0;
     for (int32_t k = start; k < start + len; ++k) {
         const int32_t o = op[k];
@@ -396,6 +396,13 @@ static __device__ __noinline__ double vm_eval_real(const DevPlan& P, const int32
         }
     }
     return st[0];
+}
+
+// the same as a call (the integrator's per-step coefficient rows inline it into their own call)
+static __device__ __noinline__ double vm_eval_real(const DevPlan& P, const int32_t* op, const int32_t* arg, const int32_t* fn,
+                                            const double* val, int32_t start, int32_t len, const double2* slots, double t,
+                                            double* st) {
+    return vm_eval_real_inl(P, op, arg, fn, val, start, len, slots, t, st);
 }
 
 }  // namespace obe
