@@ -688,18 +688,22 @@ __device__ __forceinline__ void gather_dev(const DevPlan& P, const uint32_t* __r
     const int n_iter = P.n_iter;
     // one record: its product off the accumulator's chain (one add per record on ar / ai, so the
     // products of consecutive records overlap), then the output's store when it is the last
+    // the lane's current output (packed re | im << 16), the next one loaded at each flush so that
+    // the store never waits on it
+    const int n_out = P.n_out;
+    uint32_t dcur = n_out > 0 ? s_out[lt] : 0u;
     auto sum = [&](uint32_t w, float4 c, float4 v) {
         if (w & kRecConj) { v.y = -v.y; v.w = -v.w; }
         ar += fmaf(c.x, v.x, fmaf(-c.y, v.y, fmaf(c.z, v.z, -c.w * v.w)));
         ai += fmaf(c.x, v.y, fmaf(c.y, v.x, fmaf(c.z, v.w, c.w * v.z)));
         if (w & kRecFlush) {
-            uint32_t d = s_out[o * TPT + lt];
-            K[d & 0xFFFFu] = ar;
-            uint32_t im = d >> 16;
+            K[dcur & 0xFFFFu] = ar;
+            const uint32_t im = dcur >> 16;
             if (im != kNoImag) K[im] = ai;
             ar = 0.f;
             ai = 0.f;
             ++o;
+            dcur = o < n_out ? s_out[o * TPT + lt] : 0u;
         }
     };
     uint32_t w0 = s_rec[lt];
