@@ -920,24 +920,43 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     {
                         float br = 0.f, bi = 0.f;
                         int o = 0;
-                        for (int it = 0; it < P.n_titer; ++it) {
-                            const uint32_t w = s_trec[it * TPT + lt];
-                            const float2 c = s_tab32[w >> kRecCoefShift];
-                            const float2 u = s_LS32[w & kRecIndexMask];
+                        const int n_tin = P.n_tin, n_titer = P.n_titer;
+                        uint32_t dcur = n_tin > 0 ? s_lin[lt] : 0u;  // the next input slot loaded at each flush
+                        auto tsum = [&](uint32_t w, float2 c, float2 u) {
                             const float tr = fmaf(c.x, u.x, c.y * u.y);
                             float ti = fmaf(c.x, u.y, -c.y * u.x);
                             if (w & kRecConj) ti = -ti;
                             br += tr;
                             bi += ti;
                             if (w & kRecFlush) {
-                                const uint32_t d = s_lin[o * TPT + lt];
-                                s_MU32[static_cast<size_t>(s) * N + (d & 0xFFFFu)] = br;
-                                if ((d >> 16) != kNoImag) s_MU32[static_cast<size_t>(s) * N + (d >> 16)] = bi;
+                                s_MU32[static_cast<size_t>(s) * N + (dcur & 0xFFFFu)] = br;
+                                if ((dcur >> 16) != kNoImag) s_MU32[static_cast<size_t>(s) * N + (dcur >> 16)] = bi;
                                 br = 0.f;
                                 bi = 0.f;
                                 ++o;
+                                dcur = o < n_tin ? s_lin[o * TPT + lt] : 0u;
                             }
+                        };
+                        // software-pipelined as the forward gather: two records per iteration, the
+                        // next record's operands and the word two ahead in flight
+                        uint32_t w0 = n_titer > 0 ? s_trec[lt] : 0u;
+                        uint32_t w1 = n_titer > 1 ? s_trec[TPT + lt] : 0u;
+                        float2 c0 = s_tab32[w0 >> kRecCoefShift];
+                        float2 u0 = s_LS32[w0 & kRecIndexMask];
+                        int it = 0;
+                        for (; it + 1 < n_titer; it += 2) {
+                            const uint32_t w2 = it + 2 < n_titer ? s_trec[(it + 2) * TPT + lt] : 0u;
+                            const float2 c1 = s_tab32[w1 >> kRecCoefShift];
+                            const float2 u1 = s_LS32[w1 & kRecIndexMask];
+                            tsum(w0, c0, u0);
+                            const uint32_t w3 = it + 3 < n_titer ? s_trec[(it + 3) * TPT + lt] : 0u;
+                            c0 = s_tab32[w2 >> kRecCoefShift];
+                            u0 = s_LS32[w2 & kRecIndexMask];
+                            tsum(w1, c1, u1);
+                            w0 = w2;
+                            w1 = w3;
                         }
+                        if (it < n_titer) tsum(w0, c0, u0);
                     }
                     // lambda_s^T (dL/dp) Y_s, formula by formula
                     for (int c = 0; c < nc2; ++c) s_S32[c * TPT + lt] = make_float2(0.f, 0.f);
@@ -1033,6 +1052,8 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                 {
                     double br = 0.0, bi = 0.0;
                     int o = 0;
+                    const int n_tin = P.n_tin;
+                    uint32_t dcur = n_tin > 0 ? s_lin[lt] : 0u;  // the next input slot loaded at each flush
                     for (int it = 0; it < P.n_titer; ++it) {
                         const uint32_t w = s_trec[it * TPT + lt];
                         const double2 c = s_tab[w >> kRecCoefShift];
@@ -1043,12 +1064,12 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                         br += tr;
                         bi += ti;
                         if (w & kRecFlush) {
-                            const uint32_t d = s_lin[o * TPT + lt];
-                            s_MU[static_cast<size_t>(s) * N + (d & 0xFFFFu)] = br;
-                            if ((d >> 16) != kNoImag) s_MU[static_cast<size_t>(s) * N + (d >> 16)] = bi;
+                            s_MU[static_cast<size_t>(s) * N + (dcur & 0xFFFFu)] = br;
+                            if ((dcur >> 16) != kNoImag) s_MU[static_cast<size_t>(s) * N + (dcur >> 16)] = bi;
                             br = 0.0;
                             bi = 0.0;
                             ++o;
+                            dcur = o < n_tin ? s_lin[o * TPT + lt] : 0u;
                         }
                     }
                 }

@@ -652,7 +652,8 @@ __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __r
                                            const T2* __restrict__ tab, const T2* __restrict__ G, T* __restrict__ K, int lt) {
     T ar = 0, ai = 0;
     int o = 0;
-    const int n_iter = P.n_iter;
+    const int n_iter = P.n_iter, n_out = P.n_out;
+    uint32_t dcur = n_out > 0 ? s_out[lt] : 0u;  // the lane's current output; the next one loaded at each flush
 #pragma unroll 4
     for (int it = 0; it < n_iter; ++it) {
         uint32_t w = s_rec[it * TPT + lt];
@@ -664,13 +665,13 @@ __device__ __forceinline__ void gather_rhs(const DevPlan& P, const uint32_t* __r
         ai = fma(c.x, v.y, ai);
         ai = fma(c.y, v.x, ai);
         if (w & kRecFlush) {
-            uint32_t d = s_out[o * TPT + lt];
-            K[d & 0xFFFFu] = ar;
-            uint32_t im = d >> 16;
+            K[dcur & 0xFFFFu] = ar;
+            const uint32_t im = dcur >> 16;
             if (im != kNoImag) K[im] = ai;
             ar = 0;
             ai = 0;
             ++o;
+            dcur = o < n_out ? s_out[o * TPT + lt] : 0u;
         }
     }
 }
