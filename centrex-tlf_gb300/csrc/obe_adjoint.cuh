@@ -962,8 +962,7 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                     for (int c = 0; c < nc2; ++c) s_S32[c * TPT + lt] = make_float2(0.f, 0.f);
                     {
                         float zr = 0.f, zi = 0.f;
-                        for (int it = 0; it < P.n_biter; ++it) {
-                            const uint32_t w = s_bil[it * TPT + lt];
+                        auto bsum = [&](uint32_t w, float2 a, float2 lam) {
                             if (w & kBilEnd) {
                                 const int f = static_cast<int>(w & ~kBilEnd);
                                 for (int p = P.formula_ptr[f - 1]; p < P.formula_ptr[f]; ++p) {
@@ -977,13 +976,32 @@ __global__ void __launch_bounds__(256, 1) adjoint_kernel(const DevPlan P, const 
                                 zr = 0.f;
                                 zi = 0.f;
                             } else {
-                                float2 a = s_G32[w & kBilSlotMask];
                                 if (w & kBilConj) a.y = -a.y;
-                                const float2 lam = s_LS32[(w >> kBilOutShift) & kBilSlotMask];
                                 zr = fmaf(a.x, lam.x, fmaf(a.y, lam.y, zr));
                                 zi = fmaf(a.y, lam.x, fmaf(-a.x, lam.y, zi));
                             }
+                        };
+                        // the operands of a record (slot 0 for a formula's end word, which reads none)
+                        auto a_of = [&](uint32_t w) { return s_G32[(w & kBilEnd) ? 0u : (w & kBilSlotMask)]; };
+                        auto l_of = [&](uint32_t w) { return s_LS32[(w & kBilEnd) ? 0u : ((w >> kBilOutShift) & kBilSlotMask)]; };
+                        // software-pipelined as the gathers: two records per iteration
+                        const int n_biter = P.n_biter;
+                        uint32_t w0 = n_biter > 0 ? s_bil[lt] : 0u;
+                        uint32_t w1 = n_biter > 1 ? s_bil[TPT + lt] : 0u;
+                        float2 a0 = a_of(w0), l0 = l_of(w0);
+                        int it = 0;
+                        for (; it + 1 < n_biter; it += 2) {
+                            const uint32_t w2 = it + 2 < n_biter ? s_bil[(it + 2) * TPT + lt] : 0u;
+                            const float2 a1 = a_of(w1), l1 = l_of(w1);
+                            bsum(w0, a0, l0);
+                            const uint32_t w3 = it + 3 < n_biter ? s_bil[(it + 3) * TPT + lt] : 0u;
+                            a0 = a_of(w2);
+                            l0 = l_of(w2);
+                            bsum(w1, a1, l1);
+                            w0 = w2;
+                            w1 = w3;
                         }
+                        if (it < n_biter) bsum(w0, a0, l0);
                     }
                     for (int c = 0; c < nc2; ++c) {
                         const float2 Sv = s_S32[c * TPT + lt];
