@@ -38,8 +38,9 @@ for sub in ("centrex-tlf_gb300", "oracle", "tests/golden"):
 
 METRIC = "batched OBE trajectories/s at <=1e-6 pop. error vs plain FP64"
 # DRAM bytes (read + write) per trajectory of integrate_kernel, from ncu captures of this
-# workload at 1536 points (dram__bytes_read.sum + dram__bytes_write.sum over 1536); see profiles/.
-TRAFFIC_BYTES_PER_TRAJECTORY = {"mixed": (7_699_968 + 447_232) / 1536, "fp64": 3_467_008 / 1536}
+# workload (dram__bytes_read.sum + dram__bytes_write.sum over the trajectories of the captured
+# launch): the mixed forms at 4096 points, FP64 at 1536 points; see profiles/.
+TRAFFIC_BYTES_PER_TRAJECTORY = {"mixed": (14_186_752 + 158_208) / 4096, "fp64": 3_467_008 / 1536}
 W_EXCITED = [(13, 1.0), (14, 1.0), (15, 1.0)]
 
 
