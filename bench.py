@@ -251,20 +251,33 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
             best = min(best, time.perf_counter() - start)
         return best
 
+    def grad_width(precision):
+        # the launch width at which the gradient (taped forward and reverse sweep, checkpoints
+        # every 512 steps) is fastest: the autotuner tunes the plain forward, and the reverse
+        # sweep's best width need not be the forward's
+        best = None
+        for w in (32, 64, 128):
+            plan.set_shape(w, 0)
+            t = timed(lambda: grad(512, precision=precision))
+            if best is None or t < best[1]:
+                best = (w, t)
+        plan.set_shape(best[0], 0)
+        return best
+
     t_fwd = timed(fwd)
     t_grad = timed(grad)
-    # the same at the launch shape the autotuner picks for this batch (forward, taped forward and
-    # reverse sweep all at the tuned width)
+    # the forward at the launch shape the autotuner picks for this batch; the gradient at the
+    # width where it is fastest (the ratio: the fastest gradient over the fastest forward)
     cands = plan.autotune(opts, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, probe_steps=64,
                           stream=stream.cuda_stream)
     t_fwd_t = timed(fwd)
+    w_grad, t_grad_ck = grad_width("fp64")
     t_grad_t = timed(grad)
-    t_grad_ck = timed(lambda: grad(512))
     g64 = grad().cpu().numpy()
     j64 = grad.last_values.cpu().numpy()
     # the mixed form (FP32-RHS forward with a single-precision tape, single-precision transposed
-    # and parameter products in the reverse sweep, FP64 accumulation) at the shape the autotuner
-    # picks for the mixed forward
+    # and parameter products in the reverse sweep, FP64 accumulation): the forward at the shape the
+    # autotuner picks for it, the gradient at its own fastest width
     opts_m = plan.options(t0=t0, t1=t1, abstol=1e-11, reltol=1e-8, dt=1e-3 / gamma, saveat=None, save_start=True,
                           maxiters=100000, solver="tsit5", output="excited_population", output_indices=None,
                           output_when="final", integral_weights=W_EXCITED, stop_event=None, precision="mixed")
@@ -276,8 +289,8 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
     cands_m = plan.autotune(opts_m, n_traj, d_rho.data_ptr(), slots, d_par.data_ptr(), 1, probe_steps=64,
                             stream=stream.cuda_stream)
     t_fwd_m = timed(fwd_m)
+    w_grad_m, t_grad_m_ck = grad_width("mixed")
     t_grad_m = timed(lambda: grad(precision="mixed"))
-    t_grad_m_ck = timed(lambda: grad(512, precision="mixed"))
     gm = grad(precision="mixed").cpu().numpy()
     plan.set_shape(0, 0)
     # the mixed gradients against the FP64 ones (each form on its own frozen step sequence), on
@@ -289,12 +302,14 @@ def measure_gradient(torch, d, params_all, dev, n_traj: int = 256, reps: int = 3
             "grad_over_fwd": t_grad / t_fwd,
             "autotuned": {"threads_per_trajectory": cands[0]["threads_per_trajectory"],
                           "trajectories_per_cta": cands[0]["trajectories_per_cta"], "fwd_ms": 1e3 * t_fwd_t,
+                          "gradient_threads_per_trajectory": w_grad,
                           "fwd_plus_grad_ms": 1e3 * t_grad_t, "grad_over_fwd": t_grad_t / t_fwd_t,
                           "checkpointed_512": {"fwd_plus_grad_ms": 1e3 * t_grad_ck, "grad_over_fwd": t_grad_ck / t_fwd_t,
                                                "tape_bytes_per_trajectory": 8 * plan.grad_tape_doubles(2048, 512),
                                                "full_tape_bytes_per_trajectory": 8 * plan.grad_tape_doubles(2048, 0)}},
             "mixed": {"threads_per_trajectory": cands_m[0]["threads_per_trajectory"],
                       "trajectories_per_cta": cands_m[0]["trajectories_per_cta"], "fwd_ms": 1e3 * t_fwd_m,
+                      "gradient_threads_per_trajectory": w_grad_m,
                       "fwd_plus_grad_ms": 1e3 * t_grad_m, "grad_over_fwd": t_grad_m / t_fwd_m,
                       "grad_vs_fp64_fwd": t_grad_m / t_fwd_t,
                       "checkpointed_512": {"fwd_plus_grad_ms": 1e3 * t_grad_m_ck, "grad_over_fwd": t_grad_m_ck / t_fwd_m},
