@@ -24,7 +24,7 @@ OUT = PKG / "_lib" / "libobe_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # integrator shapes (threads per trajectory, elements per thread); the RHS kernel is built with
 # the first shape of each width.  Must match OBE_FOR_EACH_SHAPE / OBE_FOR_EACH_RHS in obe_kernels.cuh.
-SHAPES = [(32, 8), (32, 16), (64, 4), (64, 16), (128, 2), (128, 16), (256, 32), (512, 16)]
+SHAPES = [(32, 8), (32, 16), (64, 4), (64, 16), (128, 2), (128, 12), (128, 16), (256, 24), (256, 32), (512, 12), (512, 16)]
 RHS_SHAPES = [(32, 8), (64, 16), (128, 16), (256, 32), (512, 16)]
 
 

@@ -1166,7 +1166,7 @@ cudaError_t launch_adjoint_shape(const DevPlan& P, const CallArgs& A, const AdjA
 }
 
 // the adjoint widths (the integrator shapes up to 256 threads per trajectory)
-#define OBE_FOR_EACH_ADJOINT(X) X(32, 8) X(32, 16) X(64, 4) X(64, 16) X(128, 2) X(128, 16) X(256, 32)
+#define OBE_FOR_EACH_ADJOINT(X) X(32, 8) X(32, 16) X(64, 4) X(64, 16) X(128, 2) X(128, 12) X(128, 16) X(256, 24) X(256, 32)
 #ifndef OBE_INSTANCE_TU
 #define OBE_EXTERN_ADJOINT(T, E)                                                                                             \
     extern template cudaError_t launch_adjoint_shape<T, E, false>(const DevPlan&, const CallArgs&, const AdjArgs&, int, int, \

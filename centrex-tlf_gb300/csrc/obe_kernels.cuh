@@ -2159,7 +2159,7 @@ cudaError_t launch_rhs_shape(const DevPlan& P, long long count, const double* ts
 
 // the integrator shapes (threads per trajectory, elements per thread) and the RHS widths; the
 // build compiles obe_instance.cu once per shape (centrex_tlf_gb300/build.py: SHAPES, RHS_SHAPES)
-#define OBE_FOR_EACH_SHAPE(X) X(32, 8) X(32, 16) X(64, 4) X(64, 16) X(128, 2) X(128, 16) X(256, 32) X(512, 16)
+#define OBE_FOR_EACH_SHAPE(X) X(32, 8) X(32, 16) X(64, 4) X(64, 16) X(128, 2) X(128, 12) X(128, 16) X(256, 24) X(256, 32) X(512, 12) X(512, 16)
 #define OBE_FOR_EACH_RHS(X) X(32) X(64) X(128) X(256) X(512)
 #ifndef OBE_INSTANCE_TU
 #define OBE_EXTERN_SHAPE(T, E)                                                                                          \

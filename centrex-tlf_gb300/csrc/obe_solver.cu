@@ -202,15 +202,18 @@ obe_status scratch(obe_plan* p, size_t bytes, unsigned char** out) {
     return OBE_OK;
 }
 
-// elements per thread of the compiled shape of a width (OBE_FOR_EACH_SHAPE): 8 or 16 at 32
-// threads, 4 or 16 at 64, 2 or 16 at 128, 32 at 256, 16 at 512
+// elements per thread of the compiled shape of a width (OBE_FOR_EACH_SHAPE), the fewest that
+// hold the state: 8 or 16 at 32 threads, 4 or 16 at 64, 2, 12 or 16 at 128, 24 or 32 at 256,
+// 12 or 16 at 512 (a 76-state system: 5,776 elements, 24 per thread at 256 threads, 12 at 512)
 int ept_for(int N, int tpt) {
     if (tpt == 32) return N <= 32 * 8 ? 8 : 16;
-    if (tpt == 256) return 32;
+    if (tpt == 256) return N <= 256 * 24 ? 24 : 32;
+    if (tpt == 512) return N <= 512 * 12 ? 12 : 16;
     // the compact shapes of a small system at a wide launch (latency-bound single solves): two or
     // four elements per thread instead of sixteen mostly idle ones
     if (tpt == 64 && N <= 64 * 4) return 4;
     if (tpt == 128 && N <= 128 * 2) return 2;
+    if (tpt == 128 && N <= 128 * 12) return 12;
     return 16;
 }
 

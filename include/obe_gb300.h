@@ -303,8 +303,9 @@ obe_status obe_effective_rhs_debug(const obe_plan* plan, double t, const double*
 /*
  * Launch-shape tuning (no counterpart in the reference, whose CPU path has no launch shape).
  * A solve runs each trajectory on a group of threads (32, 64, 128, 256 or 512: the compiled
- * widths; up to 16 packed elements per thread, 32 at 256 threads; a state of at most 256
- * elements runs 4 per thread at 64 threads and 2 at 128) and puts one or more groups in a CTA.
+ * widths; up to 16 packed elements per thread, 32 at 256 threads, the fewest of the compiled
+ * counts that hold the state: 4 or 16 at 64 threads, 2, 12 or 16 at 128, 24 or 32 at 256,
+ * 12 or 16 at 512) and puts one or more groups in a CTA.
  * By default the width is the smallest that holds the state (256 above 2,048 elements) and a
  * CTA takes as many groups as its shared memory fits, fewer for small batches.
  *
