@@ -206,6 +206,9 @@ obe_status scratch(obe_plan* p, size_t bytes, unsigned char** out) {
 // hold the state: 8 or 16 at 32 threads, 4 or 16 at 64, 2, 12 or 16 at 128, 24 or 32 at 256,
 // 12 or 16 at 512 (a 76-state system: 5,776 elements, 24 per thread at 256 threads, 12 at 512)
 int ept_for(int N, int tpt) {
+    // OBE_EPT_WIDE=1: the widest compiled count of every width (runs those shapes on systems a
+    // tighter one would take; read at every launch)
+    if (const char* env = std::getenv("OBE_EPT_WIDE"); env && env[0] && env[0] != '0') return tpt == 256 ? 32 : 16;
     if (tpt == 32) return N <= 32 * 8 ? 8 : 16;
     if (tpt == 256) return N <= 256 * 24 ? 24 : 32;
     if (tpt == 512) return N <= 512 * 12 ? 12 : 16;

@@ -429,8 +429,13 @@ def test_mixed_form_gradients_through_a_time_event(golden):
                         checkpoint_every=ck, stop_event=_t_end_event(names), hits_expected=[1, 1, 0])
 
 
-def test_mixed_form_gradients_of_the_76_state_system(golden):
-    """256 threads per trajectory (the sweep's buffers in device memory), checkpointed."""
+@pytest.mark.parametrize("wide", [False, True])
+def test_mixed_form_gradients_of_the_76_state_system(golden, monkeypatch, wide):
+    """256 threads per trajectory (the sweep's buffers in device memory), checkpointed: the tight
+    shape (24 elements per thread) and, with OBE_EPT_WIDE, the widest (32), which systems of 79-90
+    states run."""
+    if wide:
+        monkeypatch.setenv("OBE_EPT_WIDE", "1")
     d = golden("plan_rc_76")
     g = d["gamma"]
     plan = NativePlan(d["payload"])

@@ -89,8 +89,13 @@ def test_autotune_keeps_its_fastest_candidate(golden):
         plan.native.set_shape(0, 0)
 
 
-def test_76_state_wide_shape_matches_oracle(golden):
-    """512 threads per trajectory on the 76-state system, smooth drive (switching frequency 0)."""
+@pytest.mark.parametrize("wide", [False, True])
+def test_76_state_wide_shape_matches_oracle(golden, monkeypatch, wide):
+    """256 and 512 threads per trajectory on the 76-state system, smooth drive (switching
+    frequency 0): the tight shapes (24 and 12 elements per thread) and, with OBE_EPT_WIDE, the
+    widest ones (32 and 16), which systems of 79-90 states run."""
+    if wide:
+        monkeypatch.setenv("OBE_EPT_WIDE", "1")
     d = golden("plan_rc_76")
     plan = api.prepare_lindblad_problem_py(d["payload"])
     g = d["gamma"]
