@@ -22,6 +22,7 @@
 #include <math_constants.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "obe_internal.h"
 #include "obe_vm.cuh"
@@ -1521,18 +1522,31 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             }
                         }
                     } else {
+                    // one copy per stage (the stage index a constant in each), so that stage s reads
+                    // exactly its s deviations instead of issuing all five under predicates
+                    auto stage_input = [&](auto stage) {
+                        constexpr int sc = decltype(stage)::value;
 #pragma unroll
-                    for (int e = 0; e < EPT; ++e) {
-                        int i = lt + e * TPT;
-                        if (i < N) {
-                            float acc = 0.f;
+                        for (int e = 0; e < EPT; ++e) {
+                            const int i = lt + e * TPT;
+                            if (i < N) {
+                                float acc = 0.f;
 #pragma unroll
-                            for (int j = 1; j < 6; ++j)
-                                if (j <= s) acc = fmaf(kTabF.a[M][s][j], s_K32[static_cast<size_t>(j - 1) * N + i], acc);
-                            const float k1f = s_k1f[i];
-                            if (s == 5) yn[e] = y[e] + h * (s_k1[i] + f2d(acc));
-                            s_G4f[gslot32(i, n)] = hf * fmaf(csum, k1f, acc);
+                                for (int j = 1; j <= sc; ++j)
+                                    acc = fmaf(kTabF.a[M][sc][j], s_K32[static_cast<size_t>(j - 1) * N + i], acc);
+                                const float k1f = s_k1f[i];
+                                if constexpr (sc == 5) yn[e] = y[e] + h * (s_k1[i] + f2d(acc));
+                                s_G4f[gslot32(i, n)] = hf * fmaf(csum, k1f, acc);
+                            }
                         }
+                    };
+                    switch (s) {
+                    case 0: stage_input(std::integral_constant<int, 0>{}); break;
+                    case 1: stage_input(std::integral_constant<int, 1>{}); break;
+                    case 2: stage_input(std::integral_constant<int, 2>{}); break;
+                    case 3: stage_input(std::integral_constant<int, 3>{}); break;
+                    case 4: stage_input(std::integral_constant<int, 4>{}); break;
+                    default: stage_input(std::integral_constant<int, 5>{}); break;
                     }
                     }
                     if (s < 5) {  // stage 7 shares stage 6's time
