@@ -1399,18 +1399,29 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                 // stages 2..7 (stage 7 input is the solution yn)
 #pragma unroll 1
                 for (int s = 0; s < 6; ++s) {
+                    // one copy per stage: stage s issues exactly its s + 1 products per element
+                    auto stage_input = [&](auto stage) {
+                        constexpr int sc = decltype(stage)::value;
 #pragma unroll
-                    for (int e = 0; e < EPT; ++e) {
-                        int i = lt + e * TPT;
-                        if (i < N) {
-                            double acc = 0.0;
+                        for (int e = 0; e < EPT; ++e) {
+                            const int i = lt + e * TPT;
+                            if (i < N) {
+                                double acc = 0.0;
 #pragma unroll
-                            for (int j = 0; j < 6; ++j)
-                                if (j <= s) acc += kTab.a[M][s][j] * Kat(j, i);
-                            double v = y[e] + h * acc;
-                            if (s == 5) yn[e] = v;
-                            s_G64[gsl(i)] = v;
+                                for (int j = 0; j <= sc; ++j) acc += kTab.a[M][sc][j] * Kat(j, i);
+                                const double v = y[e] + h * acc;
+                                if constexpr (sc == 5) yn[e] = v;
+                                s_G64[gsl(i)] = v;
+                            }
                         }
+                    };
+                    switch (s) {
+                    case 0: stage_input(std::integral_constant<int, 0>{}); break;
+                    case 1: stage_input(std::integral_constant<int, 1>{}); break;
+                    case 2: stage_input(std::integral_constant<int, 2>{}); break;
+                    case 3: stage_input(std::integral_constant<int, 3>{}); break;
+                    case 4: stage_input(std::integral_constant<int, 4>{}); break;
+                    default: stage_input(std::integral_constant<int, 5>{}); break;
                     }
                     rhs64(s < 4 ? s : 4, s_K + static_cast<size_t>(s + 1) * N);
                 }
@@ -1446,33 +1457,44 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
 #pragma unroll
                         for (int j = 1; j < 6; ++j) ha[j - 1] = j <= s ? h * kTab.a[M][s][j] : 0.0;
                         if constexpr (TPT >= 256) {
-                            constexpr int kCh = EPT < 8 ? EPT : 8;
+                            // one copy per stage (stage s loads and combines exactly its s deviations)
+                            auto stage_input64_big = [&](auto stage) {
+                                constexpr int sc = decltype(stage)::value;
+                                constexpr int kCh = EPT < 8 ? EPT : 8;
 #pragma unroll
-                            for (int e0 = 0; e0 < EPT; e0 += kCh) {
-                                float kv[kCh][5];
-                                double k1d[kCh];
+                                for (int e0 = 0; e0 < EPT; e0 += kCh) {
+                                    float kv[kCh][sc > 0 ? sc : 1];
+                                    double k1d[kCh];
 #pragma unroll
-                                for (int c = 0; c < kCh; ++c) {
-                                    const int i = lt + (e0 + c) * TPT;
-                                    const bool in = i < N;
+                                    for (int c = 0; c < kCh; ++c) {
+                                        const int i = lt + (e0 + c) * TPT;
+                                        const bool in = i < N;
 #pragma unroll
-                                    for (int j = 1; j < 6; ++j)
-                                        kv[c][j - 1] = (in && j <= s) ? s_K32[static_cast<size_t>(j - 1) * N + i] : 0.f;
-                                    k1d[c] = in ? s_k1[i] : 0.0;
-                                }
+                                        for (int j = 1; j <= sc; ++j)
+                                            kv[c][j - 1] = in ? s_K32[static_cast<size_t>(j - 1) * N + i] : 0.f;
+                                        k1d[c] = in ? s_k1[i] : 0.0;
+                                    }
 #pragma unroll
-                                for (int c = 0; c < kCh; ++c) {
-                                    const int e = e0 + c;
-                                    const int i = lt + e * TPT;
-                                    if (i < N) {
-                                        double dv = hcs * k1d[c];
+                                    for (int c = 0; c < kCh; ++c) {
+                                        const int e = e0 + c;
+                                        const int i = lt + e * TPT;
+                                        if (i < N) {
+                                            double dv = hcs * k1d[c];
 #pragma unroll
-                                        for (int j = 1; j < 6; ++j)
-                                            if (j <= s) dv = fma(ha[j - 1], f2d(kv[c][j - 1]), dv);
-                                        if (s == 5) yn[e] = y[e] + dv;
-                                        s_G4f[gslot32(i, n)] = d2f(dv);
+                                            for (int j = 1; j <= sc; ++j) dv = fma(ha[j - 1], f2d(kv[c][j - 1]), dv);
+                                            if constexpr (sc == 5) yn[e] = y[e] + dv;
+                                            s_G4f[gslot32(i, n)] = d2f(dv);
+                                        }
                                     }
                                 }
+                            };
+                            switch (s) {
+                            case 0: stage_input64_big(std::integral_constant<int, 0>{}); break;
+                            case 1: stage_input64_big(std::integral_constant<int, 1>{}); break;
+                            case 2: stage_input64_big(std::integral_constant<int, 2>{}); break;
+                            case 3: stage_input64_big(std::integral_constant<int, 3>{}); break;
+                            case 4: stage_input64_big(std::integral_constant<int, 4>{}); break;
+                            default: stage_input64_big(std::integral_constant<int, 5>{}); break;
                             }
                         } else {
 #pragma unroll
@@ -1489,6 +1511,9 @@ __global__ void __launch_bounds__(TPT > 256 ? TPT : MIXED && TPT < 256 ? kThread
                             }
                         }
                     } else if constexpr (TPT >= 256) {
+                        // the stage buffers live in device memory here: each batch of kCh elements
+                        // issues all its loads before the first use, so the L2 round trips overlap
+                        // (the same arithmetic as below)
                         // the stage buffers live in device memory here: each batch of kCh elements
                         // issues all its loads before the first use, so the L2 round trips overlap
                         // (the same arithmetic as below)
