@@ -431,9 +431,9 @@ struct VMProg {
     const double* val;
 };
 
-// The time-dependent compounds and coefficients at time t into one coefficient row: one call
-// site per lane and step in the integrator (the registers live across a call are saved around
-// it, so the VM's work sits behind a single call).  The programs come compacted in evaluation
+// The time-dependent compounds and coefficients at time t into one coefficient row, inlined
+// with the real-only VM into the integrator (as a call, the registers live across it were saved
+// and restored through local memory every step).  The programs come compacted in evaluation
 // order: the compounds (into their slots) and then the coefficients (into the row).
 static __device__ __forceinline__ void dyn_row(const DevPlan& P, int vm_smem, VMLane L, double t, double2* row) {
     VMProg V{P.vprog, P.vop, P.varg, P.vfn, P.vval};
