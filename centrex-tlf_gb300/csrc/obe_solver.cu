@@ -425,9 +425,10 @@ obe_status plan_launch(const DevPlan& P, bool mixed, long long n_traj, int vm_de
     }
     s->gpb = gpb;
     s->smem = plan_bytes + gpb * L.bytes;
-    // the time-dependent programs in shared memory too, when that costs no trajectory group
+    // the time-dependent programs in shared memory too, when that costs no trajectory group and
+    // no resident CTA
     const size_t plan_vm = plan_smem(P, s->tpt, mixed, true).bytes;
-    if (P.n_vprog > 0 && plan_vm + gpb * L.bytes <= limit) {
+    if (P.n_vprog > 0 && plan_vm + gpb * L.bytes <= limit && limit / (plan_vm + gpb * L.bytes) >= limit / s->smem) {
         s->vm_smem = 1;
         s->smem = plan_vm + gpb * L.bytes;
     }
