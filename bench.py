@@ -170,7 +170,7 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": "trajectories/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": "q1_16state_gaussian_scan_4096pt_tsit5", "points": args.points,
+        "config": {"workload": f"q1_16state_gaussian_scan_{args.points}pt_tsit5", "points": args.points,
                    "points_per_step": args.points, "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "trajectories/s", "cores": r["cores"], "kind": "port",
                          "sample": f"the whole {args.points}-point scan every step, all {r['cores']} host threads, "
@@ -1013,7 +1013,7 @@ def run_gpu(args) -> None:
         "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32-rhs/f64-accumulate",
         "data": "synthetic (seeded scan of the reference-built 16-state plan)",
-        "config": {"workload": "q1_16state_gaussian_scan_4096pt_tsit5", "points_per_gpu": b, "solver": "tsit5",
+        "config": {"workload": f"q1_16state_gaussian_scan_{args.points}pt_tsit5", "points_per_gpu": b, "solver": "tsit5",
                    "rtol": 1e-8, "atol": 1e-11, "precision": args.precision, "l2": "flushed (256 MB write) between steps",
                    "attempted_steps_per_launch": attempted},
         "e2e": {"value": e2e_value, "unit": "trajectories/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
