@@ -325,7 +325,7 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
     z polarisation, Gaussian pulse σ = 20/Γ centred at 100/Γ), Dopri5 rtol 1e-8 atol 1e-11 over
     [0, 200/Γ]: final populations and the excited-population integral through the reference-facing
     single-solve call (host arrays, one call per output as the reference makes them), FP64 and the
-    mixed form, at the automatic launch width (32 threads) and at 64 and 128 threads; against the oracle
+    mixed forms, at the automatic launch width (32 threads) and at 64 and 128 threads; against the oracle
     solving the same trajectory on one host thread."""
     import codec
     import oracle
@@ -367,7 +367,7 @@ def measure_single(torch, dev, reps: int = 5) -> dict:
     res = {}
     for width in (0, 64, 128):
         plan.native.set_shape(width, 0)
-        for precision in ("fp64", "mixed"):
+        for precision in ("fp64", "mixed", "mixed_fp32_control"):
             res[(width, precision)] = timed(precision)
     plan.native.set_shape(0, 0)
     op = oracle.OraclePlan(d["payload"])
